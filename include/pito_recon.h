@@ -1,0 +1,240 @@
+/*
+ * pito_recon.h — C ABI of the GB300 block-reconstruction engine.
+ *
+ * The engine replaces the reconstruction half of pito-codecs' H.264 and HEVC
+ * slice decoders.  In the reference, reconstruction is interleaved with the
+ * entropy parse, one macroblock / transform unit at a time:
+ *
+ *   H.264  reconstruct_intra / predict_inter + reconstruct_inter_residual
+ *          (src/h264/dec/slicedec.rs:1743-1749, src/h264/dec/cabac_mb.rs:712-717),
+ *          then the row-lagged loop filter flush_rows -> deblock_mb
+ *          (src/h264/dec/slicedec.rs:184-208).
+ *   HEVC   intra_predict / reconstruct / motion_compensate
+ *          (src/hevc/slicedec.rs:1642-1669, 2169), then filter::ctb_decoded /
+ *          finish (src/hevc/filter.rs:13-72).
+ *
+ * Here the host parse fills syntax records for a whole picture and one call
+ * reconstructs it on the GPU against a decoded-picture buffer (DPB) that stays
+ * resident in device memory.  Every call is asynchronous on the stream's CUDA
+ * stream; the syntax buffers must stay valid until rc_stream_sync returns (or
+ * until the stream's next submit when they are host buffers, which are staged
+ * through pinned memory before the call returns).
+ *
+ * All functions return 0 on success and a negative RC_E* code on failure.
+ */
+#ifndef PITO_RECON_H
+#define PITO_RECON_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- error codes ------------------------------------------------------- */
+#define RC_OK 0
+#define RC_EINVAL (-1)       /* bad argument or syntax record rejected on the host */
+#define RC_ENOMEM (-2)       /* device or pinned allocation failed / over budget   */
+#define RC_ECUDA (-3)        /* a CUDA runtime call failed                         */
+#define RC_ETIMEOUT (-4)     /* a device wavefront wait gave up (sticky)           */
+#define RC_EDEVICE (-5)      /* the device reported a bad record (sticky)          */
+#define RC_ENODEV (-6)       /* no CUDA device / kernels not loadable              */
+
+/* ---- codecs ------------------------------------------------------------ */
+#define RC_CODEC_H264 1
+#define RC_CODEC_HEVC 2
+
+/* where a submitted syntax buffer lives */
+#define RC_MEM_HOST 0
+#define RC_MEM_DEVICE 1
+
+typedef struct rc_stream rc_stream;
+
+/* ======================================================================== */
+/*  H.264 syntax records                                                     */
+/* ======================================================================== */
+
+/* rc_h264_mb.kind — the MbKind values of src/h264/dec/picture.rs:42-53
+ * folded to what reconstruction distinguishes (P_Skip, B_Skip, B_Direct and
+ * ordinary inter macroblocks are all RC_H264_INTER). */
+#define RC_H264_NONE 0 /* not decoded (missing slice): unusable neighbour */
+#define RC_H264_I4x4 1
+#define RC_H264_I8x8 2
+#define RC_H264_I16x16 3
+#define RC_H264_IPCM 4
+#define RC_H264_INTER 5
+
+/*
+ * One macroblock.  Mirrors the reconstruction fields of MbState
+ * (src/h264/dec/picture.rs:66-84) plus the coefficient levels that the parse
+ * hands to put_luma4/put_luma8/put_luma_dc/put_chroma_dc/put_chroma_ac
+ * (src/h264/dec/slicedec.rs:1462-1555), which the device dequantises.
+ *
+ * Level payload at levels[coef_off...] (int16, scan order as parsed):
+ *   (dc_coded & 1)  16 levels  Intra16x16 luma DC, 4x4 zig-zag scan
+ *   luma blocks     for each set bit of luma_coded, ascending:
+ *                   transform_8x8 ? 64 levels (8x8 zig-zag, bit = 8x8 index)
+ *                                 : 16 levels (4x4 zig-zag, bit = 4x4 raster
+ *                                   index; level 0 ignored for Intra16x16)
+ *   (dc_coded & 2)  4 levels Cb DC;  (dc_coded & 4)  4 levels Cr DC
+ *   chroma AC       for each set bit of chroma_coded (0-3 Cb, 4-7 Cr):
+ *                   16 levels, level 0 ignored
+ *   kind == IPCM    384 samples instead: 256 Y, 64 Cb, 64 Cr (raster)
+ *
+ * mv[l][k] is the motion vector (quarter-pel) that motion-compensates 4x4
+ * block k (raster) from list l; ref_idx is per 8x8 block.  Partition shapes
+ * are not needed: every sample's prediction depends only on its block's
+ * vector, reference and weights.
+ */
+typedef struct rc_h264_mb {
+    uint8_t kind;          /* RC_H264_* */
+    uint8_t transform_8x8; /* 0/1 */
+    uint8_t qp;            /* luma QP 0..51 (0 for I_PCM)                     */
+    uint8_t qpc[2];        /* chroma QP per component after the QPC table     */
+    uint8_t i16_mode;      /* Intra16x16 prediction mode 0..3                 */
+    uint8_t chroma_mode;   /* intra chroma prediction mode 0..3               */
+    uint8_t dc_coded;      /* bit0 luma DC, bit1 Cb DC, bit2 Cr DC            */
+    uint16_t slice;        /* index into rc_h264_picture.slices               */
+    uint16_t nz_mask;      /* 4x4 blocks (raster) with non-zero coefficients  */
+    uint16_t luma_coded;   /* blocks with a level payload (see above)         */
+    uint8_t chroma_coded;  /* chroma AC blocks with a level payload           */
+    uint8_t reserved0;
+    uint32_t coef_off;     /* offset of this MB's payload, in int16 units     */
+    uint8_t intra_modes[16]; /* Intra4x4/8x8 modes per 4x4 block (raster)     */
+    int8_t ref_idx[2][4];  /* per 8x8 block and list, -1 = list unused        */
+    uint8_t wp[4];         /* weight-table entry per 8x8 block, 0xff = default */
+    int16_t mv[2][16][2];  /* per 4x4 block and list, quarter-pel (x, y)      */
+} rc_h264_mb;              /* 176 bytes */
+
+/* Per-slice state the loop filter and motion compensation read
+ * (SliceInfo, src/h264/dec/slicedec.rs:116-121; ref lists of SliceDecoder). */
+#define RC_H264_MAX_REFS 32
+typedef struct rc_h264_slice {
+    int32_t disable_deblocking_filter_idc; /* 0, 1 or 2                        */
+    int32_t alpha_offset;  /* slice_alpha_c0_offset_div2 * 2                   */
+    int32_t beta_offset;   /* slice_beta_offset_div2 * 2                       */
+    int32_t num_ref[2];    /* active references per list                      */
+    int32_t ref_slot[2][RC_H264_MAX_REFS]; /* DPB slot of each reference       */
+    uint32_t ref_id[2][RC_H264_MAX_REFS];  /* picture identity (RefPic::id)    */
+} rc_h264_slice;
+
+/* One resolved weighting (Weight after Weight::simplify,
+ * src/h264/dec/inter.rs:249-282) for Y, Cb, Cr.  Bit c of `explicit` set:
+ * component c uses the weighted formula, else the default copy / average. */
+typedef struct rc_h264_weight {
+    uint8_t explicit_mask;
+    uint8_t reserved[3];
+    int32_t log_wd[3];
+    int32_t w0[3], w1[3], o0[3], o1[3];
+} rc_h264_weight;          /* 64 bytes */
+
+typedef struct rc_h264_picture {
+    int32_t mem;                      /* RC_MEM_HOST or RC_MEM_DEVICE          */
+    int32_t constrained_intra_pred;   /* PPS flag                              */
+    uint32_t frame_id;                /* identity of this picture              */
+    int32_t num_slices;
+    int32_t num_weights;
+    int32_t reserved;
+    size_t num_levels;                /* int16 entries in levels               */
+    const rc_h264_mb *mbs;            /* mb_w * mb_h records, raster order     */
+    const rc_h264_slice *slices;
+    const rc_h264_weight *weights;
+    const int16_t *levels;
+    /* Scaling matrices of the PPS (ScalingMatrices m4[6][16], m8[6][64]);
+     * NULL = flat 16.  Always host memory. */
+    const uint8_t *scaling4;          /* [6][16] */
+    const uint8_t *scaling8;          /* [6][64] */
+} rc_h264_picture;
+
+/* ======================================================================== */
+/*  Stream / DPB lifetime                                                    */
+/* ======================================================================== */
+
+/* Make `device` the CUDA device that streams created afterwards on this
+ * thread use (the library keeps its own CUDA runtime state). */
+int rc_device_select(int device);
+
+/*
+ * Create a reconstruction stream: device DPB of `dpb_slots` pictures of the
+ * coded size (width, height rounded up to the codec's block grid), a CUDA
+ * stream and the scratch the kernels use.  `hbm_budget` bounds the device
+ * bytes the stream may hold (0 = unbounded); RC_ENOMEM if it would exceed it.
+ * Replaces Decoder::with_threads (src/h264/mod.rs:38, src/hevc/decoder.rs:87)
+ * and the decoder-owned frame pool (src/h264/dec/picture.rs:196).
+ */
+int rc_stream_create(int codec, int width, int height, int bit_depth,
+                     int dpb_slots, size_t hbm_budget, rc_stream **out);
+
+/* Release everything the stream owns (Drop of the reference Decoder). */
+void rc_stream_destroy(rc_stream *s);
+
+/* Reconstruct one H.264 picture into DPB slot `out_slot`: inter prediction
+ * with residual, intra prediction with residual, then the deblocking filter.
+ * Records are validated on the host first (slice index, ref_idx < num_ref,
+ * DPB slots, payload bounds) and rejected with RC_EINVAL before any launch,
+ * as slicedec.rs:888-892 and 1442-1446 reject bad syntax. */
+int rc_h264_submit(rc_stream *s, const rc_h264_picture *pic, int out_slot);
+
+/* Host-side validation rc_h264_submit applies to host-memory records, for a
+ * stream of mb_w x mb_h macroblocks and dpb_slots DPB slots; needs no GPU.
+ * Returns 0 or RC_EINVAL. */
+int rc_h264_validate(int mb_w, int mb_h, int dpb_slots, const rc_h264_picture *pic);
+
+/* Wait for all submitted work; returns the sticky error word (0 if none). */
+int rc_stream_sync(rc_stream *s);
+
+/* Sticky device/host error (RC_ETIMEOUT, RC_EDEVICE, ...) or 0; clears it.
+ * Replaces Decoder::take_error (src/h264/dec/decoder.rs:222). */
+int rc_stream_error(rc_stream *s);
+
+/* Copy a DPB picture into caller memory, cropped to (x, y, w, h) in luma
+ * samples (chroma: x/2, y/2, ceil(w/2), ceil(h/2)); planes tightly packed,
+ * 8-bit samples as bytes, >8-bit as little-endian uint16.  Synchronous.
+ * Replaces Frame::copy_cropped (src/h264/dec/picture.rs:596-642) and
+ * hevc Frame::copy_cropped (src/hevc/picture.rs:374). */
+int rc_picture_download(rc_stream *s, int slot, int x, int y, int w, int h,
+                        void *out_y, void *out_u, void *out_v);
+
+/* Asynchronous form of rc_picture_download, ordered on the stream's CUDA
+ * stream after all submitted work; outputs must be pinned host memory (or
+ * device memory) and are valid after rc_stream_sync. */
+int rc_picture_download_async(rc_stream *s, int slot, int x, int y, int w,
+                              int h, void *out_y, void *out_u, void *out_v);
+
+/* Fill a DPB slot from caller planes of the full coded size (tightly packed),
+ * e.g. to seed references.  Synchronous.  Counterpart of Frame::fill
+ * (src/h264/dec/picture.rs:508-519). */
+int rc_picture_upload(rc_stream *s, int slot, const void *y, const void *u,
+                      const void *v);
+
+/* Geometry of the stream's DPB planes: coded width/height in luma samples,
+ * row pitch of the luma and chroma planes in bytes, and device pointers of
+ * one slot's planes (for zero-copy consumers). */
+int rc_stream_geometry(rc_stream *s, int *coded_w, int *coded_h,
+                       int *luma_pitch, int *chroma_pitch);
+int rc_picture_device_planes(rc_stream *s, int slot, void **y, void **u,
+                             void **v);
+
+/* Per-kernel timing with CUDA events on the stream (off by default).
+ * rc_stream_profile_read syncs, then returns for each kernel id
+ * (RC_KERNEL_*) the accumulated milliseconds and launch counts since
+ * profiling was enabled; returns the number of kernel ids filled. */
+#define RC_KERNEL_H264_MB 0
+#define RC_KERNEL_H264_WAVE 1
+#define RC_KERNEL_COUNT 8
+int rc_stream_profile(rc_stream *s, int enable);
+int rc_stream_profile_read(rc_stream *s, double *ms, long long *launches,
+                           int max_kernels);
+
+/* Number of kernel launches this stream has issued so far. */
+long long rc_stream_launches(rc_stream *s);
+
+/* The CUDA stream (cudaStream_t) the stream's work is ordered on. */
+void *rc_stream_cuda_stream(rc_stream *s);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PITO_RECON_H */

@@ -1,0 +1,61 @@
+/*
+ * oracle.h — CPU restatement of pito-codecs' block reconstruction.
+ *
+ * TEST INFRASTRUCTURE ONLY.  Nothing in the shipped library links, loads or
+ * calls this code; only tests/, __graft_entry__.smoke() and bench.py's CPU
+ * baseline use it, as the checker.  Each function follows the reference's
+ * scalar implementation (cited file:line, paths inside the pito-codecs
+ * crate), driven by the same syntax records the GPU consumes
+ * (include/pito_recon.h).
+ *
+ * Planes are tightly packed at the coded size, as the reference stores them:
+ * luma stride = mb_w * 16, chroma stride = mb_w * 8 (H.264).
+ */
+#ifndef PITO_ORACLE_H
+#define PITO_ORACLE_H
+
+#include <stdint.h>
+#include "../include/pito_recon.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Reconstruct one H.264 picture (pre-deblock recon of every MB in raster
+ * order, then deblock_mb in raster order).  ref_*[slot] are the DPB planes
+ * indexed by rc_h264_slice.ref_slot.  Returns 0 or RC_EINVAL. */
+int oracle_h264_recon(int mb_w, int mb_h, const rc_h264_picture *pic,
+                      const uint8_t *const *ref_y, const uint8_t *const *ref_u,
+                      const uint8_t *const *ref_v, uint8_t *y, uint8_t *u,
+                      uint8_t *v);
+
+/* Same, but skipping the loop filter (for kernel-level tests). */
+int oracle_h264_recon_nofilter(int mb_w, int mb_h, const rc_h264_picture *pic,
+                               const uint8_t *const *ref_y,
+                               const uint8_t *const *ref_u,
+                               const uint8_t *const *ref_v, uint8_t *y,
+                               uint8_t *u, uint8_t *v);
+
+/* Deblock an already reconstructed picture in place. */
+void oracle_h264_deblock(int mb_w, int mb_h, const rc_h264_picture *pic,
+                         uint8_t *y, uint8_t *u, uint8_t *v);
+
+/* Block-level entry points used by the known-answer tests. */
+void oracle_h264_idct4_add(const int32_t d[16], uint8_t *dst, int stride);
+void oracle_h264_idct8_add(const int32_t d[64], uint8_t *dst, int stride);
+void oracle_h264_luma_dc_dequant(int32_t c[16], int qp, int32_t ls00);
+void oracle_h264_chroma_dc_dequant(int32_t c[4], int qp, int32_t ls00);
+void oracle_h264_level_scale(const uint8_t *m4, const uint8_t *m8,
+                             int32_t ls4[6][6][16], int32_t ls8[6][6][64]);
+void oracle_h264_mc_luma(const uint8_t *plane, int width, int height, int px,
+                         int py, int mvx, int mvy, int bw, int bh,
+                         uint8_t *out, int os);
+void oracle_h264_mc_chroma(const uint8_t *plane, int cwidth, int cheight,
+                           int cpx, int cpy, int mvx, int mvy, int bw, int bh,
+                           uint8_t *out, int os);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,75 @@
+"""ctypes binding of the oracle (liboracle.so).
+
+TEST INFRASTRUCTURE ONLY: used by tests/, __graft_entry__.smoke() and
+bench.py's CPU-baseline leg as the checker.  The engine never loads it.
+"""
+from __future__ import annotations
+
+import ctypes
+import pathlib
+import subprocess
+
+import numpy as np
+
+HERE = pathlib.Path(__file__).resolve().parent
+LIB = HERE / "liboracle.so"
+_lib = None
+
+
+def build() -> None:
+    r = subprocess.run(["make", "-s", "-C", str(HERE)], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"oracle build failed:\n{r.stdout}\n{r.stderr}")
+
+
+def lib() -> ctypes.CDLL:
+    global _lib
+    if _lib is None:
+        build()
+        _lib = ctypes.CDLL(str(LIB))
+        vp, i32 = ctypes.c_void_p, ctypes.c_int
+        for name in ("oracle_h264_recon", "oracle_h264_recon_nofilter"):
+            f = getattr(_lib, name)
+            f.argtypes = [i32, i32, vp, vp, vp, vp, vp, vp, vp]
+            f.restype = i32
+        _lib.oracle_h264_deblock.argtypes = [i32, i32, vp, vp, vp, vp]
+        _lib.oracle_h264_deblock.restype = None
+        _lib.oracle_h264_idct4_add.argtypes = [vp, vp, i32]
+        _lib.oracle_h264_idct8_add.argtypes = [vp, vp, i32]
+        _lib.oracle_h264_luma_dc_dequant.argtypes = [vp, i32, ctypes.c_int32]
+        _lib.oracle_h264_chroma_dc_dequant.argtypes = [vp, i32, ctypes.c_int32]
+        _lib.oracle_h264_level_scale.argtypes = [vp, vp, vp, vp]
+        _lib.oracle_h264_mc_luma.argtypes = [vp, i32, i32, i32, i32, i32, i32, i32, i32, vp, i32]
+        _lib.oracle_h264_mc_chroma.argtypes = [vp, i32, i32, i32, i32, i32, i32, i32, i32, vp, i32]
+    return _lib
+
+
+class H264Dpb:
+    """CPU decoded-picture buffer: planes per slot at the coded size."""
+
+    def __init__(self, mb_w: int, mb_h: int, slots: int):
+        self.mb_w, self.mb_h, self.slots = mb_w, mb_h, slots
+        W, H = mb_w * 16, mb_h * 16
+        self.y = [np.zeros((H, W), np.uint8) for _ in range(slots)]
+        self.u = [np.zeros((H // 2, W // 2), np.uint8) for _ in range(slots)]
+        self.v = [np.zeros((H // 2, W // 2), np.uint8) for _ in range(slots)]
+
+    def _ptrs(self, planes):
+        arr = (ctypes.c_void_p * self.slots)(*[p.ctypes.data for p in planes])
+        return arr
+
+    def recon(self, picture_ptr: int, out_slot: int, filter: bool = True) -> int:
+        L = lib()
+        f = L.oracle_h264_recon if filter else L.oracle_h264_recon_nofilter
+        ry, ru, rv = self._ptrs(self.y), self._ptrs(self.u), self._ptrs(self.v)
+        # the output slot is never its own reference: reconstruct into fresh planes
+        y = self.y[out_slot].copy()
+        u = self.u[out_slot].copy()
+        v = self.v[out_slot].copy()
+        rc = f(self.mb_w, self.mb_h, picture_ptr, ry, ru, rv, y.ctypes.data, u.ctypes.data, v.ctypes.data)
+        if rc == 0:
+            self.y[out_slot], self.u[out_slot], self.v[out_slot] = y, u, v
+        return rc
+
+    def planes(self, slot: int):
+        return self.y[slot], self.u[slot], self.v[slot]

@@ -1,0 +1,564 @@
+// recon_api.cu — the C ABI of include/pito_recon.h: stream and DPB lifetime,
+// host-side validation of syntax records, staging of host buffers through
+// pinned memory, kernel launches and the sticky error word.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "recon_internal.h"
+
+namespace {
+
+size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+// LevelScale::new, src/h264/dec/transform.rs:10-28 (normAdjust tables of
+// src/h264/dec/tables.rs:14-60): per-PPS dequantisation tables.
+void h264_level_scale(const uint8_t *m4, const uint8_t *m8, int32_t *ls4, int32_t *ls8) {
+    static const uint16_t N4[6][3] = {{10, 16, 13}, {11, 18, 14}, {13, 20, 16},
+                                      {14, 23, 18}, {16, 25, 20}, {18, 29, 23}};
+    static const uint16_t N8[6][6] = {{20, 18, 32, 19, 25, 24}, {22, 19, 35, 21, 28, 26},
+                                      {26, 23, 42, 24, 33, 31}, {28, 25, 45, 26, 35, 33},
+                                      {32, 28, 51, 30, 40, 38}, {36, 32, 58, 34, 46, 43}};
+    for (int l = 0; l < 6; l++)
+        for (int q = 0; q < 6; q++) {
+            for (int p = 0; p < 16; p++) {
+                int i = p / 4, j = p % 4;
+                int k = (i % 2 == 0 && j % 2 == 0) ? 0 : (i % 2 == 1 && j % 2 == 1) ? 1 : 2;
+                ls4[(l * 6 + q) * 16 + p] = (int32_t)(m4 ? m4[l * 16 + p] : 16) * N4[q][k];
+            }
+            for (int p = 0; p < 64; p++) {
+                int i = p / 8, j = p % 8, k;
+                if (i % 4 == 0 && j % 4 == 0) k = 0;
+                else if (i % 2 == 1 && j % 2 == 1) k = 1;
+                else if (i % 4 == 2 && j % 4 == 2) k = 2;
+                else if ((i % 4 == 0 && j % 2 == 1) || (i % 2 == 1 && j % 4 == 0)) k = 3;
+                else if ((i % 4 == 0 && j % 4 == 2) || (i % 4 == 2 && j % 4 == 0)) k = 4;
+                else k = 5;
+                ls8[(l * 6 + q) * 64 + p] = (int32_t)(m8 ? m8[l * 64 + p] : 16) * N8[q][k];
+            }
+        }
+}
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+};
+
+}  // namespace
+
+struct rc_stream {
+    int codec = 0, bit_depth = 8, slots = 0;
+    int width = 0, height = 0;  // coded size
+    int mb_w = 0, mb_h = 0;
+    int pitch = 0, cpitch = 0, cw = 0, ch = 0;
+    size_t slot_bytes = 0, u_off = 0, v_off = 0;
+    size_t budget = 0, held = 0;
+    cudaStream_t st = nullptr;
+    uint8_t *dpb = nullptr;
+    uint32_t *rflag = nullptr, *dflag = nullptr, *counter = nullptr, *error = nullptr, *tasks = nullptr;
+    int ntasks = 0;
+    DevBuf mbs, slices, weights, levels;
+    int32_t *ls = nullptr;            // device ls4 (2304 ints) + ls8 (2304*4 ints)
+    std::vector<int32_t> ls_host;     // last uploaded tables
+    bool ls_valid = false;
+    void *staging[2] = {nullptr, nullptr};
+    size_t staging_cap[2] = {0, 0};
+    cudaEvent_t staged[2] = {nullptr, nullptr};
+    int submits = 0;
+    uint32_t epoch = 0;
+    long long launches = 0;
+    int sticky = 0;
+    int wave_blocks = 0;
+    int sms = 0;
+    uint32_t wait_limit = RC_WAIT_LIMIT;
+    // per-kernel CUDA-event timing
+    bool profiling = false;
+    std::vector<cudaEvent_t> ev_free;
+    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> ev_pending;
+    double prof_ms[RC_KERNEL_COUNT] = {0};
+    long long prof_n[RC_KERNEL_COUNT] = {0};
+};
+
+namespace {
+
+cudaEvent_t take_event(rc_stream *s) {
+    if (!s->ev_free.empty()) {
+        cudaEvent_t e = s->ev_free.back();
+        s->ev_free.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+// Launch one kernel through `fn`, bracketed by timing events when profiling.
+template <class F>
+void timed(rc_stream *s, int kernel, F fn) {
+    if (!s->profiling) {
+        fn();
+        s->launches++;
+        return;
+    }
+    cudaEvent_t a = take_event(s), b = take_event(s);
+    cudaEventRecord(a, s->st);
+    fn();
+    cudaEventRecord(b, s->st);
+    s->ev_pending.push_back({kernel, {a, b}});
+    s->launches++;
+}
+
+void drain_profile(rc_stream *s) {
+    for (auto &p : s->ev_pending) {
+        float ms = 0;
+        if (cudaEventElapsedTime(&ms, p.second.first, p.second.second) == cudaSuccess) {
+            s->prof_ms[p.first] += ms;
+            s->prof_n[p.first] += 1;
+        }
+        s->ev_free.push_back(p.second.first);
+        s->ev_free.push_back(p.second.second);
+    }
+    s->ev_pending.clear();
+}
+
+int cuda_fail(rc_stream *s) {
+    if (s && !s->sticky) s->sticky = RC_ECUDA;
+    return RC_ECUDA;
+}
+
+bool dev_alloc(rc_stream *s, void **p, size_t n) {
+    if (s->budget && s->held + n > s->budget) return false;
+    if (cudaMalloc(p, n) != cudaSuccess) return false;
+    s->held += n;
+    return true;
+}
+void dev_free(rc_stream *s, void *p, size_t n) {
+    if (!p) return;
+    cudaFree(p);
+    s->held -= std::min(s->held, n);
+}
+
+// Grow a device buffer (waits for in-flight work that may read it).
+int ensure(rc_stream *s, DevBuf &b, size_t n) {
+    if (n <= b.cap) return 0;
+    if (cudaStreamSynchronize(s->st) != cudaSuccess) return cuda_fail(s);
+    size_t want = std::max(n, b.cap + b.cap / 2);
+    want = align_up(std::max<size_t>(want, 4096), 4096);
+    dev_free(s, b.p, b.cap);
+    b.p = nullptr;
+    b.cap = 0;
+    if (!dev_alloc(s, &b.p, want)) return RC_ENOMEM;
+    b.cap = want;
+    return 0;
+}
+
+bool is_pinned(const void *p) {
+    if (!p) return true;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost;
+}
+
+// Host-side validation of an H.264 picture (the checks of
+// src/h264/dec/slicedec.rs:888-892, 1442-1446 and the payload bounds).
+struct Geo {
+    int mb_w, mb_h, slots;
+};
+int validate_h264(const Geo *s, const rc_h264_picture *p) {
+    if (!p->mbs || p->num_slices <= 0 || !p->slices) return RC_EINVAL;
+    if (p->num_weights < 0 || (p->num_weights > 0 && !p->weights)) return RC_EINVAL;
+    if (p->num_levels > 0 && !p->levels) return RC_EINVAL;
+    for (int i = 0; i < p->num_slices; i++) {
+        const rc_h264_slice &sl = p->slices[i];
+        if (sl.disable_deblocking_filter_idc < 0 || sl.disable_deblocking_filter_idc > 2) return RC_EINVAL;
+        for (int l = 0; l < 2; l++) {
+            if (sl.num_ref[l] < 0 || sl.num_ref[l] > RC_H264_MAX_REFS) return RC_EINVAL;
+            for (int r = 0; r < sl.num_ref[l]; r++)
+                if (sl.ref_slot[l][r] < 0 || sl.ref_slot[l][r] >= s->slots) return RC_EINVAL;
+        }
+    }
+    const int n = s->mb_w * s->mb_h;
+    for (int a = 0; a < n; a++) {
+        const rc_h264_mb &m = p->mbs[a];
+        if (m.kind > RC_H264_INTER) return RC_EINVAL;
+        if (m.kind == RC_H264_NONE) continue;
+        if (m.slice >= p->num_slices) return RC_EINVAL;
+        if (m.qp > 51 || m.qpc[0] > 51 || m.qpc[1] > 51) return RC_EINVAL;
+        if (m.kind == RC_H264_IPCM) {
+            if ((size_t)m.coef_off + 384 > p->num_levels) return RC_EINVAL;
+            continue;
+        }
+        if ((m.kind == RC_H264_I8x8) != (m.transform_8x8 != 0) && m.kind != RC_H264_INTER) return RC_EINVAL;
+        if (m.kind == RC_H264_INTER) {
+            const rc_h264_slice &sl = p->slices[m.slice];
+            for (int b = 0; b < 4; b++) {
+                int r0 = m.ref_idx[0][b], r1 = m.ref_idx[1][b];
+                if (r0 < -1 || r1 < -1 || (r0 < 0 && r1 < 0)) return RC_EINVAL;
+                if (r0 >= sl.num_ref[0] || r1 >= sl.num_ref[1]) return RC_EINVAL;
+                if (m.wp[b] != 0xff && m.wp[b] >= p->num_weights) return RC_EINVAL;
+            }
+        } else {
+            if (m.i16_mode > 3 || m.chroma_mode > 3) return RC_EINVAL;
+            for (int i = 0; i < 16; i++)
+                if (m.intra_modes[i] > 8) return RC_EINVAL;
+        }
+        int t8 = m.transform_8x8;
+        size_t need = ((m.kind == RC_H264_I16x16 && (m.dc_coded & 1)) ? 16 : 0) +
+                      (size_t)__builtin_popcount(m.luma_coded & (t8 ? 0xf : 0xffff)) * (t8 ? 64 : 16) +
+                      (size_t)__builtin_popcount(m.dc_coded & 6) * 4 + (size_t)__builtin_popcount(m.chroma_coded) * 16;
+        if ((size_t)m.coef_off + need > p->num_levels) return RC_EINVAL;
+    }
+    return 0;
+}
+
+// Wave task list: R(x,y) at key 2(x+2y), D(x,y) at key 2(x+2y+4)+1.
+std::vector<uint32_t> h264_tasks(int mb_w, int mb_h) {
+    std::vector<std::pair<int, uint32_t>> v;
+    v.reserve(2 * mb_w * mb_h);
+    for (int y = 0; y < mb_h; y++)
+        for (int x = 0; x < mb_w; x++) {
+            uint32_t a = (uint32_t)(y * mb_w + x);
+            v.push_back({2 * (x + 2 * y), a});
+            v.push_back({2 * (x + 2 * y + 4) + 1, a | 0x80000000u});
+        }
+    std::stable_sort(v.begin(), v.end(), [](const auto &a, const auto &b) { return a.first < b.first; });
+    std::vector<uint32_t> t(v.size());
+    for (size_t i = 0; i < v.size(); i++) t[i] = v[i].second;
+    return t;
+}
+
+void destroy(rc_stream *s) {
+    if (!s) return;
+    if (s->st) cudaStreamSynchronize(s->st);
+    drain_profile(s);
+    for (cudaEvent_t e : s->ev_free) cudaEventDestroy(e);
+    dev_free(s, s->dpb, s->slot_bytes * s->slots);
+    for (DevBuf *b : {&s->mbs, &s->slices, &s->weights, &s->levels}) dev_free(s, b->p, b->cap);
+    cudaFree(s->rflag);
+    cudaFree(s->dflag);
+    cudaFree(s->counter);
+    cudaFree(s->error);
+    cudaFree(s->tasks);
+    cudaFree(s->ls);
+    for (int i = 0; i < 2; i++) {
+        if (s->staging[i]) cudaFreeHost(s->staging[i]);
+        if (s->staged[i]) cudaEventDestroy(s->staged[i]);
+    }
+    if (s->st) cudaStreamDestroy(s->st);
+    delete s;
+}
+
+}  // namespace
+
+extern "C" {
+
+int rc_device_select(int device) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        return RC_ENODEV;
+    }
+    if (device < 0 || device >= n) return RC_EINVAL;
+    return cudaSetDevice(device) == cudaSuccess ? RC_OK : RC_ECUDA;
+}
+
+int rc_stream_create(int codec, int width, int height, int bit_depth, int dpb_slots, size_t hbm_budget,
+                     rc_stream **out) {
+    if (!out) return RC_EINVAL;
+    *out = nullptr;
+    if (codec != RC_CODEC_H264) return RC_EINVAL;
+    if (width <= 0 || height <= 0 || width > 8192 || height > 8192 || dpb_slots <= 0 || dpb_slots > 64)
+        return RC_EINVAL;
+    if (bit_depth != 8) return RC_EINVAL;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return RC_ENODEV;
+    }
+    rc_stream *s = new (std::nothrow) rc_stream();
+    if (!s) return RC_ENOMEM;
+    s->codec = codec;
+    s->bit_depth = bit_depth;
+    s->slots = dpb_slots;
+    s->budget = hbm_budget;
+    s->mb_w = (width + 15) / 16;
+    s->mb_h = (height + 15) / 16;
+    s->width = s->mb_w * 16;
+    s->height = s->mb_h * 16;
+    s->cw = s->width / 2;
+    s->ch = s->height / 2;
+    s->pitch = (int)align_up(s->width, 128);
+    s->cpitch = (int)align_up(s->cw, 128);
+    s->u_off = (size_t)s->pitch * s->height;
+    s->v_off = s->u_off + (size_t)s->cpitch * s->ch;
+    s->slot_bytes = align_up(s->v_off + (size_t)s->cpitch * s->ch, 256);
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, dev);
+    s->wave_blocks = std::max(1, s->sms / 2);
+    if (const char *e = getenv("PITO_RECON_WAVE_BLOCKS")) {
+        int v = atoi(e);
+        if (v > 0 && v <= 4096) s->wave_blocks = v;
+    }
+    const int n = s->mb_w * s->mb_h;
+    std::vector<uint32_t> tasks = h264_tasks(s->mb_w, s->mb_h);
+    s->ntasks = (int)tasks.size();
+    bool ok = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking) == cudaSuccess;
+    ok = ok && dev_alloc(s, (void **)&s->dpb, s->slot_bytes * s->slots);
+    ok = ok && cudaMalloc(&s->rflag, n * sizeof(uint32_t)) == cudaSuccess;
+    ok = ok && cudaMalloc(&s->dflag, n * sizeof(uint32_t)) == cudaSuccess;
+    ok = ok && cudaMalloc(&s->counter, 64) == cudaSuccess;
+    ok = ok && cudaMalloc(&s->error, 64) == cudaSuccess;
+    ok = ok && cudaMalloc(&s->tasks, tasks.size() * sizeof(uint32_t)) == cudaSuccess;
+    ok = ok && cudaMalloc(&s->ls, (2304 + 2304 * 4) * sizeof(int32_t)) == cudaSuccess;
+    for (int i = 0; i < 2 && ok; i++) ok = cudaEventCreateWithFlags(&s->staged[i], cudaEventDisableTiming) == cudaSuccess;
+    if (ok) {
+        ok = cudaMemsetAsync(s->dpb, 0, s->slot_bytes * s->slots, s->st) == cudaSuccess &&
+             cudaMemsetAsync(s->rflag, 0, n * sizeof(uint32_t), s->st) == cudaSuccess &&
+             cudaMemsetAsync(s->dflag, 0, n * sizeof(uint32_t), s->st) == cudaSuccess &&
+             cudaMemsetAsync(s->error, 0, 64, s->st) == cudaSuccess &&
+             cudaMemcpyAsync(s->tasks, tasks.data(), tasks.size() * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                             s->st) == cudaSuccess &&
+             cudaStreamSynchronize(s->st) == cudaSuccess;
+    }
+    if (!ok) {
+        int rc = (s->budget && s->held + s->slot_bytes * s->slots > s->budget) ? RC_ENOMEM : RC_ECUDA;
+        cudaGetLastError();
+        destroy(s);
+        return rc;
+    }
+    *out = s;
+    return RC_OK;
+}
+
+void rc_stream_destroy(rc_stream *s) { destroy(s); }
+
+int rc_h264_validate(int mb_w, int mb_h, int dpb_slots, const rc_h264_picture *pic) {
+    if (mb_w <= 0 || mb_h <= 0 || dpb_slots <= 0 || !pic) return RC_EINVAL;
+    Geo g{mb_w, mb_h, dpb_slots};
+    return validate_h264(&g, pic);
+}
+
+int rc_h264_submit(rc_stream *s, const rc_h264_picture *pic, int out_slot) {
+    if (!s || !pic || s->codec != RC_CODEC_H264) return RC_EINVAL;
+    if (out_slot < 0 || out_slot >= s->slots) return RC_EINVAL;
+    if (pic->mem != RC_MEM_HOST && pic->mem != RC_MEM_DEVICE) return RC_EINVAL;
+    const int n = s->mb_w * s->mb_h;
+    int rc;
+    // level-scale tables (per PPS), uploaded only when they change
+    {
+        std::vector<int32_t> ls(2304 + 2304 * 4);
+        h264_level_scale(pic->scaling4, pic->scaling8, ls.data(), ls.data() + 2304);
+        if (!s->ls_valid || ls != s->ls_host) {
+            if (cudaStreamSynchronize(s->st) != cudaSuccess) return cuda_fail(s);
+            if (cudaMemcpy(s->ls, ls.data(), ls.size() * sizeof(int32_t), cudaMemcpyHostToDevice) != cudaSuccess)
+                return cuda_fail(s);
+            s->ls_host.swap(ls);
+            s->ls_valid = true;
+        }
+    }
+    H264Launch L;
+    memset(&L, 0, sizeof L);
+    if (pic->mem == RC_MEM_HOST) {
+        Geo g{s->mb_w, s->mb_h, s->slots};
+        if ((rc = validate_h264(&g, pic)) != 0) return rc;
+        const size_t b_mbs = sizeof(rc_h264_mb) * n, b_sl = sizeof(rc_h264_slice) * pic->num_slices;
+        const size_t b_w = sizeof(rc_h264_weight) * pic->num_weights, b_lv = sizeof(int16_t) * pic->num_levels;
+        if ((rc = ensure(s, s->mbs, b_mbs)) || (rc = ensure(s, s->slices, b_sl)) ||
+            (rc = ensure(s, s->weights, std::max<size_t>(b_w, 64))) || (rc = ensure(s, s->levels, std::max<size_t>(b_lv, 64))))
+            return rc;
+        struct Part { void *dst; const void *src; size_t n; } parts[4] = {
+            {s->mbs.p, pic->mbs, b_mbs}, {s->slices.p, pic->slices, b_sl},
+            {s->weights.p, pic->weights, b_w}, {s->levels.p, pic->levels, b_lv}};
+        bool pinned = true;
+        for (auto &p : parts) pinned = pinned && is_pinned(p.src);
+        if (pinned) {
+            for (auto &p : parts)
+                if (p.n && cudaMemcpyAsync(p.dst, p.src, p.n, cudaMemcpyHostToDevice, s->st) != cudaSuccess)
+                    return cuda_fail(s);
+        } else {
+            const int i = s->submits & 1;
+            size_t total = 0;
+            for (auto &p : parts) total += align_up(p.n, 256);
+            if (cudaEventSynchronize(s->staged[i]) != cudaSuccess) return cuda_fail(s);
+            if (total > s->staging_cap[i]) {
+                if (s->staging[i]) cudaFreeHost(s->staging[i]);
+                s->staging[i] = nullptr;
+                s->staging_cap[i] = 0;
+                size_t want = align_up(total + total / 4, 1 << 20);
+                if (cudaMallocHost(&s->staging[i], want) != cudaSuccess) return RC_ENOMEM;
+                s->staging_cap[i] = want;
+            }
+            uint8_t *stage = (uint8_t *)s->staging[i];
+            size_t off = 0;
+            for (auto &p : parts) {
+                if (!p.n) continue;
+                memcpy(stage + off, p.src, p.n);
+                if (cudaMemcpyAsync(p.dst, stage + off, p.n, cudaMemcpyHostToDevice, s->st) != cudaSuccess)
+                    return cuda_fail(s);
+                off += align_up(p.n, 256);
+            }
+            if (cudaEventRecord(s->staged[i], s->st) != cudaSuccess) return cuda_fail(s);
+        }
+        L.mbs = (const rc_h264_mb *)s->mbs.p;
+        L.slices = (const rc_h264_slice *)s->slices.p;
+        L.weights = (const rc_h264_weight *)s->weights.p;
+        L.levels = (const int16_t *)s->levels.p;
+    } else {
+        if (!pic->mbs || !pic->slices || pic->num_slices <= 0) return RC_EINVAL;
+        L.mbs = pic->mbs;
+        L.slices = pic->slices;
+        L.weights = pic->weights;
+        L.levels = pic->levels;
+    }
+    L.num_levels = pic->num_levels;
+    L.num_slices = pic->num_slices;
+    L.num_weights = pic->num_weights;
+    L.ls4 = s->ls;
+    L.ls8 = s->ls + 2304;
+    L.dpb = s->dpb;
+    L.slot_bytes = s->slot_bytes;
+    L.u_off = s->u_off;
+    L.v_off = s->v_off;
+    L.dpb_slots = s->slots;
+    L.out_slot = out_slot;
+    L.mb_w = s->mb_w;
+    L.mb_h = s->mb_h;
+    L.W = s->width;
+    L.H = s->height;
+    L.CW = s->cw;
+    L.CH = s->ch;
+    L.pitch = s->pitch;
+    L.cpitch = s->cpitch;
+    L.constrained_intra = pic->constrained_intra_pred;
+    L.epoch = ++s->epoch;
+    L.rflag = s->rflag;
+    L.dflag = s->dflag;
+    L.counter = s->counter;
+    L.tasks = s->tasks;
+    L.ntasks = s->ntasks;
+    L.error = s->error;
+    L.wait_limit = s->wait_limit;
+    timed(s, RC_KERNEL_H264_MB, [&] { rc_launch_h264_mb(L, s->st); });
+    timed(s, RC_KERNEL_H264_WAVE, [&] { rc_launch_h264_wave(L, s->st, s->wave_blocks); });
+    s->submits++;
+    if (cudaGetLastError() != cudaSuccess) return cuda_fail(s);
+    return RC_OK;
+}
+
+int rc_stream_sync(rc_stream *s) {
+    if (!s) return RC_EINVAL;
+    if (cudaStreamSynchronize(s->st) != cudaSuccess) return cuda_fail(s);
+    uint32_t e = 0;
+    if (cudaMemcpy(&e, s->error, sizeof e, cudaMemcpyDeviceToHost) != cudaSuccess) return cuda_fail(s);
+    if (e) {
+        if (!s->sticky) s->sticky = (e & RC_DEV_ERR_TIMEOUT) ? RC_ETIMEOUT : RC_EDEVICE;
+        cudaMemset(s->error, 0, sizeof e);
+    }
+    return s->sticky;
+}
+
+int rc_stream_error(rc_stream *s) {
+    if (!s) return RC_EINVAL;
+    int e = rc_stream_sync(s);
+    s->sticky = 0;
+    return e;
+}
+
+static int download(rc_stream *s, int slot, int x, int y, int w, int h, void *out_y, void *out_u, void *out_v,
+                    bool wait) {
+    if (!s || slot < 0 || slot >= s->slots || !out_y || !out_u || !out_v) return RC_EINVAL;
+    // copy_cropped's bounds rule, src/h264/dec/picture.rs:601-615
+    int cx = x / 2, cy = y / 2, ccw = (w + 1) / 2, cch = (h + 1) / 2;
+    auto fits = [](long at, long n, long size) { return n > 0 && at >= 0 && at + n <= size; };
+    if (!(fits(x, w, s->width) && fits(y, h, s->height) && fits(cx, ccw, s->cw) && fits(cy, cch, s->ch)))
+        return RC_EINVAL;
+    const int bps = s->bit_depth > 8 ? 2 : 1;
+    const uint8_t *base = s->dpb + (size_t)slot * s->slot_bytes;
+    bool ok = cudaMemcpy2DAsync(out_y, (size_t)w * bps, base + (size_t)y * s->pitch + (size_t)x * bps, s->pitch,
+                                (size_t)w * bps, h, cudaMemcpyDeviceToHost, s->st) == cudaSuccess &&
+              cudaMemcpy2DAsync(out_u, (size_t)ccw * bps, base + s->u_off + (size_t)cy * s->cpitch + (size_t)cx * bps,
+                                s->cpitch, (size_t)ccw * bps, cch, cudaMemcpyDeviceToHost, s->st) == cudaSuccess &&
+              cudaMemcpy2DAsync(out_v, (size_t)ccw * bps, base + s->v_off + (size_t)cy * s->cpitch + (size_t)cx * bps,
+                                s->cpitch, (size_t)ccw * bps, cch, cudaMemcpyDeviceToHost, s->st) == cudaSuccess &&
+              (!wait || cudaStreamSynchronize(s->st) == cudaSuccess);
+    return ok ? RC_OK : cuda_fail(s);
+}
+
+int rc_picture_download(rc_stream *s, int slot, int x, int y, int w, int h, void *out_y, void *out_u, void *out_v) {
+    return download(s, slot, x, y, w, h, out_y, out_u, out_v, true);
+}
+
+int rc_picture_download_async(rc_stream *s, int slot, int x, int y, int w, int h, void *out_y, void *out_u,
+                              void *out_v) {
+    return download(s, slot, x, y, w, h, out_y, out_u, out_v, false);
+}
+
+int rc_stream_profile(rc_stream *s, int enable) {
+    if (!s) return RC_EINVAL;
+    if (cudaStreamSynchronize(s->st) != cudaSuccess) return cuda_fail(s);
+    drain_profile(s);
+    for (int k = 0; k < RC_KERNEL_COUNT; k++) {
+        s->prof_ms[k] = 0;
+        s->prof_n[k] = 0;
+    }
+    s->profiling = enable != 0;
+    return RC_OK;
+}
+
+int rc_stream_profile_read(rc_stream *s, double *ms, long long *launches, int max_kernels) {
+    if (!s || max_kernels < 0) return RC_EINVAL;
+    if (cudaStreamSynchronize(s->st) != cudaSuccess) return cuda_fail(s);
+    drain_profile(s);
+    int n = std::min(max_kernels, RC_KERNEL_COUNT);
+    for (int k = 0; k < n; k++) {
+        if (ms) ms[k] = s->prof_ms[k];
+        if (launches) launches[k] = s->prof_n[k];
+    }
+    return n;
+}
+
+int rc_picture_upload(rc_stream *s, int slot, const void *py, const void *pu, const void *pv) {
+    if (!s || slot < 0 || slot >= s->slots || !py || !pu || !pv) return RC_EINVAL;
+    const int bps = s->bit_depth > 8 ? 2 : 1;
+    uint8_t *base = s->dpb + (size_t)slot * s->slot_bytes;
+    bool ok = cudaStreamSynchronize(s->st) == cudaSuccess &&
+              cudaMemcpy2D(base, s->pitch, py, (size_t)s->width * bps, (size_t)s->width * bps, s->height,
+                           cudaMemcpyHostToDevice) == cudaSuccess &&
+              cudaMemcpy2D(base + s->u_off, s->cpitch, pu, (size_t)s->cw * bps, (size_t)s->cw * bps, s->ch,
+                           cudaMemcpyHostToDevice) == cudaSuccess &&
+              cudaMemcpy2D(base + s->v_off, s->cpitch, pv, (size_t)s->cw * bps, (size_t)s->cw * bps, s->ch,
+                           cudaMemcpyHostToDevice) == cudaSuccess;
+    return ok ? RC_OK : cuda_fail(s);
+}
+
+int rc_stream_geometry(rc_stream *s, int *coded_w, int *coded_h, int *luma_pitch, int *chroma_pitch) {
+    if (!s) return RC_EINVAL;
+    if (coded_w) *coded_w = s->width;
+    if (coded_h) *coded_h = s->height;
+    if (luma_pitch) *luma_pitch = s->pitch;
+    if (chroma_pitch) *chroma_pitch = s->cpitch;
+    return RC_OK;
+}
+
+int rc_picture_device_planes(rc_stream *s, int slot, void **y, void **u, void **v) {
+    if (!s || slot < 0 || slot >= s->slots) return RC_EINVAL;
+    uint8_t *base = s->dpb + (size_t)slot * s->slot_bytes;
+    if (y) *y = base;
+    if (u) *u = base + s->u_off;
+    if (v) *v = base + s->v_off;
+    return RC_OK;
+}
+
+long long rc_stream_launches(rc_stream *s) { return s ? s->launches : 0; }
+
+void *rc_stream_cuda_stream(rc_stream *s) { return s ? (void *)s->st : nullptr; }
+
+}  // extern "C"

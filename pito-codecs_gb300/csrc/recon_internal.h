@@ -1,0 +1,44 @@
+// recon_internal.h — launch parameters shared by the C ABI layer and the
+// CUDA kernels.  Not part of the public interface.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/pito_recon.h"
+
+// Device error word values (sticky per stream).
+#define RC_DEV_ERR_TIMEOUT 1u  // a wavefront wait exceeded its iteration cap
+#define RC_DEV_ERR_RECORD 2u   // a record pointed outside its buffers
+
+// Spin iterations a wavefront wait may take before it gives up (each
+// iteration backs off with __nanosleep, so the cap is about a second).
+#define RC_WAIT_LIMIT (1u << 22)
+
+struct H264Launch {
+    const rc_h264_mb *mbs;
+    const rc_h264_slice *slices;
+    const rc_h264_weight *weights;
+    const int16_t *levels;
+    const int32_t *ls4;  // [6][6][16]
+    const int32_t *ls8;  // [6][6][64]
+    unsigned long long num_levels;
+    int num_slices, num_weights;
+    // DPB: slot s luma at dpb + s * slot_bytes, chroma at + u_off / + v_off
+    uint8_t *dpb;
+    unsigned long long slot_bytes, u_off, v_off;
+    int dpb_slots, out_slot;
+    int mb_w, mb_h, W, H, CW, CH, pitch, cpitch;
+    int constrained_intra;
+    uint32_t epoch;
+    uint32_t *rflag, *dflag;  // per MB: epoch when reconstructed / deblocked
+    uint32_t *counter;        // task counter (zeroed before the wave launch)
+    const uint32_t *tasks;    // wave task list (bit 31 = deblock task)
+    int ntasks;
+    uint32_t *error;
+    uint32_t wait_limit;
+};
+
+// Launchers (h264_kernels.cu).
+void rc_launch_h264_mb(const H264Launch &p, cudaStream_t st);
+void rc_launch_h264_wave(const H264Launch &p, cudaStream_t st, int wave_blocks);
