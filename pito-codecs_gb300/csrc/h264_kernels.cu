@@ -79,12 +79,17 @@ __device__ __forceinline__ uint32_t ld_acquire(const uint32_t *p) {
 __device__ __forceinline__ void st_release(uint32_t *p, uint32_t v) {
     asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
-// Wait until *f == epoch; false after `limit` polls (the caller records a
-// timeout and abandons the launch instead of spinning for ever).
-__device__ bool wait_flag(const uint32_t *f, uint32_t epoch, uint32_t limit) {
+__device__ __forceinline__ bool aborted(const uint32_t *err) {
+    return (*(const volatile uint32_t *)err & RC_DEV_ERR_TIMEOUT) != 0;
+}
+// Wait until *f == epoch; false after `limit` polls or once another warp has
+// recorded a timeout (the caller then abandons the launch instead of
+// spinning for ever).
+__device__ bool wait_flag(const uint32_t *f, uint32_t epoch, uint32_t limit, const uint32_t *err) {
     uint32_t it = 0;
     while (ld_acquire(f) != epoch) {
         if (++it > limit) return false;
+        if ((it & 63) == 0 && aborted(err)) return false;
         __nanosleep(it < 32 ? 32 : 256);
     }
     return true;
@@ -260,7 +265,7 @@ __global__ void __launch_bounds__(256) h264_mb_kernel(H264Launch P) {
         for (int l = 0; l < 2; l++) {
             int ri = m.ref_idx[l][b8];
             if (ri < 0) continue;
-            int slot = ri < __ldg(&sl->num_ref[l]) ? __ldg(&sl->ref_slot[l][ri]) : -1;
+            int slot = ri < min(__ldg(&sl->num_ref[l]), RC_H264_MAX_REFS) ? __ldg(&sl->ref_slot[l][ri]) : -1;
             if (slot < 0 || slot >= P.dpb_slots) { set_error(P.error, RC_DEV_ERR_RECORD); continue; }
             u[l] = true;
             Ref r{P.dpb + (size_t)slot * P.slot_bytes, P.pitch, P.W, P.H};
@@ -281,7 +286,7 @@ __global__ void __launch_bounds__(256) h264_mb_kernel(H264Launch P) {
         for (int l = 0; l < 2; l++) {
             int ri = m.ref_idx[l][b8];
             if (ri < 0) continue;
-            int slot = ri < __ldg(&sl->num_ref[l]) ? __ldg(&sl->ref_slot[l][ri]) : -1;
+            int slot = ri < min(__ldg(&sl->num_ref[l]), RC_H264_MAX_REFS) ? __ldg(&sl->ref_slot[l][ri]) : -1;
             if (slot < 0 || slot >= P.dpb_slots) continue;
             u[l] = true;
             Ref r{P.dpb + (size_t)slot * P.slot_bytes + (c ? P.v_off : P.u_off), P.cpitch, P.CW, P.CH};
@@ -766,7 +771,7 @@ __device__ __forceinline__ uint32_t ref_id(const H264Launch &P, const rc_h264_mb
     if (r < 0) return ID_NONE;
     if (m.slice >= P.num_slices) return ID_NONE - 1;
     const rc_h264_slice *sl = P.slices + m.slice;
-    return r < __ldg(&sl->num_ref[l]) ? __ldg(&sl->ref_id[l][r]) : ID_NONE - 1;
+    return r < min(__ldg(&sl->num_ref[l]), RC_H264_MAX_REFS) ? __ldg(&sl->ref_id[l][r]) : ID_NONE - 1;
 }
 __device__ __forceinline__ bool near_mv(int ax, int ay, int bx, int by) {
     return (uint32_t)(ax - bx + 3) < 7u && (uint32_t)(ay - by + 3) < 7u;
@@ -979,7 +984,7 @@ __global__ void __launch_bounds__(128) h264_wave_kernel(H264Launch P) {
     uint8_t *U = Y + P.u_off, *V = Y + P.v_off;
     for (;;) {
         unsigned ti = 0;
-        if (lane == 0) ti = atomicAdd(P.counter, 1u);
+        if (lane == 0) ti = aborted(P.error) ? 0xffffffffu : atomicAdd(P.counter, 1u);
         ti = __shfl_sync(0xffffffffu, ti, 0);
         if (ti >= (unsigned)P.ntasks) return;
         const uint32_t task = __ldg(P.tasks + ti);
@@ -996,7 +1001,7 @@ __global__ void __launch_bounds__(128) h264_wave_kernel(H264Launch P) {
                 int nx = mbx + dx[lane], ny = mby + dy[lane];
                 if (nx >= 0 && ny >= 0 && nx < P.mb_w) {
                     int na = ny * P.mb_w + nx;
-                    if (wave_intra(__ldg(&P.mbs[na].kind))) ok = wait_flag(P.rflag + na, P.epoch, P.wait_limit);
+                    if (wave_intra(__ldg(&P.mbs[na].kind))) ok = wait_flag(P.rflag + na, P.epoch, P.wait_limit, P.error);
                 }
             }
             if (!__all_sync(0xffffffffu, ok)) {
@@ -1039,9 +1044,9 @@ __global__ void __launch_bounds__(128) h264_wave_kernel(H264Launch P) {
                 if (nx >= 0 && ny >= 0 && nx < P.mb_w && ny < P.mb_h) {
                     int na = ny * P.mb_w + nx;
                     if (lane < 6) {
-                        if (wave_intra(__ldg(&P.mbs[na].kind))) ok = wait_flag(P.rflag + na, P.epoch, P.wait_limit);
+                        if (wave_intra(__ldg(&P.mbs[na].kind))) ok = wait_flag(P.rflag + na, P.epoch, P.wait_limit, P.error);
                     } else {
-                        ok = wait_flag(P.dflag + na, P.epoch, P.wait_limit);
+                        ok = wait_flag(P.dflag + na, P.epoch, P.wait_limit, P.error);
                     }
                 }
             }
