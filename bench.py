@@ -86,9 +86,16 @@ def picture_stats(E, p):
     mbk = inter | (kind == E.RC_H264_IPCM)
     out_frame = MB_W * 16 * MB_H * 16 * 3 // 2
     syn = p.nbytes
-    mb_kernel = int(mbk.sum() * (384 + 176) + lv_bytes[mbk].sum() + ref_bytes)
-    wave_kernel = int(wave_intra.sum() * 384 + len(kind) * 176 + lv_bytes[wave_intra].sum() + 2 * out_frame)
-    return {"mb": mb_kernel, "wave": wave_kernel, "job": out_frame + ref_bytes + syn, "syntax": syn}
+    n = len(kind)
+    # h264_mb_kernel: every record once (loop-filter parameters for all MBs:
+    # 48 B written each), plus inter/PCM samples out, their levels and refs
+    mb_kernel = int(n * (176 + 48) + mbk.sum() * 384 + lv_bytes[mbk].sum() + ref_bytes)
+    # h264_intra_kernel: intra MBs' records, levels and samples out
+    intra_kernel = int(wave_intra.sum() * (176 + 384) + lv_bytes[wave_intra].sum())
+    # h264_deblock_kernel: the picture read and written once + parameters
+    deblock_kernel = int(2 * out_frame + n * 48)
+    return {"mb": mb_kernel, "intra": intra_kernel, "deblock": deblock_kernel, "job": out_frame + ref_bytes + syn,
+            "syntax": syn}
 
 
 class ClockSampler:
@@ -359,7 +366,7 @@ def main():
     e2e = frames * args.steps * world / e2e_s
 
     # ---- roofline of the dominant kernel
-    names = {0: ("h264_mb_kernel", "mb"), 1: ("h264_wave_kernel", "wave")}
+    names = {0: ("h264_mb_kernel", "mb"), 1: ("h264_intra_kernel", "intra"), 2: ("h264_deblock_kernel", "deblock")}
     per_kernel = {}
     for k, (ms, n) in prof.items():
         name, key = names[k]

@@ -221,7 +221,8 @@ int rc_picture_device_planes(rc_stream *s, int slot, void **y, void **u,
  * (RC_KERNEL_*) the accumulated milliseconds and launch counts since
  * profiling was enabled; returns the number of kernel ids filled. */
 #define RC_KERNEL_H264_MB 0
-#define RC_KERNEL_H264_WAVE 1
+#define RC_KERNEL_H264_INTRA 1
+#define RC_KERNEL_H264_DEBLOCK 2
 #define RC_KERNEL_COUNT 8
 int rc_stream_profile(rc_stream *s, int enable);
 int rc_stream_profile_read(rc_stream *s, double *ms, long long *launches,

@@ -1,27 +1,27 @@
 // h264_kernels.cu — H.264 block reconstruction on sm_103a.
 //
-// Two kernels per picture:
+// Three launches per picture:
 //
-//  h264_mb_kernel    one CTA (256 threads) per macroblock, all in parallel.
-//                    Inter MBs: dequantisation (scale4/scale8, chroma DC
-//                    Hadamard), 4x4/8x8 inverse transforms, 6-tap luma and
-//                    bilinear chroma motion compensation with edge extension
-//                    by coordinate clamp, default / explicit weighted
-//                    prediction, residual add and clip, all fused.  I_PCM
-//                    MBs are copied.  Intra MBs are left to the wavefront.
-//
-//  h264_wave_kernel  persistent; one warp per task.  The task list holds an
-//                    intra-reconstruction task R(x,y) and a deblocking task
-//                    D(x,y) per MB, ordered by anti-diagonal key (R at
-//                    2(x+2y), D at 2(x+2y+4)+1) so every task's inputs come
-//                    from earlier tasks.  Warps take tasks in list order from
-//                    an atomic counter and wait on per-MB flags (acquire
-//                    loads, capped spin) for exactly the MBs they read:
-//                      R(x,y): intra neighbours L, T, TR, TL
-//                      D(x,y): intra R of (x-1..x+1, y..y+1), D of L, T, TR
-//                    This keeps the reference's order: every intra MB sees
-//                    unfiltered neighbours, and the loop filter runs in MB
-//                    raster semantics (src/h264/dec/slicedec.rs:184-208).
+//  h264_mb_kernel       one CTA (256 threads) per macroblock, all in parallel.
+//                       Inter MBs: dequantisation (scale4/scale8, chroma DC
+//                       Hadamard), 4x4/8x8 inverse transforms, 6-tap luma and
+//                       bilinear chroma motion compensation with edge
+//                       extension by coordinate clamp, default / explicit
+//                       weighted prediction, residual add and clip, fused.
+//                       I_PCM MBs are copied.  Every MB also gets its
+//                       loop-filter parameters (boundary strengths, QPs),
+//                       which depend on syntax only.
+//  h264_intra_kernel    persistent; one warp per intra MB in anti-diagonal
+//                       order (key x + 2y); a warp waits (acquire loads,
+//                       capped spin) for its intra neighbours L, T, TR, TL,
+//                       then predicts and adds the residual block by block
+//                       in decode order on a shared-memory canvas.
+//  h264_deblock_kernel  one warp per MB row, walking the row left to right
+//                       on a shared-memory tile (the reference's MB-raster
+//                       filter order, src/h264/dec/slicedec.rs:184-208): row
+//                       y filters MB x once row y-1 has published MBs 0..x,
+//                       so every edge sees exactly the samples it would in
+//                       raster order.
 //
 // Arithmetic follows src/h264/dec/{transform,intra,inter,deblock}.rs and the
 // reconstruction half of slicedec.rs; citations at each function.
@@ -218,6 +218,9 @@ __device__ __forceinline__ int weigh(int a, int b, bool u0, bool u1, bool ex, in
 
 __device__ __forceinline__ void set_error(uint32_t *e, uint32_t code) { atomicOr(e, code); }
 
+__device__ void compute_db(const H264Launch &P, const rc_h264_mb &q, const rc_h264_mb &left, const rc_h264_mb &top,
+                           int addr, int lane, DbMb *out);
+
 // ===========================================================================
 // Kernel 1: inter MBs (prediction + residual) and I_PCM, one CTA per MB.
 // ===========================================================================
@@ -227,16 +230,24 @@ __global__ void __launch_bounds__(256) h264_mb_kernel(H264Launch P) {
     __shared__ int32_t coefc[128];
     __shared__ uint8_t predy[256];
     __shared__ uint8_t predc[128];
+    __shared__ __align__(16) rc_h264_mb nbr[2];  // left, top (loop-filter parameters)
     __shared__ uint32_t nzl, nzc;
     const int t = threadIdx.x, addr = blockIdx.x;
-    if (t < (int)(sizeof(rc_h264_mb) / 4)) ((uint32_t *)&m)[t] = __ldg((const uint32_t *)(P.mbs + addr) + t);
+    const int mbx = addr % P.mb_w, mby = addr / P.mb_w;
+    constexpr int RW = (int)(sizeof(rc_h264_mb) / 4);
+    if (t < RW) ((uint32_t *)&m)[t] = __ldg((const uint32_t *)(P.mbs + addr) + t);
+    else if (t < 2 * RW) {
+        if (mbx > 0) ((uint32_t *)&nbr[0])[t - RW] = __ldg((const uint32_t *)(P.mbs + addr - 1) + t - RW);
+    } else if (t < 3 * RW) {
+        if (mby > 0) ((uint32_t *)&nbr[1])[t - 2 * RW] = __ldg((const uint32_t *)(P.mbs + addr - P.mb_w) + t - 2 * RW);
+    }
     if (t == 0) { nzl = 0; nzc = 0; }
     coef[t] = 0;
     if (t < 128) coefc[t] = 0;
     __syncthreads();
+    if (t < 32) compute_db(P, m, nbr[0], nbr[1], addr, t, P.db + addr);
     const int kind = m.kind;
     if (kind != RC_H264_INTER && kind != RC_H264_IPCM) return;
-    const int mbx = addr % P.mb_w, mby = addr / P.mb_w;
     uint8_t *Y = P.dpb + (size_t)P.out_slot * P.slot_bytes;
     uint8_t *U = Y + P.u_off, *V = Y + P.v_off;
     if (kind == RC_H264_IPCM) {  // write_pcm, src/h264/dec/slicedec.rs:1404-1424
@@ -383,7 +394,6 @@ __global__ void __launch_bounds__(256) h264_mb_kernel(H264Launch P) {
 // ===========================================================================
 struct __align__(16) WarpSmem {
     rc_h264_mb q;        // the task's MB
-    rc_h264_mb nb[2];    // left, top (deblocking)
     int32_t coef[256];
     int32_t coefc[128];
     uint8_t cy[17 * 32];  // luma canvas: rows -1..15, cols -1..30 -> [(r+1)*32 + c+1]
@@ -789,6 +799,67 @@ __device__ int motion_bs(const H264Launch &P, const rc_h264_mb &p, int rp, const
     return !(same || cross);
 }
 
+// Loop-filter parameters of one MB (the boundary-strength and QP part of
+// deblock_mb, deblock.rs:301-403); one warp, lane = dir*16 + edge*4 + segment.
+__device__ void compute_db(const H264Launch &P, const rc_h264_mb &q, const rc_h264_mb &left, const rc_h264_mb &top,
+                           int addr, int lane, DbMb *out) {
+    const int mx = addr % P.mb_w, my = addr / P.mb_w;
+    int bs = 0;
+    bool filt = q.kind != RC_H264_NONE && q.slice < P.num_slices;
+    int idc = 1, aoff = 0, boff = 0;
+    if (filt) {
+        const rc_h264_slice *sq = P.slices + q.slice;
+        idc = __ldg(&sq->disable_deblocking_filter_idc);
+        aoff = __ldg(&sq->alpha_offset);
+        boff = __ldg(&sq->beta_offset);
+        filt = idc != 1;
+    }
+    bool usable[2];
+    usable[0] = mx > 0 && left.kind != RC_H264_NONE && !(idc == 2 && left.slice != q.slice);
+    usable[1] = my > 0 && top.kind != RC_H264_NONE && !(idc == 2 && top.slice != q.slice);
+    if (filt) {
+        const bool t8 = q.transform_8x8;
+        const int dir = lane >> 4, e = (lane >> 2) & 3, k = lane & 3;
+        const rc_h264_mb &p = dir == 0 ? left : top;
+        if (is_intra(q.kind)) {
+            bs = e == 0 ? (usable[dir] ? 4 : 0) : ((t8 && (e & 1)) ? 0 : 3);
+        } else {
+            const int r = dir == 0 ? k * 4 + e : e * 4 + k;
+            const bool first = e == 0;
+            if (first && usable[dir] && is_intra(p.kind)) bs = 4;
+            else if (first && !usable[dir]) bs = 0;
+            else if (t8 && (e & 1)) bs = 0;
+            else {
+                const int nzq = q.nz_mask;
+                int nz;
+                if (dir == 0) nz = (nzq >> r & 1) | (e > 0 ? (nzq >> (r - 1) & 1) : (p.nz_mask >> (r + 3) & 1));
+                else nz = (nzq >> r & 1) | (e > 0 ? (nzq >> (r - 4) & 1) : (p.nz_mask >> (r + 12) & 1));
+                if (nz) bs = 2;
+                else {
+                    int rp = dir == 0 ? (first ? r + 3 : r - 1) : (first ? r + 12 : r - 4);
+                    bs = first ? motion_bs(P, p, rp, q, r) : motion_bs(P, q, rp, q, r);
+                }
+            }
+        }
+    }
+    const bool any = __ballot_sync(0xffffffffu, bs != 0) != 0;
+    out->bs[lane] = (uint8_t)bs;
+    if (lane == 0) {
+        const int qq = q.kind == RC_H264_IPCM ? 0 : q.qp;
+        out->qp[0] = (uint8_t)qq;
+        out->qp[1] = (uint8_t)(usable[0] ? (left.kind == RC_H264_IPCM ? 0 : left.qp) : qq);
+        out->qp[2] = (uint8_t)(usable[1] ? (top.kind == RC_H264_IPCM ? 0 : top.qp) : qq);
+        for (int c = 0; c < 2; c++) {
+            out->qpc[0][c] = q.qpc[c];
+            out->qpc[1][c] = usable[0] ? left.qpc[c] : q.qpc[c];
+            out->qpc[2][c] = usable[1] ? top.qpc[c] : q.qpc[c];
+        }
+        out->flags = (filt && any) ? 1 : 0;
+        out->aoff = (int8_t)aoff;
+        out->boff = (int8_t)boff;
+    }
+}
+
 // filter_lanes, deblock.rs:146-229, for one line of 8 samples s[0..7] = p3..q3
 __device__ __forceinline__ void filt_luma(int *s, int bsv, bool strong_edge, int alpha, int beta, int tc0) {
     int p3 = s[0], p2 = s[1], p1 = s[2], p0 = s[3], q0 = s[4], q1 = s[5], q2 = s[6], q3 = s[7];
@@ -834,140 +905,13 @@ __device__ __forceinline__ void filt_chroma(int *s, int bsv, bool strong_edge, i
 }
 
 // edge parameters (params closure of deblock_mb, deblock.rs:386-403)
-__device__ __forceinline__ void edge_consts(int qpp, int qpq, int bsv, int aoff, int boff, int &alpha, int &beta, int &tc0) {
+__device__ __forceinline__ void edge_consts(int qpp, int qpq, int bsv, int aoff, int boff, int &alpha, int &beta,
+                                            int &tc0) {
     int qpav = (qpp + qpq + 1) >> 1;
     int ia = clampi(qpav + aoff, 0, 51), ib = clampi(qpav + boff, 0, 51);
     alpha = cALPHA[ia];
     beta = cBETA[ib];
     tc0 = (bsv >= 1 && bsv < 4) ? cTC0[ia][bsv - 1] : 0;
-}
-
-// deblock_mb, deblock.rs:301-495, one warp
-__device__ void deblock_mb(WarpSmem &S, const H264Launch &P, int lane, int addr, uint8_t *Y, uint8_t *U, uint8_t *V) {
-    const rc_h264_mb &q = S.q;
-    if (q.kind == RC_H264_NONE || q.slice >= P.num_slices) return;
-    const rc_h264_slice *sq = P.slices + q.slice;
-    const int idc = __ldg(&sq->disable_deblocking_filter_idc);
-    if (idc == 1) return;
-    const int aoff = __ldg(&sq->alpha_offset), boff = __ldg(&sq->beta_offset);
-    const int mx = addr % P.mb_w, my = addr / P.mb_w;
-    bool usable[2];
-    usable[0] = mx > 0 && S.nb[0].kind != RC_H264_NONE && !(idc == 2 && S.nb[0].slice != q.slice);
-    usable[1] = my > 0 && S.nb[1].kind != RC_H264_NONE && !(idc == 2 && S.nb[1].slice != q.slice);
-    const bool t8 = q.transform_8x8;
-    // ---- boundary strength: lane = dir*16 + e*4 + k
-    int bs;
-    {
-        const int dir = lane >> 4, e = (lane >> 2) & 3, k = lane & 3;
-        if (is_intra(q.kind)) {
-            bs = e == 0 ? (usable[dir] ? 4 : 0) : ((t8 && (e & 1)) ? 0 : 3);
-        } else {
-            const int r = dir == 0 ? k * 4 + e : e * 4 + k;
-            const bool first = e == 0;
-            const rc_h264_mb &p = S.nb[dir];
-            if (first && usable[dir] && is_intra(p.kind)) bs = 4;
-            else if (first && !usable[dir]) bs = 0;
-            else if (t8 && (e & 1)) bs = 0;
-            else {
-                const int nzq = q.nz_mask;
-                int nz;
-                if (dir == 0) nz = (nzq >> r & 1) | (e > 0 ? (nzq >> (r - 1) & 1) : (p.nz_mask >> (r + 3) & 1));
-                else nz = (nzq >> r & 1) | (e > 0 ? (nzq >> (r - 4) & 1) : (p.nz_mask >> (r + 12) & 1));
-                if (nz) bs = 2;
-                else {
-                    int rp = dir == 0 ? (first ? r + 3 : r - 1) : (first ? r + 12 : r - 4);
-                    bs = first ? motion_bs(P, p, rp, q, r) : motion_bs(P, q, rp, q, r);
-                }
-            }
-        }
-    }
-    if (__ballot_sync(0xffffffffu, bs != 0) == 0) return;
-    const int qqp = q.kind == RC_H264_IPCM ? 0 : q.qp;
-    const int x0 = mx * 16, y0 = my * 16, cx0 = mx * 8, cy0 = my * 8;
-    const bool luma = lane < 16;
-    const int c = (lane - 16) >> 3;  // chroma component for lanes 16..31
-    const int li = luma ? lane : (lane - 16) & 7;
-    // qp of the neighbour across edge 0 for this lane's plane
-    int qpn[2], qpq;
-    if (luma) {
-        qpq = qqp;
-        for (int d = 0; d < 2; d++)
-            qpn[d] = usable[d] ? (S.nb[d].kind == RC_H264_IPCM ? 0 : S.nb[d].qp) : qqp;
-    } else {
-        qpq = q.qpc[c];
-        for (int d = 0; d < 2; d++) qpn[d] = usable[d] ? S.nb[d].qpc[c] : qpq;
-    }
-    uint8_t *plane = luma ? Y : (c ? V : U);
-    const int pitch = luma ? P.pitch : P.cpitch;
-    // ---- vertical edges: each lane filters one row
-    {
-        const int row = (luma ? y0 : cy0) + li;
-        const int xb = (luma ? x0 : cx0) - 4;
-        int s[20];
-        const int nw = luma ? 5 : 3;
-        uint8_t *base = plane + (size_t)row * pitch + xb;
-#pragma unroll
-        for (int w = 0; w < 5; w++) {
-            uint32_t v = 0;
-            if (w < nw && (xb >= 0 || w > 0)) v = __ldcg((const unsigned int *)(base + 4 * w));
-            s[4 * w] = v & 255; s[4 * w + 1] = (v >> 8) & 255; s[4 * w + 2] = (v >> 16) & 255; s[4 * w + 3] = v >> 24;
-        }
-        const int k = luma ? li >> 2 : li >> 1;
-#pragma unroll
-        for (int e = 0; e < 4; e++) {
-            int bsv = __shfl_sync(0xffffffffu, bs, (e << 2) | k);
-            int strong = __shfl_sync(0xffffffffu, bs, e << 2) >= 4;
-            int alpha, beta, tc0;
-            if (luma) {
-                edge_consts(e == 0 ? qpn[0] : qpq, qpq, bsv, aoff, boff, alpha, beta, tc0);
-                filt_luma(s + 4 * e, bsv, strong, alpha, beta, tc0);
-            } else if ((e & 1) == 0) {
-                edge_consts(e == 0 ? qpn[0] : qpq, qpq, bsv, aoff, boff, alpha, beta, tc0);
-                filt_chroma(s + 2 * e, bsv, strong, alpha, beta, tc0);
-            }
-        }
-#pragma unroll
-        for (int w = 0; w < 5; w++) {
-            if (w < nw && (xb >= 0 || w > 0)) {
-                uint32_t v = s[4 * w] | s[4 * w + 1] << 8 | s[4 * w + 2] << 16 | (uint32_t)s[4 * w + 3] << 24;
-                *(uint32_t *)(base + 4 * w) = v;
-            }
-        }
-    }
-    __syncwarp();
-    // ---- horizontal edges: each lane filters one column
-    {
-        const int col = (luma ? x0 : cx0) + li;
-        const int yb = (luma ? y0 : cy0) - 4;
-        const int nr = luma ? 20 : 12;
-        int s[20];
-#pragma unroll
-        for (int i = 0; i < 20; i++) s[i] = (i < nr && (yb + i) >= 0) ? __ldcg(plane + (size_t)(yb + i) * pitch + col) : 0;
-        const int k = luma ? li >> 2 : li >> 1;
-#pragma unroll
-        for (int e = 0; e < 4; e++) {
-            int bsv = __shfl_sync(0xffffffffu, bs, 16 | (e << 2) | k);
-            int strong = __shfl_sync(0xffffffffu, bs, 16 | (e << 2)) >= 4;
-            int alpha, beta, tc0;
-            if (luma) {
-                edge_consts(e == 0 ? qpn[1] : qpq, qpq, bsv, aoff, boff, alpha, beta, tc0);
-                filt_luma(s + 4 * e, bsv, strong, alpha, beta, tc0);
-            } else if ((e & 1) == 0) {
-                edge_consts(e == 0 ? qpn[1] : qpq, qpq, bsv, aoff, boff, alpha, beta, tc0);
-                filt_chroma(s + 2 * e, bsv, strong, alpha, beta, tc0);
-            }
-        }
-        if (luma) {
-#pragma unroll
-            for (int i = 1; i < 19; i++)
-                if (yb + i >= 0) plane[(size_t)(yb + i) * pitch + col] = (uint8_t)s[i];
-        } else {
-            if (yb + 3 >= 0) { plane[(size_t)(yb + 3) * pitch + col] = (uint8_t)s[3]; }
-            plane[(size_t)(yb + 4) * pitch + col] = (uint8_t)s[4];
-            plane[(size_t)(yb + 7) * pitch + col] = (uint8_t)s[7];
-            plane[(size_t)(yb + 8) * pitch + col] = (uint8_t)s[8];
-        }
-    }
 }
 
 __device__ __forceinline__ void load_record(rc_h264_mb &dst, const rc_h264_mb *src, int lane) {
@@ -976,7 +920,10 @@ __device__ __forceinline__ void load_record(rc_h264_mb &dst, const rc_h264_mb *s
     for (int i = lane; i < (int)(sizeof(rc_h264_mb) / 4); i += 32) d[i] = __ldg(s + i);
 }
 
-__global__ void __launch_bounds__(128) h264_wave_kernel(H264Launch P) {
+// ===========================================================================
+// Kernel 2: intra MBs in anti-diagonal order, one warp per MB.
+// ===========================================================================
+__global__ void __launch_bounds__(128) h264_intra_kernel(H264Launch P) {
     __shared__ WarpSmem sm[4];
     WarpSmem &S = sm[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31;
@@ -987,82 +934,229 @@ __global__ void __launch_bounds__(128) h264_wave_kernel(H264Launch P) {
         if (lane == 0) ti = aborted(P.error) ? 0xffffffffu : atomicAdd(P.counter, 1u);
         ti = __shfl_sync(0xffffffffu, ti, 0);
         if (ti >= (unsigned)P.ntasks) return;
-        const uint32_t task = __ldg(P.tasks + ti);
-        const int addr = task & 0x7fffffffu;
+        const int addr = __ldg(P.tasks + ti) & 0x7fffffffu;
+        const int kind = __ldg(&P.mbs[addr].kind);
+        if (!wave_intra(kind)) continue;
         const int mbx = addr % P.mb_w, mby = addr / P.mb_w;
-        if (!(task >> 31)) {
-            // ---- R(x,y): intra reconstruction
-            const int kind = __ldg(&P.mbs[addr].kind);
-            if (!wave_intra(kind)) continue;
-            // wait for intra neighbours (inter / PCM ones were written by the MB kernel)
-            bool ok = true;
-            if (lane < 4) {
-                const int dx[4] = {-1, 0, 1, -1}, dy[4] = {0, -1, -1, -1};
-                int nx = mbx + dx[lane], ny = mby + dy[lane];
-                if (nx >= 0 && ny >= 0 && nx < P.mb_w) {
-                    int na = ny * P.mb_w + nx;
-                    if (wave_intra(__ldg(&P.mbs[na].kind))) ok = wait_flag(P.rflag + na, P.epoch, P.wait_limit, P.error);
-                }
+        // wait for intra neighbours (inter / PCM ones were written by the MB kernel)
+        bool ok = true;
+        if (lane < 4) {
+            const int dx = lane == 0 ? -1 : lane == 2 ? 1 : lane == 3 ? -1 : 0, dy = lane == 0 ? 0 : -1;
+            int nx = mbx + dx, ny = mby + dy;
+            if (nx >= 0 && ny >= 0 && nx < P.mb_w) {
+                int na = ny * P.mb_w + nx;
+                if (wave_intra(__ldg(&P.mbs[na].kind))) ok = wait_flag(P.rflag + na, P.epoch, P.wait_limit, P.error);
             }
-            if (!__all_sync(0xffffffffu, ok)) {
-                if (lane == 0) set_error(P.error, RC_DEV_ERR_TIMEOUT);
-                return;
-            }
-            load_record(S.q, P.mbs + addr, lane);
-            __syncwarp();
-            // start_mb neighbour availability + intra_nb, slicedec.rs:489-508, 525-530
-            bool nb[4];
-            {
-                const int dx[4] = {-1, 0, 1, -1}, dy[4] = {0, -1, -1, -1};
-#pragma unroll
-                for (int n = 0; n < 4; n++) {
-                    int nx = mbx + dx[n], ny = mby + dy[n];
-                    bool a = false;
-                    if (nx >= 0 && ny >= 0 && nx < P.mb_w) {
-                        const rc_h264_mb *pm = P.mbs + ny * P.mb_w + nx;
-                        int k = __ldg(&pm->kind);
-                        a = k != RC_H264_NONE && __ldg(&pm->slice) == S.q.slice && (!P.constrained_intra || is_intra(k));
-                    }
-                    nb[n] = a;
-                }
-            }
-            if (!warp_levels(S, P, lane)) {
-                if (lane == 0) set_error(P.error, RC_DEV_ERR_RECORD);
-            } else {
-                intra_mb(S, P, lane, mbx, mby, nb, Y, U, V);
-            }
-            __threadfence();
-            __syncwarp();
-            if (lane == 0) st_release(P.rflag + addr, P.epoch);
-        } else {
-            // ---- D(x,y): deblocking
-            bool ok = true;
-            if (lane < 9) {
-                // lanes 0..5: intra reconstruction of (x-1..x+1, y..y+1); 6..8: deblocking of L, T, TR
-                const int dx[9] = {-1, 0, 1, -1, 0, 1, -1, 0, 1}, dy[9] = {0, 0, 0, 1, 1, 1, 0, -1, -1};
-                int nx = mbx + dx[lane], ny = mby + dy[lane];
-                if (nx >= 0 && ny >= 0 && nx < P.mb_w && ny < P.mb_h) {
-                    int na = ny * P.mb_w + nx;
-                    if (lane < 6) {
-                        if (wave_intra(__ldg(&P.mbs[na].kind))) ok = wait_flag(P.rflag + na, P.epoch, P.wait_limit, P.error);
-                    } else {
-                        ok = wait_flag(P.dflag + na, P.epoch, P.wait_limit, P.error);
-                    }
-                }
-            }
-            if (!__all_sync(0xffffffffu, ok)) {
-                if (lane == 0) set_error(P.error, RC_DEV_ERR_TIMEOUT);
-                return;
-            }
-            load_record(S.q, P.mbs + addr, lane);
-            if (mbx > 0) load_record(S.nb[0], P.mbs + addr - 1, lane);
-            if (mby > 0) load_record(S.nb[1], P.mbs + addr - P.mb_w, lane);
-            __syncwarp();
-            deblock_mb(S, P, lane, addr, Y, U, V);
-            __threadfence();
-            __syncwarp();
-            if (lane == 0) st_release(P.dflag + addr, P.epoch);
         }
+        if (!__all_sync(0xffffffffu, ok)) {
+            if (lane == 0) set_error(P.error, RC_DEV_ERR_TIMEOUT);
+            return;
+        }
+        load_record(S.q, P.mbs + addr, lane);
+        __syncwarp();
+        // start_mb neighbour availability + intra_nb, slicedec.rs:489-508, 525-530
+        bool nb[4];
+#pragma unroll
+        for (int n = 0; n < 4; n++) {
+            const int dx = n == 0 ? -1 : n == 2 ? 1 : n == 3 ? -1 : 0, dy = n == 0 ? 0 : -1;
+            int nx = mbx + dx, ny = mby + dy;
+            bool a = false;
+            if (nx >= 0 && ny >= 0 && nx < P.mb_w) {
+                const rc_h264_mb *pm = P.mbs + ny * P.mb_w + nx;
+                int k = __ldg(&pm->kind);
+                a = k != RC_H264_NONE && __ldg(&pm->slice) == S.q.slice && (!P.constrained_intra || is_intra(k));
+            }
+            nb[n] = a;
+        }
+        if (!warp_levels(S, P, lane)) {
+            if (lane == 0) set_error(P.error, RC_DEV_ERR_RECORD);
+        } else {
+            intra_mb(S, P, lane, mbx, mby, nb, Y, U, V);
+        }
+        __threadfence();
+        __syncwarp();
+        if (lane == 0) st_release(P.rflag + addr, P.epoch);
+    }
+}
+
+// ===========================================================================
+// Kernel 3: loop filter, one warp per MB row walking left to right.
+// ===========================================================================
+// Tile of the current MB: luma rows -4..15 x cols -4..15, chroma rows -4..7 x
+// cols -4..7 per component.  Columns -4..-1 hold the left MB's columns after
+// its own filtering; rows -4..-1 the MB above, read once row y-1 has
+// published it.
+struct __align__(16) RowTile {
+    uint8_t y[20][20];
+    uint8_t c[2][12][12];
+    DbMb db;
+};
+
+__device__ __forceinline__ uint32_t pack4(const int *v) {
+    return (uint32_t)v[0] | (uint32_t)v[1] << 8 | (uint32_t)v[2] << 16 | (uint32_t)v[3] << 24;
+}
+
+__global__ void __launch_bounds__(32) h264_deblock_kernel(H264Launch P) {
+    __shared__ RowTile T;
+    const int lane = threadIdx.x, my = blockIdx.x;
+    uint8_t *Y = P.dpb + (size_t)P.out_slot * P.slot_bytes;
+    uint8_t *U = Y + P.u_off, *V = Y + P.v_off;
+    const uint32_t tag = (P.epoch & 0xffffu) << 16;
+    const bool luma = lane < 16;
+    const int cc = (lane - 16) >> 3, li = luma ? lane : (lane - 16) & 7;
+    // prefetched (pre-deblock) samples of the next MB: one row per lane
+    uint4 pre_y = make_uint4(0, 0, 0, 0);
+    uint2 pre_c = make_uint2(0, 0);
+    uint32_t pre_db = 0;
+    auto prefetch = [&](int x) {
+        if (luma) pre_y = __ldcg((const uint4 *)(Y + (size_t)(my * 16 + lane) * P.pitch + x * 16));
+        else pre_c = __ldcg((const uint2 *)((cc ? V : U) + (size_t)(my * 8 + li) * P.cpitch + x * 8));
+        if (lane < 12) pre_db = __ldcg((const uint32_t *)(P.db + (size_t)my * P.mb_w + x) + lane);
+    };
+    prefetch(0);
+    for (int x = 0; x < P.mb_w; x++) {
+        // ---- stage the MB (rows 0..15 / 0..7, columns 0..15 / 0..7)
+        if (luma) {
+            uint32_t w[4] = {pre_y.x, pre_y.y, pre_y.z, pre_y.w};
+#pragma unroll
+            for (int i = 0; i < 4; i++) *(uint32_t *)&T.y[lane + 4][4 + 4 * i] = w[i];
+        } else {
+            *(uint32_t *)&T.c[cc][li + 4][4] = pre_c.x;
+            *(uint32_t *)&T.c[cc][li + 4][8] = pre_c.y;
+        }
+        if (lane < 12) ((uint32_t *)&T.db)[lane] = pre_db;
+        // ---- the MB above must be final: row y-1 has published MBs 0..x
+        if (my > 0) {
+            bool ok = true;
+            if (lane == 0) {
+                const uint32_t need = (uint32_t)min(x + 1, P.mb_w);
+                const uint32_t *f = P.rowprog + my - 1;
+                uint32_t it = 0, v;
+                while (((v = ld_acquire(f)) & 0xffff0000u) != tag || (v & 0xffffu) < need) {
+                    if (++it > P.wait_limit || ((it & 63) == 0 && aborted(P.error))) { ok = false; break; }
+                    if (it > 256) __nanosleep(64);
+                }
+            }
+            if (!__shfl_sync(0xffffffffu, ok, 0)) {
+                if (lane == 0) set_error(P.error, RC_DEV_ERR_TIMEOUT);
+                return;
+            }
+            // rows -4..-1: luma lanes 0..3 (16 bytes), chroma lanes 4..11 (8 bytes)
+            if (lane < 4) {
+                uint4 v = __ldcg((const uint4 *)(Y + (size_t)(my * 16 - 4 + lane) * P.pitch + x * 16));
+                uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+                for (int i = 0; i < 4; i++) *(uint32_t *)&T.y[lane][4 + 4 * i] = w[i];
+            } else if (lane < 12) {
+                int c = (lane - 4) >> 2, r = (lane - 4) & 3;
+                uint2 v = __ldcg((const uint2 *)((c ? V : U) + (size_t)(my * 8 - 4 + r) * P.cpitch + x * 8));
+                *(uint32_t *)&T.c[c][r][4] = v.x;
+                *(uint32_t *)&T.c[c][r][8] = v.y;
+            }
+        }
+        __syncwarp();
+        if (x + 1 < P.mb_w) prefetch(x + 1);
+        const DbMb &db = T.db;
+        if (db.flags) {
+            const int aoff = db.aoff, boff = db.boff;
+            // ---- vertical edges, one row per lane
+            {
+                int s[20];
+                uint8_t *row = luma ? T.y[lane + 4] : T.c[cc][li + 4];
+                const int n = luma ? 20 : 12;
+#pragma unroll
+                for (int i = 0; i < 20; i++) s[i] = i < n ? row[i] : 0;
+                const int k = luma ? li >> 2 : li >> 1;
+#pragma unroll
+                for (int e = 0; e < 4; e++) {
+                    const int bsv = db.bs[(e << 2) | k];
+                    const bool strong = db.bs[e << 2] >= 4;
+                    int alpha, beta, tc0;
+                    if (luma) {
+                        edge_consts(e == 0 ? db.qp[1] : db.qp[0], db.qp[0], bsv, aoff, boff, alpha, beta, tc0);
+                        filt_luma(s + 4 * e, bsv, strong, alpha, beta, tc0);
+                    } else if ((e & 1) == 0) {
+                        edge_consts(e == 0 ? db.qpc[1][cc] : db.qpc[0][cc], db.qpc[0][cc], bsv, aoff, boff, alpha,
+                                    beta, tc0);
+                        filt_chroma(s + 2 * e, bsv, strong, alpha, beta, tc0);
+                    }
+                }
+#pragma unroll
+                for (int i = 0; i < 20; i++)
+                    if (i < n) row[i] = (uint8_t)s[i];
+            }
+            __syncwarp();
+            // ---- horizontal edges, one column per lane
+            {
+                int s[20];
+                const int n = luma ? 20 : 12;
+#pragma unroll
+                for (int i = 0; i < 20; i++) s[i] = i < n ? (luma ? T.y[i][lane + 4] : T.c[cc][i][li + 4]) : 0;
+                const int k = luma ? li >> 2 : li >> 1;
+#pragma unroll
+                for (int e = 0; e < 4; e++) {
+                    const int bsv = db.bs[16 | (e << 2) | k];
+                    const bool strong = db.bs[16 | (e << 2)] >= 4;
+                    int alpha, beta, tc0;
+                    if (luma) {
+                        edge_consts(e == 0 ? db.qp[2] : db.qp[0], db.qp[0], bsv, aoff, boff, alpha, beta, tc0);
+                        filt_luma(s + 4 * e, bsv, strong, alpha, beta, tc0);
+                    } else if ((e & 1) == 0) {
+                        edge_consts(e == 0 ? db.qpc[2][cc] : db.qpc[0][cc], db.qpc[0][cc], bsv, aoff, boff, alpha,
+                                    beta, tc0);
+                        filt_chroma(s + 2 * e, bsv, strong, alpha, beta, tc0);
+                    }
+                }
+#pragma unroll
+                for (int i = 0; i < 20; i++)
+                    if (i < n) {
+                        if (luma) T.y[i][lane + 4] = (uint8_t)s[i];
+                        else T.c[cc][i][li + 4] = (uint8_t)s[i];
+                    }
+            }
+            __syncwarp();
+        }
+        // ---- write back what is final: this MB's columns 0..11 (chroma 0..3),
+        // the left MB's columns 12..15 (chroma 4..7), and the rows of the MB
+        // above that this MB's top edge modified
+        if (luma) {
+            uint8_t *dst = Y + (size_t)(my * 16 + lane) * P.pitch + x * 16;
+            const uint8_t *r = T.y[lane + 4];
+            *(uint32_t *)(dst + 0) = *(const uint32_t *)(r + 4);
+            *(uint32_t *)(dst + 4) = *(const uint32_t *)(r + 8);
+            *(uint32_t *)(dst + 8) = *(const uint32_t *)(r + 12);
+            if (x > 0) *(uint32_t *)(dst - 4) = *(const uint32_t *)(r + 0);
+            if (x == P.mb_w - 1) *(uint32_t *)(dst + 12) = *(const uint32_t *)(r + 16);
+        } else {
+            uint8_t *dst = (cc ? V : U) + (size_t)(my * 8 + li) * P.cpitch + x * 8;
+            const uint8_t *r = T.c[cc][li + 4];
+            *(uint32_t *)(dst + 0) = *(const uint32_t *)(r + 4);
+            if (x > 0) *(uint32_t *)(dst - 4) = *(const uint32_t *)(r + 0);
+            if (x == P.mb_w - 1) *(uint32_t *)(dst + 4) = *(const uint32_t *)(r + 8);
+        }
+        if (my > 0 && db.flags) {
+            if (lane < 3) {  // luma rows -3..-1
+                uint8_t *dst = Y + (size_t)(my * 16 - 3 + lane) * P.pitch + x * 16;
+                const uint8_t *r = T.y[lane + 1] + 4;
+                *(uint4 *)dst = make_uint4(*(const uint32_t *)(r), *(const uint32_t *)(r + 4),
+                                           *(const uint32_t *)(r + 8), *(const uint32_t *)(r + 12));
+            } else if (lane < 5) {  // chroma row -1
+                int c = lane - 3;
+                uint8_t *dst = (c ? V : U) + (size_t)(my * 8 - 1) * P.cpitch + x * 8;
+                const uint8_t *r = T.c[c][3] + 4;
+                *(uint2 *)dst = make_uint2(*(const uint32_t *)(r), *(const uint32_t *)(r + 4));
+            }
+        }
+        __threadfence();
+        __syncwarp();
+        if (lane == 0) st_release(P.rowprog + my, tag | (uint32_t)(x == P.mb_w - 1 ? P.mb_w : x));
+        // ---- shift: this MB's columns 12..15 become the next MB's left columns
+        if (luma) {
+            *(uint32_t *)&T.y[lane + 4][0] = *(const uint32_t *)&T.y[lane + 4][16];
+        } else {
+            *(uint32_t *)&T.c[cc][li + 4][0] = *(const uint32_t *)&T.c[cc][li + 4][8];
+        }
+        __syncwarp();
     }
 }
 
@@ -1072,7 +1166,11 @@ void rc_launch_h264_mb(const H264Launch &p, cudaStream_t st) {
     h264_mb_kernel<<<p.mb_w * p.mb_h, 256, 0, st>>>(p);
 }
 
-void rc_launch_h264_wave(const H264Launch &p, cudaStream_t st, int wave_blocks) {
+void rc_launch_h264_intra(const H264Launch &p, cudaStream_t st, int wave_blocks) {
     cudaMemsetAsync(p.counter, 0, sizeof(uint32_t), st);
-    h264_wave_kernel<<<wave_blocks, 128, 0, st>>>(p);
+    h264_intra_kernel<<<wave_blocks, 128, 0, st>>>(p);
+}
+
+void rc_launch_h264_deblock(const H264Launch &p, cudaStream_t st) {
+    h264_deblock_kernel<<<p.mb_h, 32, 0, st>>>(p);
 }

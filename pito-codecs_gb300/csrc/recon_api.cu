@@ -60,6 +60,8 @@ struct rc_stream {
     cudaStream_t st = nullptr;
     uint8_t *dpb = nullptr;
     uint32_t *rflag = nullptr, *dflag = nullptr, *counter = nullptr, *error = nullptr, *tasks = nullptr;
+    uint32_t *rowprog = nullptr;
+    DbMb *db = nullptr;
     int ntasks = 0;
     DevBuf mbs, slices, weights, levels;
     int32_t *ls = nullptr;            // device ls4 (2304 ints) + ls8 (2304*4 ints)
@@ -218,16 +220,13 @@ int validate_h264(const Geo *s, const rc_h264_picture *p) {
     return 0;
 }
 
-// Wave task list: R(x,y) at key 2(x+2y), D(x,y) at key 2(x+2y+4)+1.
+// Intra task list: MBs in anti-diagonal order x + 2y (each MB after its
+// left, top-left, top and top-right neighbours).
 std::vector<uint32_t> h264_tasks(int mb_w, int mb_h) {
     std::vector<std::pair<int, uint32_t>> v;
-    v.reserve(2 * mb_w * mb_h);
+    v.reserve(mb_w * mb_h);
     for (int y = 0; y < mb_h; y++)
-        for (int x = 0; x < mb_w; x++) {
-            uint32_t a = (uint32_t)(y * mb_w + x);
-            v.push_back({2 * (x + 2 * y), a});
-            v.push_back({2 * (x + 2 * y + 4) + 1, a | 0x80000000u});
-        }
+        for (int x = 0; x < mb_w; x++) v.push_back({x + 2 * y, (uint32_t)(y * mb_w + x)});
     std::stable_sort(v.begin(), v.end(), [](const auto &a, const auto &b) { return a.first < b.first; });
     std::vector<uint32_t> t(v.size());
     for (size_t i = 0; i < v.size(); i++) t[i] = v[i].second;
@@ -247,6 +246,8 @@ void destroy(rc_stream *s) {
     cudaFree(s->error);
     cudaFree(s->tasks);
     cudaFree(s->ls);
+    cudaFree(s->rowprog);
+    cudaFree(s->db);
     for (int i = 0; i < 2; i++) {
         if (s->staging[i]) cudaFreeHost(s->staging[i]);
         if (s->staged[i]) cudaEventDestroy(s->staged[i]);
@@ -318,11 +319,14 @@ int rc_stream_create(int codec, int width, int height, int bit_depth, int dpb_sl
     ok = ok && cudaMalloc(&s->error, 64) == cudaSuccess;
     ok = ok && cudaMalloc(&s->tasks, tasks.size() * sizeof(uint32_t)) == cudaSuccess;
     ok = ok && cudaMalloc(&s->ls, (2304 + 2304 * 4) * sizeof(int32_t)) == cudaSuccess;
+    ok = ok && cudaMalloc(&s->rowprog, (size_t)s->mb_h * sizeof(uint32_t)) == cudaSuccess;
+    ok = ok && cudaMalloc(&s->db, (size_t)n * sizeof(DbMb)) == cudaSuccess;
     for (int i = 0; i < 2 && ok; i++) ok = cudaEventCreateWithFlags(&s->staged[i], cudaEventDisableTiming) == cudaSuccess;
     if (ok) {
         ok = cudaMemsetAsync(s->dpb, 0, s->slot_bytes * s->slots, s->st) == cudaSuccess &&
              cudaMemsetAsync(s->rflag, 0, n * sizeof(uint32_t), s->st) == cudaSuccess &&
              cudaMemsetAsync(s->dflag, 0, n * sizeof(uint32_t), s->st) == cudaSuccess &&
+             cudaMemsetAsync(s->rowprog, 0, (size_t)s->mb_h * sizeof(uint32_t), s->st) == cudaSuccess &&
              cudaMemsetAsync(s->error, 0, 64, s->st) == cudaSuccess &&
              cudaMemcpyAsync(s->tasks, tasks.data(), tasks.size() * sizeof(uint32_t), cudaMemcpyHostToDevice,
                              s->st) == cudaSuccess &&
@@ -446,8 +450,11 @@ int rc_h264_submit(rc_stream *s, const rc_h264_picture *pic, int out_slot) {
     L.ntasks = s->ntasks;
     L.error = s->error;
     L.wait_limit = s->wait_limit;
+    L.db = s->db;
+    L.rowprog = s->rowprog;
     timed(s, RC_KERNEL_H264_MB, [&] { rc_launch_h264_mb(L, s->st); });
-    timed(s, RC_KERNEL_H264_WAVE, [&] { rc_launch_h264_wave(L, s->st, s->wave_blocks); });
+    timed(s, RC_KERNEL_H264_INTRA, [&] { rc_launch_h264_intra(L, s->st, s->wave_blocks); });
+    timed(s, RC_KERNEL_H264_DEBLOCK, [&] { rc_launch_h264_deblock(L, s->st); });
     s->submits++;
     if (cudaGetLastError() != cudaSuccess) return cuda_fail(s);
     return RC_OK;

@@ -15,6 +15,19 @@
 // iteration backs off with __nanosleep, so the cap is about a second).
 #define RC_WAIT_LIMIT (1u << 22)
 
+// Per-MB loop-filter parameters, derived from the records by h264_mb_kernel
+// (boundary strengths of deblock_mb, src/h264/dec/deblock.rs:327-371, and
+// the QPs / offsets its edge parameters use).
+struct DbMb {
+    uint8_t bs[32];     // [dir][edge][segment]; dir 0 = vertical edges
+    uint8_t qp[3];      // luma QP of q, of p across edge 0 for dir 0, dir 1
+    uint8_t flags;      // bit 0: some edge filters
+    uint8_t qpc[3][2];  // chroma QPs, same order
+    int8_t aoff, boff;  // slice alpha / beta offsets
+    uint8_t pad[4];
+};
+static_assert(sizeof(DbMb) == 48, "DbMb layout");
+
 struct H264Launch {
     const rc_h264_mb *mbs;
     const rc_h264_slice *slices;
@@ -37,8 +50,11 @@ struct H264Launch {
     int ntasks;
     uint32_t *error;
     uint32_t wait_limit;
+    DbMb *db;             // per-MB loop-filter parameters
+    uint32_t *rowprog;    // per MB row: (epoch & 0xffff) << 16 | MBs final
 };
 
 // Launchers (h264_kernels.cu).
 void rc_launch_h264_mb(const H264Launch &p, cudaStream_t st);
-void rc_launch_h264_wave(const H264Launch &p, cudaStream_t st, int wave_blocks);
+void rc_launch_h264_intra(const H264Launch &p, cudaStream_t st, int wave_blocks);
+void rc_launch_h264_deblock(const H264Launch &p, cudaStream_t st);
