@@ -148,6 +148,129 @@ typedef struct rc_h264_picture {
 } rc_h264_picture;
 
 /* ======================================================================== */
+/*  HEVC syntax records                                                      */
+/* ======================================================================== */
+
+/* rc_hevc_blk.flags / .edges — the Blk flags of src/hevc/slicedec.rs:19-28 */
+#define RC_HEVC_F_INTRA 1     /* the CU is intra                              */
+#define RC_HEVC_F_SKIP 2      /* skipped CU                                   */
+#define RC_HEVC_F_NOFILTER 4  /* PCM with loop filter off, or transquant bypass */
+#define RC_HEVC_F_CBF 8       /* the luma TU covering it has coefficients     */
+#define RC_HEVC_F_CODED 16    /* decoded                                      */
+#define RC_HEVC_E_TU_V 1      /* transform-unit edge on the block's left      */
+#define RC_HEVC_E_PU_V 2      /* prediction-unit edge on the left             */
+#define RC_HEVC_E_TU_H 4      /* transform-unit edge on top                   */
+#define RC_HEVC_E_PU_H 8      /* prediction-unit edge on top                  */
+
+/* Per 4x4 luma block (Blk, src/hevc/slicedec.rs:30-37, without the CABAC
+ * depth): what the loop filters and intra availability read. */
+typedef struct rc_hevc_blk {
+    uint8_t flags;  /* RC_HEVC_F_* */
+    uint8_t edges;  /* RC_HEVC_E_* */
+    int8_t qp;      /* QpY of the CU (loop-filter QP)                       */
+    uint8_t ipm;    /* luma intra mode (informational)                      */
+} rc_hevc_blk;      /* 4 bytes */
+
+/* Per 4x4 luma block motion (MvField, src/hevc/slicedec.rs:40-44):
+ * quarter-pel luma vectors, ref_idx -1 = list unused. */
+typedef struct rc_hevc_mvf {
+    int16_t mv[2][2];
+    int8_t ref_idx[2];
+    uint16_t reserved;
+} rc_hevc_mvf;      /* 12 bytes */
+
+/* SAO parameters of one CTB (SaoParams, src/hevc/slicedec.rs:62-67):
+ * type 0 off, 1 band, 2 edge; offsets already signed and scaled. */
+typedef struct rc_hevc_sao {
+    uint8_t type_idx[3];
+    uint8_t band_pos[3];
+    uint8_t eo_class[3];
+    uint8_t reserved;
+    int16_t offsets[3][4];
+} rc_hevc_sao;      /* 34 bytes */
+
+/* One CTB, raster order: its slice (index into the slice table), tile and
+ * tile-scan position (Layout::rs_to_ts / tile_id), and SAO parameters. */
+typedef struct rc_hevc_ctb {
+    uint16_t slice;
+    uint16_t tile;
+    uint32_t ts;
+    rc_hevc_sao sao;
+    uint16_t reserved;
+} rc_hevc_ctb;      /* 44 bytes */
+
+/* rc_hevc_tu.flags */
+#define RC_HEVC_TU_INTRA 1    /* intra CU: predict (mode) before the residual */
+#define RC_HEVC_TU_CBF 2      /* coefficient levels present                   */
+#define RC_HEVC_TU_SKIP 4     /* transform_skip_flag                          */
+#define RC_HEVC_TU_BYPASS 8   /* cu_transquant_bypass: levels are the residual */
+#define RC_HEVC_TU_PCM 16     /* PCM: n x n samples instead of levels         */
+
+/*
+ * One transform block of one colour component, in decode order (the order
+ * transform_unit visits them, src/hevc/slicedec.rs:1602-1671: luma, then Cb
+ * and Cr of the same TU or, for 4x4 luma blocks, after the fourth one).
+ * Levels at levels[coef_off...]: (max_y+1) x (max_x+1) int16, row-major, the
+ * parsed coefficients before dequantisation (reconstruct,
+ * src/hevc/slicedec.rs:2004-2049).  Inter CUs are predicted from the
+ * rc_hevc_mvf grid; their TUs carry only residual.
+ */
+typedef struct rc_hevc_tu {
+    uint16_t x0, y0;  /* top-left in the component's own sample grid        */
+    uint8_t log2;     /* 2..5                                               */
+    uint8_t c;        /* 0 Y, 1 Cb, 2 Cr                                    */
+    uint8_t flags;    /* RC_HEVC_TU_*                                       */
+    uint8_t mode;     /* intra mode 0..34 (chroma: after the mode-34 rule)  */
+    int8_t qp;        /* dequantisation QP: luma qp_y + 6(bd-8); chroma qp_cb/qp_cr */
+    uint8_t max_x, max_y; /* last significant column / row                  */
+    uint8_t reserved;
+    uint32_t coef_off;
+} rc_hevc_tu;         /* 16 bytes */
+
+#define RC_HEVC_MAX_REFS 16
+/* Per-slice state (SliceInfo, src/hevc/slicedec.rs:69-80) plus the
+ * reference lists and the explicit weighted-prediction table the motion
+ * compensation uses (motion_compensate, src/hevc/slicedec.rs:2205-2280). */
+typedef struct rc_hevc_slice {
+    uint32_t slice_addr;      /* SliceAddrRs: slices compare by this          */
+    int32_t deblock_disabled;
+    int32_t beta_offset;      /* slice_beta_offset_div2 * 2                   */
+    int32_t tc_offset;        /* slice_tc_offset_div2 * 2                     */
+    int32_t lf_across;        /* slice_loop_filter_across_slices_enabled_flag */
+    int32_t sao_luma, sao_chroma;
+    int32_t weighted;         /* explicit weighted prediction in this slice   */
+    int32_t luma_log2_denom, chroma_log2_denom;
+    int32_t num_ref[2];
+    int32_t ref_slot[2][RC_HEVC_MAX_REFS];
+    uint32_t ref_id[2][RC_HEVC_MAX_REFS]; /* picture identity for the bS test */
+    int16_t luma_w[2][RC_HEVC_MAX_REFS], luma_o[2][RC_HEVC_MAX_REFS];
+    int16_t chroma_w[2][RC_HEVC_MAX_REFS][2], chroma_o[2][RC_HEVC_MAX_REFS][2];
+} rc_hevc_slice;
+
+typedef struct rc_hevc_picture {
+    int32_t mem;                   /* RC_MEM_HOST or RC_MEM_DEVICE            */
+    int32_t log2_ctb;              /* 4..6                                    */
+    int32_t constrained_intra_pred;
+    int32_t strong_intra_smoothing;
+    int32_t loop_filter_across_tiles;
+    int32_t cb_qp_offset, cr_qp_offset; /* PPS offsets (loop-filter chroma QP) */
+    int32_t num_slices;
+    int32_t num_tus;
+    uint32_t frame_id;
+    size_t num_levels;
+    const rc_hevc_ctb *ctbs;       /* ceil(w/ctb) * ceil(h/ctb), raster       */
+    const rc_hevc_blk *blk;        /* (w/4) * (h/4), raster                   */
+    const rc_hevc_mvf *mvf;        /* (w/4) * (h/4), raster                   */
+    const rc_hevc_tu *tus;         /* decode order                            */
+    const rc_hevc_slice *slices;
+    const int16_t *levels;
+    /* Expanded scaling factors (the Scaling tables, src/hevc/slicedec.rs:17):
+     * for size_id 0..3 (4..32) and matrix_id 0..5 (intra Y Cb Cr, inter Y Cb
+     * Cr), n*n bytes each, size_id-major; NULL = flat 16.  Host memory. */
+    const uint8_t *scaling;        /* 6*(16+64+256+1024) bytes                */
+} rc_hevc_picture;
+
+/* ======================================================================== */
 /*  Stream / DPB lifetime                                                    */
 /* ======================================================================== */
 
@@ -180,6 +303,18 @@ int rc_h264_submit(rc_stream *s, const rc_h264_picture *pic, int out_slot);
  * stream of mb_w x mb_h macroblocks and dpb_slots DPB slots; needs no GPU.
  * Returns 0 or RC_EINVAL. */
 int rc_h264_validate(int mb_w, int mb_h, int dpb_slots, const rc_h264_picture *pic);
+
+/* Reconstruct one HEVC picture into DPB slot `out_slot`: residual for every
+ * TU, inter prediction, intra prediction in decode order, deblocking (all
+ * vertical edges, then all horizontal edges) and SAO.  Host-side validation
+ * as for H.264 (src/hevc/slicedec.rs:2153-2160 rejects bad ref_idx).
+ * Planes of >8-bit streams are uint16 samples. */
+int rc_hevc_submit(rc_stream *s, const rc_hevc_picture *pic, int out_slot);
+
+/* Host-side validation of an HEVC picture for a stream of the given luma
+ * size and DPB slots; needs no GPU.  Returns 0 or RC_EINVAL. */
+int rc_hevc_validate(int width, int height, int bit_depth, int dpb_slots,
+                     const rc_hevc_picture *pic);
 
 /* Wait for all submitted work; returns the sticky error word (0 if none). */
 int rc_stream_sync(rc_stream *s);
@@ -223,6 +358,11 @@ int rc_picture_device_planes(rc_stream *s, int slot, void **y, void **u,
 #define RC_KERNEL_H264_MB 0
 #define RC_KERNEL_H264_INTRA 1
 #define RC_KERNEL_H264_DEBLOCK 2
+#define RC_KERNEL_HEVC_RESIDUAL 3
+#define RC_KERNEL_HEVC_INTER 4
+#define RC_KERNEL_HEVC_INTRA 5
+#define RC_KERNEL_HEVC_DEBLOCK 6
+#define RC_KERNEL_HEVC_SAO 7
 #define RC_KERNEL_COUNT 8
 int rc_stream_profile(rc_stream *s, int enable);
 int rc_stream_profile_read(rc_stream *s, double *ms, long long *launches,

@@ -54,6 +54,19 @@ void oracle_h264_mc_chroma(const uint8_t *plane, int cwidth, int cheight,
                            int cpx, int cpy, int mvx, int mvy, int bw, int bh,
                            uint8_t *out, int os);
 
+/* Reconstruct one HEVC picture of width x height luma samples at
+ * bit_depth 8 or 10.  Planes are uint16_t at every bit depth, tightly
+ * packed.  stages: bit 0 deblocking, bit 1 SAO (3 = the full path).
+ * Returns 0 or RC_EINVAL. */
+int oracle_hevc_recon(int width, int height, int bit_depth, const rc_hevc_picture *pic,
+                      const uint16_t *const *ref_y, const uint16_t *const *ref_u,
+                      const uint16_t *const *ref_v, uint16_t *y, uint16_t *u, uint16_t *v,
+                      int stages);
+void oracle_hevc_inverse(int16_t *co, int log2, int dst, int max_x, int max_y, int bd_shift);
+int oracle_hevc_inverse_dc(int dc, int bd_shift);
+void oracle_hevc_intra_predict_refs(const uint16_t *left, const uint16_t *top, int mode, int log2,
+                                    int is_luma, int strong, int bd, int *out);
+
 #ifdef __cplusplus
 }
 #endif

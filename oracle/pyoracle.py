@@ -41,6 +41,12 @@ def lib() -> ctypes.CDLL:
         _lib.oracle_h264_level_scale.argtypes = [vp, vp, vp, vp]
         _lib.oracle_h264_mc_luma.argtypes = [vp, i32, i32, i32, i32, i32, i32, i32, i32, vp, i32]
         _lib.oracle_h264_mc_chroma.argtypes = [vp, i32, i32, i32, i32, i32, i32, i32, i32, vp, i32]
+        _lib.oracle_hevc_recon.argtypes = [i32, i32, i32, vp, vp, vp, vp, vp, vp, vp, i32]
+        _lib.oracle_hevc_recon.restype = i32
+        _lib.oracle_hevc_inverse.argtypes = [vp, i32, i32, i32, i32, i32]
+        _lib.oracle_hevc_inverse_dc.argtypes = [i32, i32]
+        _lib.oracle_hevc_inverse_dc.restype = i32
+        _lib.oracle_hevc_intra_predict_refs.argtypes = [vp, vp, i32, i32, i32, i32, i32, vp]
     return _lib
 
 
@@ -67,6 +73,31 @@ class H264Dpb:
         u = self.u[out_slot].copy()
         v = self.v[out_slot].copy()
         rc = f(self.mb_w, self.mb_h, picture_ptr, ry, ru, rv, y.ctypes.data, u.ctypes.data, v.ctypes.data)
+        if rc == 0:
+            self.y[out_slot], self.u[out_slot], self.v[out_slot] = y, u, v
+        return rc
+
+    def planes(self, slot: int):
+        return self.y[slot], self.u[slot], self.v[slot]
+
+
+class HevcDpb:
+    """CPU decoded-picture buffer for HEVC: uint16 planes per slot."""
+
+    def __init__(self, width: int, height: int, bit_depth: int, slots: int):
+        self.W, self.H, self.bd, self.slots = width, height, bit_depth, slots
+        self.y = [np.zeros((height, width), np.uint16) for _ in range(slots)]
+        self.u = [np.zeros((height // 2, width // 2), np.uint16) for _ in range(slots)]
+        self.v = [np.zeros((height // 2, width // 2), np.uint16) for _ in range(slots)]
+
+    def recon(self, picture_ptr: int, out_slot: int, stages: int = 3) -> int:
+        L = lib()
+        arr = lambda planes: (ctypes.c_void_p * self.slots)(*[p.ctypes.data for p in planes])
+        y = self.y[out_slot].copy()
+        u = self.u[out_slot].copy()
+        v = self.v[out_slot].copy()
+        rc = L.oracle_hevc_recon(self.W, self.H, self.bd, picture_ptr, arr(self.y), arr(self.u), arr(self.v),
+                                 y.ctypes.data, u.ctypes.data, v.ctypes.data, stages)
         if rc == 0:
             self.y[out_slot], self.u[out_slot], self.v[out_slot] = y, u, v
         return rc

@@ -32,7 +32,8 @@ ERROR_NAMES = {RC_EINVAL: "RC_EINVAL", RC_ENOMEM: "RC_ENOMEM", RC_ECUDA: "RC_ECU
                RC_ETIMEOUT: "RC_ETIMEOUT", RC_EDEVICE: "RC_EDEVICE", RC_ENODEV: "RC_ENODEV"}
 
 RC_H264_NONE, RC_H264_I4x4, RC_H264_I8x8, RC_H264_I16x16, RC_H264_IPCM, RC_H264_INTER = range(6)
-RC_KERNEL_NAMES = {0: "h264_mb_kernel", 1: "h264_intra_kernel", 2: "h264_deblock_kernel"}
+RC_KERNEL_NAMES = {0: "h264_mb_kernel", 1: "h264_intra_kernel", 2: "h264_deblock_kernel", 3: "hevc_residual_kernel",
+                   4: "hevc_inter_kernel", 5: "hevc_intra_kernel", 6: "hevc_deblock_kernel", 7: "hevc_sao_kernel"}
 RC_KERNEL_COUNT = 8
 
 
@@ -89,6 +90,71 @@ class SynthH264Opts(ctypes.Structure):
                 ("ref_id", (ctypes.c_uint32 * 4) * 2), ("frame_id", ctypes.c_uint32)]
 
 
+class HevcBlk(ctypes.Structure):
+    _fields_ = [("flags", ctypes.c_uint8), ("edges", ctypes.c_uint8), ("qp", ctypes.c_int8), ("ipm", ctypes.c_uint8)]
+
+
+class HevcMvf(ctypes.Structure):
+    _fields_ = [("mv", (ctypes.c_int16 * 2) * 2), ("ref_idx", ctypes.c_int8 * 2), ("reserved", ctypes.c_uint16)]
+
+
+class HevcSao(ctypes.Structure):
+    _fields_ = [("type_idx", ctypes.c_uint8 * 3), ("band_pos", ctypes.c_uint8 * 3), ("eo_class", ctypes.c_uint8 * 3),
+                ("reserved", ctypes.c_uint8), ("offsets", (ctypes.c_int16 * 4) * 3)]
+
+
+class HevcCtb(ctypes.Structure):
+    _fields_ = [("slice", ctypes.c_uint16), ("tile", ctypes.c_uint16), ("ts", ctypes.c_uint32), ("sao", HevcSao),
+                ("reserved", ctypes.c_uint16)]
+
+
+class HevcTu(ctypes.Structure):
+    _fields_ = [("x0", ctypes.c_uint16), ("y0", ctypes.c_uint16), ("log2", ctypes.c_uint8), ("c", ctypes.c_uint8),
+                ("flags", ctypes.c_uint8), ("mode", ctypes.c_uint8), ("qp", ctypes.c_int8), ("max_x", ctypes.c_uint8),
+                ("max_y", ctypes.c_uint8), ("reserved", ctypes.c_uint8), ("coef_off", ctypes.c_uint32)]
+
+
+class HevcSlice(ctypes.Structure):
+    _fields_ = [("slice_addr", ctypes.c_uint32), ("deblock_disabled", ctypes.c_int32), ("beta_offset", ctypes.c_int32),
+                ("tc_offset", ctypes.c_int32), ("lf_across", ctypes.c_int32), ("sao_luma", ctypes.c_int32),
+                ("sao_chroma", ctypes.c_int32), ("weighted", ctypes.c_int32), ("luma_log2_denom", ctypes.c_int32),
+                ("chroma_log2_denom", ctypes.c_int32), ("num_ref", ctypes.c_int32 * 2),
+                ("ref_slot", (ctypes.c_int32 * 16) * 2), ("ref_id", (ctypes.c_uint32 * 16) * 2),
+                ("luma_w", (ctypes.c_int16 * 16) * 2), ("luma_o", (ctypes.c_int16 * 16) * 2),
+                ("chroma_w", ((ctypes.c_int16 * 2) * 16) * 2), ("chroma_o", ((ctypes.c_int16 * 2) * 16) * 2)]
+
+
+class HevcPicture(ctypes.Structure):
+    _fields_ = [("mem", ctypes.c_int32), ("log2_ctb", ctypes.c_int32), ("constrained_intra_pred", ctypes.c_int32),
+                ("strong_intra_smoothing", ctypes.c_int32), ("loop_filter_across_tiles", ctypes.c_int32),
+                ("cb_qp_offset", ctypes.c_int32), ("cr_qp_offset", ctypes.c_int32), ("num_slices", ctypes.c_int32),
+                ("num_tus", ctypes.c_int32), ("frame_id", ctypes.c_uint32), ("num_levels", ctypes.c_size_t),
+                ("ctbs", ctypes.c_void_p), ("blk", ctypes.c_void_p), ("mvf", ctypes.c_void_p), ("tus", ctypes.c_void_p),
+                ("slices", ctypes.c_void_p), ("levels", ctypes.c_void_p), ("scaling", ctypes.c_void_p)]
+
+
+assert (ctypes.sizeof(HevcBlk), ctypes.sizeof(HevcMvf), ctypes.sizeof(HevcCtb), ctypes.sizeof(HevcTu),
+        ctypes.sizeof(HevcSlice), ctypes.sizeof(HevcPicture)) == (4, 12, 44, 16, 688, 104)
+
+
+class SynthHevcOpts(ctypes.Structure):
+    _fields_ = [("seed", ctypes.c_uint64), ("width", ctypes.c_int32), ("height", ctypes.c_int32),
+                ("bit_depth", ctypes.c_int32), ("log2_ctb", ctypes.c_int32), ("intra_only", ctypes.c_int32),
+                ("intra_permille", ctypes.c_int32), ("zero_tu_permille", ctypes.c_int32),
+                ("split_permille", ctypes.c_int32), ("mv_range", ctypes.c_int32), ("bipred_permille", ctypes.c_int32),
+                ("qp_min", ctypes.c_int32), ("qp_max", ctypes.c_int32), ("cb_qp_offset", ctypes.c_int32),
+                ("cr_qp_offset", ctypes.c_int32), ("transform_skip_permille", ctypes.c_int32),
+                ("pcm_permille", ctypes.c_int32), ("pcm_loop_filter_disabled", ctypes.c_int32),
+                ("bypass_permille", ctypes.c_int32), ("scaling_lists", ctypes.c_int32),
+                ("constrained_intra_pred", ctypes.c_int32), ("strong_intra_smoothing", ctypes.c_int32),
+                ("weighted", ctypes.c_int32), ("num_slices", ctypes.c_int32), ("tile_cols", ctypes.c_int32),
+                ("tile_rows", ctypes.c_int32), ("loop_filter_across_tiles", ctypes.c_int32),
+                ("lf_across_slices", ctypes.c_int32), ("deblock_disabled", ctypes.c_int32),
+                ("beta_offset", ctypes.c_int32), ("tc_offset", ctypes.c_int32), ("sao", ctypes.c_int32),
+                ("num_ref", ctypes.c_int32 * 2), ("ref_slot", (ctypes.c_int32 * 4) * 2),
+                ("ref_id", (ctypes.c_uint32 * 4) * 2), ("frame_id", ctypes.c_uint32)]
+
+
 # ---- library loading ------------------------------------------------------
 _LIBS: dict = {}
 
@@ -130,6 +196,10 @@ def lib() -> ctypes.CDLL:
     L.rc_h264_submit.restype = i32
     L.rc_h264_validate.argtypes = [i32, i32, i32, vp]
     L.rc_h264_validate.restype = i32
+    L.rc_hevc_submit.argtypes = [vp, vp, i32]
+    L.rc_hevc_submit.restype = i32
+    L.rc_hevc_validate.argtypes = [i32, i32, i32, i32, vp]
+    L.rc_hevc_validate.restype = i32
     L.rc_stream_sync.argtypes = [vp]
     L.rc_stream_sync.restype = i32
     L.rc_stream_error.argtypes = [vp]
@@ -170,6 +240,16 @@ def synth_lib() -> ctypes.CDLL:
     L.rc_synth_h264_bytes.restype = ctypes.c_size_t
     L.rc_synth_h264_free.argtypes = [ctypes.c_void_p]
     L.rc_synth_h264_free.restype = None
+    L.rc_synth_hevc_defaults.argtypes = [ctypes.POINTER(SynthHevcOpts)]
+    L.rc_synth_hevc_defaults.restype = None
+    L.rc_synth_hevc_new.argtypes = [ctypes.POINTER(SynthHevcOpts)]
+    L.rc_synth_hevc_new.restype = ctypes.c_void_p
+    L.rc_synth_hevc_picture.argtypes = [ctypes.c_void_p]
+    L.rc_synth_hevc_picture.restype = ctypes.c_void_p
+    L.rc_synth_hevc_bytes.argtypes = [ctypes.c_void_p]
+    L.rc_synth_hevc_bytes.restype = ctypes.c_size_t
+    L.rc_synth_hevc_free.argtypes = [ctypes.c_void_p]
+    L.rc_synth_hevc_free.restype = None
     return L
 
 
@@ -233,6 +313,57 @@ class SynthH264:
             pass
 
 
+class SynthHevc:
+    """One generated HEVC picture (owns the C buffers)."""
+
+    def __init__(self, **kw):
+        L = synth_lib()
+        o = SynthHevcOpts()
+        L.rc_synth_hevc_defaults(ctypes.byref(o))
+        refs = kw.pop("refs", None)  # [(list, slot, id), ...]
+        for k, v in kw.items():
+            if not hasattr(o, k):
+                raise TypeError(f"unknown generator option {k}")
+            setattr(o, k, v)
+        if refs is not None:
+            o.num_ref[0] = o.num_ref[1] = 0
+            for (l, slot, rid) in refs:
+                i = o.num_ref[l]
+                o.ref_slot[l][i] = slot
+                o.ref_id[l][i] = rid
+                o.num_ref[l] = i + 1
+        self.opts = o
+        self._h = L.rc_synth_hevc_new(ctypes.byref(o))
+        if not self._h:
+            raise ValueError("generator rejected its options")
+        self.ptr = L.rc_synth_hevc_picture(self._h)
+        self.pic = HevcPicture.from_address(self.ptr)
+        self.nbytes = L.rc_synth_hevc_bytes(self._h)
+
+    def buffers(self) -> dict:
+        p, o = self.pic, self.opts
+        w4, h4 = o.width // 4, o.height // 4
+        ctb = 1 << o.log2_ctb
+        nctb = ((o.width + ctb - 1) // ctb) * ((o.height + ctb - 1) // ctb)
+        def raw(addr, n):
+            return bytes((ctypes.c_uint8 * n).from_address(addr)) if (n and addr) else b""
+        return {"ctbs": raw(p.ctbs, 44 * nctb), "blk": raw(p.blk, 4 * w4 * h4), "mvf": raw(p.mvf, 12 * w4 * h4),
+                "tus": raw(p.tus, 16 * p.num_tus), "slices": raw(p.slices, 688 * p.num_slices),
+                "levels": raw(p.levels, 2 * p.num_levels),
+                "scaling": raw(p.scaling, 6 * (16 + 64 + 256 + 1024))}
+
+    def close(self):
+        if self._h:
+            synth_lib().rc_synth_hevc_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class PictureBuffers:
     """An rc_h264_picture rebuilt from raw buffers (e.g. fixture files),
     keeping the buffers alive."""
@@ -284,6 +415,10 @@ class ReconStream:
     def submit_h264(self, picture, out_slot: int):
         ptr = picture.ptr if hasattr(picture, "ptr") else picture
         _check(lib().rc_h264_submit(self._h, ptr, out_slot), "rc_h264_submit")
+
+    def submit_hevc(self, picture, out_slot: int):
+        ptr = picture.ptr if hasattr(picture, "ptr") else picture
+        _check(lib().rc_hevc_submit(self._h, ptr, out_slot), "rc_hevc_submit")
 
     def sync(self) -> int:
         return lib().rc_stream_sync(self._h)

@@ -992,10 +992,6 @@ struct __align__(16) RowTile {
     DbMb db;
 };
 
-__device__ __forceinline__ uint32_t pack4(const int *v) {
-    return (uint32_t)v[0] | (uint32_t)v[1] << 8 | (uint32_t)v[2] << 16 | (uint32_t)v[3] << 24;
-}
-
 __global__ void __launch_bounds__(32) h264_deblock_kernel(H264Launch P) {
     __shared__ RowTile T;
     const int lane = threadIdx.x, my = blockIdx.x;

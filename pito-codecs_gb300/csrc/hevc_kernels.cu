@@ -1,0 +1,786 @@
+// hevc_kernels.cu — HEVC block reconstruction on sm_103a.
+//
+// Per picture (samples are uint8_t for 8-bit, uint16_t for 10-bit streams):
+//
+//  hevc_residual_kernel  one warp per transform block, all in parallel:
+//                        dequantisation (flat or scaling lists), 4..32
+//                        inverse DCT / 4x4 DST as two matrix passes through
+//                        shared memory (clamp between), transform skip, the
+//                        DC-only shortcut, transquant bypass -> int16 residual
+//                        planes.
+//  hevc_inter_kernel     one thread per sample of every inter block: 8-tap /
+//                        4-tap interpolation with i16 intermediates, default
+//                        or explicit weighted prediction, residual add, clip.
+//  hevc_intra_kernel     persistent; one warp per intra transform block taken
+//                        in decode order; waits (acquire loads, capped spin)
+//                        only for the intra neighbour blocks it reads,
+//                        substitutes / smooths the reference samples and
+//                        predicts (planar, DC, 33 angles + edge filters).
+//  hevc_deblock_kernel   vertical edges, then (second launch) horizontal
+//                        edges, one thread per 4-sample edge segment: edges
+//                        8 samples apart never interact within a direction.
+//  hevc_sao_kernel       one thread per sample: band / edge offsets from the
+//                        deblocked picture into the DPB slot.
+//
+// Arithmetic follows src/hevc/{transform,intra,inter,filter}.rs and the
+// reconstruction half of src/hevc/slicedec.rs; citations at each function.
+#include <stdint.h>
+
+#include "recon_internal.h"
+
+namespace {
+
+__constant__ int8_t cTRANS[32][32] = {
+#include "../../oracle/hevc_trans_matrix.inc"
+};
+__constant__ int8_t cDST[4][4] = {{29, 55, 74, 84}, {74, 74, 0, -74}, {84, -29, -74, 55}, {55, -84, 74, -29}};
+__constant__ int cLEVEL_SCALE[6] = {40, 45, 51, 57, 64, 72};
+__constant__ int8_t cANGLE[35] = {0,  0,  32, 26, 21, 17, 13, 9,  5,  2,   0,   -2,  -5,  -9,  -13, -17, -21, -26,
+                                  -32, -26, -21, -17, -13, -9, -5, -2, 0, 2, 5, 9, 13, 17, 21, 26, 32};
+__constant__ int16_t cINV_ANGLE[15] = {-4096, -1638, -910, -630, -482, -390, -315, -256,
+                                       -315,  -390,  -482, -630, -910, -1638, -4096};
+__constant__ uint8_t cQPC_30_43[14] = {29, 30, 31, 32, 33, 33, 34, 34, 35, 35, 36, 36, 37, 37};
+__constant__ uint8_t cBETA[52] = {0,  0,  0,  0,  0,  0,  0,  0,  0,  0,  0,  0,  0,  0,  0,  0,  6,  7,
+                                  8,  9,  10, 11, 12, 13, 14, 15, 16, 17, 18, 20, 22, 24, 26, 28, 30, 32,
+                                  34, 36, 38, 40, 42, 44, 46, 48, 50, 52, 54, 56, 58, 60, 62, 64};
+__constant__ uint8_t cTC[54] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 1, 1, 1, 1, 1, 1, 1, 1, 1,
+                                2, 2, 2, 2, 3, 3, 3, 3, 4, 4, 4, 5, 5, 6, 6, 7, 8, 9, 10, 11, 13, 14, 16, 18, 20, 22, 24};
+__constant__ int8_t cLUMA_F[4][8] = {
+    {0, 0, 0, 64, 0, 0, 0, 0}, {-1, 4, -10, 58, 17, -5, 1, 0}, {-1, 4, -11, 40, 40, -11, 4, -1}, {0, 1, -5, 17, 58, -10, 4, -1}};
+__constant__ int8_t cCHROMA_F[8][4] = {{0, 64, 0, 0},    {-2, 58, 10, -2}, {-4, 54, 16, -2}, {-6, 46, 28, -4},
+                                       {-4, 36, 36, -4}, {-4, 28, 46, -6}, {-2, 16, 54, -4}, {-2, 10, 58, -2}};
+
+__device__ __forceinline__ int clampi(int v, int lo, int hi) { return min(max(v, lo), hi); }
+__device__ __forceinline__ int qpc_420(int q) { return q < 30 ? q : q > 43 ? q - 6 : cQPC_30_43[q - 30]; }
+
+__device__ __forceinline__ uint32_t ld_acquire(const uint32_t *p) {
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release(uint32_t *p, uint32_t v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ bool aborted(const uint32_t *err) {
+    return (*(const volatile uint32_t *)err & RC_DEV_ERR_TIMEOUT) != 0;
+}
+__device__ bool wait_flag(const uint32_t *f, uint32_t epoch, uint32_t limit, const uint32_t *err) {
+    uint32_t it = 0;
+    while (ld_acquire(f) != epoch) {
+        if (++it > limit) return false;
+        if ((it & 63) == 0 && aborted(err)) return false;
+        if (it > 256) __nanosleep(64);
+    }
+    return true;
+}
+
+// Plane access in the DPB / work layout (pitch in bytes).
+template <class T>
+__device__ __forceinline__ T *plane_ptr(uint8_t *base, const HevcLaunch &P, int c) {
+    return (T *)(base + (c == 0 ? 0 : c == 1 ? P.u_off : P.v_off));
+}
+__device__ __forceinline__ int pitch_el(const HevcLaunch &P, int c, int size) { return (c ? P.cpitch : P.pitch) / size; }
+__device__ __forceinline__ int16_t *res_plane(const HevcLaunch &P, int c) {
+    return P.res + (c == 0 ? 0 : (size_t)P.W * P.H + (size_t)(c - 1) * P.CW * P.CH);
+}
+__device__ __forceinline__ const rc_hevc_slice *slice_of_ctb(const HevcLaunch &P, int ctb) {
+    int s = P.ctbs[ctb].slice;
+    return P.slices + (s < P.num_slices ? s : 0);
+}
+__device__ __forceinline__ int ctb_of(const HevcLaunch &P, int x, int y) {
+    return (y >> P.log2ctb) * P.wctb + (x >> P.log2ctb);
+}
+__device__ __forceinline__ uint32_t slice_addr(const HevcLaunch &P, int ctb) { return slice_of_ctb(P, ctb)->slice_addr; }
+
+// ===========================================================================
+// Residuals: reconstruct, src/hevc/slicedec.rs:2004-2049 with dequant /
+// inverse / inverse_dc / transform_skip of src/hevc/transform.rs.
+// ===========================================================================
+__global__ void __launch_bounds__(128) hevc_residual_kernel(HevcLaunch P) {
+    __shared__ int8_t mat[32][32];
+    __shared__ int32_t buf[4][2][1024];
+    for (int i = threadIdx.x; i < 1024; i += blockDim.x) mat[i >> 5][i & 31] = cTRANS[i >> 5][i & 31];
+    __syncthreads();
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int32_t *co = buf[w][0], *col = buf[w][1];
+    for (int ti = blockIdx.x * 4 + w; ti < P.num_tus; ti += gridDim.x * 4) {
+        const rc_hevc_tu t = P.tus[ti];
+        if (!(t.flags & RC_HEVC_TU_CBF) || (t.flags & RC_HEVC_TU_PCM)) continue;
+        const int log2 = t.log2, n = 1 << log2, c = t.c, mx = t.max_x, my = t.max_y;
+        const unsigned long long cnt = (unsigned long long)(mx + 1) * (my + 1);
+        const int pw = c ? P.CW : P.W, ph = c ? P.CH : P.H;
+        if (log2 < 2 || log2 > 5 || c > 2 || mx >= n || my >= n || t.coef_off + cnt > P.num_levels ||
+            t.x0 + n > pw || t.y0 + n > ph || (!(t.flags & RC_HEVC_TU_BYPASS) && t.qp < 0)) {
+            if (lane == 0) atomicOr(P.error, RC_DEV_ERR_RECORD);
+            continue;
+        }
+        for (int i = lane; i < n * n; i += 32) co[i] = 0;
+        __syncwarp();
+        const int16_t *lv = P.levels + t.coef_off;
+        for (int i = lane; i < (int)cnt; i += 32) co[(i / (mx + 1)) * n + i % (mx + 1)] = lv[i];
+        __syncwarp();
+        const int bd = P.bd, intra = t.flags & RC_HEVC_TU_INTRA;
+        int16_t *rp = res_plane(P, c) + (size_t)t.y0 * (c ? P.CW : P.W) + t.x0;
+        const int rpitch = c ? P.CW : P.W;
+        if (!(t.flags & RC_HEVC_TU_BYPASS)) {
+            const bool ts = t.flags & RC_HEVC_TU_SKIP;
+            const int qp = t.qp, bd_shift = bd + log2 - 5;
+            const long long round = 1ll << (bd_shift - 1);
+            const long long scale = (long long)cLEVEL_SCALE[qp % 6] << (qp / 6);
+            const uint8_t *m = nullptr;
+            if (P.scaling && !(ts && n > 4)) {
+                const int off[4] = {0, 6 * 16, 6 * (16 + 64), 6 * (16 + 64 + 256)};
+                m = P.scaling + off[log2 - 2] + (intra ? c : 3 + c) * (n * n);
+            }
+            // dequant, transform.rs:84-108
+            for (int i = lane; i < (int)cnt; i += 32) {
+                int y = i / (mx + 1), x = i % (mx + 1);
+                int v = co[y * n + x];
+                if (v) {
+                    long long f = m ? m[y * n + x] : 16;
+                    long long r = ((long long)v * f * scale + round) >> bd_shift;
+                    co[y * n + x] = (int32_t)(r < -32768 ? -32768 : r > 32767 ? 32767 : r);
+                }
+            }
+            __syncwarp();
+            const int bs2 = 20 - bd, round2 = 1 << (bs2 - 1);
+            if (ts) {  // transform_skip, transform.rs:73-81
+                for (int i = lane; i < n * n; i += 32)
+                    co[i] = clampi(((co[i] << (5 + log2)) + round2) >> bs2, -32768, 32767);
+            } else if (mx == 0 && my == 0 && !(intra && c == 0 && n == 4)) {  // inverse_dc, transform.rs:68-71
+                int e = clampi((64 * co[0] + 64) >> 7, -32768, 32767);
+                int v = clampi((64 * e + round2) >> bs2, -32768, 32767);
+                __syncwarp();
+                for (int i = lane; i < n * n; i += 32) co[i] = v;
+            } else {  // inverse::<N>, transform.rs:26-66
+                const bool dst = intra && c == 0 && n == 4;
+                const int step = 32 / n;
+                for (int pr = lane; pr < (mx + 1) * n; pr += 32) {
+                    int x = pr / n, i = pr % n, acc = 0;
+                    for (int j = 0; j <= my; j++) acc += (dst ? cDST[j][i] : mat[j * step][i]) * co[j * n + x];
+                    col[x * n + i] = clampi((acc + 64) >> 7, -32768, 32767);
+                }
+                __syncwarp();
+                for (int pr = lane; pr < n * n; pr += 32) {
+                    int y = pr / n, i = pr % n, out = round2;
+                    for (int j = 0; j <= mx; j++) out += (dst ? cDST[j][i] : mat[j * step][i]) * col[j * n + y];
+                    co[y * n + i] = clampi(out >> bs2, -32768, 32767);
+                }
+            }
+            __syncwarp();
+        }
+        for (int i = lane; i < n * n; i += 32) rp[(i >> log2) * rpitch + (i & (n - 1))] = (int16_t)co[i];
+        __syncwarp();
+    }
+}
+
+// ===========================================================================
+// Inter prediction (src/hevc/inter.rs, motion_compensate of slicedec.rs)
+// ===========================================================================
+template <class T>
+__device__ __forceinline__ int rsamp(const T *p, int pitch, int w, int h, int x, int y) {
+    return __ldg(p + (size_t)clampi(y, 0, h - 1) * pitch + clampi(x, 0, w - 1));
+}
+
+// interpolate, inter.rs:86-133, one sample at integer position (xi, yi)
+template <class T, int TAPS>
+__device__ int interp(const T *p, int pitch, int w, int h, int xi, int yi, int fx, int fy, int bd) {
+    constexpr int m = TAPS / 2 - 1;
+    const int shift1 = min(bd, 12) - 8, shift3 = 14 - bd;
+    if (fx == 0 && fy == 0) return (int16_t)(rsamp(p, pitch, w, h, xi, yi) << shift3);
+    const int8_t *hf = TAPS == 8 ? cLUMA_F[fx] : cCHROMA_F[fx];
+    const int8_t *vf = TAPS == 8 ? cLUMA_F[fy] : cCHROMA_F[fy];
+    if (fy == 0) {
+        int s = 0;
+#pragma unroll
+        for (int k = 0; k < TAPS; k++) s += hf[k] * rsamp(p, pitch, w, h, xi - m + k, yi);
+        return (int16_t)(s >> shift1);
+    }
+    if (fx == 0) {
+        int s = 0;
+#pragma unroll
+        for (int k = 0; k < TAPS; k++) s += vf[k] * rsamp(p, pitch, w, h, xi, yi - m + k);
+        return (int16_t)(s >> shift1);
+    }
+    int v = 0;
+#pragma unroll
+    for (int r = 0; r < TAPS; r++) {
+        int s = 0;
+#pragma unroll
+        for (int k = 0; k < TAPS; k++) s += hf[k] * rsamp(p, pitch, w, h, xi - m + k, yi - m + r);
+        v += vf[r] * (int16_t)(s >> shift1);
+    }
+    return (int16_t)(v >> 6);
+}
+
+// motion_compensate + put_uni / put_bi / put_weighted_*, for one sample
+template <class T>
+__device__ int mc_sample(const HevcLaunch &P, int c, int x, int y, const rc_hevc_mvf &f, const rc_hevc_slice *sl) {
+    const int bd = P.bd, max = (1 << bd) - 1;
+    int pv[2] = {0, 0};
+    bool use[2] = {false, false};
+    const int pw = c ? P.CW : P.W, ph = c ? P.CH : P.H, pitch = pitch_el(P, c, sizeof(T));
+#pragma unroll
+    for (int l = 0; l < 2; l++) {
+        int ri = f.ref_idx[l];
+        if (ri < 0) continue;
+        int slot = ri < min(sl->num_ref[l], RC_HEVC_MAX_REFS) ? sl->ref_slot[l][ri] : -1;
+        if (slot < 0 || slot >= P.dpb_slots) { atomicOr(P.error, RC_DEV_ERR_RECORD); continue; }
+        use[l] = true;
+        const T *p = plane_ptr<T>(P.dpb + (size_t)slot * P.slot_bytes, P, c);
+        int mvx = f.mv[l][0], mvy = f.mv[l][1];
+        if (c == 0) pv[l] = interp<T, 8>(p, pitch, pw, ph, x + (mvx >> 2), y + (mvy >> 2), mvx & 3, mvy & 3, bd);
+        else pv[l] = interp<T, 4>(p, pitch, pw, ph, x + (mvx >> 3), y + (mvy >> 3), mvx & 7, mvy & 7, bd);
+    }
+    const bool bi = use[0] && use[1];
+    if (!sl->weighted) {
+        if (bi) {
+            const int shift = 15 - bd;
+            return clampi((pv[0] + pv[1] + (1 << (shift - 1))) >> shift, 0, max);
+        }
+        const int shift = 14 - bd, off = shift > 0 ? 1 << (shift - 1) : 0;
+        return clampi((pv[use[0] ? 0 : 1] + off) >> shift, 0, max);
+    }
+    const int log2wd = (c ? sl->chroma_log2_denom : sl->luma_log2_denom) + 14 - bd;
+    int w[2] = {0, 0}, o[2] = {0, 0};
+#pragma unroll
+    for (int l = 0; l < 2; l++) {
+        if (!use[l]) continue;
+        int ri = f.ref_idx[l];
+        w[l] = c ? sl->chroma_w[l][ri][c - 1] : sl->luma_w[l][ri];
+        o[l] = (c ? sl->chroma_o[l][ri][c - 1] : sl->luma_o[l][ri]) * (1 << (bd - 8));
+    }
+    if (bi) return clampi((pv[0] * w[0] + pv[1] * w[1] + ((o[0] + o[1] + 1) << log2wd)) >> (log2wd + 1), 0, max);
+    const int l = use[0] ? 0 : 1;
+    int v = pv[l] * w[l];
+    v = log2wd >= 1 ? ((v + (1 << (log2wd - 1))) >> log2wd) + o[l] : v + o[l];
+    return clampi(v, 0, max);
+}
+
+// One CTA per 8x8 luma block: 64 luma samples + 2x16 chroma samples.
+template <class T>
+__global__ void __launch_bounds__(64) hevc_inter_kernel(HevcLaunch P) {
+    const int t = threadIdx.x;
+    const int bx8 = blockIdx.x, by8 = blockIdx.y;
+    uint8_t *work = P.work;
+    const int max = (1 << P.bd) - 1;
+    {
+        const int x = bx8 * 8 + (t & 7), y = by8 * 8 + (t >> 3);
+        const int bi = (y >> 2) * P.w4 + (x >> 2);
+        const rc_hevc_blk b = P.blk[bi];
+        if ((b.flags & RC_HEVC_F_CODED) && !(b.flags & RC_HEVC_F_INTRA)) {
+            const rc_hevc_mvf f = P.mvf[bi];
+            const rc_hevc_slice *sl = slice_of_ctb(P, ctb_of(P, x, y));
+            int v = mc_sample<T>(P, 0, x, y, f, sl);
+            v = clampi(v + res_plane(P, 0)[(size_t)y * P.W + x], 0, max);
+            plane_ptr<T>(work, P, 0)[(size_t)y * pitch_el(P, 0, sizeof(T)) + x] = (T)v;
+        }
+    }
+    if (t < 32) {
+        const int c = 1 + (t >> 4), x = bx8 * 4 + (t & 3), y = by8 * 4 + ((t >> 2) & 3);
+        const int bi = ((2 * y) >> 2) * P.w4 + ((2 * x) >> 2);
+        const rc_hevc_blk b = P.blk[bi];
+        if ((b.flags & RC_HEVC_F_CODED) && !(b.flags & RC_HEVC_F_INTRA)) {
+            const rc_hevc_mvf f = P.mvf[bi];
+            const rc_hevc_slice *sl = slice_of_ctb(P, ctb_of(P, 2 * x, 2 * y));
+            int v = mc_sample<T>(P, c, x, y, f, sl);
+            v = clampi(v + res_plane(P, c)[(size_t)y * P.CW + x], 0, max);
+            plane_ptr<T>(work, P, c)[(size_t)y * pitch_el(P, c, sizeof(T)) + x] = (T)v;
+        }
+    }
+}
+
+// ===========================================================================
+// Intra prediction in decode order (src/hevc/intra.rs, intra_predict of
+// src/hevc/slicedec.rs:1673-1738)
+// ===========================================================================
+__device__ __forceinline__ uint32_t morton4(uint32_t x, uint32_t y) {
+    uint32_t r = 0;
+#pragma unroll
+    for (int i = 0; i < 5; i++) r |= ((x >> i) & 1u) << (2 * i) | ((y >> i) & 1u) << (2 * i + 1);
+    return r;
+}
+// zavail, src/hevc/slicedec.rs:625-643 (luma coordinates)
+__device__ bool zavail(const HevcLaunch &P, int xc, int yc, int xn, int yn) {
+    if (xn < 0 || yn < 0 || xn >= P.W || yn >= P.H) return false;
+    const int s = P.log2ctb;
+    const int cn = (yn >> s) * P.wctb + (xn >> s), cc = (yc >> s) * P.wctb + (xc >> s);
+    if (cn != cc) {
+        const rc_hevc_ctb &n = P.ctbs[cn], &q = P.ctbs[cc];
+        return n.ts < q.ts && slice_addr(P, cn) == slice_addr(P, cc) && n.tile == q.tile;
+    }
+    const int m = (1 << s) - 1;
+    return morton4((xn & m) >> 2, (yn & m) >> 2) <= morton4((xc & m) >> 2, (yc & m) >> 2);
+}
+
+struct __align__(16) IntraSmem {
+    uint16_t left[136], top[136];   // reference samples (index 0 = corner)
+    uint16_t fleft[136], ftop[136]; // smoothed copy
+    uint8_t al[136], at[136];
+    int refa[200];
+};
+
+template <class T>
+__device__ void intra_tu(const HevcLaunch &P, IntraSmem &S, const rc_hevc_tu &t, int lane) {
+    const int log2 = t.log2, n = 1 << log2, c = t.c, sc = c ? 2 : 1, unit = 4 / sc;
+    const int x0 = t.x0, y0 = t.y0, xl = x0 * sc, yl = y0 * sc, bd = P.bd, max = (1 << bd) - 1;
+    T *pl = plane_ptr<T>(P.work, P, c);
+    const int pitch = pitch_el(P, c, sizeof(T));
+    const int n2 = 2 * n, nunits = 1 + 2 * (n2 / unit);
+    // ---- availability of each reference unit; wait for intra neighbours
+    bool ok = true;
+    for (int u = lane; u < nunits; u += 32) {
+        int xn, yn;
+        if (u == 0) { xn = xl - 1; yn = yl - 1; }
+        else if (u <= n2 / unit) { xn = xl - 1; yn = (y0 + (u - 1) * unit) * sc; }
+        else { xn = (x0 + (u - 1 - n2 / unit) * unit) * sc; yn = yl - 1; }
+        bool a = zavail(P, xl, yl, xn, yn);
+        uint8_t bf = a ? P.blk[(yn >> 2) * P.w4 + (xn >> 2)].flags : 0;
+        if (a && P.constrained_intra && !(bf & RC_HEVC_F_INTRA)) a = false;
+        if (a && (bf & RC_HEVC_F_INTRA))
+            ok = ok && wait_flag(P.ready + (size_t)c * P.w4 * P.h4 + (yn >> 2) * P.w4 + (xn >> 2), P.epoch, P.wait_limit,
+                                 P.error);
+        if (u == 0) S.al[0] = S.at[0] = a;
+        else if (u <= n2 / unit) for (int i = 0; i < unit; i++) S.al[1 + (u - 1) * unit + i] = a;
+        else for (int i = 0; i < unit; i++) S.at[1 + (u - 1 - n2 / unit) * unit + i] = a;
+    }
+    if (!__all_sync(0xffffffffu, ok)) {
+        if (lane == 0) atomicOr(P.error, RC_DEV_ERR_TIMEOUT);
+        return;
+    }
+    __syncwarp();
+    // ---- reference samples (pre-deblock picture)
+    for (int i = lane; i <= n2; i += 32) {
+        if (i == 0) {
+            uint16_t v = S.al[0] ? (uint16_t)__ldcg(pl + (size_t)(y0 - 1) * pitch + x0 - 1) : 0;
+            S.left[0] = S.top[0] = v;
+        } else {
+            S.left[i] = S.al[i] ? (uint16_t)__ldcg(pl + (size_t)(y0 + i - 1) * pitch + x0 - 1) : 0;
+            S.top[i] = S.at[i] ? (uint16_t)__ldcg(pl + (size_t)(y0 - 1) * pitch + x0 + i - 1) : 0;
+        }
+    }
+    __syncwarp();
+    // ---- substitute, src/hevc/intra.rs:19-65 (sequential scan)
+    if (lane == 0) {
+        bool any = false;
+        for (int i = 0; i <= n2; i++) any |= S.al[i];
+        for (int i = 1; i <= n2; i++) any |= S.at[i];
+        if (!any) {
+            for (int i = 0; i <= n2; i++) S.left[i] = S.top[i] = (uint16_t)(1 << (bd - 1));
+        } else {
+            if (!S.al[n2]) {
+                int found = -1;
+                for (int y = n2 - 1; y >= 0 && found < 0; y--)
+                    if (S.al[y]) found = S.left[y];
+                for (int x = 1; x <= n2 && found < 0; x++)
+                    if (S.at[x]) found = S.top[x];
+                S.left[n2] = (uint16_t)(found < 0 ? 0 : found);
+            }
+            for (int y = n2 - 1; y >= 0; y--)
+                if (!S.al[y]) S.left[y] = S.left[y + 1];
+            S.top[0] = S.left[0];
+            for (int x = 1; x <= n2; x++)
+                if (!S.at[x]) S.top[x] = S.top[x - 1];
+        }
+    }
+    __syncwarp();
+    const int mode = t.mode;
+    // ---- filter, src/hevc/intra.rs:67-111 (luma only)
+    const uint16_t *L = S.left, *Tp = S.top;
+    if (c == 0 && mode != 1 && n != 4) {
+        int md = min(abs(mode - 26), abs(mode - 10));
+        int thres = n == 8 ? 7 : n == 16 ? 1 : 0;
+        if (md > thres) {
+            const int cc = S.left[0];
+            bool strong = false;
+            if (P.strong_intra && n == 32) {
+                int bl = S.left[n2], tr = S.top[n2], thr = 1 << (bd - 5);
+                strong = abs(cc + tr - 2 * S.top[n]) < thr && abs(cc + bl - 2 * S.left[n]) < thr;
+                if (strong) {
+                    for (int i = lane; i < 63; i += 32) {
+                        S.fleft[1 + i] = (uint16_t)(((63 - i) * cc + (i + 1) * bl + 32) >> 6);
+                        S.ftop[1 + i] = (uint16_t)(((63 - i) * cc + (i + 1) * tr + 32) >> 6);
+                    }
+                    if (lane == 0) {
+                        S.fleft[0] = S.left[0]; S.ftop[0] = S.top[0];
+                        S.fleft[64] = S.left[64]; S.ftop[64] = S.top[64];
+                    }
+                }
+            }
+            if (!strong) {
+                for (int i = lane; i <= n2; i += 32) {
+                    if (i == 0) S.fleft[0] = S.ftop[0] = (uint16_t)((S.left[1] + 2 * cc + S.top[1] + 2) >> 2);
+                    else if (i == n2) { S.fleft[i] = S.left[i]; S.ftop[i] = S.top[i]; }
+                    else {
+                        S.fleft[i] = (uint16_t)((S.left[i - 1] + 2 * S.left[i] + S.left[i + 1] + 2) >> 2);
+                        S.ftop[i] = (uint16_t)((S.top[i - 1] + 2 * S.top[i] + S.top[i + 1] + 2) >> 2);
+                    }
+                }
+            }
+            L = S.fleft;
+            Tp = S.ftop;
+        }
+    }
+    __syncwarp();
+    // ---- predict, src/hevc/intra.rs:113-222
+    const bool edge = c == 0 && n < 32;
+    int dc = 0;
+    if (mode == 1) {
+        int s = 0;
+        for (int i = lane; i < n; i += 32) s += Tp[1 + i] + L[1 + i];
+        s = __reduce_add_sync(0xffffffffu, (unsigned)s);
+        dc = (s + n) >> (log2 + 1);
+    } else if (mode >= 2) {
+        const int angle = cANGLE[mode], base = n;
+        const uint16_t *mn = mode >= 18 ? Tp : L, *sd = mode >= 18 ? L : Tp;
+        for (int x = lane; x <= 2 * n; x += 32) {
+            if (x <= n) S.refa[base + x] = mn[x];
+            else if (angle >= 0) S.refa[base + x] = mn[x];
+        }
+        if (angle < 0) {
+            const int lim = (n * angle) >> 5;
+            if (lim < -1) {
+                const int inv = cINV_ANGLE[mode - 11];
+                for (int x = lim + lane; x <= -1; x += 32) S.refa[base + x] = sd[-1 + ((x * inv + 128) >> 8) + 1];
+            }
+        }
+        __syncwarp();
+    }
+    const int16_t *rp = res_plane(P, c);
+    const int rpitch = c ? P.CW : P.W;
+    for (int i = lane; i < n * n; i += 32) {
+        const int y = i >> log2, x = i & (n - 1);
+        int v;
+        if (mode == 0) {
+            v = ((n - 1 - x) * L[1 + y] + (x + 1) * Tp[1 + n] + (n - 1 - y) * Tp[1 + x] + (y + 1) * L[1 + n] + n) >>
+                (log2 + 1);
+        } else if (mode == 1) {
+            v = dc;
+            if (edge) {
+                if (x == 0 && y == 0) v = (L[1] + 2 * dc + Tp[1] + 2) >> 2;
+                else if (y == 0) v = (Tp[1 + x] + 3 * dc + 2) >> 2;
+                else if (x == 0) v = (L[1 + y] + 3 * dc + 2) >> 2;
+            }
+        } else {
+            const int angle = cANGLE[mode];
+            const bool horizontal = mode < 18;
+            // output (x, y): horizontal modes run j along x, vertical along y
+            const int j = horizontal ? x : y, ii = horizontal ? y : x;
+            const int pos = (j + 1) * angle, idx = pos >> 5, fact = pos & 31;
+            const int k = n + ii + idx + 1;
+            v = fact ? ((32 - fact) * S.refa[k] + fact * S.refa[k + 1] + 16) >> 5 : S.refa[k];
+            if (edge) {
+                if (mode == 26 && x == 0) v = clampi(Tp[1] + ((L[1 + y] - L[0]) >> 1), 0, max);
+                else if (mode == 10 && y == 0) v = clampi(L[1] + ((Tp[1 + x] - Tp[0]) >> 1), 0, max);
+            }
+        }
+        if (t.flags & RC_HEVC_TU_CBF) v = clampi(v + rp[(size_t)(y0 + y) * rpitch + x0 + x], 0, max);
+        pl[(size_t)(y0 + y) * pitch + x0 + x] = (T)v;
+    }
+}
+
+template <class T>
+__device__ void pcm_tu(const HevcLaunch &P, const rc_hevc_tu &t, int lane) {
+    const int n = 1 << t.log2;
+    T *pl = plane_ptr<T>(P.work, P, t.c);
+    const int pitch = pitch_el(P, t.c, sizeof(T));
+    if (t.coef_off + (unsigned long long)n * n > P.num_levels) {
+        if (lane == 0) atomicOr(P.error, RC_DEV_ERR_RECORD);
+        return;
+    }
+    const int16_t *s = P.levels + t.coef_off;
+    for (int i = lane; i < n * n; i += 32) pl[(size_t)(t.y0 + (i >> t.log2)) * pitch + t.x0 + (i & (n - 1))] = (T)s[i];
+}
+
+template <class T>
+__global__ void __launch_bounds__(128) hevc_intra_kernel(HevcLaunch P) {
+    __shared__ IntraSmem sm[4];
+    IntraSmem &S = sm[threadIdx.x >> 5];
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        unsigned ti = 0;
+        if (lane == 0) ti = aborted(P.error) ? 0xffffffffu : atomicAdd(P.counter, 1u);
+        ti = __shfl_sync(0xffffffffu, ti, 0);
+        if (ti >= (unsigned)P.num_tus) return;
+        const rc_hevc_tu t = P.tus[ti];
+        if (!(t.flags & RC_HEVC_TU_INTRA)) continue;
+        const int n = 1 << t.log2, sc = t.c ? 2 : 1;
+        if (t.log2 < 2 || t.log2 > 5 || t.c > 2 || t.mode > 34 || (t.x0 + n) * sc > P.W || (t.y0 + n) * sc > P.H) {
+            if (lane == 0) atomicOr(P.error, RC_DEV_ERR_RECORD);
+            continue;
+        }
+        if (t.flags & RC_HEVC_TU_PCM) pcm_tu<T>(P, t, lane);
+        else intra_tu<T>(P, S, t, lane);
+        if (aborted(P.error)) return;
+        __threadfence();
+        __syncwarp();
+        // publish the 4x4 luma-grid blocks this TU covers
+        const int bw = (n * sc) >> 2, bx0 = (t.x0 * sc) >> 2, by0 = (t.y0 * sc) >> 2;
+        uint32_t *rdy = P.ready + (size_t)t.c * P.w4 * P.h4;
+        for (int i = lane; i < bw * bw; i += 32) st_release(rdy + (size_t)(by0 + i / bw) * P.w4 + bx0 + i % bw, P.epoch);
+    }
+}
+
+// ===========================================================================
+// Deblocking, src/hevc/filter.rs:75-519
+// ===========================================================================
+__device__ __forceinline__ uint32_t h_ref_id(const HevcLaunch &P, int ctb, const rc_hevc_mvf &f, int l) {
+    const rc_hevc_slice *sl = slice_of_ctb(P, ctb);
+    int r = f.ref_idx[l];
+    return (r >= 0 && r < min(sl->num_ref[l], RC_HEVC_MAX_REFS)) ? sl->ref_id[l][r] : 0xfffffffeu;
+}
+__device__ __forceinline__ bool far_mv(const int16_t *a, const int16_t *b) {
+    return abs(a[0] - b[0]) >= 4 || abs(a[1] - b[1]) >= 4;
+}
+// boundary_strength + motion_bs, filter.rs:84-144
+__device__ int boundary_strength(const HevcLaunch &P, int pi, int qi, bool tu_edge, int pctb, int qctb) {
+    const rc_hevc_blk p = P.blk[pi], q = P.blk[qi];
+    if ((p.flags | q.flags) & RC_HEVC_F_INTRA) return 2;
+    if (tu_edge && ((p.flags | q.flags) & RC_HEVC_F_CBF)) return 1;
+    const rc_hevc_mvf mp = P.mvf[pi], mq = P.mvf[qi];
+    const int np = (mp.ref_idx[0] >= 0) + (mp.ref_idx[1] >= 0), nq = (mq.ref_idx[0] >= 0) + (mq.ref_idx[1] >= 0);
+    if (np != nq) return 1;
+    if (np == 1) {
+        int lp = mp.ref_idx[0] >= 0 ? 0 : 1, lq = mq.ref_idx[0] >= 0 ? 0 : 1;
+        if (h_ref_id(P, pctb, mp, lp) != h_ref_id(P, qctb, mq, lq)) return 1;
+        return far_mv(mp.mv[lp], mq.mv[lq]);
+    }
+    uint32_t p0 = h_ref_id(P, pctb, mp, 0), p1 = h_ref_id(P, pctb, mp, 1);
+    uint32_t q0 = h_ref_id(P, qctb, mq, 0), q1 = h_ref_id(P, qctb, mq, 1);
+    if (!((p0 == q0 && p1 == q1) || (p0 == q1 && p1 == q0))) return 1;
+    if (p0 != p1) {
+        if (p0 == q0) return far_mv(mp.mv[0], mq.mv[0]) || far_mv(mp.mv[1], mq.mv[1]);
+        return far_mv(mp.mv[0], mq.mv[1]) || far_mv(mp.mv[1], mq.mv[0]);
+    }
+    return (far_mv(mp.mv[0], mq.mv[0]) || far_mv(mp.mv[1], mq.mv[1])) &&
+           (far_mv(mp.mv[0], mq.mv[1]) || far_mv(mp.mv[1], mq.mv[0]));
+}
+// edge_params, filter.rs:146-176
+__device__ bool edge_params(const HevcLaunch &P, int px, int py, int qx, int qy, int &tc_off, int &beta_off) {
+    const int pc = ctb_of(P, px, py), qc = ctb_of(P, qx, qy);
+    const rc_hevc_slice *sq = slice_of_ctb(P, qc);
+    if (sq->deblock_disabled) return false;
+    if (pc != qc) {
+        if (slice_addr(P, pc) != slice_addr(P, qc) && !sq->lf_across) return false;
+        if (!P.lf_across_tiles && P.ctbs[pc].tile != P.ctbs[qc].tile) return false;
+    }
+    tc_off = sq->tc_offset;
+    beta_off = sq->beta_offset;
+    return true;
+}
+
+// filter_luma, filter.rs:409-492; o = q0 of line 0
+template <class T>
+__device__ void filter_luma(T *s, long o, long step, long along, int tc, int beta, bool nfp, bool nfq, int bd) {
+#define PX(k, i) ((int)s[o + (k) * along - ((i) + 1) * step])
+#define QX(k, i) ((int)s[o + (k) * along + (i) * step])
+    const int dp0 = abs(PX(0, 2) - 2 * PX(0, 1) + PX(0, 0)), dp3 = abs(PX(3, 2) - 2 * PX(3, 1) + PX(3, 0));
+    const int dq0 = abs(QX(0, 2) - 2 * QX(0, 1) + QX(0, 0)), dq3 = abs(QX(3, 2) - 2 * QX(3, 1) + QX(3, 0));
+    const int dpq0 = dp0 + dq0, dpq3 = dp3 + dq3, dp = dp0 + dp3, dq = dq0 + dq3, d = dpq0 + dpq3;
+    if (d >= beta) return;
+#define DSAM(k, dpq)                                                                                     \
+    ((dpq) < (beta >> 2) && abs(PX(k, 3) - PX(k, 0)) + abs(QX(k, 0) - QX(k, 3)) < (beta >> 3) &&      \
+     abs(PX(k, 0) - QX(k, 0)) < ((5 * tc + 1) >> 1))
+    const bool strong = DSAM(0, 2 * dpq0) && DSAM(3, 2 * dpq3);
+#undef DSAM
+#undef PX
+#undef QX
+    const bool dep = dp < ((beta + (beta >> 1)) >> 3), deq = dq < ((beta + (beta >> 1)) >> 3);
+    const int max = (1 << bd) - 1;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const long b = o + k * along;
+        const int p0 = s[b - step], p1 = s[b - 2 * step], p2 = s[b - 3 * step], p3 = s[b - 4 * step];
+        const int q0 = s[b], q1 = s[b + step], q2 = s[b + 2 * step], q3 = s[b + 3 * step];
+        if (strong) {
+            const int t2 = 2 * tc;
+            if (!nfp) {
+                s[b - step] = (T)clampi((p2 + 2 * p1 + 2 * p0 + 2 * q0 + q1 + 4) >> 3, p0 - t2, p0 + t2);
+                s[b - 2 * step] = (T)clampi((p2 + p1 + p0 + q0 + 2) >> 2, p1 - t2, p1 + t2);
+                s[b - 3 * step] = (T)clampi((2 * p3 + 3 * p2 + p1 + p0 + q0 + 4) >> 3, p2 - t2, p2 + t2);
+            }
+            if (!nfq) {
+                s[b] = (T)clampi((p1 + 2 * p0 + 2 * q0 + 2 * q1 + q2 + 4) >> 3, q0 - t2, q0 + t2);
+                s[b + step] = (T)clampi((p0 + q0 + q1 + q2 + 2) >> 2, q1 - t2, q1 + t2);
+                s[b + 2 * step] = (T)clampi((p0 + q0 + q1 + 3 * q2 + 2 * q3 + 4) >> 3, q2 - t2, q2 + t2);
+            }
+        } else {
+            int delta = (9 * (q0 - p0) - 3 * (q1 - p1) + 8) >> 4;
+            if (abs(delta) >= tc * 10) continue;
+            delta = clampi(delta, -tc, tc);
+            if (!nfp) s[b - step] = (T)clampi(p0 + delta, 0, max);
+            if (!nfq) s[b] = (T)clampi(q0 - delta, 0, max);
+            if (dep && !nfp) s[b - 2 * step] = (T)clampi(p1 + clampi((((p2 + p0 + 1) >> 1) - p1 + delta) >> 1, -(tc >> 1), tc >> 1), 0, max);
+            if (deq && !nfq) s[b + step] = (T)clampi(q1 + clampi((((q2 + q0 + 1) >> 1) - q1 - delta) >> 1, -(tc >> 1), tc >> 1), 0, max);
+        }
+    }
+}
+// filter_chroma, filter.rs:494-519
+template <class T>
+__device__ void filter_chroma(T *s, long o, long step, long along, int tc, bool nfp, bool nfq, int bd) {
+    const int max = (1 << bd) - 1;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const long b = o + k * along;
+        const int p0 = s[b - step], p1 = s[b - 2 * step], q0 = s[b], q1 = s[b + step];
+        const int delta = clampi((((q0 - p0) << 2) + p1 - q1 + 4) >> 3, -tc, tc);
+        if (!nfp) s[b - step] = (T)clampi(p0 + delta, 0, max);
+        if (!nfq) s[b] = (T)clampi(q0 - delta, 0, max);
+    }
+}
+
+// One thread per edge segment.  dir 0: vertical edges (luma segments at
+// x = 8k, 4 rows; chroma at luma x = 16k, 8 luma rows), dir 1 horizontal.
+template <class T, int DIR>
+__global__ void __launch_bounds__(128) hevc_deblock_kernel(HevcLaunch P) {
+    const int nl = DIR == 0 ? ((P.w4 - 1) / 2) * P.h4 : P.w4 * ((P.h4 - 1) / 2);
+    const int nc = DIR == 0 ? ((P.w4 - 1) / 4) * ((P.h4 + 1) / 2) : ((P.w4 + 1) / 2) * ((P.h4 - 1) / 4);
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nl + nc) return;
+    const bool chroma = i >= nl;
+    const int j = chroma ? i - nl : i;
+    int bx, by;
+    if (DIR == 0) {
+        const int ne = chroma ? (P.w4 - 1) / 4 : (P.w4 - 1) / 2;
+        bx = chroma ? 4 * (1 + j % ne) : 2 * (1 + j % ne);
+        by = chroma ? 2 * (j / ne) : j / ne;
+    } else {
+        const int ne = chroma ? (P.w4 + 1) / 2 : P.w4;
+        bx = chroma ? 2 * (j % ne) : j % ne;
+        by = chroma ? 4 * (1 + j / ne) : 2 * (1 + j / ne);
+    }
+    const int qi = by * P.w4 + bx, pi = DIR == 0 ? qi - 1 : qi - P.w4;
+    const int x = bx * 4, y = by * 4;
+    const int px = DIR == 0 ? x - 1 : x, py = DIR == 0 ? y : y - 1;
+    const rc_hevc_blk q = P.blk[qi], p = P.blk[pi];
+    const int emask = DIR == 0 ? (RC_HEVC_E_TU_V | RC_HEVC_E_PU_V) : (RC_HEVC_E_TU_H | RC_HEVC_E_PU_H);
+    if (!(q.edges & emask) || !(q.flags & RC_HEVC_F_CODED)) return;
+    int tco, bo;
+    if (!edge_params(P, px, py, x, y, tco, bo)) return;
+    const int bs = boundary_strength(P, pi, qi, (q.edges & (DIR == 0 ? RC_HEVC_E_TU_V : RC_HEVC_E_TU_H)) != 0,
+                                     ctb_of(P, px, py), ctb_of(P, x, y));
+    const bool nfp = p.flags & RC_HEVC_F_NOFILTER, nfq = q.flags & RC_HEVC_F_NOFILTER;
+    const int bd = P.bd;
+    if (!chroma) {
+        if (bs == 0) return;
+        // tc_beta, filter.rs:74-82
+        const int qpl = (p.qp + q.qp + 1) >> 1;
+        const int qb = clampi(qpl + bo, 0, 51), qt = clampi(qpl + 2 * (bs - 1) + tco, 0, 53);
+        const int tc = cTC[qt] << (bd - 8), beta = cBETA[qb] << (bd - 8);
+        T *s = plane_ptr<T>(P.work, P, 0);
+        const long pitch = pitch_el(P, 0, sizeof(T));
+        filter_luma<T>(s, (long)y * pitch + x, DIR == 0 ? 1 : pitch, DIR == 0 ? pitch : 1, tc, beta, nfp, nfq, bd);
+    } else {
+        if (bs != 2) return;
+        for (int c = 1; c < 3; c++) {
+            const int qpi = ((p.qp + q.qp + 1) >> 1) + (c == 1 ? P.cb_qp_offset : P.cr_qp_offset);
+            const int qt = clampi(qpc_420(qpi) + 2 + tco, 0, 53), tc = cTC[qt] << (bd - 8);
+            T *s = plane_ptr<T>(P.work, P, c);
+            const long pitch = pitch_el(P, c, sizeof(T));
+            filter_chroma<T>(s, (long)(y / 2) * pitch + x / 2, DIR == 0 ? 1 : pitch, DIR == 0 ? pitch : 1, tc, nfp, nfq, bd);
+        }
+    }
+}
+
+// ===========================================================================
+// SAO, src/hevc/filter.rs:521-894: one thread per sample, deblocked work
+// picture -> DPB slot
+// ===========================================================================
+// cross_ok, filter.rs:605-632
+__device__ bool cross_ok(const HevcLaunch &P, int rs, int nrs) {
+    if (nrs == rs) return true;
+    const rc_hevc_ctb &n = P.ctbs[nrs], &q = P.ctbs[rs];
+    if (n.slice >= P.num_slices) return false;
+    if (slice_addr(P, nrs) != slice_addr(P, rs)) {
+        if (n.ts < q.ts && !slice_of_ctb(P, rs)->lf_across) return false;
+        if (q.ts < n.ts && !P.slices[n.slice].lf_across) return false;
+    }
+    return P.lf_across_tiles || n.tile == q.tile;
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) hevc_sao_kernel(HevcLaunch P) {
+    const int c = blockIdx.z, sc = c ? 1 : 0;
+    const int w = c ? P.CW : P.W, h = c ? P.CH : P.H;
+    const int x = blockIdx.x * 32 + (threadIdx.x & 31), y = blockIdx.y * 8 + (threadIdx.x >> 5);
+    if (x >= w || y >= h) return;
+    const long pitch = pitch_el(P, c, sizeof(T));
+    const T *in = plane_ptr<T>(P.work, P, c);
+    T *out = plane_ptr<T>(P.dpb + (size_t)P.out_slot * P.slot_bytes, P, c);
+    const int v = in[(size_t)y * pitch + x];
+    int res = v;
+    const int s = P.log2ctb - sc;
+    const int rs = (y >> s) * P.wctb + (x >> s);
+    const rc_hevc_ctb &ct = P.ctbs[rs];
+    const rc_hevc_slice *sl = slice_of_ctb(P, rs);
+    const int type = ct.sao.type_idx[c];
+    const bool nof = P.blk[((y << sc) >> 2) * P.w4 + ((x << sc) >> 2)].flags & RC_HEVC_F_NOFILTER;
+    if ((c ? sl->sao_chroma : sl->sao_luma) && type != 0 && !nof && ct.slice < P.num_slices) {
+        const int bd = P.bd, max = (1 << bd) - 1;
+        if (type == 1) {
+            const int band = v >> (bd - 5), k = (band - ct.sao.band_pos[c]) & 31;
+            if (k < 4) res = clampi(v + ct.sao.offsets[c][k], 0, max);
+        } else {
+            const int cls = ct.sao.eo_class[c] & 3;
+            const int hp0 = cls == 1 ? 0 : cls == 3 ? 1 : -1, hp1 = -hp0;
+            const int vp0 = cls == 0 ? 0 : -1, vp1 = -vp0;
+            bool ok = true;
+            int sum = 0;
+#pragma unroll
+            for (int j = 0; j < 2; j++) {
+                const int xn = x + (j ? hp1 : hp0), yn = y + (j ? vp1 : vp0);
+                if (xn < 0 || yn < 0 || xn >= w || yn >= h) { ok = false; break; }
+                const int nrs = (yn >> s) * P.wctb + (xn >> s);
+                if (!cross_ok(P, rs, nrs)) { ok = false; break; }
+                const int nv = in[(size_t)yn * pitch + xn];
+                sum += (v > nv) - (v < nv);
+            }
+            if (ok) {
+                // edge_map [1, 2, 0, 3, 4]: sum -2 -> offsets[0], -1 -> [1], 0 -> none, 1 -> [2], 2 -> [3]
+                const int e = sum == -2 ? 0 : sum == -1 ? 1 : sum == 1 ? 2 : sum == 2 ? 3 : -1;
+                if (e >= 0) res = clampi(v + ct.sao.offsets[c][e], 0, max);
+            }
+        }
+    }
+    out[(size_t)y * pitch + x] = (T)res;
+}
+
+template <class T>
+void launch_all_deblock(const HevcLaunch &p, cudaStream_t st) {
+    const int nv = ((p.w4 - 1) / 2) * p.h4 + ((p.w4 - 1) / 4) * ((p.h4 + 1) / 2);
+    const int nh = p.w4 * ((p.h4 - 1) / 2) + ((p.w4 + 1) / 2) * ((p.h4 - 1) / 4);
+    if (nv > 0) hevc_deblock_kernel<T, 0><<<(nv + 127) / 128, 128, 0, st>>>(p);
+    if (nh > 0) hevc_deblock_kernel<T, 1><<<(nh + 127) / 128, 128, 0, st>>>(p);
+}
+
+}  // namespace
+
+void rc_launch_hevc_residual(const HevcLaunch &p, cudaStream_t st) {
+    cudaMemsetAsync(p.res, 0, ((size_t)p.W * p.H + 2 * (size_t)p.CW * p.CH) * sizeof(int16_t), st);
+    int blocks = (p.num_tus + 3) / 4;
+    blocks = blocks < 1 ? 1 : blocks > 4096 ? 4096 : blocks;
+    hevc_residual_kernel<<<blocks, 128, 0, st>>>(p);
+}
+
+void rc_launch_hevc_inter(const HevcLaunch &p, cudaStream_t st) {
+    dim3 grid(p.W / 8, p.H / 8);
+    if (p.bd > 8) hevc_inter_kernel<uint16_t><<<grid, 64, 0, st>>>(p);
+    else hevc_inter_kernel<uint8_t><<<grid, 64, 0, st>>>(p);
+}
+
+void rc_launch_hevc_intra(const HevcLaunch &p, cudaStream_t st, int blocks) {
+    cudaMemsetAsync(p.counter, 0, sizeof(uint32_t), st);
+    if (p.bd > 8) hevc_intra_kernel<uint16_t><<<blocks, 128, 0, st>>>(p);
+    else hevc_intra_kernel<uint8_t><<<blocks, 128, 0, st>>>(p);
+}
+
+void rc_launch_hevc_deblock(const HevcLaunch &p, cudaStream_t st) {
+    if (p.bd > 8) launch_all_deblock<uint16_t>(p, st);
+    else launch_all_deblock<uint8_t>(p, st);
+}
+
+void rc_launch_hevc_sao(const HevcLaunch &p, cudaStream_t st) {
+    dim3 grid((p.W + 31) / 32, (p.H + 7) / 8, 3);
+    if (p.bd > 8) hevc_sao_kernel<uint16_t><<<grid, 256, 0, st>>>(p);
+    else hevc_sao_kernel<uint8_t><<<grid, 256, 0, st>>>(p);
+}

@@ -62,6 +62,13 @@ struct rc_stream {
     uint32_t *rflag = nullptr, *dflag = nullptr, *counter = nullptr, *error = nullptr, *tasks = nullptr;
     uint32_t *rowprog = nullptr;
     DbMb *db = nullptr;
+    // HEVC
+    DevBuf ctbs, blk, mvf, tus, hslices, scaling;
+    uint8_t *work = nullptr;     // picture being reconstructed (pre-SAO)
+    int16_t *res = nullptr;      // residual planes
+    uint32_t *ready = nullptr;   // per 4x4 block and component
+    int w4 = 0, h4 = 0, log2ctb_alloc = 0;
+    int bps = 1;
     int ntasks = 0;
     DevBuf mbs, slices, weights, levels;
     int32_t *ls = nullptr;            // device ls4 (2304 ints) + ls8 (2304*4 ints)
@@ -239,7 +246,12 @@ void destroy(rc_stream *s) {
     drain_profile(s);
     for (cudaEvent_t e : s->ev_free) cudaEventDestroy(e);
     dev_free(s, s->dpb, s->slot_bytes * s->slots);
-    for (DevBuf *b : {&s->mbs, &s->slices, &s->weights, &s->levels}) dev_free(s, b->p, b->cap);
+    for (DevBuf *b : {&s->mbs, &s->slices, &s->weights, &s->levels, &s->ctbs, &s->blk, &s->mvf, &s->tus, &s->hslices,
+                      &s->scaling})
+        dev_free(s, b->p, b->cap);
+    cudaFree(s->work);
+    cudaFree(s->res);
+    cudaFree(s->ready);
     cudaFree(s->rflag);
     cudaFree(s->dflag);
     cudaFree(s->counter);
@@ -254,6 +266,105 @@ void destroy(rc_stream *s) {
     }
     if (s->st) cudaStreamDestroy(s->st);
     delete s;
+}
+
+struct Part {
+    DevBuf *dst;
+    const void *src;
+    size_t n;
+};
+
+// Copy host buffers to device buffers on the stream: directly when every
+// source is pinned, else through the stream's double-buffered pinned staging.
+int upload(rc_stream *s, Part *parts, int np) {
+    int rc;
+    for (int i = 0; i < np; i++)
+        if ((rc = ensure(s, *parts[i].dst, std::max<size_t>(parts[i].n, 64)))) return rc;
+    bool pinned = true;
+    for (int i = 0; i < np; i++) pinned = pinned && is_pinned(parts[i].src);
+    if (pinned) {
+        for (int i = 0; i < np; i++)
+            if (parts[i].n &&
+                cudaMemcpyAsync(parts[i].dst->p, parts[i].src, parts[i].n, cudaMemcpyHostToDevice, s->st) != cudaSuccess)
+                return cuda_fail(s);
+        return 0;
+    }
+    const int k = s->submits & 1;
+    size_t total = 0;
+    for (int i = 0; i < np; i++) total += align_up(parts[i].n, 256);
+    if (cudaEventSynchronize(s->staged[k]) != cudaSuccess) return cuda_fail(s);
+    if (total > s->staging_cap[k]) {
+        if (s->staging[k]) cudaFreeHost(s->staging[k]);
+        s->staging[k] = nullptr;
+        s->staging_cap[k] = 0;
+        size_t want = align_up(total + total / 4, 1 << 20);
+        if (cudaMallocHost(&s->staging[k], want) != cudaSuccess) return RC_ENOMEM;
+        s->staging_cap[k] = want;
+    }
+    uint8_t *stage = (uint8_t *)s->staging[k];
+    size_t off = 0;
+    for (int i = 0; i < np; i++) {
+        if (!parts[i].n) continue;
+        memcpy(stage + off, parts[i].src, parts[i].n);
+        if (cudaMemcpyAsync(parts[i].dst->p, stage + off, parts[i].n, cudaMemcpyHostToDevice, s->st) != cudaSuccess)
+            return cuda_fail(s);
+        off += align_up(parts[i].n, 256);
+    }
+    if (cudaEventRecord(s->staged[k], s->st) != cudaSuccess) return cuda_fail(s);
+    return 0;
+}
+
+struct HGeo {
+    int W, H, bd, slots;
+};
+
+// Host-side validation of an HEVC picture (ranges, reference indices,
+// payload bounds; src/hevc/slicedec.rs:2153-2160 rejects bad ref_idx).
+int validate_hevc(const HGeo *g, const rc_hevc_picture *p) {
+    if (p->log2_ctb < 4 || p->log2_ctb > 6 || p->num_slices <= 0 || !p->slices || !p->ctbs || !p->blk || !p->mvf)
+        return RC_EINVAL;
+    if (p->num_tus < 0 || (p->num_tus > 0 && !p->tus) || (p->num_levels > 0 && !p->levels)) return RC_EINVAL;
+    const int ctb = 1 << p->log2_ctb, wctb = (g->W + ctb - 1) / ctb, hctb = (g->H + ctb - 1) / ctb;
+    const int w4 = g->W / 4, h4 = g->H / 4, CW = g->W / 2, CH = g->H / 2;
+    for (int i = 0; i < p->num_slices; i++) {
+        const rc_hevc_slice &sl = p->slices[i];
+        for (int l = 0; l < 2; l++) {
+            if (sl.num_ref[l] < 0 || sl.num_ref[l] > RC_HEVC_MAX_REFS) return RC_EINVAL;
+            for (int r = 0; r < sl.num_ref[l]; r++)
+                if (sl.ref_slot[l][r] < 0 || sl.ref_slot[l][r] >= g->slots) return RC_EINVAL;
+        }
+        if (sl.weighted && (sl.luma_log2_denom < 0 || sl.luma_log2_denom > 7 || sl.chroma_log2_denom < 0 ||
+                            sl.chroma_log2_denom > 7))
+            return RC_EINVAL;
+    }
+    for (int i = 0; i < wctb * hctb; i++)
+        if (p->ctbs[i].slice >= p->num_slices) return RC_EINVAL;
+    for (int by = 0; by < h4; by++)
+        for (int bx = 0; bx < w4; bx++) {
+            const rc_hevc_blk &b = p->blk[by * w4 + bx];
+            if (b.qp < -6 * (g->bd - 8) || b.qp > 51) return RC_EINVAL;
+            if (!(b.flags & RC_HEVC_F_CODED) || (b.flags & RC_HEVC_F_INTRA)) continue;
+            const rc_hevc_mvf &f = p->mvf[by * w4 + bx];
+            const rc_hevc_slice &sl = p->slices[p->ctbs[(by * 4 / ctb) * wctb + bx * 4 / ctb].slice];
+            if (f.ref_idx[0] < 0 && f.ref_idx[1] < 0) return RC_EINVAL;
+            for (int l = 0; l < 2; l++)
+                if (f.ref_idx[l] < -1 || f.ref_idx[l] >= sl.num_ref[l]) return RC_EINVAL;
+        }
+    for (int i = 0; i < p->num_tus; i++) {
+        const rc_hevc_tu &t = p->tus[i];
+        if (t.log2 < 2 || t.log2 > 5 || t.c > 2 || t.mode > 34) return RC_EINVAL;
+        const int n = 1 << t.log2, pw = t.c ? CW : g->W, ph = t.c ? CH : g->H;
+        if (t.x0 + n > pw || t.y0 + n > ph) return RC_EINVAL;
+        if (t.flags & RC_HEVC_TU_PCM) {
+            if ((size_t)t.coef_off + (size_t)n * n > p->num_levels) return RC_EINVAL;
+            continue;
+        }
+        if (!(t.flags & RC_HEVC_TU_CBF)) continue;
+        if (t.max_x >= n || t.max_y >= n) return RC_EINVAL;
+        if (!(t.flags & RC_HEVC_TU_BYPASS) && (t.qp < 0 || t.qp > 51 + 6 * (g->bd - 8))) return RC_EINVAL;
+        if ((size_t)t.coef_off + (size_t)(t.max_x + 1) * (t.max_y + 1) > p->num_levels) return RC_EINVAL;
+    }
+    return 0;
 }
 
 }  // namespace
@@ -274,10 +385,12 @@ int rc_stream_create(int codec, int width, int height, int bit_depth, int dpb_sl
                      rc_stream **out) {
     if (!out) return RC_EINVAL;
     *out = nullptr;
-    if (codec != RC_CODEC_H264) return RC_EINVAL;
+    if (codec != RC_CODEC_H264 && codec != RC_CODEC_HEVC) return RC_EINVAL;
     if (width <= 0 || height <= 0 || width > 8192 || height > 8192 || dpb_slots <= 0 || dpb_slots > 64)
         return RC_EINVAL;
-    if (bit_depth != 8) return RC_EINVAL;
+    if (codec == RC_CODEC_H264 && bit_depth != 8) return RC_EINVAL;
+    if (codec == RC_CODEC_HEVC && ((bit_depth != 8 && bit_depth != 10) || (width & 7) || (height & 7)))
+        return RC_EINVAL;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
         cudaGetLastError();
@@ -289,14 +402,23 @@ int rc_stream_create(int codec, int width, int height, int bit_depth, int dpb_sl
     s->bit_depth = bit_depth;
     s->slots = dpb_slots;
     s->budget = hbm_budget;
-    s->mb_w = (width + 15) / 16;
-    s->mb_h = (height + 15) / 16;
-    s->width = s->mb_w * 16;
-    s->height = s->mb_h * 16;
+    s->bps = bit_depth > 8 ? 2 : 1;
+    if (codec == RC_CODEC_H264) {
+        s->mb_w = (width + 15) / 16;
+        s->mb_h = (height + 15) / 16;
+        s->width = s->mb_w * 16;
+        s->height = s->mb_h * 16;
+    } else {
+        s->width = width;
+        s->height = height;
+        s->mb_w = s->mb_h = 1;
+        s->w4 = width / 4;
+        s->h4 = height / 4;
+    }
     s->cw = s->width / 2;
     s->ch = s->height / 2;
-    s->pitch = (int)align_up(s->width, 128);
-    s->cpitch = (int)align_up(s->cw, 128);
+    s->pitch = (int)align_up((size_t)s->width * s->bps, 128);
+    s->cpitch = (int)align_up((size_t)s->cw * s->bps, 128);
     s->u_off = (size_t)s->pitch * s->height;
     s->v_off = s->u_off + (size_t)s->cpitch * s->ch;
     s->slot_bytes = align_up(s->v_off + (size_t)s->cpitch * s->ch, 256);
@@ -321,6 +443,14 @@ int rc_stream_create(int codec, int width, int height, int bit_depth, int dpb_sl
     ok = ok && cudaMalloc(&s->ls, (2304 + 2304 * 4) * sizeof(int32_t)) == cudaSuccess;
     ok = ok && cudaMalloc(&s->rowprog, (size_t)s->mb_h * sizeof(uint32_t)) == cudaSuccess;
     ok = ok && cudaMalloc(&s->db, (size_t)n * sizeof(DbMb)) == cudaSuccess;
+    if (codec == RC_CODEC_HEVC) {
+        const size_t nres = (size_t)s->width * s->height + 2 * (size_t)s->cw * s->ch;
+        ok = ok && dev_alloc(s, (void **)&s->work, s->slot_bytes);
+        ok = ok && dev_alloc(s, (void **)&s->res, nres * sizeof(int16_t));
+        ok = ok && dev_alloc(s, (void **)&s->ready, 3 * (size_t)s->w4 * s->h4 * sizeof(uint32_t));
+        ok = ok && cudaMemsetAsync(s->ready, 0, 3 * (size_t)s->w4 * s->h4 * sizeof(uint32_t), s->st) == cudaSuccess;
+        ok = ok && cudaMemsetAsync(s->work, 0, s->slot_bytes, s->st) == cudaSuccess;
+    }
     for (int i = 0; i < 2 && ok; i++) ok = cudaEventCreateWithFlags(&s->staged[i], cudaEventDisableTiming) == cudaSuccess;
     if (ok) {
         ok = cudaMemsetAsync(s->dpb, 0, s->slot_bytes * s->slots, s->st) == cudaSuccess &&
@@ -375,42 +505,9 @@ int rc_h264_submit(rc_stream *s, const rc_h264_picture *pic, int out_slot) {
         if ((rc = validate_h264(&g, pic)) != 0) return rc;
         const size_t b_mbs = sizeof(rc_h264_mb) * n, b_sl = sizeof(rc_h264_slice) * pic->num_slices;
         const size_t b_w = sizeof(rc_h264_weight) * pic->num_weights, b_lv = sizeof(int16_t) * pic->num_levels;
-        if ((rc = ensure(s, s->mbs, b_mbs)) || (rc = ensure(s, s->slices, b_sl)) ||
-            (rc = ensure(s, s->weights, std::max<size_t>(b_w, 64))) || (rc = ensure(s, s->levels, std::max<size_t>(b_lv, 64))))
-            return rc;
-        struct Part { void *dst; const void *src; size_t n; } parts[4] = {
-            {s->mbs.p, pic->mbs, b_mbs}, {s->slices.p, pic->slices, b_sl},
-            {s->weights.p, pic->weights, b_w}, {s->levels.p, pic->levels, b_lv}};
-        bool pinned = true;
-        for (auto &p : parts) pinned = pinned && is_pinned(p.src);
-        if (pinned) {
-            for (auto &p : parts)
-                if (p.n && cudaMemcpyAsync(p.dst, p.src, p.n, cudaMemcpyHostToDevice, s->st) != cudaSuccess)
-                    return cuda_fail(s);
-        } else {
-            const int i = s->submits & 1;
-            size_t total = 0;
-            for (auto &p : parts) total += align_up(p.n, 256);
-            if (cudaEventSynchronize(s->staged[i]) != cudaSuccess) return cuda_fail(s);
-            if (total > s->staging_cap[i]) {
-                if (s->staging[i]) cudaFreeHost(s->staging[i]);
-                s->staging[i] = nullptr;
-                s->staging_cap[i] = 0;
-                size_t want = align_up(total + total / 4, 1 << 20);
-                if (cudaMallocHost(&s->staging[i], want) != cudaSuccess) return RC_ENOMEM;
-                s->staging_cap[i] = want;
-            }
-            uint8_t *stage = (uint8_t *)s->staging[i];
-            size_t off = 0;
-            for (auto &p : parts) {
-                if (!p.n) continue;
-                memcpy(stage + off, p.src, p.n);
-                if (cudaMemcpyAsync(p.dst, stage + off, p.n, cudaMemcpyHostToDevice, s->st) != cudaSuccess)
-                    return cuda_fail(s);
-                off += align_up(p.n, 256);
-            }
-            if (cudaEventRecord(s->staged[i], s->st) != cudaSuccess) return cuda_fail(s);
-        }
+        Part parts[4] = {{&s->mbs, pic->mbs, b_mbs}, {&s->slices, pic->slices, b_sl},
+                         {&s->weights, pic->weights, b_w}, {&s->levels, pic->levels, b_lv}};
+        if ((rc = upload(s, parts, 4)) != 0) return rc;
         L.mbs = (const rc_h264_mb *)s->mbs.p;
         L.slices = (const rc_h264_slice *)s->slices.p;
         L.weights = (const rc_h264_weight *)s->weights.p;
@@ -460,6 +557,99 @@ int rc_h264_submit(rc_stream *s, const rc_h264_picture *pic, int out_slot) {
     return RC_OK;
 }
 
+int rc_hevc_validate(int width, int height, int bit_depth, int dpb_slots, const rc_hevc_picture *pic) {
+    if (!pic || width <= 0 || height <= 0 || (width & 7) || (height & 7) || dpb_slots <= 0 ||
+        (bit_depth != 8 && bit_depth != 10))
+        return RC_EINVAL;
+    HGeo g{width, height, bit_depth, dpb_slots};
+    return validate_hevc(&g, pic);
+}
+
+int rc_hevc_submit(rc_stream *s, const rc_hevc_picture *pic, int out_slot) {
+    if (!s || !pic || s->codec != RC_CODEC_HEVC) return RC_EINVAL;
+    if (out_slot < 0 || out_slot >= s->slots) return RC_EINVAL;
+    if (pic->mem != RC_MEM_HOST && pic->mem != RC_MEM_DEVICE) return RC_EINVAL;
+    if (pic->log2_ctb < 4 || pic->log2_ctb > 6) return RC_EINVAL;
+    int rc;
+    const int ctb = 1 << pic->log2_ctb, wctb = (s->width + ctb - 1) / ctb, hctb = (s->height + ctb - 1) / ctb;
+    const size_t nblk = (size_t)s->w4 * s->h4;
+    const size_t b_scal = 6 * (16 + 64 + 256 + 1024);
+    HevcLaunch L;
+    memset(&L, 0, sizeof L);
+    if (pic->scaling) {  // scaling factors are host memory in both modes
+        Part sp{&s->scaling, pic->scaling, b_scal};
+        if ((rc = upload(s, &sp, 1)) != 0) return rc;
+        L.scaling = (const uint8_t *)s->scaling.p;
+    }
+    if (pic->mem == RC_MEM_HOST) {
+        HGeo g{s->width, s->height, s->bit_depth, s->slots};
+        if ((rc = validate_hevc(&g, pic)) != 0) return rc;
+        Part parts[6] = {{&s->ctbs, pic->ctbs, sizeof(rc_hevc_ctb) * wctb * hctb},
+                         {&s->blk, pic->blk, sizeof(rc_hevc_blk) * nblk},
+                         {&s->mvf, pic->mvf, sizeof(rc_hevc_mvf) * nblk},
+                         {&s->tus, pic->tus, sizeof(rc_hevc_tu) * pic->num_tus},
+                         {&s->hslices, pic->slices, sizeof(rc_hevc_slice) * pic->num_slices},
+                         {&s->levels, pic->levels, sizeof(int16_t) * pic->num_levels}};
+        if ((rc = upload(s, parts, 6)) != 0) return rc;
+        L.ctbs = (const rc_hevc_ctb *)s->ctbs.p;
+        L.blk = (const rc_hevc_blk *)s->blk.p;
+        L.mvf = (const rc_hevc_mvf *)s->mvf.p;
+        L.tus = (const rc_hevc_tu *)s->tus.p;
+        L.slices = (const rc_hevc_slice *)s->hslices.p;
+        L.levels = (const int16_t *)s->levels.p;
+    } else {
+        if (!pic->ctbs || !pic->blk || !pic->mvf || !pic->slices || pic->num_slices <= 0) return RC_EINVAL;
+        L.ctbs = pic->ctbs;
+        L.blk = pic->blk;
+        L.mvf = pic->mvf;
+        L.tus = pic->tus;
+        L.slices = pic->slices;
+        L.levels = pic->levels;
+    }
+    L.num_levels = pic->num_levels;
+    L.num_tus = pic->num_tus;
+    L.num_slices = pic->num_slices;
+    L.W = s->width;
+    L.H = s->height;
+    L.CW = s->cw;
+    L.CH = s->ch;
+    L.bd = s->bit_depth;
+    L.w4 = s->w4;
+    L.h4 = s->h4;
+    L.log2ctb = pic->log2_ctb;
+    L.wctb = wctb;
+    L.hctb = hctb;
+    L.constrained_intra = pic->constrained_intra_pred;
+    L.strong_intra = pic->strong_intra_smoothing;
+    L.lf_across_tiles = pic->loop_filter_across_tiles;
+    L.cb_qp_offset = pic->cb_qp_offset;
+    L.cr_qp_offset = pic->cr_qp_offset;
+    L.dpb = s->dpb;
+    L.slot_bytes = s->slot_bytes;
+    L.u_off = s->u_off;
+    L.v_off = s->v_off;
+    L.dpb_slots = s->slots;
+    L.out_slot = out_slot;
+    L.pitch = s->pitch;
+    L.cpitch = s->cpitch;
+    L.work = s->work;
+    L.res = s->res;
+    L.ready = s->ready;
+    L.counter = s->counter;
+    L.error = s->error;
+    L.epoch = ++s->epoch;
+    L.wait_limit = s->wait_limit;
+    timed(s, RC_KERNEL_HEVC_RESIDUAL, [&] { rc_launch_hevc_residual(L, s->st); });
+    timed(s, RC_KERNEL_HEVC_INTER, [&] { rc_launch_hevc_inter(L, s->st); });
+    timed(s, RC_KERNEL_HEVC_INTRA, [&] { rc_launch_hevc_intra(L, s->st, s->wave_blocks); });
+    timed(s, RC_KERNEL_HEVC_DEBLOCK, [&] { rc_launch_hevc_deblock(L, s->st); });
+    timed(s, RC_KERNEL_HEVC_SAO, [&] { rc_launch_hevc_sao(L, s->st); });
+    s->launches += 1;  // the deblocking step is two launches (vertical, horizontal edges)
+    s->submits++;
+    if (cudaGetLastError() != cudaSuccess) return cuda_fail(s);
+    return RC_OK;
+}
+
 int rc_stream_sync(rc_stream *s) {
     if (!s) return RC_EINVAL;
     if (cudaStreamSynchronize(s->st) != cudaSuccess) return cuda_fail(s);
@@ -487,7 +677,7 @@ static int download(rc_stream *s, int slot, int x, int y, int w, int h, void *ou
     auto fits = [](long at, long n, long size) { return n > 0 && at >= 0 && at + n <= size; };
     if (!(fits(x, w, s->width) && fits(y, h, s->height) && fits(cx, ccw, s->cw) && fits(cy, cch, s->ch)))
         return RC_EINVAL;
-    const int bps = s->bit_depth > 8 ? 2 : 1;
+    const int bps = s->bps;
     const uint8_t *base = s->dpb + (size_t)slot * s->slot_bytes;
     bool ok = cudaMemcpy2DAsync(out_y, (size_t)w * bps, base + (size_t)y * s->pitch + (size_t)x * bps, s->pitch,
                                 (size_t)w * bps, h, cudaMemcpyDeviceToHost, s->st) == cudaSuccess &&
@@ -534,7 +724,7 @@ int rc_stream_profile_read(rc_stream *s, double *ms, long long *launches, int ma
 
 int rc_picture_upload(rc_stream *s, int slot, const void *py, const void *pu, const void *pv) {
     if (!s || slot < 0 || slot >= s->slots || !py || !pu || !pv) return RC_EINVAL;
-    const int bps = s->bit_depth > 8 ? 2 : 1;
+    const int bps = s->bps;
     uint8_t *base = s->dpb + (size_t)slot * s->slot_bytes;
     bool ok = cudaStreamSynchronize(s->st) == cudaSuccess &&
               cudaMemcpy2D(base, s->pitch, py, (size_t)s->width * bps, (size_t)s->width * bps, s->height,

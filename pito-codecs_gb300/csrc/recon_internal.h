@@ -54,6 +54,37 @@ struct H264Launch {
     uint32_t *rowprog;    // per MB row: (epoch & 0xffff) << 16 | MBs final
 };
 
+struct HevcLaunch {
+    const rc_hevc_ctb *ctbs;
+    const rc_hevc_blk *blk;
+    const rc_hevc_mvf *mvf;
+    const rc_hevc_tu *tus;
+    const rc_hevc_slice *slices;
+    const int16_t *levels;
+    const uint8_t *scaling;       // device copy of the expanded scaling factors, or null
+    unsigned long long num_levels;
+    int num_tus, num_slices;
+    int W, H, CW, CH, bd, w4, h4, log2ctb, wctb, hctb;
+    int constrained_intra, strong_intra, lf_across_tiles, cb_qp_offset, cr_qp_offset;
+    // DPB (references + output slot) and the picture being reconstructed
+    uint8_t *dpb;
+    unsigned long long slot_bytes, u_off, v_off;
+    int dpb_slots, out_slot;
+    int pitch, cpitch;            // bytes
+    uint8_t *work;                // pre-SAO picture, same layout as a slot
+    int16_t *res;                 // residual planes: luma W*H, then Cb, Cr CW*CH
+    uint32_t *ready;              // 3 planes of w4*h4 flags: epoch when reconstructed
+    uint32_t *counter;
+    uint32_t *error;
+    uint32_t epoch, wait_limit;
+};
+
+void rc_launch_hevc_residual(const HevcLaunch &p, cudaStream_t st);
+void rc_launch_hevc_inter(const HevcLaunch &p, cudaStream_t st);
+void rc_launch_hevc_intra(const HevcLaunch &p, cudaStream_t st, int blocks);
+void rc_launch_hevc_deblock(const HevcLaunch &p, cudaStream_t st);
+void rc_launch_hevc_sao(const HevcLaunch &p, cudaStream_t st);
+
 // Launchers (h264_kernels.cu).
 void rc_launch_h264_mb(const H264Launch &p, cudaStream_t st);
 void rc_launch_h264_intra(const H264Launch &p, cudaStream_t st, int wave_blocks);

@@ -56,6 +56,49 @@ const rc_h264_picture *rc_synth_h264_picture(void *h);
 size_t rc_synth_h264_bytes(void *h);
 void rc_synth_h264_free(void *h);
 
+/* Knobs of the HEVC generator (fractions in 1/1000). */
+typedef struct rc_synth_hevc_opts {
+    uint64_t seed;
+    int32_t width, height;       /* multiples of 8                            */
+    int32_t bit_depth;           /* 8 or 10                                   */
+    int32_t log2_ctb;            /* 4..6                                      */
+    int32_t intra_only;
+    int32_t intra_permille;      /* share of intra CUs in inter pictures      */
+    int32_t zero_tu_permille;    /* share of TUs without coefficients         */
+    int32_t split_permille;      /* CU / TU quadtree split probability        */
+    int32_t mv_range;            /* max |mv| in full pels                     */
+    int32_t bipred_permille;
+    int32_t qp_min, qp_max;
+    int32_t cb_qp_offset, cr_qp_offset;
+    int32_t transform_skip_permille; /* of 4x4 TUs                           */
+    int32_t pcm_permille;        /* of intra 2Nx2N CUs (8..32)                */
+    int32_t pcm_loop_filter_disabled;
+    int32_t bypass_permille;     /* CUs with cu_transquant_bypass             */
+    int32_t scaling_lists;       /* 1 = random scaling lists                  */
+    int32_t constrained_intra_pred;
+    int32_t strong_intra_smoothing;
+    int32_t weighted;            /* explicit weighted prediction              */
+    int32_t num_slices;          /* slices split in tile-scan order           */
+    int32_t tile_cols, tile_rows;
+    int32_t loop_filter_across_tiles;
+    int32_t lf_across_slices;
+    int32_t deblock_disabled;
+    int32_t beta_offset, tc_offset;
+    int32_t sao;                 /* 1 = SAO on (band/edge, offsets +-7)       */
+    int32_t num_ref[2];
+    int32_t ref_slot[2][4];
+    uint32_t ref_id[2][4];
+    uint32_t frame_id;
+} rc_synth_hevc_opts;
+
+/* 1080p-style defaults: 25% intra, 75% zero TUs, +-256 px, QP 22-37,
+ * deblocking and SAO on, CTB 64, 8-bit. */
+void rc_synth_hevc_defaults(rc_synth_hevc_opts *o);
+void *rc_synth_hevc_new(const rc_synth_hevc_opts *o);
+const rc_hevc_picture *rc_synth_hevc_picture(void *h);
+size_t rc_synth_hevc_bytes(void *h);
+void rc_synth_hevc_free(void *h);
+
 #ifdef __cplusplus
 }
 #endif
