@@ -368,6 +368,34 @@ int rc_stream_profile(rc_stream *s, int enable);
 int rc_stream_profile_read(rc_stream *s, double *ms, long long *launches,
                            int max_kernels);
 
+/* Allocation-free H.264 deblocking (no counterpart in the reference).
+ *
+ * For callers that cannot allocate device memory once they are running:
+ * processes whose device memory is carved up by their own allocator at
+ * start-up, real-time pipelines that must not stall in cudaMalloc, or code
+ * issuing work while a stream is being captured.  It runs the same loop
+ * filter rc_h264_submit applies, in place on caller planes (device memory:
+ * the picture's coded size, luma 16-byte aligned with a pitch multiple of
+ * 16, chroma 8-byte aligned with a pitch multiple of 8), from the picture's
+ * syntax records in device memory (pic->mem == RC_MEM_DEVICE).  It allocates
+ * nothing: its scratch is a static device array the library holds on every
+ * device that loads it, sized for RC_NOALLOC_MAX_MBS macroblocks (8704:
+ * up to 2048x1088) and RC_NOALLOC_MAX_ROWS MB rows; larger pictures get
+ * RC_EINVAL.  The first call on a device looks up that array's device
+ * address, so make the first call before any stream capture.  Every call
+ * shares the one array: calls whose work overlaps on the GPU (on different
+ * streams, or on different host threads) race and must be serialised by the
+ * caller.  *status (device memory, 4 bytes) receives 0 or RC_DEV_* error bits
+ * (1 a wait timed out, 2 a record pointed outside its buffers) once the
+ * queued work completes on cuda_stream (a cudaStream_t; NULL = the default
+ * stream). */
+#define RC_NOALLOC_MAX_MBS 8704
+#define RC_NOALLOC_MAX_ROWS 128
+int rc_h264_deblock_noalloc(const rc_h264_picture *pic, int mb_w, int mb_h,
+                            void *y, void *u, void *v, int luma_pitch,
+                            int chroma_pitch, uint32_t *status,
+                            void *cuda_stream);
+
 /* Number of kernel launches this stream has issued so far. */
 long long rc_stream_launches(rc_stream *s);
 

@@ -222,6 +222,8 @@ def lib() -> ctypes.CDLL:
     L.rc_stream_launches.restype = ctypes.c_longlong
     L.rc_stream_cuda_stream.argtypes = [vp]
     L.rc_stream_cuda_stream.restype = vp
+    L.rc_h264_deblock_noalloc.argtypes = [vp, i32, i32, vp, vp, vp, i32, i32, vp, vp]
+    L.rc_h264_deblock_noalloc.restype = i32
     return L
 
 

@@ -26,6 +26,7 @@
 // Arithmetic follows src/h264/dec/{transform,intra,inter,deblock}.rs and the
 // reconstruction half of slicedec.rs; citations at each function.
 #include <stdint.h>
+#include <string.h>
 
 #include "recon_internal.h"
 
@@ -1156,6 +1157,21 @@ __global__ void __launch_bounds__(32) h264_deblock_kernel(H264Launch P) {
     }
 }
 
+// Loop-filter parameters of every MB on their own (one warp per MB); the
+// allocation-free deblocking entry point needs them without the MB kernel.
+__global__ void __launch_bounds__(128) h264_db_params_kernel(H264Launch P) {
+    __shared__ __align__(16) rc_h264_mb rec[4][3];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int addr = blockIdx.x * 4 + w;
+    if (addr >= P.mb_w * P.mb_h) return;
+    const int mbx = addr % P.mb_w, mby = addr / P.mb_w;
+    load_record(rec[w][0], P.mbs + addr, lane);
+    if (mbx > 0) load_record(rec[w][1], P.mbs + addr - 1, lane);
+    if (mby > 0) load_record(rec[w][2], P.mbs + addr - P.mb_w, lane);
+    __syncwarp();
+    compute_db(P, rec[w][0], rec[w][1], rec[w][2], addr, lane, P.db + addr);
+}
+
 }  // namespace
 
 void rc_launch_h264_mb(const H264Launch &p, cudaStream_t st) {
@@ -1169,4 +1185,90 @@ void rc_launch_h264_intra(const H264Launch &p, cudaStream_t st, int wave_blocks)
 
 void rc_launch_h264_deblock(const H264Launch &p, cudaStream_t st) {
     h264_deblock_kernel<<<p.mb_h, 32, 0, st>>>(p);
+}
+
+// ===========================================================================
+// Allocation-free deblocking: rc_h264_deblock_noalloc
+// ===========================================================================
+// Callers that own every byte of device memory (a decoder embedded in a
+// process whose allocator is fixed at start-up, a real-time pipeline that
+// must not stall in cudaMalloc, code running while a stream is captured) can
+// deblock an already reconstructed picture without the library allocating.
+// The scratch the loop filter needs -- per-MB filter parameters (48 bytes per
+// MB) and per-row progress words -- lives in this one static device array,
+// sized for RC_NOALLOC_MAX_MBS macroblocks and RC_NOALLOC_MAX_ROWS rows; every
+// device that loads the library holds it until the process exits.
+#define RC_NOALLOC_DB_WORDS (RC_NOALLOC_MAX_MBS * (int)(sizeof(DbMb) / 4))
+static __device__ __align__(256) uint32_t g_noalloc_scratch[RC_NOALLOC_DB_WORDS + RC_NOALLOC_MAX_ROWS];
+
+#include <mutex>
+
+namespace {
+std::mutex g_noalloc_mu;
+uint32_t *g_noalloc_addr[64];
+bool g_noalloc_ready[64];
+
+// Device address of the static scratch for the current device; looked up once
+// per device (the host-side name is not a device address).
+int noalloc_scratch(uint32_t **out) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return RC_ENODEV;
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ready[dev]) {
+        void *p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) {
+            cudaGetLastError();
+            return RC_ECUDA;
+        }
+        g_noalloc_addr[dev] = (uint32_t *)p;
+        g_noalloc_ready[dev] = true;
+    }
+    *out = g_noalloc_addr[dev];
+    return RC_OK;
+}
+}  // namespace
+
+extern "C" int rc_h264_deblock_noalloc(const rc_h264_picture *pic, int mb_w, int mb_h, void *y, void *u, void *v,
+                                       int luma_pitch, int chroma_pitch, uint32_t *status, void *cuda_stream) {
+    if (!pic || pic->mem != RC_MEM_DEVICE || !pic->mbs || !pic->slices || pic->num_slices <= 0) return RC_EINVAL;
+    if (mb_w <= 0 || mb_h <= 0 || !y || !u || !v || !status) return RC_EINVAL;
+    if ((long long)mb_w * mb_h > RC_NOALLOC_MAX_MBS || mb_h > RC_NOALLOC_MAX_ROWS) return RC_EINVAL;
+    if (luma_pitch < mb_w * 16 || chroma_pitch < mb_w * 8 || (luma_pitch & 15) || (chroma_pitch & 7)) return RC_EINVAL;
+    if (((uintptr_t)y & 15) || ((uintptr_t)u & 7) || ((uintptr_t)v & 7)) return RC_EINVAL;
+    uint32_t *scratch = nullptr;
+    int rc = noalloc_scratch(&scratch);
+    if (rc != RC_OK) return rc;
+    cudaStream_t st = (cudaStream_t)cuda_stream;
+    uint32_t *rows = scratch + RC_NOALLOC_DB_WORDS;
+    // row progress must start at zero; the parameters are rewritten each call
+    if (cudaMemsetAsync(rows, 0, (size_t)mb_h * sizeof(uint32_t), st) != cudaSuccess ||
+        cudaMemsetAsync(status, 0, sizeof(uint32_t), st) != cudaSuccess)
+        return RC_ECUDA;
+    H264Launch L;
+    memset(&L, 0, sizeof L);
+    L.mbs = pic->mbs;
+    L.slices = pic->slices;
+    L.num_slices = pic->num_slices;
+    L.mb_w = mb_w;
+    L.mb_h = mb_h;
+    L.W = mb_w * 16;
+    L.H = mb_h * 16;
+    L.CW = mb_w * 8;
+    L.CH = mb_h * 8;
+    L.pitch = luma_pitch;
+    L.cpitch = chroma_pitch;
+    L.dpb = (uint8_t *)y;
+    L.slot_bytes = 0;
+    L.out_slot = 0;
+    L.u_off = (unsigned long long)((uintptr_t)u - (uintptr_t)y);
+    L.v_off = (unsigned long long)((uintptr_t)v - (uintptr_t)y);
+    L.dpb_slots = 1;
+    L.db = (DbMb *)scratch;
+    L.rowprog = rows;
+    L.error = status;
+    L.epoch = 1;
+    L.wait_limit = RC_WAIT_LIMIT;
+    h264_db_params_kernel<<<(mb_w * mb_h + 3) / 4, 128, 0, st>>>(L);
+    h264_deblock_kernel<<<mb_h, 32, 0, st>>>(L);
+    return cudaGetLastError() == cudaSuccess ? RC_OK : RC_ECUDA;
 }
