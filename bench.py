@@ -87,15 +87,15 @@ def picture_stats(E, p):
     out_frame = MB_W * 16 * MB_H * 16 * 3 // 2
     syn = p.nbytes
     n = len(kind)
-    # h264_mb_kernel: every record once (loop-filter parameters for all MBs:
-    # 48 B written each), plus inter/PCM samples out, their levels and refs
-    mb_kernel = int(n * (176 + 48) + mbk.sum() * 384 + lv_bytes[mbk].sum() + ref_bytes)
-    # h264_intra_kernel: intra MBs' records, levels and samples out
-    intra_kernel = int(wave_intra.sum() * (176 + 384) + lv_bytes[wave_intra].sum())
-    # h264_deblock_kernel: the picture read and written once + parameters
-    deblock_kernel = int(2 * out_frame + n * 48)
-    return {"mb": mb_kernel, "intra": intra_kernel, "deblock": deblock_kernel, "job": out_frame + ref_bytes + syn,
-            "syntax": syn}
+    # h264_mb_kernel: every record and its levels once, loop-filter parameters
+    # for all MBs (48 B), inter/PCM samples out with their references, and the
+    # intra MBs' residuals (768 B) and parameters (32 B) out
+    mb_kernel = int(n * (176 + 48) + lv_bytes.sum() + mbk.sum() * 384 + ref_bytes + wave_intra.sum() * (768 + 32))
+    # h264_wave_kernel: intra MBs' parameters (32 B) and residuals (768 B) in,
+    # then the whole picture read and written once by the loop filter + its
+    # per-MB parameters (48 B)
+    wave_kernel = int(wave_intra.sum() * (32 + 768) + 2 * out_frame + n * 48)
+    return {"mb": mb_kernel, "wave": wave_kernel, "job": out_frame + ref_bytes + syn, "syntax": syn}
 
 
 class ClockSampler:
@@ -366,7 +366,7 @@ def main():
     e2e = frames * args.steps * world / e2e_s
 
     # ---- roofline of the dominant kernel
-    names = {0: ("h264_mb_kernel", "mb"), 1: ("h264_intra_kernel", "intra"), 2: ("h264_deblock_kernel", "deblock")}
+    names = {0: ("h264_mb_kernel", "mb"), 1: ("h264_wave_kernel", "wave")}
     per_kernel = {}
     for k, (ms, n) in prof.items():
         name, key = names[k]

@@ -248,7 +248,7 @@ __global__ void __launch_bounds__(256) h264_mb_kernel(H264Launch P) {
     __syncthreads();
     if (t < 32) compute_db(P, m, nbr[0], nbr[1], addr, t, P.db + addr);
     const int kind = m.kind;
-    if (kind != RC_H264_INTER && kind != RC_H264_IPCM) return;
+    if (kind == RC_H264_NONE || kind > RC_H264_INTER) return;
     uint8_t *Y = P.dpb + (size_t)P.out_slot * P.slot_bytes;
     uint8_t *U = Y + P.u_off, *V = Y + P.v_off;
     if (kind == RC_H264_IPCM) {  // write_pcm, src/h264/dec/slicedec.rs:1404-1424
@@ -263,11 +263,38 @@ __global__ void __launch_bounds__(256) h264_mb_kernel(H264Launch P) {
     }
     if (m.slice >= P.num_slices) { if (t == 0) set_error(P.error, RC_DEV_ERR_RECORD); return; }
     const rc_h264_slice *sl = P.slices + m.slice;
-    const int t8 = m.transform_8x8;
+    const bool intra = kind != RC_H264_INTER;
+    const int t8 = m.transform_8x8, i16 = kind == RC_H264_I16x16;
     const int nl = __popc(m.luma_coded & (t8 ? 0xf : 0xffff)), ndc = __popc(m.dc_coded & 6);
-    const unsigned long long need = (unsigned long long)nl * (t8 ? 64 : 16) + ndc * 4 + __popc(m.chroma_coded) * 16;
+    const int nlum = (i16 && (m.dc_coded & 1)) ? 16 : 0;
+    const unsigned long long need =
+        nlum + (unsigned long long)nl * (t8 ? 64 : 16) + ndc * 4 + __popc(m.chroma_coded) * 16;
     if (m.coef_off + need > P.num_levels) { if (t == 0) set_error(P.error, RC_DEV_ERR_RECORD); return; }
-
+    __shared__ uint32_t ibits;  // intra: availability (bits 0..3) and waits (bits 4..7)
+    if (intra) {
+        if (t == 0) ibits = 0;
+        __syncthreads();
+        if (t < 4) {
+            // start_mb neighbour availability + intra_nb, slicedec.rs:489-508, 525-530
+            const int dx = t == 0 ? -1 : t == 2 ? 1 : t == 3 ? -1 : 0, dy = t == 0 ? 0 : -1;
+            const int nx = mbx + dx, ny = mby + dy;
+            if (nx >= 0 && ny >= 0 && nx < P.mb_w) {
+                const rc_h264_mb *pm = P.mbs + ny * P.mb_w + nx;
+                const int nk = __ldg(&pm->kind);
+                const bool a = nk != RC_H264_NONE && __ldg(&pm->slice) == m.slice && (!P.constrained_intra || is_intra(nk));
+                // the top-right MB is read only by Intra4x4 block (3,0) in modes 3 / 7 (diagonal down-left,
+                // vertical-left) and by the top-using modes of Intra8x8 block 1 (intra.rs:31-62, 199-233)
+                bool uses = true;
+                if (t == 2)
+                    uses = kind == RC_H264_I4x4 ? (m.intra_modes[3] == 3 || m.intra_modes[3] == 7)
+                           : kind == RC_H264_I8x8 ? (m.intra_modes[2] != 1 && m.intra_modes[2] != 8) : false;
+                uint32_t b = a ? (1u << t) : 0;
+                if (a && uses && wave_intra(nk)) b |= 16u << t;
+                atomicOr(&ibits, b);
+            }
+        }
+    }
+    if (!intra) {
     // ---- prediction (mc_rect, slicedec.rs:996-1087), one luma sample per thread
     {
         const int x = t & 15, y = t >> 4, k = (y >> 2) * 4 + (x >> 2), b8 = (y >> 3) * 2 + (x >> 3);
@@ -312,37 +339,48 @@ __global__ void __launch_bounds__(256) h264_mb_kernel(H264Launch P) {
         predc[t] = (uint8_t)weigh(v[0], v[1], u[0], u[1], ex, ex ? w->log_wd[cc] : 0, ex ? w->w0[cc] : 0,
                                   ex ? w->w1[cc] : 0, ex ? w->o0[cc] : 0, ex ? w->o1[cc] : 0);
     }
+    }
 
-    // ---- level placement + dequantisation (put_luma4/8, put_chroma_dc/ac,
-    // slicedec.rs:1462-1555); inter lists: luma4 3, luma8 1, chroma 4+c
+    // ---- level placement + dequantisation (put_luma4/8, put_luma_dc,
+    // put_chroma_dc/ac, slicedec.rs:1462-1555); lists: luma4 intra 0 / inter 3,
+    // luma8 intra 0 / inter 1, chroma intra 1+c / inter 4+c
     const int16_t *lv = P.levels + m.coef_off;
-    const int qp = m.qp;
+    const int qp = m.qp, l4 = intra ? 0 : 3, l8 = intra ? 0 : 1, lc = intra ? 1 : 4;
+    if (nlum && t == 0) {  // put_luma_dc, slicedec.rs:1501-1515
+        int32_t c[16];
+        for (int k = 0; k < 16; k++) c[cZZ4[k]] = lv[k];
+        luma_dc_dequant(c, qp, __ldg(P.ls4 + (0 * 6 + qp % 6) * 16));
+        uint32_t bits = 0;
+        for (int r = 0; r < 16; r++)
+            if (c[r]) { coef[r * 16] = c[r]; bits |= 1u << r; }
+        atomicOr(&nzl, bits);
+    }
     if (t8) {
         int b8 = t >> 6, kk = t & 63;
         if (m.luma_coded >> b8 & 1) {
-            int l = lv[__popc(m.luma_coded & ((1u << b8) - 1)) * 64 + kk];
+            int l = lv[nlum + __popc(m.luma_coded & ((1u << b8) - 1)) * 64 + kk];
             if (l) {
                 int p = cZZ8[kk];
-                coef[b8 * 64 + p] = scale8(l, __ldg(P.ls8 + (1 * 6 + qp % 6) * 64 + p), qp);
+                coef[b8 * 64 + p] = scale8(l, __ldg(P.ls8 + (l8 * 6 + qp % 6) * 64 + p), qp);
                 atomicOr(&nzl, 1u << b8);
             }
         }
     } else {
         int r = t >> 4, kk = t & 15;
-        if (m.luma_coded >> r & 1) {
-            int l = lv[__popc(m.luma_coded & ((1u << r) - 1)) * 16 + kk];
+        if (kk >= i16 && (m.luma_coded >> r & 1)) {
+            int l = lv[nlum + __popc(m.luma_coded & ((1u << r) - 1)) * 16 + kk];
             if (l) {
                 int p = cZZ4[kk];
-                coef[r * 16 + p] = scale4(l, __ldg(P.ls4 + (3 * 6 + qp % 6) * 16 + p), qp);
+                coef[r * 16 + p] = scale4(l, __ldg(P.ls4 + (l4 * 6 + qp % 6) * 16 + p), qp);
                 atomicOr(&nzl, 1u << r);
             }
         }
     }
-    const int off_dc = nl * (t8 ? 64 : 16), off_ac = off_dc + ndc * 4;
+    const int off_dc = nlum + nl * (t8 ? 64 : 16), off_ac = off_dc + ndc * 4;
     if (t < 2 && (m.dc_coded >> (1 + t) & 1)) {
         int c = t, at = off_dc + ((c == 1 && (m.dc_coded & 2)) ? 4 : 0), qpc = m.qpc[c];
         int32_t d[4] = {lv[at], lv[at + 1], lv[at + 2], lv[at + 3]};
-        chroma_dc_dequant(d, qpc, __ldg(P.ls4 + ((4 + c) * 6 + qpc % 6) * 16));
+        chroma_dc_dequant(d, qpc, __ldg(P.ls4 + ((lc + c) * 6 + qpc % 6) * 16));
         for (int b = 0; b < 4; b++)
             if (d[b]) { coefc[c * 64 + b * 16] = d[b]; atomicOr(&nzc, 1u << (c * 4 + b)); }
     }
@@ -352,7 +390,7 @@ __global__ void __launch_bounds__(256) h264_mb_kernel(H264Launch P) {
             int l = lv[off_ac + __popc(m.chroma_coded & ((1u << bit) - 1)) * 16 + kk];
             if (l) {
                 int qpc = m.qpc[c], p = cZZ4[kk];
-                coefc[c * 64 + b * 16 + p] = scale4(l, __ldg(P.ls4 + ((4 + c) * 6 + qpc % 6) * 16 + p), qpc);
+                coefc[c * 64 + b * 16 + p] = scale4(l, __ldg(P.ls4 + ((lc + c) * 6 + qpc % 6) * 16 + p), qpc);
                 atomicOr(&nzc, 1u << bit);
             }
         }
@@ -369,6 +407,42 @@ __global__ void __launch_bounds__(256) h264_mb_kernel(H264Launch P) {
     } else if (t < 64 && (nzl >> (t >> 2) & 1)) idct4_1d(coef + (t >> 2) * 16 + (t & 3), 4);
     if (t >= 64 && t < 96 && (nzc >> ((t - 64) >> 2) & 1)) idct4_1d(coefc + ((t - 64) >> 2) * 16 + (t & 3), 4);
     __syncthreads();
+    if (intra) {
+        // residual samples ((v + 32) >> 6, idct4_add / idct8_add) and the
+        // prediction parameters for the intra wavefront
+        int16_t *res = P.ires + (size_t)addr * 384;
+        {
+            const int x = t & 15, y = t >> 4;
+            int r = 0;
+            if (t8) {
+                int b8 = (y >> 3) * 2 + (x >> 3);
+                if (nzl >> b8 & 1) r = (coef[b8 * 64 + (y & 7) * 8 + (x & 7)] + 32) >> 6;
+            } else {
+                int b = (y >> 2) * 4 + (x >> 2);
+                if (nzl >> b & 1) r = (coef[b * 16 + (y & 3) * 4 + (x & 3)] + 32) >> 6;
+            }
+            res[t] = (int16_t)max(-32768, min(32767, r));
+        }
+        if (t < 128) {
+            const int c = t >> 6, x = t & 7, y = (t >> 3) & 7, blk = c * 4 + (y >> 2) * 2 + (x >> 2);
+            int r = (nzc >> blk & 1) ? (coefc[blk * 16 + (y & 3) * 4 + (x & 3)] + 32) >> 6 : 0;
+            res[256 + t] = (int16_t)max(-32768, min(32767, r));
+        }
+        if (t == 0) {
+            IntraInfo in;
+            in.kind = (uint8_t)kind;
+            in.t8 = (uint8_t)t8;
+            in.i16_mode = m.i16_mode;
+            in.chroma_mode = m.chroma_mode;
+            in.nb = (uint8_t)(ibits & 15);
+            in.wait = (uint8_t)(ibits >> 4);
+            in.pad0 = in.pad1 = 0;
+            for (int i = 0; i < 16; i++) in.modes[i] = m.intra_modes[i];
+            in.pad2[0] = in.pad2[1] = 0;
+            P.iinfo[addr] = in;
+        }
+        return;
+    }
     // ---- residual add + clip, store
     {
         const int x = t & 15, y = t >> 4;
@@ -394,14 +468,12 @@ __global__ void __launch_bounds__(256) h264_mb_kernel(H264Launch P) {
 // Kernel 2: intra + deblocking wavefront, one warp per task.
 // ===========================================================================
 struct __align__(16) WarpSmem {
-    rc_h264_mb q;        // the task's MB
-    int32_t coef[256];
-    int32_t coefc[128];
+    IntraInfo q;          // the task's MB (modes, availability)
+    int16_t res[384];     // residual samples: 16x16 luma, then 8x8 Cb, 8x8 Cr
     uint8_t cy[17 * 32];  // luma canvas: rows -1..15, cols -1..30 -> [(r+1)*32 + c+1]
     uint8_t cc[2][9 * 12];  // chroma canvas: rows -1..7, cols -1..10
     int32_t e[32];       // reference samples: top 0..15, left 16..23, corner 24
     int32_t f[32];       // smoothed reference samples (8x8)
-    uint32_t nzl, nzc;
 };
 
 __device__ __forceinline__ int cvy(const WarpSmem &S, int r, int c) { return S.cy[(r + 1) * 32 + c + 1]; }
@@ -509,108 +581,11 @@ __device__ __forceinline__ void smooth8(WarpSmem &S, int lane, Avail a) {
     }
 }
 
-// Level placement for one MB by a warp (intra lists: luma 0, chroma 1+c).
-__device__ bool warp_levels(WarpSmem &S, const H264Launch &P, int lane) {
-    const rc_h264_mb &m = S.q;
-    for (int i = lane; i < 256; i += 32) S.coef[i] = 0;
-    for (int i = lane; i < 128; i += 32) S.coefc[i] = 0;
-    if (lane == 0) { S.nzl = 0; S.nzc = 0; }
-    const int t8 = m.transform_8x8, i16 = m.kind == RC_H264_I16x16;
-    const int nl = __popc(m.luma_coded & (t8 ? 0xf : 0xffff)), ndc = __popc(m.dc_coded & 6);
-    const int nlum = (i16 && (m.dc_coded & 1)) ? 16 : 0;
-    const unsigned long long need = nlum + (unsigned long long)nl * (t8 ? 64 : 16) + ndc * 4 + __popc(m.chroma_coded) * 16;
-    if (m.coef_off + need > P.num_levels) return false;
-    __syncwarp();
-    const int16_t *lv = P.levels + m.coef_off;
-    const int qp = m.qp;
-    if (nlum && lane == 0) {  // put_luma_dc, slicedec.rs:1501-1515
-        int32_t c[16];
-        for (int k = 0; k < 16; k++) c[cZZ4[k]] = lv[k];
-        luma_dc_dequant(c, qp, __ldg(P.ls4 + (0 * 6 + qp % 6) * 16));
-        uint32_t bits = 0;
-        for (int r = 0; r < 16; r++)
-            if (c[r]) { S.coef[r * 16] = c[r]; bits |= 1u << r; }
-        atomicOr(&S.nzl, bits);
-    }
-    if (t8) {
-        for (int i = lane; i < 256; i += 32) {
-            int b8 = i >> 6, kk = i & 63;
-            if (!(m.luma_coded >> b8 & 1)) continue;
-            int l = lv[nlum + __popc(m.luma_coded & ((1u << b8) - 1)) * 64 + kk];
-            if (l) {
-                int p = cZZ8[kk];
-                S.coef[b8 * 64 + p] = scale8(l, __ldg(P.ls8 + (0 * 6 + qp % 6) * 64 + p), qp);
-                atomicOr(&S.nzl, 1u << b8);
-            }
-        }
-    } else {
-        for (int i = lane; i < 256; i += 32) {
-            int r = i >> 4, kk = i & 15;
-            if (kk < i16 || !(m.luma_coded >> r & 1)) continue;
-            int l = lv[nlum + __popc(m.luma_coded & ((1u << r) - 1)) * 16 + kk];
-            if (l) {
-                int p = cZZ4[kk];
-                S.coef[r * 16 + p] = scale4(l, __ldg(P.ls4 + (0 * 6 + qp % 6) * 16 + p), qp);
-                atomicOr(&S.nzl, 1u << r);
-            }
-        }
-    }
-    const int off_dc = nlum + nl * (t8 ? 64 : 16), off_ac = off_dc + ndc * 4;
-    if (lane < 2 && (m.dc_coded >> (1 + lane) & 1)) {
-        int c = lane, at = off_dc + ((c == 1 && (m.dc_coded & 2)) ? 4 : 0), qpc = m.qpc[c];
-        int32_t d[4] = {lv[at], lv[at + 1], lv[at + 2], lv[at + 3]};
-        chroma_dc_dequant(d, qpc, __ldg(P.ls4 + ((1 + c) * 6 + qpc % 6) * 16));
-        uint32_t bits = 0;
-        for (int b = 0; b < 4; b++)
-            if (d[b]) { S.coefc[c * 64 + b * 16] = d[b]; bits |= 1u << (c * 4 + b); }
-        atomicOr(&S.nzc, bits);
-    }
-    for (int i = lane; i < 128; i += 32) {
-        int c = i >> 6, b = (i >> 4) & 3, kk = i & 15, bit = c * 4 + b;
-        if (kk < 1 || !(m.chroma_coded >> bit & 1)) continue;
-        int l = lv[off_ac + __popc(m.chroma_coded & ((1u << bit) - 1)) * 16 + kk];
-        if (l) {
-            int qpc = m.qpc[c], p = cZZ4[kk];
-            S.coefc[c * 64 + b * 16 + p] = scale4(l, __ldg(P.ls4 + ((1 + c) * 6 + qpc % 6) * 16 + p), qpc);
-            atomicOr(&S.nzc, 1u << bit);
-        }
-    }
-    __syncwarp();
-    // inverse transforms, rows then columns
-    if (t8) {
-        if (S.nzl >> (lane >> 3) & 1) idct8_1d(S.coef + (lane >> 3) * 64 + (lane & 7) * 8, 1);
-    } else {
-        for (int i = lane; i < 64; i += 32)
-            if (S.nzl >> (i >> 2) & 1) idct4_1d(S.coef + (i >> 2) * 16 + (i & 3) * 4, 1);
-    }
-    if (S.nzc >> (lane >> 2) & 1) idct4_1d(S.coefc + (lane >> 2) * 16 + (lane & 3) * 4, 1);
-    __syncwarp();
-    if (t8) {
-        if (S.nzl >> (lane >> 3) & 1) idct8_1d(S.coef + (lane >> 3) * 64 + (lane & 7), 8);
-    } else {
-        for (int i = lane; i < 64; i += 32)
-            if (S.nzl >> (i >> 2) & 1) idct4_1d(S.coef + (i >> 2) * 16 + (i & 3), 4);
-    }
-    if (S.nzc >> (lane >> 2) & 1) idct4_1d(S.coefc + (lane >> 2) * 16 + (lane & 3), 4);
-    __syncwarp();
-    return true;
-}
-
-// residual of luma sample (x, y) of the MB, 0 when its block has no coefficients
-__device__ __forceinline__ int luma_res(const WarpSmem &S, int x, int y) {
-    if (S.q.transform_8x8) {
-        int b8 = (y >> 3) * 2 + (x >> 3);
-        return (S.nzl >> b8 & 1) ? (S.coef[b8 * 64 + (y & 7) * 8 + (x & 7)] + 32) >> 6 : 0;
-    }
-    int r = (y >> 2) * 4 + (x >> 2);
-    return (S.nzl >> r & 1) ? (S.coef[r * 16 + (y & 3) * 4 + (x & 3)] + 32) >> 6 : 0;
-}
-
 // reconstruct_intra, src/h264/dec/slicedec.rs:1325-1388, one warp.
 // nb: availability of neighbours L, T, TR, TL for intra prediction.
 __device__ void intra_mb(WarpSmem &S, const H264Launch &P, int lane, int mbx, int mby, const bool nb[4], uint8_t *Y,
                          uint8_t *U, uint8_t *V) {
-    const rc_h264_mb &m = S.q;
+    const IntraInfo &m = S.q;
     const int x0 = mbx * 16, y0 = mby * 16, cx0 = mbx * 8, cy0 = mby * 8;
     // canvas: neighbour samples
     if (mby > 0) {
@@ -640,9 +615,8 @@ __device__ void intra_mb(WarpSmem &S, const H264Launch &P, int lane, int mbx, in
             __syncwarp();
             if (lane < 16) {
                 int x = lane & 3, y = lane >> 2;
-                int v = pred_nxn_px(m.intra_modes[by * 4 + bx], S.e, S.e + 16, S.e[24], 4, a, x, y);
-                int r = by * 4 + bx;
-                if (S.nzl >> r & 1) v = clip255(v + ((S.coef[r * 16 + y * 4 + x] + 32) >> 6));
+                int v = pred_nxn_px(m.modes[by * 4 + bx], S.e, S.e + 16, S.e[24], 4, a, x, y);
+                v = clip255(v + S.res[(by * 4 + y) * 16 + bx * 4 + x]);
                 S.cy[(by * 4 + y + 1) * 32 + bx * 4 + x + 1] = (uint8_t)v;
             }
             __syncwarp();
@@ -662,8 +636,8 @@ __device__ void intra_mb(WarpSmem &S, const H264Launch &P, int lane, int mbx, in
 #pragma unroll
             for (int h = 0; h < 2; h++) {
                 int idx = lane + 32 * h, x = idx & 7, y = idx >> 3;
-                int v = pred_nxn_px(m.intra_modes[by * 4 + bx], S.f, S.f + 16, S.f[24], 8, a, x, y);
-                if (S.nzl >> b8 & 1) v = clip255(v + ((S.coef[b8 * 64 + y * 8 + x] + 32) >> 6));
+                int v = pred_nxn_px(m.modes[by * 4 + bx], S.f, S.f + 16, S.f[24], 8, a, x, y);
+                v = clip255(v + S.res[(by * 4 + y) * 16 + bx * 4 + x]);
                 S.cy[(by * 4 + y + 1) * 32 + bx * 4 + x + 1] = (uint8_t)v;
             }
             __syncwarp();
@@ -704,7 +678,7 @@ __device__ void intra_mb(WarpSmem &S, const H264Launch &P, int lane, int mbx, in
             else if (mode == 1) v = al ? cvy(S, y, -1) : 0;
             else if (mode == 2) v = dc;
             else v = clip255((aa + bb * (x - 7) + cc * (y - 7) + 16) >> 5);
-            v = clip255(v + luma_res(S, x, y));
+            v = clip255(v + S.res[y * 16 + x]);
             // rows 0..15 of the canvas are not read again by this MB's prediction
             S.cy[(y + 1) * 32 + x + 1] = (uint8_t)v;
         }
@@ -746,8 +720,7 @@ __device__ void intra_mb(WarpSmem &S, const H264Launch &P, int lane, int mbx, in
             }
 #undef CT
 #undef CL
-            int blk = c * 4 + (y >> 2) * 2 + (x >> 2);
-            if (S.nzc >> blk & 1) v = clip255(v + ((S.coefc[blk * 16 + (y & 3) * 4 + (x & 3)] + 32) >> 6));
+            v = clip255(v + S.res[256 + c * 64 + y * 8 + x]);
             outv[h] = v;
         }
         __syncwarp();
@@ -919,65 +892,6 @@ __device__ __forceinline__ void load_record(rc_h264_mb &dst, const rc_h264_mb *s
     const uint32_t *s = (const uint32_t *)src;
     uint32_t *d = (uint32_t *)&dst;
     for (int i = lane; i < (int)(sizeof(rc_h264_mb) / 4); i += 32) d[i] = __ldg(s + i);
-}
-
-// ===========================================================================
-// Kernel 2: intra MBs in anti-diagonal order, one warp per MB.
-// ===========================================================================
-__global__ void __launch_bounds__(128) h264_intra_kernel(H264Launch P) {
-    __shared__ WarpSmem sm[4];
-    WarpSmem &S = sm[threadIdx.x >> 5];
-    const int lane = threadIdx.x & 31;
-    uint8_t *Y = P.dpb + (size_t)P.out_slot * P.slot_bytes;
-    uint8_t *U = Y + P.u_off, *V = Y + P.v_off;
-    for (;;) {
-        unsigned ti = 0;
-        if (lane == 0) ti = aborted(P.error) ? 0xffffffffu : atomicAdd(P.counter, 1u);
-        ti = __shfl_sync(0xffffffffu, ti, 0);
-        if (ti >= (unsigned)P.ntasks) return;
-        const int addr = __ldg(P.tasks + ti) & 0x7fffffffu;
-        const int kind = __ldg(&P.mbs[addr].kind);
-        if (!wave_intra(kind)) continue;
-        const int mbx = addr % P.mb_w, mby = addr / P.mb_w;
-        // wait for intra neighbours (inter / PCM ones were written by the MB kernel)
-        bool ok = true;
-        if (lane < 4) {
-            const int dx = lane == 0 ? -1 : lane == 2 ? 1 : lane == 3 ? -1 : 0, dy = lane == 0 ? 0 : -1;
-            int nx = mbx + dx, ny = mby + dy;
-            if (nx >= 0 && ny >= 0 && nx < P.mb_w) {
-                int na = ny * P.mb_w + nx;
-                if (wave_intra(__ldg(&P.mbs[na].kind))) ok = wait_flag(P.rflag + na, P.epoch, P.wait_limit, P.error);
-            }
-        }
-        if (!__all_sync(0xffffffffu, ok)) {
-            if (lane == 0) set_error(P.error, RC_DEV_ERR_TIMEOUT);
-            return;
-        }
-        load_record(S.q, P.mbs + addr, lane);
-        __syncwarp();
-        // start_mb neighbour availability + intra_nb, slicedec.rs:489-508, 525-530
-        bool nb[4];
-#pragma unroll
-        for (int n = 0; n < 4; n++) {
-            const int dx = n == 0 ? -1 : n == 2 ? 1 : n == 3 ? -1 : 0, dy = n == 0 ? 0 : -1;
-            int nx = mbx + dx, ny = mby + dy;
-            bool a = false;
-            if (nx >= 0 && ny >= 0 && nx < P.mb_w) {
-                const rc_h264_mb *pm = P.mbs + ny * P.mb_w + nx;
-                int k = __ldg(&pm->kind);
-                a = k != RC_H264_NONE && __ldg(&pm->slice) == S.q.slice && (!P.constrained_intra || is_intra(k));
-            }
-            nb[n] = a;
-        }
-        if (!warp_levels(S, P, lane)) {
-            if (lane == 0) set_error(P.error, RC_DEV_ERR_RECORD);
-        } else {
-            intra_mb(S, P, lane, mbx, mby, nb, Y, U, V);
-        }
-        __threadfence();
-        __syncwarp();
-        if (lane == 0) st_release(P.rflag + addr, P.epoch);
-    }
 }
 
 // ===========================================================================
@@ -1172,19 +1086,339 @@ __global__ void __launch_bounds__(128) h264_db_params_kernel(H264Launch P) {
     compute_db(P, rec[w][0], rec[w][1], rec[w][2], addr, lane, P.db + addr);
 }
 
+
+// ===========================================================================
+// Wave kernel: intra reconstruction and the loop filter in one cooperative
+// launch.  CTAs [0, intra_blocks) take intra MBs in anti-diagonal order, one
+// warp per MB; the remaining CTAs each filter a band of WAVE_WARPS MB rows,
+// one warp per row walking left to right.  Inside a band the MB above comes
+// through shared memory (a ring of final bottom rows per row); across bands
+// through global memory and a per-row progress word.  A row filters MB x once
+// the intra MBs among (x-1..x+1, y..y+1) are reconstructed and the row above
+// has finished MBs 0..x.
+// ===========================================================================
+constexpr int WAVE_WARPS = 8;
+constexpr int RING = 8;
+
+struct __align__(16) BandRow {
+    RowTile T;
+    uint8_t ring[RING][128];  // bottom rows 12..15 of each final MB: luma 4x16, Cb 4x8, Cr 4x8
+};
+struct __align__(16) BandSmem {
+    BandRow r[WAVE_WARPS];
+    volatile int prog[WAVE_WARPS];  // MBs of each row that are final (in this CTA's rows)
+};
+union __align__(16) WaveSmem {
+    WarpSmem iw[WAVE_WARPS];
+    BandSmem band;
+};
+
+__device__ void wave_intra_worker(const H264Launch &P, WarpSmem &S, int lane) {
+    uint8_t *Y = P.dpb + (size_t)P.out_slot * P.slot_bytes;
+    uint8_t *U = Y + P.u_off, *V = Y + P.v_off;
+    for (;;) {
+        unsigned ti = 0;
+        if (lane == 0) ti = aborted(P.error) ? 0xffffffffu : atomicAdd(P.counter, 1u);
+        ti = __shfl_sync(0xffffffffu, ti, 0);
+        if (ti >= (unsigned)P.ntasks) return;
+        const int addr = __ldg(P.tasks + ti) & 0x7fffffffu;
+        if (!wave_intra(__ldg(&P.mbs[addr].kind))) continue;
+        const int mbx = addr % P.mb_w, mby = addr / P.mb_w;
+        // prediction parameters and residual (independent of the neighbours)
+        if (lane < 8) ((uint32_t *)&S.q)[lane] = __ldcg((const uint32_t *)(P.iinfo + addr) + lane);
+        {
+            const uint4 *src = (const uint4 *)(P.ires + (size_t)addr * 384);
+            uint4 *dst = (uint4 *)S.res;
+            dst[lane] = __ldcg(src + lane);
+            if (lane < 16) dst[32 + lane] = __ldcg(src + 32 + lane);
+        }
+        __syncwarp();
+        // wait for the intra neighbours whose samples the modes read
+        bool ok = true;
+        const int waits = S.q.wait;
+        if (lane < 4 && (waits >> lane & 1)) {
+            const int dx = lane == 0 ? -1 : lane == 2 ? 1 : lane == 3 ? -1 : 0, dy = lane == 0 ? 0 : -1;
+            ok = wait_flag(P.rflag + (mby + dy) * P.mb_w + mbx + dx, P.epoch, P.wait_limit, P.error);
+        }
+        if (!__all_sync(0xffffffffu, ok)) {
+            if (lane == 0) set_error(P.error, RC_DEV_ERR_TIMEOUT);
+            return;
+        }
+        bool nb[4];
+#pragma unroll
+        for (int n = 0; n < 4; n++) nb[n] = S.q.nb >> n & 1;
+        intra_mb(S, P, lane, mbx, mby, nb, Y, U, V);
+        __threadfence();
+        __syncwarp();
+        if (lane == 0) st_release(P.rflag + addr, P.epoch);
+    }
+}
+
+// One MB row of a band.  w: row index inside the band; last: w is the band's
+// last row (publishes to global memory for the next band).
+__device__ void wave_band_row(const H264Launch &P, BandSmem &B, int w, int my, bool last, int lane) {
+    RowTile &T = B.r[w].T;
+    uint8_t *Y = P.dpb + (size_t)P.out_slot * P.slot_bytes;
+    uint8_t *U = Y + P.u_off, *V = Y + P.v_off;
+    const uint32_t tag = (P.epoch & 0xffffu) << 16;
+    const bool luma = lane < 16;
+    const int cc = (lane - 16) >> 3, li = luma ? lane : (lane - 16) & 7;
+    const bool below = my + 1 < P.mb_h;
+    const bool ring_out = !last && below;  // the next row of the band reads this row's ring
+    uint4 pre_y = make_uint4(0, 0, 0, 0);
+    uint2 pre_c = make_uint2(0, 0);
+    uint32_t pre_db = 0;
+    // intra reconstruction of MB column x in rows y, y+1 (lanes 0, 1)
+    auto wait_intra = [&](int x) -> bool {
+        bool ok = true;
+        if (lane < 2 && x < P.mb_w) {
+            const int ry = my + lane;
+            if (ry < P.mb_h) {
+                const int a = ry * P.mb_w + x;
+                if (wave_intra(__ldg(&P.mbs[a].kind))) ok = wait_flag(P.rflag + a, P.epoch, P.wait_limit, P.error);
+            }
+        }
+        return __all_sync(0xffffffffu, ok);
+    };
+    auto prefetch = [&](int x) {
+        if (luma) pre_y = __ldcg((const uint4 *)(Y + (size_t)(my * 16 + lane) * P.pitch + x * 16));
+        else pre_c = __ldcg((const uint2 *)((cc ? V : U) + (size_t)(my * 8 + li) * P.cpitch + x * 8));
+        if (lane < 12) pre_db = __ldcg((const uint32_t *)(P.db + (size_t)my * P.mb_w + x) + lane);
+    };
+    if (!wait_intra(0)) { if (lane == 0) set_error(P.error, RC_DEV_ERR_TIMEOUT); return; }
+    prefetch(0);
+    for (int x = 0; x < P.mb_w; x++) {
+        // ---- stage MB x
+        if (luma) {
+            uint32_t q[4] = {pre_y.x, pre_y.y, pre_y.z, pre_y.w};
+#pragma unroll
+            for (int i = 0; i < 4; i++) *(uint32_t *)&T.y[lane + 4][4 + 4 * i] = q[i];
+        } else {
+            *(uint32_t *)&T.c[cc][li + 4][4] = pre_c.x;
+            *(uint32_t *)&T.c[cc][li + 4][8] = pre_c.y;
+        }
+        if (lane < 12) ((uint32_t *)&T.db)[lane] = pre_db;
+        // ---- intra MBs this MB's edges touch: (x+1, y) and (x+1, y+1) are new
+        if (!wait_intra(x + 1)) { if (lane == 0) set_error(P.error, RC_DEV_ERR_TIMEOUT); return; }
+        // ---- the MB above, rows 12..15 (final once row y-1 has finished MBs 0..x)
+        if (my > 0) {
+            const uint32_t need = (uint32_t)min(x + 1, P.mb_w);
+            bool ok = true;
+            if (w == 0) {
+                if (lane == 0) {
+                    const uint32_t *f = P.rowprog + my - 1;
+                    uint32_t it = 0, v;
+                    while (((v = ld_acquire(f)) & 0xffff0000u) != tag || (v & 0xffffu) < need) {
+                        if (++it > P.wait_limit || ((it & 63) == 0 && aborted(P.error))) { ok = false; break; }
+                        if (it > 256) __nanosleep(64);
+                    }
+                }
+                if (!__shfl_sync(0xffffffffu, ok, 0)) { if (lane == 0) set_error(P.error, RC_DEV_ERR_TIMEOUT); return; }
+                if (lane < 4) {
+                    uint4 v = __ldcg((const uint4 *)(Y + (size_t)(my * 16 - 4 + lane) * P.pitch + x * 16));
+                    uint32_t q[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+                    for (int i = 0; i < 4; i++) *(uint32_t *)&T.y[lane][4 + 4 * i] = q[i];
+                } else if (lane < 12) {
+                    int c = (lane - 4) >> 2, r = (lane - 4) & 3;
+                    uint2 v = __ldcg((const uint2 *)((c ? V : U) + (size_t)(my * 8 - 4 + r) * P.cpitch + x * 8));
+                    *(uint32_t *)&T.c[c][r][4] = v.x;
+                    *(uint32_t *)&T.c[c][r][8] = v.y;
+                }
+            } else {
+                if (lane == 0) {
+                    uint32_t it = 0;
+                    while (B.prog[w - 1] < (int)need) {
+                        if (++it > P.wait_limit || ((it & 63) == 0 && aborted(P.error))) { ok = false; break; }
+                        if (it > 1024) __nanosleep(32);
+                    }
+                }
+                if (!__shfl_sync(0xffffffffu, ok, 0)) { if (lane == 0) set_error(P.error, RC_DEV_ERR_TIMEOUT); return; }
+                __threadfence_block();
+                const uint8_t *slot = B.r[w - 1].ring[x % RING];
+                if (lane < 16) {  // luma rows 12..15: 4 rows x 16 bytes as 16 words
+                    *(uint32_t *)&T.y[lane >> 2][4 + 4 * (lane & 3)] = *(const uint32_t *)(slot + 4 * lane);
+                } else {          // chroma: 2 planes x 4 rows x 8 bytes as 16 words
+                    int k = lane - 16, c = k >> 3, r = (k >> 1) & 3, h = k & 1;
+                    *(uint32_t *)&T.c[c][r][4 + 4 * h] = *(const uint32_t *)(slot + 64 + 4 * k);
+                }
+            }
+        }
+        __syncwarp();
+        if (x + 1 < P.mb_w) prefetch(x + 1);
+        const DbMb &db = T.db;
+        if (db.flags) {
+            const int aoff = db.aoff, boff = db.boff;
+            {  // vertical edges, one row per lane
+                int sv[20];
+                uint8_t *row = luma ? T.y[lane + 4] : T.c[cc][li + 4];
+                const int n = luma ? 20 : 12;
+#pragma unroll
+                for (int i = 0; i < 20; i++) sv[i] = i < n ? row[i] : 0;
+                const int k = luma ? li >> 2 : li >> 1;
+#pragma unroll
+                for (int e = 0; e < 4; e++) {
+                    const int bsv = db.bs[(e << 2) | k];
+                    const bool strong = db.bs[e << 2] >= 4;
+                    int alpha, beta, tc0;
+                    if (luma) {
+                        edge_consts(e == 0 ? db.qp[1] : db.qp[0], db.qp[0], bsv, aoff, boff, alpha, beta, tc0);
+                        filt_luma(sv + 4 * e, bsv, strong, alpha, beta, tc0);
+                    } else if ((e & 1) == 0) {
+                        edge_consts(e == 0 ? db.qpc[1][cc] : db.qpc[0][cc], db.qpc[0][cc], bsv, aoff, boff, alpha,
+                                    beta, tc0);
+                        filt_chroma(sv + 2 * e, bsv, strong, alpha, beta, tc0);
+                    }
+                }
+#pragma unroll
+                for (int i = 0; i < 20; i++)
+                    if (i < n) row[i] = (uint8_t)sv[i];
+            }
+            __syncwarp();
+            {  // horizontal edges, one column per lane
+                int sv[20];
+                const int n = luma ? 20 : 12;
+#pragma unroll
+                for (int i = 0; i < 20; i++) sv[i] = i < n ? (luma ? T.y[i][lane + 4] : T.c[cc][i][li + 4]) : 0;
+                const int k = luma ? li >> 2 : li >> 1;
+#pragma unroll
+                for (int e = 0; e < 4; e++) {
+                    const int bsv = db.bs[16 | (e << 2) | k];
+                    const bool strong = db.bs[16 | (e << 2)] >= 4;
+                    int alpha, beta, tc0;
+                    if (luma) {
+                        edge_consts(e == 0 ? db.qp[2] : db.qp[0], db.qp[0], bsv, aoff, boff, alpha, beta, tc0);
+                        filt_luma(sv + 4 * e, bsv, strong, alpha, beta, tc0);
+                    } else if ((e & 1) == 0) {
+                        edge_consts(e == 0 ? db.qpc[2][cc] : db.qpc[0][cc], db.qpc[0][cc], bsv, aoff, boff, alpha,
+                                    beta, tc0);
+                        filt_chroma(sv + 2 * e, bsv, strong, alpha, beta, tc0);
+                    }
+                }
+#pragma unroll
+                for (int i = 0; i < 20; i++)
+                    if (i < n) {
+                        if (luma) T.y[i][lane + 4] = (uint8_t)sv[i];
+                        else T.c[cc][i][li + 4] = (uint8_t)sv[i];
+                    }
+            }
+            __syncwarp();
+        }
+        // ---- final samples to the picture (as h264_deblock_kernel)
+        if (luma) {
+            uint8_t *dst = Y + (size_t)(my * 16 + lane) * P.pitch + x * 16;
+            const uint8_t *r = T.y[lane + 4];
+            *(uint32_t *)(dst + 0) = *(const uint32_t *)(r + 4);
+            *(uint32_t *)(dst + 4) = *(const uint32_t *)(r + 8);
+            *(uint32_t *)(dst + 8) = *(const uint32_t *)(r + 12);
+            if (x > 0) *(uint32_t *)(dst - 4) = *(const uint32_t *)(r + 0);
+            if (x == P.mb_w - 1) *(uint32_t *)(dst + 12) = *(const uint32_t *)(r + 16);
+        } else {
+            uint8_t *dst = (cc ? V : U) + (size_t)(my * 8 + li) * P.cpitch + x * 8;
+            const uint8_t *r = T.c[cc][li + 4];
+            *(uint32_t *)(dst + 0) = *(const uint32_t *)(r + 4);
+            if (x > 0) *(uint32_t *)(dst - 4) = *(const uint32_t *)(r + 0);
+            if (x == P.mb_w - 1) *(uint32_t *)(dst + 4) = *(const uint32_t *)(r + 8);
+        }
+        if (my > 0 && db.flags) {
+            if (lane < 3) {
+                uint8_t *dst = Y + (size_t)(my * 16 - 3 + lane) * P.pitch + x * 16;
+                const uint8_t *r = T.y[lane + 1] + 4;
+                *(uint4 *)dst = make_uint4(*(const uint32_t *)(r), *(const uint32_t *)(r + 4),
+                                           *(const uint32_t *)(r + 8), *(const uint32_t *)(r + 12));
+            } else if (lane < 5) {
+                int c = lane - 3;
+                uint8_t *dst = (c ? V : U) + (size_t)(my * 8 - 1) * P.cpitch + x * 8;
+                const uint8_t *r = T.c[c][3] + 4;
+                *(uint2 *)dst = make_uint2(*(const uint32_t *)(r), *(const uint32_t *)(r + 4));
+            }
+        }
+        // ---- bottom rows for the next row of the band: MB x columns 0..11
+        // now, MB x-1 columns 12..15 (final after this MB's left edge)
+        if (ring_out) {
+            bool ok = true;
+            if (lane == 0) {
+                uint32_t it = 0;
+                while (B.prog[w + 1] < x - RING + 1) {
+                    if (++it > P.wait_limit || ((it & 63) == 0 && aborted(P.error))) { ok = false; break; }
+                    if (it > 1024) __nanosleep(32);
+                }
+            }
+            if (!__shfl_sync(0xffffffffu, ok, 0)) { if (lane == 0) set_error(P.error, RC_DEV_ERR_TIMEOUT); return; }
+            uint8_t *cur = B.r[w].ring[x % RING], *prev = B.r[w].ring[(x + RING - 1) % RING];
+            if (lane < 16) {
+                const int r = lane >> 2, q = lane & 3;  // luma row 12 + r, word q (columns 4q..4q+3)
+                if (q < 3) *(uint32_t *)(cur + 4 * lane) = *(const uint32_t *)&T.y[16 + r][4 + 4 * q];
+                else {
+                    if (x > 0) *(uint32_t *)(prev + 4 * lane) = *(const uint32_t *)&T.y[16 + r][0];
+                    if (x == P.mb_w - 1) *(uint32_t *)(cur + 4 * lane) = *(const uint32_t *)&T.y[16 + r][16];
+                }
+            } else {
+                const int k = lane - 16, c = k >> 3, r = (k >> 1) & 3, h = k & 1;  // chroma row 4 + r, half h
+                if (h == 0) *(uint32_t *)(cur + 64 + 4 * k) = *(const uint32_t *)&T.c[c][8 + r][4];
+                else {
+                    if (x > 0) *(uint32_t *)(prev + 64 + 4 * k) = *(const uint32_t *)&T.c[c][8 + r][0];
+                    if (x == P.mb_w - 1) *(uint32_t *)(cur + 64 + 4 * k) = *(const uint32_t *)&T.c[c][8 + r][8];
+                }
+            }
+        }
+        __syncwarp();
+        const int done = x == P.mb_w - 1 ? P.mb_w : x;
+        if (last) {
+            __threadfence();
+            __syncwarp();
+            if (lane == 0) st_release(P.rowprog + my, tag | (uint32_t)done);
+        } else {
+            __threadfence_block();
+            __syncwarp();
+            if (lane == 0) B.prog[w] = done;
+        }
+        // ---- shift: this MB's columns 12..15 become the next MB's left columns
+        if (luma) *(uint32_t *)&T.y[lane + 4][0] = *(const uint32_t *)&T.y[lane + 4][16];
+        else *(uint32_t *)&T.c[cc][li + 4][0] = *(const uint32_t *)&T.c[cc][li + 4][8];
+        __syncwarp();
+    }
+}
+
+__global__ void __launch_bounds__(WAVE_WARPS * 32) h264_wave_kernel(H264Launch P) {
+    __shared__ WaveSmem sm;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if ((int)blockIdx.x < P.intra_blocks) {
+        wave_intra_worker(P, sm.iw[warp], lane);
+        return;
+    }
+    const int band = blockIdx.x - P.intra_blocks;
+    const int my = band * WAVE_WARPS + warp;
+    if (lane == 0) sm.band.prog[warp] = 0;
+    __syncthreads();
+    if (my >= P.mb_h) return;
+    const bool last = warp == WAVE_WARPS - 1 || my == P.mb_h - 1;
+    wave_band_row(P, sm.band, warp, my, last, lane);
+}
+
 }  // namespace
 
 void rc_launch_h264_mb(const H264Launch &p, cudaStream_t st) {
     h264_mb_kernel<<<p.mb_w * p.mb_h, 256, 0, st>>>(p);
 }
 
-void rc_launch_h264_intra(const H264Launch &p, cudaStream_t st, int wave_blocks) {
-    cudaMemsetAsync(p.counter, 0, sizeof(uint32_t), st);
-    h264_intra_kernel<<<wave_blocks, 128, 0, st>>>(p);
+int rc_h264_wave_capacity() {
+    int dev = 0, sms = 0, per = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, h264_wave_kernel, WAVE_WARPS * 32, 0) != cudaSuccess)
+        return 0;
+    return per * sms;
 }
 
-void rc_launch_h264_deblock(const H264Launch &p, cudaStream_t st) {
-    h264_deblock_kernel<<<p.mb_h, 32, 0, st>>>(p);
+int rc_launch_h264_wave(const H264Launch &p, cudaStream_t st) {
+    cudaMemsetAsync(p.counter, 0, sizeof(uint32_t), st);
+    const int bands = (p.mb_h + WAVE_WARPS - 1) / WAVE_WARPS;
+    H264Launch q = p;
+    void *args[] = {&q};
+    cudaError_t e = cudaLaunchCooperativeKernel((const void *)h264_wave_kernel, dim3(p.intra_blocks + bands),
+                                                dim3(WAVE_WARPS * 32), args, 0, st);
+    return e == cudaSuccess ? 0 : -1;
 }
 
 // ===========================================================================

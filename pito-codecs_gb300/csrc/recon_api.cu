@@ -62,6 +62,9 @@ struct rc_stream {
     uint32_t *rflag = nullptr, *dflag = nullptr, *counter = nullptr, *error = nullptr, *tasks = nullptr;
     uint32_t *rowprog = nullptr;
     DbMb *db = nullptr;
+    IntraInfo *iinfo = nullptr;
+    int16_t *ires = nullptr;
+    int intra_blocks = 0;
     // HEVC
     DevBuf ctbs, blk, mvf, tus, hslices, scaling;
     uint8_t *work = nullptr;     // picture being reconstructed (pre-SAO)
@@ -260,6 +263,8 @@ void destroy(rc_stream *s) {
     cudaFree(s->ls);
     cudaFree(s->rowprog);
     cudaFree(s->db);
+    dev_free(s, s->iinfo, (size_t)s->mb_w * s->mb_h * sizeof(IntraInfo));
+    dev_free(s, s->ires, (size_t)s->mb_w * s->mb_h * 384 * sizeof(int16_t));
     for (int i = 0; i < 2; i++) {
         if (s->staging[i]) cudaFreeHost(s->staging[i]);
         if (s->staged[i]) cudaEventDestroy(s->staged[i]);
@@ -443,6 +448,18 @@ int rc_stream_create(int codec, int width, int height, int bit_depth, int dpb_sl
     ok = ok && cudaMalloc(&s->ls, (2304 + 2304 * 4) * sizeof(int32_t)) == cudaSuccess;
     ok = ok && cudaMalloc(&s->rowprog, (size_t)s->mb_h * sizeof(uint32_t)) == cudaSuccess;
     ok = ok && cudaMalloc(&s->db, (size_t)n * sizeof(DbMb)) == cudaSuccess;
+    if (codec == RC_CODEC_H264) {
+        ok = ok && dev_alloc(s, (void **)&s->iinfo, (size_t)n * sizeof(IntraInfo));
+        ok = ok && dev_alloc(s, (void **)&s->ires, (size_t)n * 384 * sizeof(int16_t));
+        // wave kernel: loop-filter bands of 8 MB rows plus intra CTAs, all resident (cooperative launch)
+        const int bands = (s->mb_h + 7) / 8, cap = rc_h264_wave_capacity();
+        s->intra_blocks = std::min(32, cap - bands);
+        if (const char *e = getenv("PITO_RECON_INTRA_BLOCKS")) {
+            int v = atoi(e);
+            if (v > 0) s->intra_blocks = std::min(v, cap - bands);
+        }
+        ok = ok && s->intra_blocks >= 1;
+    }
     if (codec == RC_CODEC_HEVC) {
         const size_t nres = (size_t)s->width * s->height + 2 * (size_t)s->cw * s->ch;
         ok = ok && dev_alloc(s, (void **)&s->work, s->slot_bytes);
@@ -550,8 +567,12 @@ int rc_h264_submit(rc_stream *s, const rc_h264_picture *pic, int out_slot) {
     L.db = s->db;
     L.rowprog = s->rowprog;
     timed(s, RC_KERNEL_H264_MB, [&] { rc_launch_h264_mb(L, s->st); });
-    timed(s, RC_KERNEL_H264_INTRA, [&] { rc_launch_h264_intra(L, s->st, s->wave_blocks); });
-    timed(s, RC_KERNEL_H264_DEBLOCK, [&] { rc_launch_h264_deblock(L, s->st); });
+    L.iinfo = s->iinfo;
+    L.ires = s->ires;
+    L.intra_blocks = s->intra_blocks;
+    int lrc = 0;
+    timed(s, RC_KERNEL_H264_WAVE, [&] { lrc = rc_launch_h264_wave(L, s->st); });
+    if (lrc != 0) return cuda_fail(s);
     s->submits++;
     if (cudaGetLastError() != cudaSuccess) return cuda_fail(s);
     return RC_OK;

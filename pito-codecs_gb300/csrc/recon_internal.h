@@ -28,6 +28,18 @@ struct DbMb {
 };
 static_assert(sizeof(DbMb) == 48, "DbMb layout");
 
+// What an intra MB's reconstruction needs besides its residual, prepared by
+// h264_mb_kernel: neighbour availability for intra prediction (bits 0..3:
+// left, top, top-right, top-left) and the intra neighbours whose samples the
+// MB's modes actually read (same bits) -- the ones the wavefront waits for.
+struct IntraInfo {
+    uint8_t kind, t8, i16_mode, chroma_mode;
+    uint8_t nb, wait, pad0, pad1;
+    uint8_t modes[16];
+    uint32_t pad2[2];
+};
+static_assert(sizeof(IntraInfo) == 32, "IntraInfo layout");
+
 struct H264Launch {
     const rc_h264_mb *mbs;
     const rc_h264_slice *slices;
@@ -52,6 +64,9 @@ struct H264Launch {
     uint32_t wait_limit;
     DbMb *db;             // per-MB loop-filter parameters
     uint32_t *rowprog;    // per MB row: (epoch & 0xffff) << 16 | MBs final
+    IntraInfo *iinfo;     // per MB (intra MBs)
+    int16_t *ires;        // per MB: 256 luma + 2 x 64 chroma residual samples (intra MBs)
+    int intra_blocks;     // CTAs of the wave kernel that run intra MBs; the rest run loop-filter bands
 };
 
 struct HevcLaunch {
@@ -87,5 +102,7 @@ void rc_launch_hevc_sao(const HevcLaunch &p, cudaStream_t st);
 
 // Launchers (h264_kernels.cu).
 void rc_launch_h264_mb(const H264Launch &p, cudaStream_t st);
-void rc_launch_h264_intra(const H264Launch &p, cudaStream_t st, int wave_blocks);
-void rc_launch_h264_deblock(const H264Launch &p, cudaStream_t st);
+// Intra reconstruction and the loop filter in one cooperative launch.
+int rc_launch_h264_wave(const H264Launch &p, cudaStream_t st);
+// CTAs of the wave kernel that can be resident at once (0 if unknown).
+int rc_h264_wave_capacity();
