@@ -1138,7 +1138,8 @@ __device__ void wave_intra_worker(const H264Launch &P, WarpSmem &S, int lane) {
         const int waits = S.q.wait;
         if (lane < 4 && (waits >> lane & 1)) {
             const int dx = lane == 0 ? -1 : lane == 2 ? 1 : lane == 3 ? -1 : 0, dy = lane == 0 ? 0 : -1;
-            ok = wait_flag(P.rflag + (mby + dy) * P.mb_w + mbx + dx, P.epoch, P.wait_limit, P.error);
+            const int nx = mbx + dx, ny = mby + dy;
+            if (nx >= 0 && ny >= 0 && nx < P.mb_w) ok = wait_flag(P.rflag + ny * P.mb_w + nx, P.epoch, P.wait_limit, P.error);
         }
         if (!__all_sync(0xffffffffu, ok)) {
             if (lane == 0) set_error(P.error, RC_DEV_ERR_TIMEOUT);

@@ -566,10 +566,10 @@ int rc_h264_submit(rc_stream *s, const rc_h264_picture *pic, int out_slot) {
     L.wait_limit = s->wait_limit;
     L.db = s->db;
     L.rowprog = s->rowprog;
-    timed(s, RC_KERNEL_H264_MB, [&] { rc_launch_h264_mb(L, s->st); });
     L.iinfo = s->iinfo;
     L.ires = s->ires;
     L.intra_blocks = s->intra_blocks;
+    timed(s, RC_KERNEL_H264_MB, [&] { rc_launch_h264_mb(L, s->st); });
     int lrc = 0;
     timed(s, RC_KERNEL_H264_WAVE, [&] { lrc = rc_launch_h264_wave(L, s->st); });
     if (lrc != 0) return cuda_fail(s);
