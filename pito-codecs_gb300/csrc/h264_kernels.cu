@@ -1365,10 +1365,16 @@ __device__ void wave_band_row(const H264Launch &P, BandSmem &B, int w, int my, b
         }
         __syncwarp();
         const int done = x == P.mb_w - 1 ? P.mb_w : x;
+        // progress: in shared memory for the rows of this band (the row below
+        // reads it, the row above throttles its ring on it), and in global
+        // memory for the band's last row (read by the next band)
         if (last) {
             __threadfence();
             __syncwarp();
-            if (lane == 0) st_release(P.rowprog + my, tag | (uint32_t)done);
+            if (lane == 0) {
+                st_release(P.rowprog + my, tag | (uint32_t)done);
+                B.prog[w] = done;
+            }
         } else {
             __threadfence_block();
             __syncwarp();
