@@ -1107,6 +1107,8 @@ struct __align__(16) BandRow {
 struct __align__(16) BandSmem {
     BandRow r[WAVE_WARPS];
     volatile int prog[WAVE_WARPS];  // MBs of each row that are final (in this CTA's rows)
+    volatile int icol;              // columns whose intra MBs (band rows + the row below) are reconstructed
+    volatile int above;             // MBs of the row above the band that are final
 };
 union __align__(16) WaveSmem {
     WarpSmem iw[WAVE_WARPS];
@@ -1186,7 +1188,22 @@ __device__ void wave_band_row(const H264Launch &P, BandSmem &B, int w, int my, b
         else pre_c = __ldcg((const uint2 *)((cc ? V : U) + (size_t)(my * 8 + li) * P.cpitch + x * 8));
         if (lane < 12) pre_db = __ldcg((const uint32_t *)(P.db + (size_t)my * P.mb_w + x) + lane);
     };
-    if (!wait_intra(0)) { if (lane == 0) set_error(P.error, RC_DEV_ERR_TIMEOUT); return; }
+    // wait until a helper-published shared counter reaches `need`
+    auto wait_shared = [&](volatile int *c, int need) -> bool {
+        bool ok = true;
+        if (lane == 0) {
+            uint32_t it = 0;
+            while (*c < need) {
+                if (++it > P.wait_limit || ((it & 63) == 0 && aborted(P.error))) { ok = false; break; }
+                if (it > 1024) __nanosleep(32);
+            }
+        }
+        ok = __shfl_sync(0xffffffffu, ok, 0);
+        __threadfence_block();
+        return ok;
+    };
+    (void)wait_intra;
+    if (!wait_shared(&B.icol, min(1, P.mb_w))) { if (lane == 0) set_error(P.error, RC_DEV_ERR_TIMEOUT); return; }
     prefetch(0);
     for (int x = 0; x < P.mb_w; x++) {
         // ---- stage MB x
@@ -1200,21 +1217,13 @@ __device__ void wave_band_row(const H264Launch &P, BandSmem &B, int w, int my, b
         }
         if (lane < 12) ((uint32_t *)&T.db)[lane] = pre_db;
         // ---- intra MBs this MB's edges touch: (x+1, y) and (x+1, y+1) are new
-        if (!wait_intra(x + 1)) { if (lane == 0) set_error(P.error, RC_DEV_ERR_TIMEOUT); return; }
+        if (!wait_shared(&B.icol, min(x + 2, P.mb_w))) { if (lane == 0) set_error(P.error, RC_DEV_ERR_TIMEOUT); return; }
         // ---- the MB above, rows 12..15 (final once row y-1 has finished MBs 0..x)
         if (my > 0) {
             const uint32_t need = (uint32_t)min(x + 1, P.mb_w);
             bool ok = true;
             if (w == 0) {
-                if (lane == 0) {
-                    const uint32_t *f = P.rowprog + my - 1;
-                    uint32_t it = 0, v;
-                    while (((v = ld_acquire(f)) & 0xffff0000u) != tag || (v & 0xffffu) < need) {
-                        if (++it > P.wait_limit || ((it & 63) == 0 && aborted(P.error))) { ok = false; break; }
-                        if (it > 256) __nanosleep(64);
-                    }
-                }
-                if (!__shfl_sync(0xffffffffu, ok, 0)) { if (lane == 0) set_error(P.error, RC_DEV_ERR_TIMEOUT); return; }
+                if (!wait_shared(&B.above, (int)need)) { if (lane == 0) set_error(P.error, RC_DEV_ERR_TIMEOUT); return; }
                 if (lane < 4) {
                     uint4 v = __ldcg((const uint4 *)(Y + (size_t)(my * 16 - 4 + lane) * P.pitch + x * 16));
                     uint32_t q[4] = {v.x, v.y, v.z, v.w};
@@ -1367,8 +1376,8 @@ __device__ void wave_band_row(const H264Launch &P, BandSmem &B, int w, int my, b
         const int done = x == P.mb_w - 1 ? P.mb_w : x;
         // progress: in shared memory for the rows of this band (the row below
         // reads it, the row above throttles its ring on it), and in global
-        // memory for the band's last row (read by the next band)
-        if (last) {
+        // memory for the band's last row (read by the next band; every 4 MBs)
+        if (last && ((x & 3) == 3 || done == P.mb_w)) {
             __threadfence();
             __syncwarp();
             if (lane == 0) {
@@ -1387,17 +1396,69 @@ __device__ void wave_band_row(const H264Launch &P, BandSmem &B, int w, int my, b
     }
 }
 
-__global__ void __launch_bounds__(WAVE_WARPS * 32) h264_wave_kernel(H264Launch P) {
+// Helper warp 0 of a band: confirms, column by column, that the intra MBs of
+// the band's rows and of the row below are reconstructed (acquire loads of
+// their flags) and publishes the count of ready columns in shared memory.
+__device__ void wave_band_intra_helper(const H264Launch &P, BandSmem &B, int y0, int rows, int lane) {
+    const int ry = y0 + lane;
+    const bool mine = lane <= rows && ry < P.mb_h;
+    for (int x = 0; x < P.mb_w; x++) {
+        bool ok = true;
+        if (mine) {
+            const int a = ry * P.mb_w + x;
+            if (wave_intra(__ldg(&P.mbs[a].kind))) ok = wait_flag(P.rflag + a, P.epoch, P.wait_limit, P.error);
+        }
+        if (!__all_sync(0xffffffffu, ok)) {
+            if (lane == 0) set_error(P.error, RC_DEV_ERR_TIMEOUT);
+            return;
+        }
+        __threadfence_block();
+        __syncwarp();
+        if (lane == 0) B.icol = x + 1;
+    }
+}
+
+// Helper warp 1 of a band: mirrors the global progress word of the row above
+// the band into shared memory.
+__device__ void wave_band_above_helper(const H264Launch &P, BandSmem &B, int y0, int lane) {
+    if (lane != 0) return;
+    if (y0 == 0) { B.above = P.mb_w; return; }
+    const uint32_t tag = (P.epoch & 0xffffu) << 16;
+    const uint32_t *f = P.rowprog + y0 - 1;
+    uint32_t it = 0;
+    int seen = 0;
+    while (seen < P.mb_w) {
+        const uint32_t v = ld_acquire(f);
+        if ((v & 0xffff0000u) == tag && (int)(v & 0xffffu) > seen) {
+            seen = v & 0xffffu;
+            __threadfence_block();
+            B.above = seen;
+            it = 0;
+            continue;
+        }
+        if (++it > P.wait_limit || ((it & 63) == 0 && aborted(P.error))) {
+            set_error(P.error, RC_DEV_ERR_TIMEOUT);
+            return;
+        }
+        if (it > 256) __nanosleep(64);
+    }
+}
+
+__global__ void __launch_bounds__((WAVE_WARPS + 2) * 32) h264_wave_kernel(H264Launch P) {
     __shared__ WaveSmem sm;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if ((int)blockIdx.x < P.intra_blocks) {
-        wave_intra_worker(P, sm.iw[warp], lane);
+        if (warp < WAVE_WARPS) wave_intra_worker(P, sm.iw[warp], lane);
         return;
     }
     const int band = blockIdx.x - P.intra_blocks;
-    const int my = band * WAVE_WARPS + warp;
-    if (lane == 0) sm.band.prog[warp] = 0;
+    const int y0 = band * WAVE_WARPS, rows = min(WAVE_WARPS, P.mb_h - y0);
+    if (threadIdx.x < WAVE_WARPS) sm.band.prog[threadIdx.x] = 0;
+    if (threadIdx.x == 0) { sm.band.icol = 0; sm.band.above = 0; }
     __syncthreads();
+    if (warp == WAVE_WARPS) { wave_band_intra_helper(P, sm.band, y0, rows, lane); return; }
+    if (warp == WAVE_WARPS + 1) { wave_band_above_helper(P, sm.band, y0, lane); return; }
+    const int my = y0 + warp;
     if (my >= P.mb_h) return;
     const bool last = warp == WAVE_WARPS - 1 || my == P.mb_h - 1;
     wave_band_row(P, sm.band, warp, my, last, lane);
@@ -1413,7 +1474,7 @@ int rc_h264_wave_capacity() {
     int dev = 0, sms = 0, per = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, h264_wave_kernel, WAVE_WARPS * 32, 0) != cudaSuccess)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, h264_wave_kernel, (WAVE_WARPS + 2) * 32, 0) != cudaSuccess)
         return 0;
     return per * sms;
 }
@@ -1424,7 +1485,7 @@ int rc_launch_h264_wave(const H264Launch &p, cudaStream_t st) {
     H264Launch q = p;
     void *args[] = {&q};
     cudaError_t e = cudaLaunchCooperativeKernel((const void *)h264_wave_kernel, dim3(p.intra_blocks + bands),
-                                                dim3(WAVE_WARPS * 32), args, 0, st);
+                                                dim3((WAVE_WARPS + 2) * 32), args, 0, st);
     return e == cudaSuccess ? 0 : -1;
 }
 
