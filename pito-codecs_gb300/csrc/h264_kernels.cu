@@ -55,9 +55,6 @@ __constant__ uint8_t cTC0[52][3] = {
     {4, 6, 9},  {5, 7, 10}, {6, 8, 11}, {6, 8, 13}, {7, 10, 14}, {8, 11, 16}, {9, 12, 18},
     {10, 13, 20}, {11, 15, 23}, {13, 17, 25}};
 // decode order of 4x4 blocks (BLK4_XY) and its inverse (RASTER_TO_BLK4)
-__constant__ uint8_t cBLK4X[16] = {0, 1, 0, 1, 2, 3, 2, 3, 0, 1, 0, 1, 2, 3, 2, 3};
-__constant__ uint8_t cBLK4Y[16] = {0, 0, 1, 1, 0, 0, 1, 1, 2, 2, 3, 3, 2, 2, 3, 3};
-__constant__ uint8_t cR2B[16] = {0, 1, 4, 5, 2, 3, 6, 7, 8, 9, 12, 13, 10, 11, 14, 15};
 
 constexpr uint32_t ID_NONE = 0xffffffffu;
 
@@ -82,18 +79,6 @@ __device__ __forceinline__ void st_release(uint32_t *p, uint32_t v) {
 }
 __device__ __forceinline__ bool aborted(const uint32_t *err) {
     return (*(const volatile uint32_t *)err & RC_DEV_ERR_TIMEOUT) != 0;
-}
-// Wait until *f == epoch; false after `limit` polls or once another warp has
-// recorded a timeout (the caller then abandons the launch instead of
-// spinning for ever).
-__device__ bool wait_flag(const uint32_t *f, uint32_t epoch, uint32_t limit, const uint32_t *err) {
-    uint32_t it = 0;
-    while (ld_acquire(f) != epoch) {
-        if (++it > limit) return false;
-        if ((it & 63) == 0 && aborted(err)) return false;
-        __nanosleep(it < 32 ? 32 : 256);
-    }
-    return true;
 }
 
 // scale4 / scale8, src/h264/dec/transform.rs:30-46
@@ -221,6 +206,7 @@ __device__ __forceinline__ void set_error(uint32_t *e, uint32_t code) { atomicOr
 
 __device__ void compute_db(const H264Launch &P, const rc_h264_mb &q, const rc_h264_mb &left, const rc_h264_mb &top,
                            int addr, int lane, DbMb *out);
+__device__ void edge_words(const DbMb &d, int lane, uint32_t *out);
 
 // ===========================================================================
 // Kernel 1: inter MBs (prediction + residual) and I_PCM, one CTA per MB.
@@ -246,7 +232,12 @@ __global__ void __launch_bounds__(256) h264_mb_kernel(H264Launch P) {
     coef[t] = 0;
     if (t < 128) coefc[t] = 0;
     __syncthreads();
-    if (t < 32) compute_db(P, m, nbr[0], nbr[1], addr, t, P.db + addr);
+    if (t < 32) {
+        __shared__ DbMb dbm;
+        compute_db(P, m, nbr[0], nbr[1], addr, t, &dbm);
+        __syncwarp();
+        edge_words(dbm, t, P.edges + (size_t)addr * RC_EDGE_WORDS);
+    }
     const int kind = m.kind;
     if (kind == RC_H264_NONE || kind > RC_H264_INTER) return;
     uint8_t *Y = P.dpb + (size_t)P.out_slot * P.slot_bytes;
@@ -270,7 +261,7 @@ __global__ void __launch_bounds__(256) h264_mb_kernel(H264Launch P) {
     const unsigned long long need =
         nlum + (unsigned long long)nl * (t8 ? 64 : 16) + ndc * 4 + __popc(m.chroma_coded) * 16;
     if (m.coef_off + need > P.num_levels) { if (t == 0) set_error(P.error, RC_DEV_ERR_RECORD); return; }
-    __shared__ uint32_t ibits;  // intra: availability (bits 0..3) and waits (bits 4..7)
+    __shared__ uint32_t ibits;  // intra: neighbour availability (bits 0..3: left, top, top-right, top-left)
     if (intra) {
         if (t == 0) ibits = 0;
         __syncthreads();
@@ -282,15 +273,7 @@ __global__ void __launch_bounds__(256) h264_mb_kernel(H264Launch P) {
                 const rc_h264_mb *pm = P.mbs + ny * P.mb_w + nx;
                 const int nk = __ldg(&pm->kind);
                 const bool a = nk != RC_H264_NONE && __ldg(&pm->slice) == m.slice && (!P.constrained_intra || is_intra(nk));
-                // the top-right MB is read only by Intra4x4 block (3,0) in modes 3 / 7 (diagonal down-left,
-                // vertical-left) and by the top-using modes of Intra8x8 block 1 (intra.rs:31-62, 199-233)
-                bool uses = true;
-                if (t == 2)
-                    uses = kind == RC_H264_I4x4 ? (m.intra_modes[3] == 3 || m.intra_modes[3] == 7)
-                           : kind == RC_H264_I8x8 ? (m.intra_modes[2] != 1 && m.intra_modes[2] != 8) : false;
-                uint32_t b = a ? (1u << t) : 0;
-                if (a && uses && wave_intra(nk)) b |= 16u << t;
-                atomicOr(&ibits, b);
+                if (a) atomicOr(&ibits, 1u << t);
             }
         }
     }
@@ -435,10 +418,9 @@ __global__ void __launch_bounds__(256) h264_mb_kernel(H264Launch P) {
             in.i16_mode = m.i16_mode;
             in.chroma_mode = m.chroma_mode;
             in.nb = (uint8_t)(ibits & 15);
-            in.wait = (uint8_t)(ibits >> 4);
-            in.pad0 = in.pad1 = 0;
+            in.pad0 = in.pad1 = in.pad2 = 0;
             for (int i = 0; i < 16; i++) in.modes[i] = m.intra_modes[i];
-            in.pad2[0] = in.pad2[1] = 0;
+            in.pad3[0] = in.pad3[1] = 0;
             P.iinfo[addr] = in;
         }
         return;
@@ -472,7 +454,6 @@ struct __align__(16) WarpSmem {
     int16_t res[384];     // residual samples: 16x16 luma, then 8x8 Cb, 8x8 Cr
     uint8_t cy[17 * 32];  // luma canvas: rows -1..15, cols -1..30 -> [(r+1)*32 + c+1]
     uint8_t cc[2][9 * 12];  // chroma canvas: rows -1..7, cols -1..10
-    int32_t e[32];       // reference samples: top 0..15, left 16..23, corner 24
     int32_t f[32];       // smoothed reference samples (8x8)
 };
 
@@ -482,142 +463,189 @@ struct Avail {
     bool left, top, tl, tr;
 };
 
-// pred_nxn, src/h264/dec/intra.rs:64-192, one sample (x, y) of an n x n block
-// with reference samples top[0..2n), left[0..n), corner tl
-__device__ int pred_nxn_px(int mode, const int32_t *top, const int32_t *left, int tl, int n, Avail a, int x, int y) {
-#define ET(i) ((i) < 0 ? tl : top[(i)])
-#define EL(i) ((i) < 0 ? tl : left[(i)])
-    switch (mode) {
-    case 0: return ET(x);
-    case 1: return EL(y);
-    case 2: {
-        int shift = n == 4 ? 2 : 3, st = 0, sl = 0;
-        for (int i = 0; i < n; i++) { st += top[i]; sl += left[i]; }
-        if (a.top && a.left) return (st + sl + n) >> (shift + 1);
-        if (a.left) return (sl + (n >> 1)) >> shift;
-        if (a.top) return (st + (n >> 1)) >> shift;
-        return 128;
-    }
-    case 3:
-        if (x == n - 1 && y == n - 1) return (ET(2 * n - 2) + 3 * ET(2 * n - 1) + 2) >> 2;
-        return (ET(x + y) + 2 * ET(x + y + 1) + ET(x + y + 2) + 2) >> 2;
-    case 4:
-        if (x > y) return (ET(x - y - 2) + 2 * ET(x - y - 1) + ET(x - y) + 2) >> 2;
-        if (x < y) return (EL(y - x - 2) + 2 * EL(y - x - 1) + EL(y - x) + 2) >> 2;
-        return (ET(0) + 2 * tl + EL(0) + 2) >> 2;
-    case 5: {
-        int z = 2 * x - y, i = x - (y >> 1);
-        if (z >= 0 && (z & 1) == 0) return (ET(i - 1) + ET(i) + 1) >> 1;
-        if (z > 0) return (ET(i - 2) + 2 * ET(i - 1) + ET(i) + 2) >> 2;
-        if (z == -1) return (EL(0) + 2 * tl + ET(0) + 2) >> 2;
-        return (EL(y - 2 * x - 1) + 2 * EL(y - 2 * x - 2) + EL(y - 2 * x - 3) + 2) >> 2;
-    }
-    case 6: {
-        int z = 2 * y - x, i = y - (x >> 1);
-        if (z >= 0 && (z & 1) == 0) return (EL(i - 1) + EL(i) + 1) >> 1;
-        if (z > 0) return (EL(i - 2) + 2 * EL(i - 1) + EL(i) + 2) >> 2;
-        if (z == -1) return (EL(0) + 2 * tl + ET(0) + 2) >> 2;
-        return (ET(x - 2 * y - 1) + 2 * ET(x - 2 * y - 2) + ET(x - 2 * y - 3) + 2) >> 2;
-    }
-    case 7: {
-        int i = x + (y >> 1);
-        if ((y & 1) == 0) return (ET(i) + ET(i + 1) + 1) >> 1;
-        return (ET(i) + 2 * ET(i + 1) + ET(i + 2) + 2) >> 2;
-    }
-    default: {
-        int zmax = 2 * n - 3, z = x + 2 * y, i = y + (x >> 1);
-        if (z < zmax && (z & 1) == 0) return (EL(i) + EL(i + 1) + 1) >> 1;
-        if (z < zmax) return (EL(i) + 2 * EL(i + 1) + EL(i + 2) + 2) >> 2;
-        if (z == zmax) return (EL(n - 2) + 3 * EL(n - 1) + 2) >> 2;
-        return EL(n - 1);
-    }
-    }
-#undef ET
-#undef EL
-}
-
-// load_edge, src/h264/dec/intra.rs:31-62, into S.e (lanes 0..24)
-__device__ __forceinline__ void load_edge(WarpSmem &S, int lane, int bx0, int by0, int n, Avail a) {
+// Reference samples of an 8x8 block (load_edge, src/h264/dec/intra.rs:31-62:
+// 128 where unavailable, the last top sample where the top-right is) after
+// pred8x8's smoothing (intra.rs:199-231), into S.f: top 0..15, left 16..23,
+// corner 24.  Each lane reads the raw samples it needs straight from the
+// canvas.
+__device__ __forceinline__ void edge8(WarpSmem &S, int lane, int bx0, int by0, Avail a) {
+    auto ET = [&](int i) -> int { return a.top ? (int)cvy(S, by0 - 1, bx0 + ((i < 8 || a.tr) ? i : 7)) : 128; };
+    auto EL = [&](int j) -> int { return a.left ? (int)cvy(S, by0 + j, bx0 - 1) : 128; };
+    const int tl = a.tl ? (int)cvy(S, by0 - 1, bx0 - 1) : 128;
     if (lane < 16) {
-        int v = 128;
-        if (a.top && lane < 2 * n) v = cvy(S, by0 - 1, bx0 + ((lane < n || a.tr) ? lane : n - 1));
-        S.e[lane] = v;
-    } else if (lane < 24) {
-        int j = lane - 16;
-        S.e[lane] = (a.left && j < n) ? cvy(S, by0 + j, bx0 - 1) : 128;
-    } else if (lane == 24) {
-        S.e[24] = a.tl ? cvy(S, by0 - 1, bx0 - 1) : 128;
-    }
-}
-
-// pred8x8 reference-sample smoothing, src/h264/dec/intra.rs:199-231, S.e -> S.f
-__device__ __forceinline__ void smooth8(WarpSmem &S, int lane, Avail a) {
-    const int32_t *pt = S.e, *pl = S.e + 16;
-    int ptl = S.e[24];
-    if (lane < 16) {
-        int v = pt[lane];
+        const int i = lane, c = ET(i);
+        int v = c;
         if (a.top) {
-            if (lane == 0) v = a.tl ? (ptl + 2 * pt[0] + pt[1] + 2) >> 2 : (3 * pt[0] + pt[1] + 2) >> 2;
-            else if (lane == 15) v = (pt[14] + 3 * pt[15] + 2) >> 2;
-            else v = (pt[lane - 1] + 2 * pt[lane] + pt[lane + 1] + 2) >> 2;
+            if (i == 0) v = a.tl ? (tl + 2 * c + ET(1) + 2) >> 2 : (3 * c + ET(1) + 2) >> 2;
+            else if (i == 15) v = (ET(14) + 3 * c + 2) >> 2;
+            else v = (ET(i - 1) + 2 * c + ET(i + 1) + 2) >> 2;
         }
-        S.f[lane] = v;
+        S.f[i] = v;
     } else if (lane < 24) {
-        int j = lane - 16, v = pl[j];
+        const int j = lane - 16, c = EL(j);
+        int v = c;
         if (a.left) {
-            if (j == 0) v = a.tl ? (ptl + 2 * pl[0] + pl[1] + 2) >> 2 : (3 * pl[0] + pl[1] + 2) >> 2;
-            else if (j == 7) v = (pl[6] + 3 * pl[7] + 2) >> 2;
-            else v = (pl[j - 1] + 2 * pl[j] + pl[j + 1] + 2) >> 2;
+            if (j == 0) v = a.tl ? (tl + 2 * c + EL(1) + 2) >> 2 : (3 * c + EL(1) + 2) >> 2;
+            else if (j == 7) v = (EL(6) + 3 * c + 2) >> 2;
+            else v = (EL(j - 1) + 2 * c + EL(j + 1) + 2) >> 2;
         }
         S.f[lane] = v;
     } else if (lane == 24) {
-        int v = ptl;
+        int v = tl;
         if (a.tl) {
-            if (a.top && a.left) v = (pt[0] + 2 * ptl + pl[0] + 2) >> 2;
-            else if (a.top) v = (3 * ptl + pt[0] + 2) >> 2;
-            else if (a.left) v = (3 * ptl + pl[0] + 2) >> 2;
+            if (a.top && a.left) v = (ET(0) + 2 * tl + EL(0) + 2) >> 2;
+            else if (a.top) v = (3 * tl + ET(0) + 2) >> 2;
+            else if (a.left) v = (3 * tl + EL(0) + 2) >> 2;
         }
         S.f[24] = v;
     }
 }
 
-// reconstruct_intra, src/h264/dec/slicedec.rs:1325-1388, one warp.
+// pred_nxn (src/h264/dec/intra.rs:64-192) as data: for every mode and
+// sample position of an n x n block (n = 4, 8) the reference samples the
+// prediction reads and how it combines them, so that a warp predicts samples
+// of different modes with one branch-free instruction sequence (a switch over
+// the mode costs several times the arithmetic).  Entry: taps i0, i1, i2 and
+// the kind k (bits 3n..): 0 copy i0; 1 (i0 + i1 + 1) >> 1; 2 (i0 + 2 i1 + i2
+// + 2) >> 2; 3 (i0 + 3 i1 + 2) >> 2; 4 DC.  Reference indices: 4x4 -- 0
+// corner, 1..8 top 0..7, 9..12 left 0..3 (4 bits); 8x8 -- the smoothed
+// samples of edge8: top 0..15, left 16..23, corner 24 (5 bits).
+template <int N>
+struct PredTab {
+    uint32_t e[9][N * N];
+};
+template <int N>
+__host__ __device__ constexpr int ptT(int i) { return N == 4 ? (i < 0 ? 0 : 1 + i) : (i < 0 ? 24 : i); }
+template <int N>
+__host__ __device__ constexpr int ptL(int j) { return N == 4 ? (j < 0 ? 0 : 9 + j) : (j < 0 ? 24 : 16 + j); }
+template <int N>
+__host__ __device__ constexpr uint32_t ptE(int k, int a, int b = 0, int c = 0) {
+    return (uint32_t)a | (uint32_t)b << (N == 4 ? 4 : 5) | (uint32_t)c << (N == 4 ? 8 : 10) |
+           (uint32_t)k << (N == 4 ? 12 : 15);
+}
+template <int N>
+__host__ __device__ constexpr uint32_t pt_entry(int mode, int x, int y) {
+    constexpr int n = N;
+    switch (mode) {
+    case 0: return ptE<N>(0, ptT<N>(x));
+    case 1: return ptE<N>(0, ptL<N>(y));
+    case 2: return ptE<N>(4, 0);
+    case 3:
+        if (x == n - 1 && y == n - 1) return ptE<N>(3, ptT<N>(2 * n - 2), ptT<N>(2 * n - 1));
+        return ptE<N>(2, ptT<N>(x + y), ptT<N>(x + y + 1), ptT<N>(x + y + 2));
+    case 4:
+        if (x > y) return ptE<N>(2, ptT<N>(x - y - 2), ptT<N>(x - y - 1), ptT<N>(x - y));
+        if (x < y) return ptE<N>(2, ptL<N>(y - x - 2), ptL<N>(y - x - 1), ptL<N>(y - x));
+        return ptE<N>(2, ptT<N>(0), ptT<N>(-1), ptL<N>(0));
+    case 5: {
+        const int z = 2 * x - y, i = x - (y >> 1);
+        if (z >= 0 && (z & 1) == 0) return ptE<N>(1, ptT<N>(i - 1), ptT<N>(i));
+        if (z > 0) return ptE<N>(2, ptT<N>(i - 2), ptT<N>(i - 1), ptT<N>(i));
+        if (z == -1) return ptE<N>(2, ptL<N>(0), ptT<N>(-1), ptT<N>(0));
+        return ptE<N>(2, ptL<N>(y - 2 * x - 1), ptL<N>(y - 2 * x - 2), ptL<N>(y - 2 * x - 3));
+    }
+    case 6: {
+        const int z = 2 * y - x, i = y - (x >> 1);
+        if (z >= 0 && (z & 1) == 0) return ptE<N>(1, ptL<N>(i - 1), ptL<N>(i));
+        if (z > 0) return ptE<N>(2, ptL<N>(i - 2), ptL<N>(i - 1), ptL<N>(i));
+        if (z == -1) return ptE<N>(2, ptL<N>(0), ptT<N>(-1), ptT<N>(0));
+        return ptE<N>(2, ptT<N>(x - 2 * y - 1), ptT<N>(x - 2 * y - 2), ptT<N>(x - 2 * y - 3));
+    }
+    case 7: {
+        const int i = x + (y >> 1);
+        if ((y & 1) == 0) return ptE<N>(1, ptT<N>(i), ptT<N>(i + 1));
+        return ptE<N>(2, ptT<N>(i), ptT<N>(i + 1), ptT<N>(i + 2));
+    }
+    default: {
+        const int zmax = 2 * n - 3, z = x + 2 * y, i = y + (x >> 1);
+        if (z < zmax && (z & 1) == 0) return ptE<N>(1, ptL<N>(i), ptL<N>(i + 1));
+        if (z < zmax) return ptE<N>(2, ptL<N>(i), ptL<N>(i + 1), ptL<N>(i + 2));
+        if (z == zmax) return ptE<N>(3, ptL<N>(n - 2), ptL<N>(n - 1));
+        return ptE<N>(0, ptL<N>(n - 1));
+    }
+    }
+}
+template <int N>
+__host__ __device__ constexpr PredTab<N> make_predtab() {
+    PredTab<N> t{};
+    for (int m = 0; m < 9; m++)
+        for (int i = 0; i < N * N; i++) t.e[m][i] = pt_entry<N>(m, i % N, i / N);
+    return t;
+}
+__constant__ PredTab<4> cPRED4 = make_predtab<4>();
+__constant__ PredTab<8> cPRED8 = make_predtab<8>();
+
+// One sample of a 4x4 block at (bx0, by0) from its table entry; reference
+// samples straight from the canvas with load_edge's substitutions
+// (intra.rs:31-62): 128 where a neighbour is unavailable, the last top
+// sample where the top-right one is.
+__device__ __forceinline__ int tap4(const WarpSmem &S, int idx, int bx0, int by0, Avail a) {
+    const bool isT = (unsigned)(idx - 1) < 8u, isL = idx >= 9;
+    const int i = (idx - 1 < 4 || a.tr) ? idx - 1 : 3;
+    const int row = isL ? by0 + idx - 9 : by0 - 1;
+    const int col = isL ? bx0 - 1 : isT ? bx0 + i : bx0 - 1;
+    const bool ok = isL ? a.left : isT ? a.top : a.tl;
+    const int v = S.cy[(row + 1) * 32 + col + 1];
+    return ok ? v : 128;
+}
+__device__ __forceinline__ int pred4(const WarpSmem &S, uint32_t e, int bx0, int by0, Avail a) {
+    const int k = e >> 12;
+    const int r0 = tap4(S, e & 15, bx0, by0, a), r1 = tap4(S, (e >> 4) & 15, bx0, by0, a),
+              r2 = tap4(S, (e >> 8) & 15, bx0, by0, a);
+    const uint8_t *tp = S.cy + by0 * 32 + bx0 + 1;  // row -1 of the block
+    const int st = tp[0] + tp[1] + tp[2] + tp[3];
+    const int sl = S.cy[(by0 + 1) * 32 + bx0] + S.cy[(by0 + 2) * 32 + bx0] + S.cy[(by0 + 3) * 32 + bx0] +
+                   S.cy[(by0 + 4) * 32 + bx0];
+    const int dc = (a.top && a.left) ? (st + sl + 4) >> 3 : a.left ? (sl + 2) >> 2 : a.top ? (st + 2) >> 2 : 128;
+    const int v1 = (r0 + r1 + 1) >> 1, v2 = (r0 + 2 * r1 + r2 + 2) >> 2, v3 = (r0 + 3 * r1 + 2) >> 2;
+    return k == 0 ? r0 : k == 1 ? v1 : k == 2 ? v2 : k == 3 ? v3 : dc;
+}
+// One sample of an 8x8 block from its table entry and the smoothed reference
+// samples in S.f.
+__device__ __forceinline__ int pred8(const WarpSmem &S, uint32_t e, int dc) {
+    const int k = e >> 15;
+    const int r0 = S.f[e & 31], r1 = S.f[(e >> 5) & 31], r2 = S.f[(e >> 10) & 31];
+    const int v1 = (r0 + r1 + 1) >> 1, v2 = (r0 + 2 * r1 + r2 + 2) >> 2, v3 = (r0 + 3 * r1 + 2) >> 2;
+    return k == 0 ? r0 : k == 1 ? v1 : k == 2 ? v2 : k == 3 ? v3 : dc;
+}
+
+// reconstruct_intra, src/h264/dec/slicedec.rs:1325-1388, one warp, on the
+// canvas (neighbour samples already in row -1 and column -1).
 // nb: availability of neighbours L, T, TR, TL for intra prediction.
-__device__ void intra_mb(WarpSmem &S, const H264Launch &P, int lane, int mbx, int mby, const bool nb[4], uint8_t *Y,
-                         uint8_t *U, uint8_t *V) {
+__device__ void intra_mb(WarpSmem &S, int lane, const bool nb[4], const uint32_t *tab4, const uint32_t *tab8) {
     const IntraInfo &m = S.q;
-    const int x0 = mbx * 16, y0 = mby * 16, cx0 = mbx * 8, cy0 = mby * 8;
-    // canvas: neighbour samples
-    if (mby > 0) {
-        int gx = x0 + lane - 1;
-        S.cy[lane] = (gx >= 0 && gx < P.W) ? __ldcg(Y + (size_t)(y0 - 1) * P.pitch + gx) : 0;
-        if (lane < 20) {
-            int c = lane / 10, gxc = cx0 + lane % 10 - 1;
-            S.cc[c][lane % 10] = (gxc >= 0 && gxc < P.CW) ? __ldcg((c ? V : U) + (size_t)(cy0 - 1) * P.cpitch + gxc) : 0;
-        }
-    }
-    if (mbx > 0) {
-        if (lane < 16) S.cy[(lane + 1) * 32] = __ldcg(Y + (size_t)(y0 + lane) * P.pitch + x0 - 1);
-        int c = lane >> 3, r = lane & 7;
-        if (lane < 16) S.cc[c][(r + 1) * 12] = __ldcg((c ? V : U) + (size_t)(cy0 + r) * P.cpitch + cx0 - 1);
-    }
-    __syncwarp();
     // ---- luma
     if (m.kind == RC_H264_I4x4) {
-        for (int i = 0; i < 16; i++) {
-            const int bx = cBLK4X[i], by = cBLK4Y[i];
-            Avail a;  // luma_avail4, slicedec.rs:1297-1323
-            a.left = bx > 0 ? true : nb[0];
-            a.top = by > 0 ? true : nb[1];
-            a.tl = (bx > 0 && by > 0) ? true : by > 0 ? nb[0] : bx > 0 ? nb[1] : nb[3];
-            a.tr = by == 0 ? (bx < 3 ? nb[1] : nb[2]) : bx == 3 ? false : cR2B[(by - 1) * 4 + bx + 1] < cR2B[by * 4 + bx];
-            load_edge(S, lane, bx * 4, by * 4, 4, a);
-            __syncwarp();
-            if (lane < 16) {
-                int x = lane & 3, y = lane >> 2;
-                int v = pred_nxn_px(m.modes[by * 4 + bx], S.e, S.e + 16, S.e[24], 4, a, x, y);
-                v = clip255(v + S.res[(by * 4 + y) * 16 + bx * 4 + x]);
-                S.cy[(by * 4 + y + 1) * 32 + bx * 4 + x + 1] = (uint8_t)v;
+        // the 16 blocks in wavefront order bx + 2 by (each after its left, top,
+        // top-left and top-right blocks), two blocks per step, 16 lanes each
+        constexpr int8_t kA[10] = {0, 1, 2, 3, 6, 7, 10, 11, 14, 15};
+        constexpr int8_t kB[10] = {-1, -1, 4, 5, 8, 9, 12, 13, -1, -1};
+        // raster block index -> decode (8x8 zig-zag) order, for the top-right rule
+        constexpr int8_t kDec[16] = {0, 1, 4, 5, 2, 3, 6, 7, 8, 9, 12, 13, 10, 11, 14, 15};
+        const int g = lane >> 4, px = lane & 3, py = (lane >> 2) & 3;
+        const uint2 m0 = *(const uint2 *)m.modes, m1 = *(const uint2 *)(m.modes + 8);
+        const uint32_t mword[4] = {m0.x, m0.y, m1.x, m1.y};
+#pragma unroll
+        for (int st = 0; st < 10; st++) {
+            const int ba = kA[st], bb = kB[st];
+            const int blk = g ? bb : ba;
+            if (blk >= 0) {
+                const int bx = blk & 3, by = blk >> 2;
+                Avail a;  // luma_avail4, slicedec.rs:1297-1323
+                a.left = bx > 0 ? true : nb[0];
+                a.top = by > 0 ? true : nb[1];
+                a.tl = (bx > 0 && by > 0) ? true : by > 0 ? nb[0] : bx > 0 ? nb[1] : nb[3];
+                const bool tr_a = (ba >> 2) == 0 ? ((ba & 3) < 3 ? nb[1] : nb[2])
+                                  : (ba & 3) == 3 ? false : kDec[ba - 3] < kDec[ba];
+                const bool tr_b = bb < 0 ? false : (bb >> 2) == 0 ? ((bb & 3) < 3 ? nb[1] : nb[2])
+                                  : (bb & 3) == 3 ? false : kDec[bb - 3] < kDec[bb];
+                a.tr = g ? tr_b : tr_a;
+                const int mode_a = (mword[ba >> 2] >> ((ba & 3) * 8)) & 255;
+                const int mode_b = bb < 0 ? 0 : (mword[bb >> 2] >> ((bb & 3) * 8)) & 255;
+                const uint32_t e = tab4[(g ? mode_b : mode_a) * 16 + py * 4 + px];
+                int v = pred4(S, e, bx * 4, by * 4, a);
+                v = clip255(v + S.res[(by * 4 + py) * 16 + bx * 4 + px]);
+                S.cy[(by * 4 + py + 1) * 32 + bx * 4 + px + 1] = (uint8_t)v;
             }
             __syncwarp();
         }
@@ -629,14 +657,17 @@ __device__ void intra_mb(WarpSmem &S, const H264Launch &P, int lane, int mbx, in
             a.top = by > 0 ? true : nb[1];
             a.tl = (bx > 0 && by > 0) ? true : by > 0 ? nb[0] : bx > 0 ? nb[1] : nb[3];
             a.tr = b8 == 0 ? nb[1] : b8 == 1 ? nb[2] : b8 == 2;
-            load_edge(S, lane, bx * 4, by * 4, 8, a);
+            edge8(S, lane, bx * 4, by * 4, a);
             __syncwarp();
-            smooth8(S, lane, a);
-            __syncwarp();
+            const int mode = m.modes[by * 4 + bx];
+            int st = 0, sl = 0;
+#pragma unroll
+            for (int i = 0; i < 8; i++) { st += S.f[i]; sl += S.f[16 + i]; }
+            const int dc = (a.top && a.left) ? (st + sl + 8) >> 4 : a.left ? (sl + 4) >> 3 : a.top ? (st + 4) >> 3 : 128;
 #pragma unroll
             for (int h = 0; h < 2; h++) {
                 int idx = lane + 32 * h, x = idx & 7, y = idx >> 3;
-                int v = pred_nxn_px(m.modes[by * 4 + bx], S.f, S.f + 16, S.f[24], 8, a, x, y);
+                int v = pred8(S, tab8[mode * 64 + idx], dc);
                 v = clip255(v + S.res[(by * 4 + y) * 16 + bx * 4 + x]);
                 S.cy[(by * 4 + y + 1) * 32 + bx * 4 + x + 1] = (uint8_t)v;
             }
@@ -731,21 +762,6 @@ __device__ void intra_mb(WarpSmem &S, const H264Launch &P, int lane, int mbx, in
         }
     }
     __syncwarp();
-    // ---- store the MB
-    {
-        int r = lane >> 1, half = lane & 1;
-        const uint8_t *s = S.cy + (r + 1) * 32 + 1 + half * 8;
-        uint32_t lo = s[0] | s[1] << 8 | s[2] << 16 | (uint32_t)s[3] << 24;
-        uint32_t hi = s[4] | s[5] << 8 | s[6] << 16 | (uint32_t)s[7] << 24;
-        *(uint2 *)(Y + (size_t)(y0 + r) * P.pitch + x0 + half * 8) = make_uint2(lo, hi);
-        if (lane < 16) {
-            int c = lane >> 3, rr = lane & 7;
-            const uint8_t *q = S.cc[c] + (rr + 1) * 12 + 1;
-            uint32_t a0 = q[0] | q[1] << 8 | q[2] << 16 | (uint32_t)q[3] << 24;
-            uint32_t a1 = q[4] | q[5] << 8 | q[6] << 16 | (uint32_t)q[7] << 24;
-            *(uint2 *)((c ? V : U) + (size_t)(cy0 + rr) * P.cpitch + cx0) = make_uint2(a0, a1);
-        }
-    }
 }
 
 // ---- deblocking (src/h264/dec/deblock.rs) -------------------------------
@@ -886,6 +902,35 @@ __device__ __forceinline__ void edge_consts(int qpp, int qpq, int bsv, int aoff,
     alpha = cALPHA[ia];
     beta = cBETA[ib];
     tc0 = (bsv >= 1 && bsv < 4) ? cTC0[ia][bsv - 1] : 0;
+}
+
+// The RC_EDGE_WORDS loop-filter words of one MB from its DbMb (edge
+// parameters of deblock_mb, deblock.rs:386-403), two words per lane.
+__device__ void edge_words(const DbMb &d, int lane, uint32_t *out) {
+    const bool f = d.flags != 0;
+    {  // luma word `lane`: dir, 4-line segment k, edge e
+        const int dir = lane >> 4, k = (lane >> 2) & 3, e = lane & 3;
+        const int bsv = f ? d.bs[(dir << 4) | (e << 2) | k] : 0;
+        uint32_t w = 0;
+        if (bsv) {
+            int alpha, beta, tc0;
+            edge_consts(e == 0 ? d.qp[1 + dir] : d.qp[0], d.qp[0], bsv, d.aoff, d.boff, alpha, beta, tc0);
+            w = (uint32_t)alpha | (uint32_t)beta << 8 | (uint32_t)tc0 << 16 | (uint32_t)bsv << 24;
+        }
+        out[lane] = w;
+    }
+    {  // chroma word 32 + lane: dir, component c, 2-line segment k, chroma edge e (luma edge 2e)
+        const int dir = lane >> 4, c = (lane >> 3) & 1, k = (lane >> 1) & 3, e = lane & 1;
+        const int bsv = f ? d.bs[(dir << 4) | (e << 3) | k] : 0;
+        uint32_t w = 0;
+        if (bsv) {
+            int alpha, beta, tc0;
+            edge_consts(e == 0 ? d.qpc[1 + dir][c] : d.qpc[0][c], d.qpc[0][c], bsv, d.aoff, d.boff, alpha, beta,
+                        tc0);
+            w = (uint32_t)alpha | (uint32_t)beta << 8 | (uint32_t)tc0 << 16 | (uint32_t)bsv << 24;
+        }
+        out[32 + lane] = w;
+    }
 }
 
 __device__ __forceinline__ void load_record(rc_h264_mb &dst, const rc_h264_mb *src, int lane) {
@@ -1088,351 +1133,496 @@ __global__ void __launch_bounds__(128) h264_db_params_kernel(H264Launch P) {
 
 
 // ===========================================================================
-// Wave kernel: intra reconstruction and the loop filter in one cooperative
-// launch.  CTAs [0, intra_blocks) take intra MBs in anti-diagonal order, one
-// warp per MB; the remaining CTAs each filter a band of WAVE_WARPS MB rows,
-// one warp per row walking left to right.  Inside a band the MB above comes
-// through shared memory (a ring of final bottom rows per row); across bands
-// through global memory and a per-row progress word.  A row filters MB x once
-// the intra MBs among (x-1..x+1, y..y+1) are reconstructed and the row above
-// has finished MBs 0..x.
+// Band kernel: intra reconstruction and the loop filter of one picture in one
+// cooperative launch.  CTA b owns MB rows [b*BR, b*BR + BR).  For each of its
+// rows it runs three warps that walk the row left to right: an intra warp
+// (reconstruct_intra of the row's intra MBs), a luma and a chroma loop-filter
+// warp (deblock_mb: an MB's vertical edges, then its horizontal edges).  Rows
+// of a band hand over through shared memory, bands through per-row progress
+// words in global memory that the band's helper warp mirrors and publishes.
+//
+// Order (every wait is capped, see wait_ge):
+//   intra MB (x, y)    after intra row y-1 has reconstructed MBs 0..x+1;
+//   filter MB (x, y)   after rows y and y+1 have reconstructed MBs 0..x+2 and
+//                      0..x+1 (every intra MB that reads samples this step
+//                      changes, and MB x+2, which the step prefetches), and
+//                      after row y-1 has filtered and stored MBs 0..x+1 (MB
+//                      x+1's left edge is the last change to MB (x, y-1)).
+// A filter row stores MB x-1 once MB x's left edge is filtered (its last
+// change in the row) and the three rows above MB x after MB x's top edge.
 // ===========================================================================
-constexpr int WAVE_WARPS = 8;
-constexpr int RING = 8;
+constexpr int BR = RC_H264_BAND_ROWS;
+constexpr int DRING = 8;  // ring slots between filter rows of a band
+constexpr int BAND_THREADS = (3 * BR + 1) * 32;
 
-struct __align__(16) BandRow {
-    RowTile T;
-    uint8_t ring[RING][128];  // bottom rows 12..15 of each final MB: luma 4x16, Cb 4x8, Cr 4x8
+struct __align__(16) LumaRow {
+    uint8_t t[20][16];        // rows -4..15 of the MB being filtered (horizontal edges)
+    uint8_t ring[DRING][64];  // final rows 12..15 of this row's MBs, for the row below
+    uint4 st[3][3][16];       // staged MBs x..x+2 (slot x % 3): sample rows, vertical and horizontal edge words
+};
+struct __align__(16) ChromaRow {
+    uint8_t t[2][10][8];      // per component, rows -2..7
+    uint8_t ring[DRING][32];  // final rows 6..7 per component, for the row below
+    uint2 st[3][3][16];       // staged MBs, as LumaRow::st
 };
 struct __align__(16) BandSmem {
-    BandRow r[WAVE_WARPS];
-    volatile int prog[WAVE_WARPS];  // MBs of each row that are final (in this CTA's rows)
-    volatile int icol;              // columns whose intra MBs (band rows + the row below) are reconstructed
-    volatile int above;             // MBs of the row above the band that are final
-};
-union __align__(16) WaveSmem {
-    WarpSmem iw[WAVE_WARPS];
-    BandSmem band;
+    uint32_t tab4[9 * 16];  // copies of cPRED4 / cPRED8
+    uint32_t tab8[9 * 64];
+    WarpSmem iw[BR];
+    LumaRow l[BR];
+    ChromaRow c[BR];
+    // progress: index 0 = the row above the band (mirrored), 1..BR = the band's
+    // rows, BR + 1 = the row below the band (intra, mirrored)
+    volatile int iprog[BR + 2];  // MBs 0..v-1 reconstructed
+    volatile int lprog[BR + 1];  // MBs 0..v-1 luma-filtered and stored, ring slots 0..v-1 written
+    volatile int cprog[BR + 1];  // same for chroma
 };
 
-__device__ void wave_intra_worker(const H264Launch &P, WarpSmem &S, int lane) {
-    uint8_t *Y = P.dpb + (size_t)P.out_slot * P.slot_bytes;
-    uint8_t *U = Y + P.u_off, *V = Y + P.v_off;
-    for (;;) {
-        unsigned ti = 0;
-        if (lane == 0) ti = aborted(P.error) ? 0xffffffffu : atomicAdd(P.counter, 1u);
-        ti = __shfl_sync(0xffffffffu, ti, 0);
-        if (ti >= (unsigned)P.ntasks) return;
-        const int addr = __ldg(P.tasks + ti) & 0x7fffffffu;
-        if (!wave_intra(__ldg(&P.mbs[addr].kind))) continue;
-        const int mbx = addr % P.mb_w, mby = addr / P.mb_w;
-        // prediction parameters and residual (independent of the neighbours)
-        if (lane < 8) ((uint32_t *)&S.q)[lane] = __ldcg((const uint32_t *)(P.iinfo + addr) + lane);
-        {
-            const uint4 *src = (const uint4 *)(P.ires + (size_t)addr * 384);
-            uint4 *dst = (uint4 *)S.res;
-            dst[lane] = __ldcg(src + lane);
-            if (lane < 16) dst[32 + lane] = __ldcg(src + 32 + lane);
-        }
-        __syncwarp();
-        // wait for the intra neighbours whose samples the modes read
-        bool ok = true;
-        const int waits = S.q.wait;
-        if (lane < 4 && (waits >> lane & 1)) {
-            const int dx = lane == 0 ? -1 : lane == 2 ? 1 : lane == 3 ? -1 : 0, dy = lane == 0 ? 0 : -1;
-            const int nx = mbx + dx, ny = mby + dy;
-            if (nx >= 0 && ny >= 0 && nx < P.mb_w) ok = wait_flag(P.rflag + ny * P.mb_w + nx, P.epoch, P.wait_limit, P.error);
-        }
-        if (!__all_sync(0xffffffffu, ok)) {
-            if (lane == 0) set_error(P.error, RC_DEV_ERR_TIMEOUT);
-            return;
-        }
-        bool nb[4];
-#pragma unroll
-        for (int n = 0; n < 4; n++) nb[n] = S.q.nb >> n & 1;
-        intra_mb(S, P, lane, mbx, mby, nb, Y, U, V);
-        __threadfence();
-        __syncwarp();
-        if (lane == 0) st_release(P.rflag + addr, P.epoch);
+// Warp-wide wait until *c >= need.  Lane 0 polls shared memory and sleeps
+// between polls (16 ns doubling to 128 ns): a band CTA holds about twenty
+// warps, and waiting ones must leave the issue slots to the working ones.
+// False after the iteration cap or once another warp has reported an error.
+__device__ __forceinline__ bool wait_ge(volatile int *c, int need, const H264Launch &P, int lane) {
+    bool ok = true;
+    if (lane == 0 && *c < need) {
+        uint32_t it = 0, ns = 16;
+        do {
+            if (++it > P.wait_limit || ((it & 63) == 0 && aborted(P.error))) { ok = false; break; }
+            __nanosleep(ns);
+            ns = min(ns * 2, 128u);
+        } while (*c < need);
     }
+    ok = __shfl_sync(0xffffffffu, ok, 0);
+    __threadfence_block();
+    return ok;
 }
 
-// One MB row of a band.  w: row index inside the band; last: w is the band's
-// last row (publishes to global memory for the next band).
-__device__ void wave_band_row(const H264Launch &P, BandSmem &B, int w, int my, bool last, int lane) {
-    RowTile &T = B.r[w].T;
+// filter_lanes (deblock.rs:146-229) for one luma line s[0..7] = p3..q3 and
+// one edge word (alpha | beta << 8 | tc0 << 16 | bS << 24), without
+// branches: every candidate is computed and the results selected, so that a
+// warp's lanes never diverge.  STRONG: the edge may carry bS 4 (MB edges);
+// internal edges never do.
+template <bool STRONG>
+__device__ __forceinline__ void lf_luma(int *s, uint32_t wd) {
+    const int alpha = wd & 255, beta = (wd >> 8) & 255, tc0 = (wd >> 16) & 255, bS = wd >> 24;
+    const int p3 = s[0], p2 = s[1], p1 = s[2], p0 = s[3], q0 = s[4], q1 = s[5], q2 = s[6], q3 = s[7];
+    const int d0 = abs(p0 - q0);
+    const bool on = (bS != 0) & (d0 < alpha) & (abs(p1 - p0) < beta) & (abs(q1 - q0) < beta);
+    const bool ap = abs(p2 - p0) < beta, aq = abs(q2 - q0) < beta;
+    // bS 1..3
+    const int tc = tc0 + ap + aq;
+    const int delta = clampi((((q0 - p0) << 2) + (p1 - q1) + 4) >> 3, -tc, tc);
+    const int avg = (p0 + q0 + 1) >> 1;
+    int np0 = clip255(p0 + delta), nq0 = clip255(q0 - delta);
+    int np1 = ap ? p1 + clampi((p2 + avg - (p1 << 1)) >> 1, -tc0, tc0) : p1;
+    int nq1 = aq ? q1 + clampi((q2 + avg - (q1 << 1)) >> 1, -tc0, tc0) : q1;
+    int np2 = p2, nq2 = q2;
+    if (STRONG) {  // bS 4
+        const bool big = bS >= 4, sm = d0 < ((alpha >> 2) + 2), sp = ap & sm, sq = aq & sm;
+        const int sp0 = sp ? (p2 + 2 * p1 + 2 * p0 + 2 * q0 + q1 + 4) >> 3 : (2 * p1 + p0 + q1 + 2) >> 2;
+        const int sp1 = sp ? (p2 + p1 + p0 + q0 + 2) >> 2 : p1;
+        const int sp2 = sp ? (2 * p3 + 3 * p2 + p1 + p0 + q0 + 4) >> 3 : p2;
+        const int sq0 = sq ? (p1 + 2 * p0 + 2 * q0 + 2 * q1 + q2 + 4) >> 3 : (2 * q1 + q0 + p1 + 2) >> 2;
+        const int sq1 = sq ? (p0 + q0 + q1 + q2 + 2) >> 2 : q1;
+        const int sq2 = sq ? (2 * q3 + 3 * q2 + q1 + q0 + p0 + 4) >> 3 : q2;
+        np0 = big ? sp0 : np0;
+        np1 = big ? sp1 : np1;
+        np2 = big ? sp2 : np2;
+        nq0 = big ? sq0 : nq0;
+        nq1 = big ? sq1 : nq1;
+        nq2 = big ? sq2 : nq2;
+    }
+    s[1] = on ? np2 : p2;
+    s[2] = on ? np1 : p1;
+    s[3] = on ? np0 : p0;
+    s[4] = on ? nq0 : q0;
+    s[5] = on ? nq1 : q1;
+    s[6] = on ? nq2 : q2;
+}
+
+// the chroma filter (deblock.rs:146-229, chroma lanes) for s[0..3] = p1, p0,
+// q0, q1, without branches
+__device__ __forceinline__ void lf_chroma(int *s, uint32_t wd) {
+    const int alpha = wd & 255, beta = (wd >> 8) & 255, tc0 = (wd >> 16) & 255, bS = wd >> 24;
+    const int p1 = s[0], p0 = s[1], q0 = s[2], q1 = s[3];
+    const bool on = (bS != 0) & (abs(p0 - q0) < alpha) & (abs(p1 - p0) < beta) & (abs(q1 - q0) < beta);
+    const int tc = tc0 + 1;
+    const int delta = clampi((((q0 - p0) << 2) + (p1 - q1) + 4) >> 3, -tc, tc);
+    const bool big = bS >= 4;
+    const int np0 = big ? (2 * p1 + p0 + q1 + 2) >> 2 : clip255(p0 + delta);
+    const int nq0 = big ? (2 * q1 + q0 + p1 + 2) >> 2 : clip255(q0 - delta);
+    s[1] = on ? np0 : p0;
+    s[2] = on ? nq0 : q0;
+}
+
+__device__ __forceinline__ void band_fail(const H264Launch &P, int lane) {
+    if (lane == 0) set_error(P.error, RC_DEV_ERR_TIMEOUT);
+}
+
+// Asynchronous global -> shared copies (tracked per thread by commit groups,
+// not by the warp's register scoreboards, so that a filter warp can keep two
+// MBs in flight without stalling on them).
+__device__ __forceinline__ void cp_async16(void *dst, const void *src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async8(void *dst, const void *src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_wait_all_but_1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+
+// Intra warp of band row w (picture row my).  `lines` holds, per band row,
+// the row's unfiltered bottom samples (luma row 15, then Cb and Cr row 7):
+// filled from the picture at the start (inter MBs are final already) and
+// updated as the row's intra MBs are reconstructed, so that the row below
+// reads its top neighbours from shared memory.
+__device__ void band_intra_row(const H264Launch &P, BandSmem &B, uint8_t *lines, int w, int my, int lane) {
+    WarpSmem &S = B.iw[w];
     uint8_t *Y = P.dpb + (size_t)P.out_slot * P.slot_bytes;
     uint8_t *U = Y + P.u_off, *V = Y + P.v_off;
-    const uint32_t tag = (P.epoch & 0xffffu) << 16;
-    const bool luma = lane < 16;
-    const int cc = (lane - 16) >> 3, li = luma ? lane : (lane - 16) & 7;
-    const bool below = my + 1 < P.mb_h;
-    const bool ring_out = !last && below;  // the next row of the band reads this row's ring
-    uint4 pre_y = make_uint4(0, 0, 0, 0);
-    uint2 pre_c = make_uint2(0, 0);
-    uint32_t pre_db = 0;
-    // intra reconstruction of MB column x in rows y, y+1 (lanes 0, 1)
-    auto wait_intra = [&](int x) -> bool {
-        bool ok = true;
-        if (lane < 2 && x < P.mb_w) {
-            const int ry = my + lane;
-            if (ry < P.mb_h) {
-                const int a = ry * P.mb_w + x;
-                if (wave_intra(__ldg(&P.mbs[a].kind))) ok = wait_flag(P.rflag + a, P.epoch, P.wait_limit, P.error);
-            }
+    const int LW = P.mb_w * 32;
+    uint8_t *ly = lines + (size_t)w * LW, *lu = ly + P.mb_w * 16, *lv = lu + P.mb_w * 8;
+    const uint8_t *ay = ly - LW, *au = lu - LW, *av = lv - LW;  // the row above (w > 0)
+    volatile int *above = &B.iprog[w], *mine = &B.iprog[w + 1];
+    {
+        const uint32_t *gy = (const uint32_t *)(Y + (size_t)(my * 16 + 15) * P.pitch);
+        const uint32_t *gu = (const uint32_t *)(U + (size_t)(my * 8 + 7) * P.cpitch);
+        const uint32_t *gv = (const uint32_t *)(V + (size_t)(my * 8 + 7) * P.cpitch);
+        for (int i = lane; i < P.mb_w * 4; i += 32) ((uint32_t *)ly)[i] = __ldcg(gy + i);
+        for (int i = lane; i < P.mb_w * 2; i += 32) {
+            ((uint32_t *)lu)[i] = __ldcg(gu + i);
+            ((uint32_t *)lv)[i] = __ldcg(gv + i);
         }
-        return __all_sync(0xffffffffu, ok);
-    };
-    auto prefetch = [&](int x) {
-        if (luma) pre_y = __ldcg((const uint4 *)(Y + (size_t)(my * 16 + lane) * P.pitch + x * 16));
-        else pre_c = __ldcg((const uint2 *)((cc ? V : U) + (size_t)(my * 8 + li) * P.cpitch + x * 8));
-        if (lane < 12) pre_db = __ldcg((const uint32_t *)(P.db + (size_t)my * P.mb_w + x) + lane);
-    };
-    // wait until a helper-published shared counter reaches `need`
-    auto wait_shared = [&](volatile int *c, int need) -> bool {
-        bool ok = true;
-        if (lane == 0) {
-            uint32_t it = 0;
-            while (*c < need) {
-                if (++it > P.wait_limit || ((it & 63) == 0 && aborted(P.error))) { ok = false; break; }
-                if (it > 1024) __nanosleep(32);
-            }
-        }
-        ok = __shfl_sync(0xffffffffu, ok, 0);
+        __syncwarp();
         __threadfence_block();
-        return ok;
-    };
-    (void)wait_intra;
-    if (!wait_shared(&B.icol, min(1, P.mb_w))) { if (lane == 0) set_error(P.error, RC_DEV_ERR_TIMEOUT); return; }
-    prefetch(0);
-    for (int x = 0; x < P.mb_w; x++) {
-        // ---- stage MB x
-        if (luma) {
-            uint32_t q[4] = {pre_y.x, pre_y.y, pre_y.z, pre_y.w};
-#pragma unroll
-            for (int i = 0; i < 4; i++) *(uint32_t *)&T.y[lane + 4][4 + 4 * i] = q[i];
-        } else {
-            *(uint32_t *)&T.c[cc][li + 4][4] = pre_c.x;
-            *(uint32_t *)&T.c[cc][li + 4][8] = pre_c.y;
-        }
-        if (lane < 12) ((uint32_t *)&T.db)[lane] = pre_db;
-        // ---- intra MBs this MB's edges touch: (x+1, y) and (x+1, y+1) are new
-        if (!wait_shared(&B.icol, min(x + 2, P.mb_w))) { if (lane == 0) set_error(P.error, RC_DEV_ERR_TIMEOUT); return; }
-        // ---- the MB above, rows 12..15 (final once row y-1 has finished MBs 0..x)
-        if (my > 0) {
-            const uint32_t need = (uint32_t)min(x + 1, P.mb_w);
-            bool ok = true;
-            if (w == 0) {
-                if (!wait_shared(&B.above, (int)need)) { if (lane == 0) set_error(P.error, RC_DEV_ERR_TIMEOUT); return; }
-                if (lane < 4) {
-                    uint4 v = __ldcg((const uint4 *)(Y + (size_t)(my * 16 - 4 + lane) * P.pitch + x * 16));
-                    uint32_t q[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-                    for (int i = 0; i < 4; i++) *(uint32_t *)&T.y[lane][4 + 4 * i] = q[i];
-                } else if (lane < 12) {
-                    int c = (lane - 4) >> 2, r = (lane - 4) & 3;
-                    uint2 v = __ldcg((const uint2 *)((c ? V : U) + (size_t)(my * 8 - 4 + r) * P.cpitch + x * 8));
-                    *(uint32_t *)&T.c[c][r][4] = v.x;
-                    *(uint32_t *)&T.c[c][r][8] = v.y;
-                }
-            } else {
-                if (lane == 0) {
-                    uint32_t it = 0;
-                    while (B.prog[w - 1] < (int)need) {
-                        if (++it > P.wait_limit || ((it & 63) == 0 && aborted(P.error))) { ok = false; break; }
-                        if (it > 1024) __nanosleep(32);
-                    }
-                }
-                if (!__shfl_sync(0xffffffffu, ok, 0)) { if (lane == 0) set_error(P.error, RC_DEV_ERR_TIMEOUT); return; }
-                __threadfence_block();
-                const uint8_t *slot = B.r[w - 1].ring[x % RING];
-                if (lane < 16) {  // luma rows 12..15: 4 rows x 16 bytes as 16 words
-                    *(uint32_t *)&T.y[lane >> 2][4 + 4 * (lane & 3)] = *(const uint32_t *)(slot + 4 * lane);
-                } else {          // chroma: 2 planes x 4 rows x 8 bytes as 16 words
-                    int k = lane - 16, c = k >> 3, r = (k >> 1) & 3, h = k & 1;
-                    *(uint32_t *)&T.c[c][r][4 + 4 * h] = *(const uint32_t *)(slot + 64 + 4 * k);
+    }
+    int last = -2;  // the MB reconstructed last (its right column is still in the canvas)
+    for (int x0 = 0; x0 < P.mb_w; x0 += 32) {
+        const int xl = x0 + lane;
+        const int kind = xl < P.mb_w ? __ldg(&P.mbs[my * P.mb_w + xl].kind) : RC_H264_NONE;
+        uint32_t todo = __ballot_sync(0xffffffffu, wave_intra(kind));
+        while (todo) {
+            const int mx = x0 + __ffs(todo) - 1;
+            todo &= todo - 1;
+            const int addr = my * P.mb_w + mx;
+            // the MBs before mx are reconstructed (inter ones by h264_mb_kernel)
+            if (lane == 0 && *mine < mx) *mine = mx;
+            // prediction parameters and residual (independent of the neighbours)
+            if (lane < 8) ((uint32_t *)&S.q)[lane] = __ldcg((const uint32_t *)(P.iinfo + addr) + lane);
+            {
+                const uint4 *src = (const uint4 *)(P.ires + (size_t)addr * 384);
+                uint4 *dst = (uint4 *)S.res;
+                dst[lane] = __ldcg(src + lane);
+                if (lane < 16) dst[32 + lane] = __ldcg(src + 32 + lane);
+            }
+            // canvas column -1: MB mx-1's right column, from the canvas when this
+            // warp reconstructed it, else from the picture (an inter MB)
+            if (mx > 0) {
+                const int c = (lane >> 3) & 1, rr = lane & 7;
+                if (last == mx - 1) {
+                    if (lane < 16) S.cy[(lane + 1) * 32] = S.cy[(lane + 1) * 32 + 16];
+                    else S.cc[c][(rr + 1) * 12] = S.cc[c][(rr + 1) * 12 + 8];
+                } else {
+                    if (lane < 16) S.cy[(lane + 1) * 32] = __ldcg(Y + (size_t)(my * 16 + lane) * P.pitch + mx * 16 - 1);
+                    else S.cc[c][(rr + 1) * 12] = __ldcg((c ? V : U) + (size_t)(my * 8 + rr) * P.cpitch + mx * 8 - 1);
                 }
             }
-        }
-        __syncwarp();
-        if (x + 1 < P.mb_w) prefetch(x + 1);
-        const DbMb &db = T.db;
-        if (db.flags) {
-            const int aoff = db.aoff, boff = db.boff;
-            {  // vertical edges, one row per lane
-                int sv[20];
-                uint8_t *row = luma ? T.y[lane + 4] : T.c[cc][li + 4];
-                const int n = luma ? 20 : 12;
-#pragma unroll
-                for (int i = 0; i < 20; i++) sv[i] = i < n ? row[i] : 0;
-                const int k = luma ? li >> 2 : li >> 1;
-#pragma unroll
-                for (int e = 0; e < 4; e++) {
-                    const int bsv = db.bs[(e << 2) | k];
-                    const bool strong = db.bs[e << 2] >= 4;
-                    int alpha, beta, tc0;
-                    if (luma) {
-                        edge_consts(e == 0 ? db.qp[1] : db.qp[0], db.qp[0], bsv, aoff, boff, alpha, beta, tc0);
-                        filt_luma(sv + 4 * e, bsv, strong, alpha, beta, tc0);
-                    } else if ((e & 1) == 0) {
-                        edge_consts(e == 0 ? db.qpc[1][cc] : db.qpc[0][cc], db.qpc[0][cc], bsv, aoff, boff, alpha,
-                                    beta, tc0);
-                        filt_chroma(sv + 2 * e, bsv, strong, alpha, beta, tc0);
-                    }
+            if (my > 0 && !wait_ge(above, min(mx + 2, P.mb_w), P, lane)) { band_fail(P, lane); return; }
+            // canvas row -1: the row above's bottom samples, columns -1..30 (chroma -1..8)
+            if (my > 0) {
+                const int gx = mx * 16 + lane - 1;
+                uint8_t v = 0;
+                if (gx >= 0 && gx < P.W) v = w > 0 ? ay[gx] : __ldcg(Y + (size_t)(my * 16 - 1) * P.pitch + gx);
+                S.cy[lane] = v;
+                if (lane < 20) {
+                    const int c = lane / 10, gxc = mx * 8 + lane % 10 - 1;
+                    uint8_t u = 0;
+                    if (gxc >= 0 && gxc < P.CW)
+                        u = w > 0 ? (c ? av : au)[gxc] : __ldcg((c ? V : U) + (size_t)(my * 8 - 1) * P.cpitch + gxc);
+                    S.cc[c][lane % 10] = u;
                 }
-#pragma unroll
-                for (int i = 0; i < 20; i++)
-                    if (i < n) row[i] = (uint8_t)sv[i];
             }
             __syncwarp();
-            {  // horizontal edges, one column per lane
-                int sv[20];
-                const int n = luma ? 20 : 12;
+            bool nb[4];
 #pragma unroll
-                for (int i = 0; i < 20; i++) sv[i] = i < n ? (luma ? T.y[i][lane + 4] : T.c[cc][i][li + 4]) : 0;
-                const int k = luma ? li >> 2 : li >> 1;
-#pragma unroll
-                for (int e = 0; e < 4; e++) {
-                    const int bsv = db.bs[16 | (e << 2) | k];
-                    const bool strong = db.bs[16 | (e << 2)] >= 4;
-                    int alpha, beta, tc0;
-                    if (luma) {
-                        edge_consts(e == 0 ? db.qp[2] : db.qp[0], db.qp[0], bsv, aoff, boff, alpha, beta, tc0);
-                        filt_luma(sv + 4 * e, bsv, strong, alpha, beta, tc0);
-                    } else if ((e & 1) == 0) {
-                        edge_consts(e == 0 ? db.qpc[2][cc] : db.qpc[0][cc], db.qpc[0][cc], bsv, aoff, boff, alpha,
-                                    beta, tc0);
-                        filt_chroma(sv + 2 * e, bsv, strong, alpha, beta, tc0);
-                    }
+            for (int n = 0; n < 4; n++) nb[n] = S.q.nb >> n & 1;
+            intra_mb(S, lane, nb, B.tab4, B.tab8);
+            // store the MB; its bottom samples into this row's line
+            {
+                const int r = lane >> 1, half = lane & 1;
+                const uint8_t *q = S.cy + (r + 1) * 32 + 1 + half * 8;
+                const uint32_t lo = q[0] | q[1] << 8 | q[2] << 16 | (uint32_t)q[3] << 24;
+                const uint32_t hi = q[4] | q[5] << 8 | q[6] << 16 | (uint32_t)q[7] << 24;
+                *(uint2 *)(Y + (size_t)(my * 16 + r) * P.pitch + mx * 16 + half * 8) = make_uint2(lo, hi);
+                if (lane < 16) {
+                    const int c = lane >> 3, rr = lane & 7;
+                    const uint8_t *t = S.cc[c] + (rr + 1) * 12 + 1;
+                    const uint32_t a0 = t[0] | t[1] << 8 | t[2] << 16 | (uint32_t)t[3] << 24;
+                    const uint32_t a1 = t[4] | t[5] << 8 | t[6] << 16 | (uint32_t)t[7] << 24;
+                    *(uint2 *)((c ? V : U) + (size_t)(my * 8 + rr) * P.cpitch + mx * 8) = make_uint2(a0, a1);
+                    ly[mx * 16 + lane] = S.cy[16 * 32 + lane + 1];
+                } else {
+                    const int c = (lane >> 3) & 1, i = lane & 7;
+                    (c ? lv : lu)[mx * 8 + i] = S.cc[c][8 * 12 + i + 1];
                 }
-#pragma unroll
-                for (int i = 0; i < 20; i++)
-                    if (i < n) {
-                        if (luma) T.y[i][lane + 4] = (uint8_t)sv[i];
-                        else T.c[cc][i][li + 4] = (uint8_t)sv[i];
-                    }
             }
+            last = mx;
             __syncwarp();
-        }
-        // ---- final samples to the picture (as h264_deblock_kernel)
-        if (luma) {
-            uint8_t *dst = Y + (size_t)(my * 16 + lane) * P.pitch + x * 16;
-            const uint8_t *r = T.y[lane + 4];
-            *(uint32_t *)(dst + 0) = *(const uint32_t *)(r + 4);
-            *(uint32_t *)(dst + 4) = *(const uint32_t *)(r + 8);
-            *(uint32_t *)(dst + 8) = *(const uint32_t *)(r + 12);
-            if (x > 0) *(uint32_t *)(dst - 4) = *(const uint32_t *)(r + 0);
-            if (x == P.mb_w - 1) *(uint32_t *)(dst + 12) = *(const uint32_t *)(r + 16);
-        } else {
-            uint8_t *dst = (cc ? V : U) + (size_t)(my * 8 + li) * P.cpitch + x * 8;
-            const uint8_t *r = T.c[cc][li + 4];
-            *(uint32_t *)(dst + 0) = *(const uint32_t *)(r + 4);
-            if (x > 0) *(uint32_t *)(dst - 4) = *(const uint32_t *)(r + 0);
-            if (x == P.mb_w - 1) *(uint32_t *)(dst + 4) = *(const uint32_t *)(r + 8);
-        }
-        if (my > 0 && db.flags) {
-            if (lane < 3) {
-                uint8_t *dst = Y + (size_t)(my * 16 - 3 + lane) * P.pitch + x * 16;
-                const uint8_t *r = T.y[lane + 1] + 4;
-                *(uint4 *)dst = make_uint4(*(const uint32_t *)(r), *(const uint32_t *)(r + 4),
-                                           *(const uint32_t *)(r + 8), *(const uint32_t *)(r + 12));
-            } else if (lane < 5) {
-                int c = lane - 3;
-                uint8_t *dst = (c ? V : U) + (size_t)(my * 8 - 1) * P.cpitch + x * 8;
-                const uint8_t *r = T.c[c][3] + 4;
-                *(uint2 *)dst = make_uint2(*(const uint32_t *)(r), *(const uint32_t *)(r + 4));
-            }
-        }
-        // ---- bottom rows for the next row of the band: MB x columns 0..11
-        // now, MB x-1 columns 12..15 (final after this MB's left edge)
-        if (ring_out) {
-            bool ok = true;
-            if (lane == 0) {
-                uint32_t it = 0;
-                while (B.prog[w + 1] < x - RING + 1) {
-                    if (++it > P.wait_limit || ((it & 63) == 0 && aborted(P.error))) { ok = false; break; }
-                    if (it > 1024) __nanosleep(32);
-                }
-            }
-            if (!__shfl_sync(0xffffffffu, ok, 0)) { if (lane == 0) set_error(P.error, RC_DEV_ERR_TIMEOUT); return; }
-            uint8_t *cur = B.r[w].ring[x % RING], *prev = B.r[w].ring[(x + RING - 1) % RING];
-            if (lane < 16) {
-                const int r = lane >> 2, q = lane & 3;  // luma row 12 + r, word q (columns 4q..4q+3)
-                if (q < 3) *(uint32_t *)(cur + 4 * lane) = *(const uint32_t *)&T.y[16 + r][4 + 4 * q];
-                else {
-                    if (x > 0) *(uint32_t *)(prev + 4 * lane) = *(const uint32_t *)&T.y[16 + r][0];
-                    if (x == P.mb_w - 1) *(uint32_t *)(cur + 4 * lane) = *(const uint32_t *)&T.y[16 + r][16];
-                }
-            } else {
-                const int k = lane - 16, c = k >> 3, r = (k >> 1) & 3, h = k & 1;  // chroma row 4 + r, half h
-                if (h == 0) *(uint32_t *)(cur + 64 + 4 * k) = *(const uint32_t *)&T.c[c][8 + r][4];
-                else {
-                    if (x > 0) *(uint32_t *)(prev + 64 + 4 * k) = *(const uint32_t *)&T.c[c][8 + r][0];
-                    if (x == P.mb_w - 1) *(uint32_t *)(cur + 64 + 4 * k) = *(const uint32_t *)&T.c[c][8 + r][8];
-                }
-            }
-        }
-        __syncwarp();
-        const int done = x == P.mb_w - 1 ? P.mb_w : x;
-        // progress: in shared memory for the rows of this band (the row below
-        // reads it, the row above throttles its ring on it), and in global
-        // memory for the band's last row (read by the next band; every 4 MBs)
-        if (last && ((x & 3) == 3 || done == P.mb_w)) {
-            __threadfence();
-            __syncwarp();
-            if (lane == 0) {
-                st_release(P.rowprog + my, tag | (uint32_t)done);
-                B.prog[w] = done;
-            }
-        } else {
             __threadfence_block();
-            __syncwarp();
-            if (lane == 0) B.prog[w] = done;
+            if (lane == 0) *mine = mx + 1;
         }
-        // ---- shift: this MB's columns 12..15 become the next MB's left columns
-        if (luma) *(uint32_t *)&T.y[lane + 4][0] = *(const uint32_t *)&T.y[lane + 4][16];
-        else *(uint32_t *)&T.c[cc][li + 4][0] = *(const uint32_t *)&T.c[cc][li + 4][8];
-        __syncwarp();
     }
+    __syncwarp();
+    if (lane == 0) *mine = P.mb_w;
 }
 
-// Helper warp 0 of a band: confirms, column by column, that the intra MBs of
-// the band's rows and of the row below are reconstructed (acquire loads of
-// their flags) and publishes the count of ready columns in shared memory.
-__device__ void wave_band_intra_helper(const H264Launch &P, BandSmem &B, int y0, int rows, int lane) {
-    const int ry = y0 + lane;
-    const bool mine = lane <= rows && ry < P.mb_h;
+// Luma loop-filter warp of band row w (picture row my); lanes 0..15 hold one
+// sample row (vertical edges) or one column (horizontal edges) of the MB.
+__device__ void band_luma_row(const H264Launch &P, BandSmem &B, int w, int my, int rows, int lane) {
+    LumaRow &R = B.l[w];
+    uint8_t *Y = P.dpb + (size_t)P.out_slot * P.slot_bytes;
+    const bool act = lane < 16;
+    const int r = lane & 15, k = r >> 2;
+    const bool below = my + 1 < P.mb_h, ring_out = w + 1 < rows;
+    volatile int *iown = &B.iprog[w + 1], *ibelow = &B.iprog[w + 2];
+    volatile int *dup = &B.lprog[w], *dmine = &B.lprog[w + 1], *ddown = &B.lprog[min(w + 2, BR)];
+    const uint4 *E = (const uint4 *)(P.edges + (size_t)my * P.mb_w * RC_EDGE_WORDS);
+    const uint4 z4 = make_uint4(0, 0, 0, 0);
+    uint4 prev = z4;
+    // MB x's sample rows and edge words into slot x % 3; every lane commits a
+    // group per MB so that the group counts stay uniform
+    auto stage = [&](int x) {
+        if (act && x < P.mb_w) {
+            const int sl = x % 3;
+            cp_async16(&R.st[sl][0][r], Y + (size_t)(my * 16 + r) * P.pitch + x * 16);
+            cp_async16(&R.st[sl][1][r], E + (size_t)x * (RC_EDGE_WORDS / 4) + k);
+            cp_async16(&R.st[sl][2][r], E + (size_t)x * (RC_EDGE_WORDS / 4) + 4 + k);
+        }
+        cp_commit();
+    };
+    if (!wait_ge(iown, min(2, P.mb_w), P, lane)) { band_fail(P, lane); return; }
+    stage(0);
+    stage(1);
     for (int x = 0; x < P.mb_w; x++) {
-        bool ok = true;
-        if (mine) {
-            const int a = ry * P.mb_w + x;
-            if (wave_intra(__ldg(&P.mbs[a].kind))) ok = wait_flag(P.rflag + a, P.epoch, P.wait_limit, P.error);
+        if (!wait_ge(iown, min(x + 3, P.mb_w), P, lane)) { band_fail(P, lane); return; }
+        if (below && !wait_ge(ibelow, min(x + 2, P.mb_w), P, lane)) { band_fail(P, lane); return; }
+        if (my > 0 && !wait_ge(dup, x + 1, P, lane)) { band_fail(P, lane); return; }
+        // rows -4..-1: the row above's ring, or the picture for the band's first row
+        uint4 t4 = z4;
+        if (my > 0 && lane < 4)
+            t4 = w > 0 ? *(const uint4 *)(B.l[w - 1].ring[x % DRING] + lane * 16)
+                       : __ldcg((const uint4 *)(Y + (size_t)(my * 16 - 4 + lane) * P.pitch + x * 16));
+        stage(x + 2);
+        cp_wait_all_but_1();
+        const int sl = x % 3;
+        const uint4 cur = act ? R.st[sl][0][r] : z4, pv = act ? R.st[sl][1][r] : z4,
+                    ph = act ? R.st[sl][2][r] : z4;
+        // ---- vertical edges: lane r holds columns -4..15 of sample row r
+        uint32_t wd[5] = {prev.w, cur.x, cur.y, cur.z, cur.w};
+        const uint32_t ev[4] = {pv.x, pv.y, pv.z, pv.w};
+        if (__any_sync(0xffffffffu, (ev[0] | ev[1] | ev[2] | ev[3]) != 0)) {
+            int sv[20];
+#pragma unroll
+            for (int i = 0; i < 20; i++) sv[i] = (wd[i >> 2] >> (8 * (i & 3))) & 255;
+            if (__any_sync(0xffffffffu, (ev[0] >> 24) >= 4)) lf_luma<true>(sv, ev[0]);
+            else if (__any_sync(0xffffffffu, ev[0] != 0)) lf_luma<false>(sv, ev[0]);
+#pragma unroll
+            for (int e = 1; e < 4; e++)
+                if (__any_sync(0xffffffffu, ev[e] != 0)) lf_luma<false>(sv + 4 * e, ev[e]);
+#pragma unroll
+            for (int j = 0; j < 5; j++)
+                wd[j] = (uint32_t)sv[4 * j] | (uint32_t)sv[4 * j + 1] << 8 | (uint32_t)sv[4 * j + 2] << 16 |
+                        (uint32_t)sv[4 * j + 3] << 24;
         }
-        if (!__all_sync(0xffffffffu, ok)) {
-            if (lane == 0) set_error(P.error, RC_DEV_ERR_TIMEOUT);
-            return;
+        // ---- MB x-1 is final in this row: store it, and its rows 12..15 for the row below
+        if (x > 0) {
+            prev.w = wd[0];
+            if (act) *(uint4 *)(Y + (size_t)(my * 16 + r) * P.pitch + (x - 1) * 16) = prev;
+            if (ring_out) {
+                if (x - DRING > 0 && !wait_ge(ddown, x - DRING, P, lane)) { band_fail(P, lane); return; }
+                if (act && r >= 12) *(uint4 *)(R.ring[(x - 1) % DRING] + (r - 12) * 16) = prev;
+            }
         }
-        __threadfence_block();
+        // ---- horizontal edges: lane r holds rows -4..15 of sample column r
+        if (act) *(uint4 *)R.t[4 + r] = make_uint4(wd[1], wd[2], wd[3], wd[4]);
+        if (my > 0 && lane < 4) *(uint4 *)R.t[lane] = t4;
         __syncwarp();
-        if (lane == 0) B.icol = x + 1;
+        const uint32_t eh[4] = {ph.x, ph.y, ph.z, ph.w};
+        const bool top = my > 0 && __any_sync(0xffffffffu, eh[0] != 0);
+        if (__any_sync(0xffffffffu, (eh[0] | eh[1] | eh[2] | eh[3]) != 0)) {
+            int sv[20];
+#pragma unroll
+            for (int i = 0; i < 20; i++) sv[i] = R.t[i][r];
+            if (__any_sync(0xffffffffu, (eh[0] >> 24) >= 4)) lf_luma<true>(sv, eh[0]);
+            else if (__any_sync(0xffffffffu, eh[0] != 0)) lf_luma<false>(sv, eh[0]);
+#pragma unroll
+            for (int e = 1; e < 4; e++)
+                if (__any_sync(0xffffffffu, eh[e] != 0)) lf_luma<false>(sv + 4 * e, eh[e]);
+            __syncwarp();
+            if (act) {
+#pragma unroll
+                for (int i = 1; i < 19; i++) R.t[i][r] = (uint8_t)sv[i];
+            }
+            __syncwarp();
+        }
+        prev = act ? *(const uint4 *)R.t[4 + r] : z4;
+        // rows 13..15 of the MB above are final after this MB's top edge
+        if (top && lane < 3)
+            *(uint4 *)(Y + (size_t)(my * 16 - 3 + lane) * P.pitch + x * 16) = *(const uint4 *)R.t[1 + lane];
+        __syncwarp();
+        __threadfence_block();
+        if (lane == 0) *dmine = x;
     }
+    // the row's last MB
+    if (act) *(uint4 *)(Y + (size_t)(my * 16 + r) * P.pitch + (P.mb_w - 1) * 16) = prev;
+    if (ring_out) {
+        if (P.mb_w - DRING > 0 && !wait_ge(ddown, P.mb_w - DRING, P, lane)) { band_fail(P, lane); return; }
+        if (act && r >= 12) *(uint4 *)(R.ring[(P.mb_w - 1) % DRING] + (r - 12) * 16) = prev;
+    }
+    __syncwarp();
+    __threadfence_block();
+    if (lane == 0) *dmine = P.mb_w;
 }
 
-// Helper warp 1 of a band: mirrors the global progress word of the row above
-// the band into shared memory.
-__device__ void wave_band_above_helper(const H264Launch &P, BandSmem &B, int y0, int lane) {
-    if (lane != 0) return;
-    if (y0 == 0) { B.above = P.mb_w; return; }
+// Chroma loop-filter warp of band row w: lanes 0..7 Cb, 8..15 Cr, each one
+// sample row (vertical edges) or column (horizontal edges) of the MB.
+__device__ void band_chroma_row(const H264Launch &P, BandSmem &B, int w, int my, int rows, int lane) {
+    ChromaRow &R = B.c[w];
+    uint8_t *Y = P.dpb + (size_t)P.out_slot * P.slot_bytes;
+    const bool act = lane < 16;
+    const int c = (lane >> 3) & 1, r = lane & 7, k = r >> 1;
+    uint8_t *Cp = Y + (c ? P.v_off : P.u_off);
+    const bool below = my + 1 < P.mb_h, ring_out = w + 1 < rows;
+    volatile int *iown = &B.iprog[w + 1], *ibelow = &B.iprog[w + 2];
+    volatile int *dup = &B.cprog[w], *dmine = &B.cprog[w + 1], *ddown = &B.cprog[min(w + 2, BR)];
+    const uint2 *E = (const uint2 *)(P.edges + (size_t)my * P.mb_w * RC_EDGE_WORDS);
+    const uint2 z2 = make_uint2(0, 0);
+    uint2 prev = z2;
+    auto stage = [&](int x) {
+        if (act && x < P.mb_w) {
+            const int sl = x % 3;
+            cp_async8(&R.st[sl][0][lane], Cp + (size_t)(my * 8 + r) * P.cpitch + x * 8);
+            cp_async8(&R.st[sl][1][lane], E + (size_t)x * (RC_EDGE_WORDS / 2) + 16 + c * 4 + k);
+            cp_async8(&R.st[sl][2][lane], E + (size_t)x * (RC_EDGE_WORDS / 2) + 24 + c * 4 + k);
+        }
+        cp_commit();
+    };
+    if (!wait_ge(iown, min(2, P.mb_w), P, lane)) { band_fail(P, lane); return; }
+    stage(0);
+    stage(1);
+    for (int x = 0; x < P.mb_w; x++) {
+        if (!wait_ge(iown, min(x + 3, P.mb_w), P, lane)) { band_fail(P, lane); return; }
+        if (below && !wait_ge(ibelow, min(x + 2, P.mb_w), P, lane)) { band_fail(P, lane); return; }
+        if (my > 0 && !wait_ge(dup, x + 1, P, lane)) { band_fail(P, lane); return; }
+        // rows -2..-1 per component (lanes 0..3: component lane >> 1, row lane & 1)
+        uint2 t2 = z2;
+        if (my > 0 && lane < 4) {
+            const int cc = lane >> 1, rr = lane & 1;
+            t2 = w > 0 ? *(const uint2 *)(B.c[w - 1].ring[x % DRING] + cc * 16 + rr * 8)
+                       : __ldcg((const uint2 *)(Y + (cc ? P.v_off : P.u_off) + (size_t)(my * 8 - 2 + rr) * P.cpitch +
+                                                x * 8));
+        }
+        stage(x + 2);
+        cp_wait_all_but_1();
+        const int sl = x % 3;
+        const uint2 cur = act ? R.st[sl][0][lane] : z2, pv = act ? R.st[sl][1][lane] : z2,
+                    ph = act ? R.st[sl][2][lane] : z2;
+        // ---- vertical edges: lane holds columns -4..7 of its row
+        uint32_t wd[3] = {prev.y, cur.x, cur.y};
+        if (__any_sync(0xffffffffu, (pv.x | pv.y) != 0)) {
+            int sv[12];
+#pragma unroll
+            for (int i = 0; i < 12; i++) sv[i] = (wd[i >> 2] >> (8 * (i & 3))) & 255;
+            if (__any_sync(0xffffffffu, pv.x != 0)) lf_chroma(sv + 2, pv.x);
+            if (__any_sync(0xffffffffu, pv.y != 0)) lf_chroma(sv + 6, pv.y);
+#pragma unroll
+            for (int j = 0; j < 3; j++)
+                wd[j] = (uint32_t)sv[4 * j] | (uint32_t)sv[4 * j + 1] << 8 | (uint32_t)sv[4 * j + 2] << 16 |
+                        (uint32_t)sv[4 * j + 3] << 24;
+        }
+        if (x > 0) {
+            prev.y = wd[0];
+            if (act) *(uint2 *)(Cp + (size_t)(my * 8 + r) * P.cpitch + (x - 1) * 8) = prev;
+            if (ring_out) {
+                if (x - DRING > 0 && !wait_ge(ddown, x - DRING, P, lane)) { band_fail(P, lane); return; }
+                if (act && r >= 6) *(uint2 *)(R.ring[(x - 1) % DRING] + c * 16 + (r - 6) * 8) = prev;
+            }
+        }
+        // ---- horizontal edges: lane holds rows -2..7 of its column
+        if (act) *(uint2 *)R.t[c][2 + r] = make_uint2(wd[1], wd[2]);
+        if (my > 0 && lane < 4) *(uint2 *)R.t[lane >> 1][lane & 1] = t2;
+        __syncwarp();
+        const bool top = my > 0 && __any_sync(0xffffffffu, ph.x != 0);
+        if (__any_sync(0xffffffffu, (ph.x | ph.y) != 0)) {
+            int sv[10];
+#pragma unroll
+            for (int i = 0; i < 10; i++) sv[i] = R.t[c][i][r];
+            if (__any_sync(0xffffffffu, ph.x != 0)) lf_chroma(sv + 0, ph.x);
+            if (__any_sync(0xffffffffu, ph.y != 0)) lf_chroma(sv + 4, ph.y);
+            __syncwarp();
+            if (act) {
+#pragma unroll
+                for (int i = 1; i < 9; i++) R.t[c][i][r] = (uint8_t)sv[i];
+            }
+            __syncwarp();
+        }
+        prev = act ? *(const uint2 *)R.t[c][2 + r] : z2;
+        // row 7 of the MB above is final after this MB's top edge
+        if (top && lane < 2)
+            *(uint2 *)(Y + (lane ? P.v_off : P.u_off) + (size_t)(my * 8 - 1) * P.cpitch + x * 8) =
+                *(const uint2 *)R.t[lane][1];
+        __syncwarp();
+        __threadfence_block();
+        if (lane == 0) *dmine = x;
+    }
+    if (act) *(uint2 *)(Cp + (size_t)(my * 8 + r) * P.cpitch + (P.mb_w - 1) * 8) = prev;
+    if (ring_out) {
+        if (P.mb_w - DRING > 0 && !wait_ge(ddown, P.mb_w - DRING, P, lane)) { band_fail(P, lane); return; }
+        if (act && r >= 6) *(uint2 *)(R.ring[(P.mb_w - 1) % DRING] + c * 16 + (r - 6) * 8) = prev;
+    }
+    __syncwarp();
+    __threadfence_block();
+    if (lane == 0) *dmine = P.mb_w;
+}
+
+// Helper warp: lanes 0..2 mirror the progress of the neighbouring bands'
+// rows (global, acquire) into shared memory; lanes 3..5 publish this band's
+// boundary rows (release).  Each lane runs its own loop.
+__device__ void band_helper(const H264Launch &P, BandSmem &B, int y0, int rows, int lane) {
     const uint32_t tag = (P.epoch & 0xffffu) << 16;
-    const uint32_t *f = P.rowprog + y0 - 1;
-    uint32_t it = 0;
+    const bool above = y0 > 0, below = y0 + rows < P.mb_h;
+    const uint32_t *src = nullptr;
+    uint32_t *dst = nullptr;
+    if (lane == 0) { if (!above) { B.lprog[0] = P.mb_w; B.cprog[0] = P.mb_w; return; } src = P.rowprog + y0 - 1; }
+    else if (lane == 1) { if (!above) { B.iprog[0] = P.mb_w; return; } src = P.irowprog + y0 - 1; }
+    else if (lane == 2) { if (!below) { B.iprog[rows + 1] = P.mb_w; return; } src = P.irowprog + y0 + rows; }
+    else if (lane == 3) { if (!below) return; dst = P.rowprog + y0 + rows - 1; }
+    else if (lane == 4) { if (!below) return; dst = P.irowprog + y0 + rows - 1; }
+    else if (lane == 5) { if (!above) return; dst = P.irowprog + y0; }
+    else return;
     int seen = 0;
+    uint32_t it = 0;
     while (seen < P.mb_w) {
-        const uint32_t v = ld_acquire(f);
-        if ((v & 0xffff0000u) == tag && (int)(v & 0xffffu) > seen) {
-            seen = v & 0xffffu;
-            __threadfence_block();
-            B.above = seen;
+        int n;
+        if (src) {
+            const uint32_t v = ld_acquire(src);
+            n = (v & 0xffff0000u) == tag ? (int)(v & 0xffffu) : 0;
+        } else {
+            n = lane == 3 ? min(B.lprog[rows], B.cprog[rows]) : lane == 4 ? B.iprog[rows] : B.iprog[1];
+        }
+        if (n > seen) {
+            seen = n;
+            if (src) {
+                __threadfence_block();
+                if (lane == 0) { B.lprog[0] = seen; B.cprog[0] = seen; }
+                else if (lane == 1) B.iprog[0] = seen;
+                else B.iprog[rows + 1] = seen;
+            } else {
+                __threadfence();
+                st_release(dst, tag | (uint32_t)seen);
+            }
             it = 0;
             continue;
         }
@@ -1440,28 +1630,29 @@ __device__ void wave_band_above_helper(const H264Launch &P, BandSmem &B, int y0,
             set_error(P.error, RC_DEV_ERR_TIMEOUT);
             return;
         }
-        if (it > 256) __nanosleep(64);
+        __nanosleep(src ? 256 : 64);
     }
 }
 
-__global__ void __launch_bounds__((WAVE_WARPS + 2) * 32) h264_wave_kernel(H264Launch P) {
-    __shared__ WaveSmem sm;
+__global__ void __launch_bounds__(BAND_THREADS, 1) h264_band_kernel(H264Launch P) {
+    __shared__ BandSmem B;
+    extern __shared__ __align__(16) uint8_t band_lines[];  // BR rows x mb_w x 32 bytes
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if ((int)blockIdx.x < P.intra_blocks) {
-        if (warp < WAVE_WARPS) wave_intra_worker(P, sm.iw[warp], lane);
-        return;
+    const int y0 = blockIdx.x * BR, rows = min(BR, P.mb_h - y0);
+    for (int i = threadIdx.x; i < 9 * 16; i += blockDim.x) B.tab4[i] = (&cPRED4.e[0][0])[i];
+    for (int i = threadIdx.x; i < 9 * 64; i += blockDim.x) B.tab8[i] = (&cPRED8.e[0][0])[i];
+    if (threadIdx.x < BR + 2) B.iprog[threadIdx.x] = 0;
+    if (threadIdx.x < BR + 1) {
+        B.lprog[threadIdx.x] = 0;
+        B.cprog[threadIdx.x] = 0;
     }
-    const int band = blockIdx.x - P.intra_blocks;
-    const int y0 = band * WAVE_WARPS, rows = min(WAVE_WARPS, P.mb_h - y0);
-    if (threadIdx.x < WAVE_WARPS) sm.band.prog[threadIdx.x] = 0;
-    if (threadIdx.x == 0) { sm.band.icol = 0; sm.band.above = 0; }
     __syncthreads();
-    if (warp == WAVE_WARPS) { wave_band_intra_helper(P, sm.band, y0, rows, lane); return; }
-    if (warp == WAVE_WARPS + 1) { wave_band_above_helper(P, sm.band, y0, lane); return; }
-    const int my = y0 + warp;
-    if (my >= P.mb_h) return;
-    const bool last = warp == WAVE_WARPS - 1 || my == P.mb_h - 1;
-    wave_band_row(P, sm.band, warp, my, last, lane);
+    if (warp == 3 * BR) { band_helper(P, B, y0, rows, lane); return; }
+    const int role = warp / BR, w = warp % BR;
+    if (w >= rows) return;
+    if (role == 0) band_intra_row(P, B, band_lines, w, y0 + w, lane);
+    else if (role == 1) band_luma_row(P, B, w, y0 + w, rows, lane);
+    else band_chroma_row(P, B, w, y0 + w, rows, lane);
 }
 
 }  // namespace
@@ -1470,22 +1661,28 @@ void rc_launch_h264_mb(const H264Launch &p, cudaStream_t st) {
     h264_mb_kernel<<<p.mb_w * p.mb_h, 256, 0, st>>>(p);
 }
 
-int rc_h264_wave_capacity() {
+size_t rc_h264_band_smem(int mb_w) { return (size_t)BR * mb_w * 32; }
+
+int rc_h264_band_capacity(int mb_w) {
     int dev = 0, sms = 0, per = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, h264_wave_kernel, (WAVE_WARPS + 2) * 32, 0) != cudaSuccess)
+    const size_t dyn = rc_h264_band_smem(mb_w);
+    if (cudaFuncSetAttribute(h264_band_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, h264_band_kernel, BAND_THREADS, dyn) != cudaSuccess)
         return 0;
     return per * sms;
 }
 
-int rc_launch_h264_wave(const H264Launch &p, cudaStream_t st) {
-    cudaMemsetAsync(p.counter, 0, sizeof(uint32_t), st);
-    const int bands = (p.mb_h + WAVE_WARPS - 1) / WAVE_WARPS;
+int rc_launch_h264_band(const H264Launch &p, cudaStream_t st) {
+    const int bands = (p.mb_h + BR - 1) / BR;
     H264Launch q = p;
     void *args[] = {&q};
-    cudaError_t e = cudaLaunchCooperativeKernel((const void *)h264_wave_kernel, dim3(p.intra_blocks + bands),
-                                                dim3((WAVE_WARPS + 2) * 32), args, 0, st);
+    cudaError_t e = cudaLaunchCooperativeKernel((const void *)h264_band_kernel, dim3(bands), dim3(BAND_THREADS),
+                                                args, rc_h264_band_smem(p.mb_w), st);
     return e == cudaSuccess ? 0 : -1;
 }
 

@@ -59,12 +59,10 @@ struct rc_stream {
     size_t budget = 0, held = 0;
     cudaStream_t st = nullptr;
     uint8_t *dpb = nullptr;
-    uint32_t *rflag = nullptr, *dflag = nullptr, *counter = nullptr, *error = nullptr, *tasks = nullptr;
-    uint32_t *rowprog = nullptr;
-    DbMb *db = nullptr;
+    uint32_t *counter = nullptr, *error = nullptr;
+    uint32_t *rowprog = nullptr, *irowprog = nullptr, *edges = nullptr;
     IntraInfo *iinfo = nullptr;
     int16_t *ires = nullptr;
-    int intra_blocks = 0;
     // HEVC
     DevBuf ctbs, blk, mvf, tus, hslices, scaling;
     uint8_t *work = nullptr;     // picture being reconstructed (pre-SAO)
@@ -72,7 +70,6 @@ struct rc_stream {
     uint32_t *ready = nullptr;   // per 4x4 block and component
     int w4 = 0, h4 = 0, log2ctb_alloc = 0;
     int bps = 1;
-    int ntasks = 0;
     DevBuf mbs, slices, weights, levels;
     int32_t *ls = nullptr;            // device ls4 (2304 ints) + ls8 (2304*4 ints)
     std::vector<int32_t> ls_host;     // last uploaded tables
@@ -230,19 +227,6 @@ int validate_h264(const Geo *s, const rc_h264_picture *p) {
     return 0;
 }
 
-// Intra task list: MBs in anti-diagonal order x + 2y (each MB after its
-// left, top-left, top and top-right neighbours).
-std::vector<uint32_t> h264_tasks(int mb_w, int mb_h) {
-    std::vector<std::pair<int, uint32_t>> v;
-    v.reserve(mb_w * mb_h);
-    for (int y = 0; y < mb_h; y++)
-        for (int x = 0; x < mb_w; x++) v.push_back({x + 2 * y, (uint32_t)(y * mb_w + x)});
-    std::stable_sort(v.begin(), v.end(), [](const auto &a, const auto &b) { return a.first < b.first; });
-    std::vector<uint32_t> t(v.size());
-    for (size_t i = 0; i < v.size(); i++) t[i] = v[i].second;
-    return t;
-}
-
 void destroy(rc_stream *s) {
     if (!s) return;
     if (s->st) cudaStreamSynchronize(s->st);
@@ -255,14 +239,12 @@ void destroy(rc_stream *s) {
     cudaFree(s->work);
     cudaFree(s->res);
     cudaFree(s->ready);
-    cudaFree(s->rflag);
-    cudaFree(s->dflag);
     cudaFree(s->counter);
     cudaFree(s->error);
-    cudaFree(s->tasks);
     cudaFree(s->ls);
     cudaFree(s->rowprog);
-    cudaFree(s->db);
+    cudaFree(s->irowprog);
+    dev_free(s, s->edges, (size_t)s->mb_w * s->mb_h * RC_EDGE_WORDS * sizeof(uint32_t));
     dev_free(s, s->iinfo, (size_t)s->mb_w * s->mb_h * sizeof(IntraInfo));
     dev_free(s, s->ires, (size_t)s->mb_w * s->mb_h * 384 * sizeof(int16_t));
     for (int i = 0; i < 2; i++) {
@@ -436,29 +418,20 @@ int rc_stream_create(int codec, int width, int height, int bit_depth, int dpb_sl
         if (v > 0 && v <= 4096) s->wave_blocks = v;
     }
     const int n = s->mb_w * s->mb_h;
-    std::vector<uint32_t> tasks = h264_tasks(s->mb_w, s->mb_h);
-    s->ntasks = (int)tasks.size();
     bool ok = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking) == cudaSuccess;
     ok = ok && dev_alloc(s, (void **)&s->dpb, s->slot_bytes * s->slots);
-    ok = ok && cudaMalloc(&s->rflag, n * sizeof(uint32_t)) == cudaSuccess;
-    ok = ok && cudaMalloc(&s->dflag, n * sizeof(uint32_t)) == cudaSuccess;
     ok = ok && cudaMalloc(&s->counter, 64) == cudaSuccess;
     ok = ok && cudaMalloc(&s->error, 64) == cudaSuccess;
-    ok = ok && cudaMalloc(&s->tasks, tasks.size() * sizeof(uint32_t)) == cudaSuccess;
     ok = ok && cudaMalloc(&s->ls, (2304 + 2304 * 4) * sizeof(int32_t)) == cudaSuccess;
     ok = ok && cudaMalloc(&s->rowprog, (size_t)s->mb_h * sizeof(uint32_t)) == cudaSuccess;
-    ok = ok && cudaMalloc(&s->db, (size_t)n * sizeof(DbMb)) == cudaSuccess;
+    ok = ok && cudaMalloc(&s->irowprog, (size_t)s->mb_h * sizeof(uint32_t)) == cudaSuccess;
     if (codec == RC_CODEC_H264) {
+        ok = ok && dev_alloc(s, (void **)&s->edges, (size_t)n * RC_EDGE_WORDS * sizeof(uint32_t));
         ok = ok && dev_alloc(s, (void **)&s->iinfo, (size_t)n * sizeof(IntraInfo));
         ok = ok && dev_alloc(s, (void **)&s->ires, (size_t)n * 384 * sizeof(int16_t));
-        // wave kernel: loop-filter bands of 8 MB rows plus intra CTAs, all resident (cooperative launch)
-        const int bands = (s->mb_h + 7) / 8, cap = rc_h264_wave_capacity();
-        s->intra_blocks = std::min(32, cap - bands);
-        if (const char *e = getenv("PITO_RECON_INTRA_BLOCKS")) {
-            int v = atoi(e);
-            if (v > 0) s->intra_blocks = std::min(v, cap - bands);
-        }
-        ok = ok && s->intra_blocks >= 1;
+        // band kernel: one CTA per RC_H264_BAND_ROWS MB rows, all resident (cooperative launch)
+        const int bands = (s->mb_h + RC_H264_BAND_ROWS - 1) / RC_H264_BAND_ROWS;
+        ok = ok && bands <= rc_h264_band_capacity(s->mb_w);
     }
     if (codec == RC_CODEC_HEVC) {
         const size_t nres = (size_t)s->width * s->height + 2 * (size_t)s->cw * s->ch;
@@ -471,12 +444,9 @@ int rc_stream_create(int codec, int width, int height, int bit_depth, int dpb_sl
     for (int i = 0; i < 2 && ok; i++) ok = cudaEventCreateWithFlags(&s->staged[i], cudaEventDisableTiming) == cudaSuccess;
     if (ok) {
         ok = cudaMemsetAsync(s->dpb, 0, s->slot_bytes * s->slots, s->st) == cudaSuccess &&
-             cudaMemsetAsync(s->rflag, 0, n * sizeof(uint32_t), s->st) == cudaSuccess &&
-             cudaMemsetAsync(s->dflag, 0, n * sizeof(uint32_t), s->st) == cudaSuccess &&
              cudaMemsetAsync(s->rowprog, 0, (size_t)s->mb_h * sizeof(uint32_t), s->st) == cudaSuccess &&
+             cudaMemsetAsync(s->irowprog, 0, (size_t)s->mb_h * sizeof(uint32_t), s->st) == cudaSuccess &&
              cudaMemsetAsync(s->error, 0, 64, s->st) == cudaSuccess &&
-             cudaMemcpyAsync(s->tasks, tasks.data(), tasks.size() * sizeof(uint32_t), cudaMemcpyHostToDevice,
-                             s->st) == cudaSuccess &&
              cudaStreamSynchronize(s->st) == cudaSuccess;
     }
     if (!ok) {
@@ -557,21 +527,17 @@ int rc_h264_submit(rc_stream *s, const rc_h264_picture *pic, int out_slot) {
     L.cpitch = s->cpitch;
     L.constrained_intra = pic->constrained_intra_pred;
     L.epoch = ++s->epoch;
-    L.rflag = s->rflag;
-    L.dflag = s->dflag;
-    L.counter = s->counter;
-    L.tasks = s->tasks;
-    L.ntasks = s->ntasks;
     L.error = s->error;
     L.wait_limit = s->wait_limit;
-    L.db = s->db;
+    L.db = nullptr;
+    L.edges = s->edges;
     L.rowprog = s->rowprog;
+    L.irowprog = s->irowprog;
     L.iinfo = s->iinfo;
     L.ires = s->ires;
-    L.intra_blocks = s->intra_blocks;
     timed(s, RC_KERNEL_H264_MB, [&] { rc_launch_h264_mb(L, s->st); });
     int lrc = 0;
-    timed(s, RC_KERNEL_H264_WAVE, [&] { lrc = rc_launch_h264_wave(L, s->st); });
+    timed(s, RC_KERNEL_H264_BAND, [&] { lrc = rc_launch_h264_band(L, s->st); });
     if (lrc != 0) return cuda_fail(s);
     s->submits++;
     if (cudaGetLastError() != cudaSuccess) return cuda_fail(s);

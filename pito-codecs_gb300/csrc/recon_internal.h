@@ -30,15 +30,23 @@ static_assert(sizeof(DbMb) == 48, "DbMb layout");
 
 // What an intra MB's reconstruction needs besides its residual, prepared by
 // h264_mb_kernel: neighbour availability for intra prediction (bits 0..3:
-// left, top, top-right, top-left) and the intra neighbours whose samples the
-// MB's modes actually read (same bits) -- the ones the wavefront waits for.
+// left, top, top-right, top-left).
 struct IntraInfo {
     uint8_t kind, t8, i16_mode, chroma_mode;
-    uint8_t nb, wait, pad0, pad1;
+    uint8_t nb, pad0, pad1, pad2;
     uint8_t modes[16];
-    uint32_t pad2[2];
+    uint32_t pad3[2];
 };
 static_assert(sizeof(IntraInfo) == 32, "IntraInfo layout");
+
+// Loop-filter edge words: per MB, 64 words of (alpha | beta << 8 | tc0 << 16
+// | bS << 24), bS 0 meaning the line segment is not filtered.  Order, so that
+// each filtering lane loads its words with one vector load:
+//   [ 0..15] luma vertical edges    k * 4 + e    (k: 4-line segment, e: edge)
+//   [16..31] luma horizontal edges  16 + k * 4 + e
+//   [32..47] chroma vertical edges  32 + c * 8 + k * 2 + e   (c: Cb/Cr, e: chroma edge 0 / 4)
+//   [48..63] chroma horizontal      48 + c * 8 + k * 2 + e
+#define RC_EDGE_WORDS 64
 
 struct H264Launch {
     const rc_h264_mb *mbs;
@@ -56,17 +64,14 @@ struct H264Launch {
     int mb_w, mb_h, W, H, CW, CH, pitch, cpitch;
     int constrained_intra;
     uint32_t epoch;
-    uint32_t *rflag, *dflag;  // per MB: epoch when reconstructed / deblocked
-    uint32_t *counter;        // task counter (zeroed before the wave launch)
-    const uint32_t *tasks;    // wave task list (bit 31 = deblock task)
-    int ntasks;
     uint32_t *error;
     uint32_t wait_limit;
-    DbMb *db;             // per-MB loop-filter parameters
-    uint32_t *rowprog;    // per MB row: (epoch & 0xffff) << 16 | MBs final
+    DbMb *db;             // per-MB loop-filter parameters (allocation-free entry point)
+    uint32_t *edges;      // per MB: RC_EDGE_WORDS loop-filter edge words (band kernel)
+    uint32_t *rowprog;    // per MB row: (epoch & 0xffff) << 16 | MBs loop-filtered and stored
+    uint32_t *irowprog;   // per MB row: (epoch & 0xffff) << 16 | MBs reconstructed (intra included)
     IntraInfo *iinfo;     // per MB (intra MBs)
     int16_t *ires;        // per MB: 256 luma + 2 x 64 chroma residual samples (intra MBs)
-    int intra_blocks;     // CTAs of the wave kernel that run intra MBs; the rest run loop-filter bands
 };
 
 struct HevcLaunch {
@@ -102,7 +107,11 @@ void rc_launch_hevc_sao(const HevcLaunch &p, cudaStream_t st);
 
 // Launchers (h264_kernels.cu).
 void rc_launch_h264_mb(const H264Launch &p, cudaStream_t st);
-// Intra reconstruction and the loop filter in one cooperative launch.
-int rc_launch_h264_wave(const H264Launch &p, cudaStream_t st);
-// CTAs of the wave kernel that can be resident at once (0 if unknown).
-int rc_h264_wave_capacity();
+// Intra reconstruction and the loop filter in one cooperative launch, one
+// CTA per band of RC_H264_BAND_ROWS MB rows; returns 0 or -1 (launch failed).
+#define RC_H264_BAND_ROWS 7
+int rc_launch_h264_band(const H264Launch &p, cudaStream_t st);
+// Band CTAs that can be resident at once for pictures mb_w MBs wide (0 if
+// unknown); the band kernel's dynamic shared memory for that width.
+int rc_h264_band_capacity(int mb_w);
+size_t rc_h264_band_smem(int mb_w);
