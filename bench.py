@@ -1,21 +1,27 @@
 #!/usr/bin/env python3
-"""Throughput of H.264 1080p block reconstruction on GB300.
+"""Throughput of H.264 / HEVC block reconstruction on GB300.
 
-Workload: Plain H.264 High 1920x1080 (coded 1920x1088, 8160 MBs/frame),
-120 frames from seeded per-MB syntax records: frame 0 all intra, then P
-frames with 2 references, 30% intra MBs (I4x4/I8x8/I16x16), 70% inter
-(16x16..4x4 partitions), quarter-pel motion within +-128 px with 5% off the
-picture, 20% of inter MBs with explicit weighted prediction, 80% all-zero
-blocks with Laplacian(b=2) levels elsewhere, transform_8x8 on half of the
-eligible MBs, QP 20..40, deblocking on.
+Default workload (h264_1080p): Plain H.264 High 1920x1080 (coded 1920x1088,
+8160 MBs/frame), 120 frames from seeded per-MB syntax records: frame 0 all
+intra, then P frames with 2 references, 30% intra MBs (I4x4/I8x8/I16x16),
+70% inter (16x16..4x4 partitions), quarter-pel motion within +-128 px with
+5% off the picture, 20% of inter MBs with explicit weighted prediction, 80%
+all-zero blocks with Laplacian(b=2) levels elsewhere, transform_8x8 on half
+of the eligible MBs, QP 20..40, deblocking on.
 
-One step = reconstructing the whole 120-frame sequence (every picture
-through rc_h264_submit: inter/residual kernel + intra/deblocking wavefront).
+--workload hevc_1080p_8 | hevc_1080p_10 | hevc_2160p_8 | hevc_2160p_10:
+Plain HEVC Main / Main10, 60 frames from seeded per-CTB syntax records:
+CTB 64, random quadtree (CU 8..64, TU 4..32), frame 0 all intra, then 25%
+intra / 75% inter with 4 references, motion within +-256 px, 75% zero TUs
+with Laplacian(b=3) levels, QP 22..37, deblocking and SAO on.
+
+One step = reconstructing the whole sequence (every picture through the C
+ABI submit call of its codec).
 
   value   frames/s with the syntax records resident in HBM (RC_MEM_DEVICE)
   e2e     frames/s through the same C ABI from pinned host records
           (host->device copies inside the timed region) with every output
-          frame copied back to pinned host memory (cropped 1920x1080)
+          frame copied back to pinned host memory (cropped)
 
 --impl reference times the oracle (the CPU restatement of the reference's
 reconstruction) on the host's cores instead.
@@ -36,8 +42,6 @@ import time
 import numpy as np
 
 REPO = pathlib.Path(__file__).resolve().parent
-MB_W, MB_H = 120, 68
-CROP = (0, 0, 1920, 1080)
 SEED = 20261203
 
 
@@ -62,42 +66,158 @@ def oracle():
     return _load("pyoracle", REPO / "oracle" / "pyoracle.py")
 
 
-def make_sequence(E, frames, seed):
-    pics = []
-    for n in range(frames):
-        refs = [(0, (n - k) % 4, n - k) for k in (1, 2) if n - k >= 0]
-        pics.append(E.SynthH264(seed=seed + n, mb_w=MB_W, mb_h=MB_H, intra_only=int(n == 0), refs=refs,
-                                frame_id=n))
-    return pics
+# ---------------------------------------------------------------------------
+# Workloads
+# ---------------------------------------------------------------------------
+class H264Workload:
+    name = "h264_1080p"
+    metric = "1080p H.264 recon frames/s"
+    W, H, bd, frames = 1920, 1080, 8, 120
+    MB_W, MB_H = 120, 68
+    slots = 4
+    crop = (0, 0, 1920, 1080)
+    description = ("h264_1080p_plain: 1920x1080 High 8-bit 4:2:0, 120 frames, I then P with 2 refs, 30% intra, "
+                   "20% explicit WP, 80% zero blocks, QP 20-40, deblocking on")
+    kernels = {0: ("h264_mb_kernel", "mb"), 1: ("h264_band_kernel", "band")}
+    buffer_keys = ("mbs", "slices", "weights", "levels")
+
+    def __init__(self, E, frames=None):
+        self.E = E
+        if frames:
+            self.frames = frames
+
+    def codec(self):
+        return self.E.RC_CODEC_H264
+
+    def sequence(self, seed, frames=None):
+        E, pics = self.E, []
+        for n in range(frames or self.frames):
+            refs = [(0, (n - k) % self.slots, n - k) for k in (1, 2) if n - k >= 0]
+            pics.append(E.SynthH264(seed=seed + n, mb_w=self.MB_W, mb_h=self.MB_H, intra_only=int(n == 0),
+                                    refs=refs, frame_id=n))
+        return pics
+
+    def picture_struct(self):
+        return self.E.H264Picture()
+
+    def copy_header(self, dst, p):
+        for f in ("constrained_intra_pred", "frame_id", "num_slices", "num_weights", "num_levels"):
+            setattr(dst, f, getattr(p.pic, f))
+
+    def submit(self, st, ptr, slot):
+        st.submit_h264(ptr, slot)
+
+    def stats(self, p):
+        """Algorithmic bytes of one picture per kernel and for the whole job."""
+        E = self.E
+        recs = p.mbs().reshape(-1, 176)
+        kind = recs[:, E.H264Mb.kind.offset]
+        off = recs[:, E.H264Mb.coef_off.offset:E.H264Mb.coef_off.offset + 4].copy().view(np.uint32)[:, 0]
+        off = off.astype(np.int64)
+        nxt = np.append(off[1:], p.pic.num_levels)
+        lv_bytes = (nxt - off) * 2
+        ref = recs[:, E.H264Mb.ref_idx.offset:E.H264Mb.ref_idx.offset + 8].view(np.int8).reshape(-1, 2, 4)
+        inter = kind == E.RC_H264_INTER
+        lists_b8 = (ref >= 0).sum(axis=1)
+        ref_bytes = int((lists_b8[inter] * 96).sum())  # 64 luma + 2 x 16 chroma samples per 8x8 and list
+        intra = np.isin(kind, [1, 2, 3])
+        mbk = inter | (kind == E.RC_H264_IPCM)
+        out_frame = self.MB_W * 16 * self.MB_H * 16 * 3 // 2
+        n = len(kind)
+        edges = 256  # loop-filter edge words per MB
+        # h264_mb_kernel: every record (176 B) and its left/top neighbours' (L2), its
+        # levels, the edge words out; inter/PCM samples out with their reference
+        # samples in; intra MBs' residuals (768 B) and parameters (32 B) out
+        mb = int(n * (176 + edges) + lv_bytes.sum() + mbk.sum() * 384 + ref_bytes + intra.sum() * (768 + 32))
+        # h264_band_kernel: intra MBs' parameters and residuals in; the picture
+        # read and written once by the loop filter with the edge words in
+        band = int(intra.sum() * (32 + 768) + 2 * out_frame + n * edges)
+        return {"mb": mb, "band": band, "job": out_frame + ref_bytes + p.nbytes, "syntax": p.nbytes}
+
+    def oracle_dpb(self, O):
+        return O.H264Dpb(self.MB_W, self.MB_H, self.slots)
 
 
-def picture_stats(E, p):
-    """Algorithmic bytes of one picture, per kernel and for the whole job."""
-    recs = p.mbs().reshape(-1, 176)
-    kind = recs[:, E.H264Mb.kind.offset]
-    off = recs[:, E.H264Mb.coef_off.offset:E.H264Mb.coef_off.offset + 4].copy().view(np.uint32)[:, 0].astype(np.int64)
-    nxt = np.append(off[1:], p.pic.num_levels)
-    lv_bytes = (nxt - off) * 2
-    ref = recs[:, E.H264Mb.ref_idx.offset:E.H264Mb.ref_idx.offset + 8].view(np.int8).reshape(-1, 2, 4)
-    inter = kind == E.RC_H264_INTER
-    lists_b8 = (ref >= 0).sum(axis=1)  # lists used per 8x8
-    ref_bytes = int((lists_b8[inter] * 96).sum())  # 64 luma + 2*16 chroma samples per 8x8 per list
-    wave_intra = np.isin(kind, [1, 2, 3])
-    mbk = inter | (kind == E.RC_H264_IPCM)
-    out_frame = MB_W * 16 * MB_H * 16 * 3 // 2
-    syn = p.nbytes
-    n = len(kind)
-    # h264_mb_kernel: every record and its levels once, loop-filter parameters
-    # for all MBs (48 B), inter/PCM samples out with their references, and the
-    # intra MBs' residuals (768 B) and parameters (32 B) out
-    mb_kernel = int(n * (176 + 48) + lv_bytes.sum() + mbk.sum() * 384 + ref_bytes + wave_intra.sum() * (768 + 32))
-    # h264_wave_kernel: intra MBs' parameters (32 B) and residuals (768 B) in,
-    # then the whole picture read and written once by the loop filter + its
-    # per-MB parameters (48 B)
-    wave_kernel = int(wave_intra.sum() * (32 + 768) + 2 * out_frame + n * 48)
-    return {"mb": mb_kernel, "wave": wave_kernel, "job": out_frame + ref_bytes + syn, "syntax": syn}
+class HevcWorkload:
+    frames = 60
+    slots = 5
+    kernels = {3: ("hevc_residual_kernel", "residual"), 4: ("hevc_inter_kernel", "inter"),
+               5: ("hevc_intra_kernel", "intra"), 6: ("hevc_deblock_kernel", "deblock"),
+               7: ("hevc_sao_kernel", "sao")}
+    buffer_keys = ("ctbs", "blk", "mvf", "tus", "slices", "levels", "scaling")
+
+    def __init__(self, E, W, H, bd, frames=None):
+        self.E, self.W, self.H, self.bd = E, W, H, bd
+        if frames:
+            self.frames = frames
+        tag = "1080p" if H == 1080 else "2160p"
+        self.name = f"hevc_{tag}_{bd}"
+        self.metric = f"{tag} HEVC recon frames/s"
+        self.crop = (0, 0, W, H)
+        self.description = (f"hevc_{tag}_{'main10' if bd == 10 else 'main'}: {W}x{H} {bd}-bit 4:2:0, "
+                            f"{self.frames} frames, I then P/B with 4 refs, CTB 64, 25% intra, 75% zero TUs, "
+                            "QP 22-37, deblocking + SAO on")
+
+    def codec(self):
+        return self.E.RC_CODEC_HEVC
+
+    def sequence(self, seed, frames=None):
+        E, pics = self.E, []
+        for n in range(frames or self.frames):
+            refs = [(0, (n - k) % self.slots, n - k) for k in (1, 2, 3, 4) if n - k >= 0]
+            pics.append(E.SynthHevc(seed=seed + n, width=self.W, height=self.H, bit_depth=self.bd,
+                                    intra_only=int(n == 0), refs=refs, frame_id=n))
+        return pics
+
+    def picture_struct(self):
+        return self.E.HevcPicture()
+
+    def copy_header(self, dst, p):
+        for f in ("log2_ctb", "constrained_intra_pred", "strong_intra_smoothing", "loop_filter_across_tiles",
+                  "cb_qp_offset", "cr_qp_offset", "num_slices", "num_tus", "frame_id", "num_levels"):
+            setattr(dst, f, getattr(p.pic, f))
+
+    def submit(self, st, ptr, slot):
+        st.submit_hevc(ptr, slot)
+
+    def stats(self, p):
+        """Coarse algorithmic bytes per kernel (whole planes) and for the job."""
+        b = p.buffers()
+        bps = 2 if self.bd > 8 else 1
+        samples = self.W * self.H * 3 // 2
+        plane = samples * bps
+        res = samples * 2
+        mvf = np.frombuffer(b["mvf"], np.uint8).reshape(-1, 12)
+        ref_idx = mvf[:, 8:10].view(np.int8)
+        lists = (ref_idx >= 0).sum(axis=1)
+        inter_frac = float((lists > 0).mean()) if len(lists) else 0.0
+        ref_bytes = int(lists.sum()) * 24 * bps  # 16 luma + 2 x 4 chroma samples per 4x4 and list
+        syn = p.nbytes
+        return {
+            "residual": len(b["tus"]) + len(b["levels"]) + res,
+            "inter": ref_bytes + int(inter_frac * (res + plane)),
+            "intra": int((1 - inter_frac) * (res + plane)),
+            "deblock": 2 * plane + len(b["blk"]),
+            "sao": 2 * plane + len(b["ctbs"]),
+            "job": plane + ref_bytes + syn,
+            "syntax": syn,
+        }
+
+    def oracle_dpb(self, O):
+        return O.HevcDpb(self.W, self.H, self.bd, self.slots)
 
 
+def workload(E, name, frames=None):
+    if name == "h264_1080p":
+        return H264Workload(E, frames)
+    table = {"hevc_1080p_8": (1920, 1080, 8), "hevc_1080p_10": (1920, 1080, 10),
+             "hevc_2160p_8": (3840, 2160, 8), "hevc_2160p_10": (3840, 2160, 10)}
+    if name not in table:
+        raise SystemExit(f"unknown workload {name}")
+    return HevcWorkload(E, *table[name], frames=frames)
+
+
+# ---------------------------------------------------------------------------
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons during the timed region."""
 
@@ -158,21 +278,21 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(E, O, pics, budget_s=10.0):
+def cpu_baseline(wl, O, pics, budget_s=10.0):
     """Oracle (CPU restatement) on one host thread over the first frames of
     the same sequence, bounded to about budget_s seconds."""
-    dpb = O.H264Dpb(MB_W, MB_H, 4)
+    dpb = wl.oracle_dpb(O)
     t0 = time.perf_counter()
     n = 0
     for i, p in enumerate(pics):
-        if dpb.recon(p.ptr, i % 4) != 0:
+        if dpb.recon(p.ptr, i % wl.slots) != 0:
             raise RuntimeError("oracle rejected a picture")
         n += 1
         if time.perf_counter() - t0 > budget_s:
             break
     dt = time.perf_counter() - t0
     return {"value": n / dt, "unit": "frames/s", "cores": 1, "kind": "port",
-            "sample": f"first {n} of the 120 frames of the same sequence, one host thread"}
+            "sample": f"first {n} of the {len(pics)} frames of the same sequence, one host thread"}
 
 
 def peaks():
@@ -183,11 +303,11 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def traffic_for(kernel: str):
+def traffic_for(kernel: str, workload_name: str):
     f = REPO / "profiles" / "traffic.json"
     if f.exists():
         d = json.loads(f.read_text())
-        v = d.get(kernel)
+        v = d.get(workload_name, {}).get(kernel)
         if isinstance(v, dict):
             return v.get("bytes_per_launch")
     return None
@@ -197,15 +317,16 @@ def run_reference(args, rank):
     if rank != 0:
         return
     E, O = engine(), oracle()
+    wl = workload(E, args.workload)
     frames = args.ref_frames
-    pics = make_sequence(E, frames, SEED)
+    pics = wl.sequence(SEED, frames)
     threads = os.cpu_count() or 1
 
     def one_step():
         def work():
-            dpb = O.H264Dpb(MB_W, MB_H, 4)
+            dpb = wl.oracle_dpb(O)
             for i, p in enumerate(pics):
-                dpb.recon(p.ptr, i % 4)
+                dpb.recon(p.ptr, i % wl.slots)
         ts = [threading.Thread(target=work) for _ in range(threads)]
         for t in ts:
             t.start()
@@ -221,13 +342,13 @@ def run_reference(args, rank):
     value = threads * frames * args.steps / dt
     sample = (f"{threads} host threads, each reconstructing frames 0..{frames - 1} of the sequence "
               f"(independent replicas) per step")
-    line = {"metric": "1080p H.264 recon frames/s", "value": value, "unit": "frames/s", "n_gpus": args.gpus,
+    line = {"metric": wl.metric, "value": value, "unit": "frames/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1000,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
-            "data": "synthetic (seeded per-MB syntax records)", "impl": "reference",
-            "config": {"workload": "h264_1080p_plain: 1920x1080 High 8-bit 4:2:0, P with 2 refs, sample of "
-                                   f"{frames} frames per replica", "frames_per_step": threads * frames,
-                       "parallelism": f"{threads} CPU threads"},
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "u8" if wl.bd == 8 else "u16",
+            "data": "synthetic (seeded syntax records)", "impl": "reference",
+            "config": {"workload": wl.description + f"; sample of {frames} frames per replica",
+                       "frames_per_step": threads * frames, "parallelism": f"{threads} CPU threads"},
             "cpu_baseline": {"value": value, "unit": "frames/s", "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -238,7 +359,9 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--frames", type=int, default=120)
+    ap.add_argument("--frames", type=int, default=0, help="pictures per step (default: the workload's)")
+    ap.add_argument("--workload", default="h264_1080p",
+                    choices=["h264_1080p", "hevc_1080p_8", "hevc_1080p_10", "hevc_2160p_8", "hevc_2160p_10"])
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--ref-frames", type=int, default=6)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -262,9 +385,11 @@ def main():
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
 
-    frames = args.frames
-    pics = make_sequence(E, frames, SEED + 7919 * rank)
-    stats = [picture_stats(E, p) for p in pics]
+    wl = workload(E, args.workload, args.frames or None)
+    frames = wl.frames
+    pics = wl.sequence(SEED + 7919 * rank)
+    stats = [wl.stats(p) for p in pics]
+    bps = 2 if wl.bd > 8 else 1
 
     # device-resident and pinned-host copies of every picture's records
     keep = []
@@ -272,35 +397,34 @@ def main():
     h2d_bytes = 0
     for p in pics:
         b = p.buffers()
-        dp = E.H264Picture()
-        hp = E.H264Picture()
+        dp, hp = wl.picture_struct(), wl.picture_struct()
         for obj, mem in ((dp, E.RC_MEM_DEVICE), (hp, E.RC_MEM_HOST)):
             obj.mem = mem
-            obj.constrained_intra_pred = p.pic.constrained_intra_pred
-            obj.frame_id = p.pic.frame_id
-            obj.num_slices = p.pic.num_slices
-            obj.num_weights = p.pic.num_weights
-            obj.num_levels = p.pic.num_levels
-        for key in ("mbs", "slices", "weights", "levels"):
-            raw = b[key]
+            wl.copy_header(obj, p)
+        for key in wl.buffer_keys:
+            raw = b.get(key)
             if not raw:
                 continue
             h = torch.frombuffer(bytearray(raw), dtype=torch.uint8).pin_memory()
-            d = h.to(dev)
-            keep += [h, d]
+            keep.append(h)
             setattr(hp, key, h.data_ptr())
-            setattr(dp, key, d.data_ptr())
             h2d_bytes += len(raw)
+            if key == "scaling":  # the scaling factors stay in host memory (rc_hevc_picture)
+                setattr(dp, key, h.data_ptr())
+                continue
+            d = h.to(dev)
+            keep.append(d)
+            setattr(dp, key, d.data_ptr())
         dev_pics.append(dp)
         host_pics.append(hp)
     torch.cuda.synchronize()
 
-    st = E.ReconStream(E.RC_CODEC_H264, 1920, 1080, 8, 4)
+    st = E.ReconStream(wl.codec(), wl.W, wl.H, wl.bd, wl.slots)
     cs = torch.cuda.ExternalStream(st.cuda_stream(), device=dev)
 
     def step(src):
         for n, pic in enumerate(src):
-            st.submit_h264(ctypes.addressof(pic), n % 4)
+            wl.submit(st, ctypes.addressof(pic), n % wl.slots)
 
     # ---- value: records resident in HBM
     for _ in range(args.warmup):
@@ -336,16 +460,18 @@ def main():
     value = frames * args.steps * world / (t_ms / 1000.0)
 
     # ---- e2e: pinned host records in, cropped frames out, through the C ABI
+    cw, chh = wl.W, wl.H
     ring = []
     for _ in range(8):
-        ring.append(tuple(torch.empty(n, dtype=torch.uint8).pin_memory() for n in (1920 * 1080, 960 * 540, 960 * 540)))
-    d2h_bytes = frames * (1920 * 1080 + 2 * 960 * 540)
+        ring.append(tuple(torch.empty(n * bps, dtype=torch.uint8).pin_memory()
+                          for n in (cw * chh, cw * chh // 4, cw * chh // 4)))
+    d2h_bytes = frames * (cw * chh * 3 // 2) * bps
 
     def e2e_step():
         for n, pic in enumerate(host_pics):
-            st.submit_h264(ctypes.addressof(pic), n % 4)
+            wl.submit(st, ctypes.addressof(pic), n % wl.slots)
             y, u, v = ring[n % 8]
-            st.download_async(n % 4, CROP, y.data_ptr(), u.data_ptr(), v.data_ptr())
+            st.download_async(n % wl.slots, wl.crop, y.data_ptr(), u.data_ptr(), v.data_ptr())
 
     for _ in range(args.warmup):
         e2e_step()
@@ -366,10 +492,11 @@ def main():
     e2e = frames * args.steps * world / e2e_s
 
     # ---- roofline of the dominant kernel
-    names = {0: ("h264_mb_kernel", "mb"), 1: ("h264_wave_kernel", "wave")}
     per_kernel = {}
     for k, (ms, n) in prof.items():
-        name, key = names[k]
+        if k not in wl.kernels or n == 0:
+            continue
+        name, key = wl.kernels[k]
         alg = statistics.mean(s[key] for s in stats)
         per_kernel[name] = {"launches": n, "ms_total": ms, "us_per_launch": ms / n * 1000,
                             "alg_bytes_per_launch": alg, "achieved_gbs": alg / (ms / n / 1000) / 1e9}
@@ -378,17 +505,16 @@ def main():
     ach = per_kernel[dom]["achieved_gbs"]
     job_bytes = statistics.mean(s["job"] for s in stats)
     result = {
-        "metric": "1080p H.264 recon frames/s", "value": value, "unit": "frames/s", "n_gpus": world,
+        "metric": wl.metric, "value": value, "unit": "frames/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "u8",
-        "data": "synthetic (seeded per-MB syntax records; no public clip available)",
-        "config": {"workload": "h264_1080p_plain: 1920x1080 High 8-bit 4:2:0, 120 frames, I then P with 2 refs, "
-                               "30% intra, 20% explicit WP, 80% zero blocks, QP 20-40, deblocking on",
-                   "frames_per_step": frames, "parallelism": "replicas" if world > 1 else "single stream",
+        "scaling": "weak", "vs_baseline": None, "dtype": "u8" if wl.bd == 8 else "u16",
+        "data": "synthetic (seeded syntax records; no public clip available)",
+        "config": {"workload": wl.description, "frames_per_step": frames,
+                   "parallelism": "replicas" if world > 1 else "single stream",
                    "l2": f"inputs larger than L2 (syntax {sum(s['syntax'] for s in stats) / 1e6:.0f} MB per step)",
-                   "luma_msamples_per_s": value * 1920 * 1080 / 1e6},
+                   "luma_msamples_per_s": value * wl.W * wl.H / 1e6},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peak, "unit": "GB/s",
-                     "frac": ach / peak, "peak_source": peak_kind, "traffic": traffic_for(dom)},
+                     "frac": ach / peak, "peak_source": peak_kind, "traffic": traffic_for(dom, wl.name)},
         "roofline_job": {"alg_bytes_per_frame": job_bytes, "achieved": job_bytes * value / world / 1e9,
                          "peak": peak, "unit": "GB/s", "frac": job_bytes * value / world / 1e9 / peak},
         "kernels": per_kernel,
@@ -397,7 +523,7 @@ def main():
         "clocks": clk,
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        result["cpu_baseline"] = cpu_baseline(E, oracle(), pics)
+        result["cpu_baseline"] = cpu_baseline(wl, oracle(), pics)
     if rank == 0:
         print(json.dumps(result), flush=True)
     st.close()

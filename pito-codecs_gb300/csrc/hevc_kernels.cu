@@ -58,8 +58,8 @@ __device__ __forceinline__ uint32_t ld_acquire(const uint32_t *p) {
     asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
     return v;
 }
-__device__ __forceinline__ void st_release(uint32_t *p, uint32_t v) {
-    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+__device__ __forceinline__ void st_relaxed(uint32_t *p, uint32_t v) {
+    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 __device__ __forceinline__ bool aborted(const uint32_t *err) {
     return (*(const volatile uint32_t *)err & RC_DEV_ERR_TIMEOUT) != 0;
@@ -69,7 +69,7 @@ __device__ bool wait_flag(const uint32_t *f, uint32_t epoch, uint32_t limit, con
     while (ld_acquire(f) != epoch) {
         if (++it > limit) return false;
         if ((it & 63) == 0 && aborted(err)) return false;
-        if (it > 256) __nanosleep(64);
+        if (it > 16) __nanosleep(32);
     }
     return true;
 }
@@ -91,6 +91,13 @@ __device__ __forceinline__ int ctb_of(const HevcLaunch &P, int x, int y) {
     return (y >> P.log2ctb) * P.wctb + (x >> P.log2ctb);
 }
 __device__ __forceinline__ uint32_t slice_addr(const HevcLaunch &P, int ctb) { return slice_of_ctb(P, ctb)->slice_addr; }
+// CTB of a transform block (records outside the picture map to CTB 0; the
+// kernels that use the block reject it)
+__device__ __forceinline__ int tu_ctb(const HevcLaunch &P, const rc_hevc_tu &t) {
+    const int sc = t.c ? 2 : 1, x = t.x0 * sc, y = t.y0 * sc;
+    if (x < 0 || y < 0 || x >= P.W || y >= P.H) return 0;
+    return (y >> P.log2ctb) * P.wctb + (x >> P.log2ctb);
+}
 
 // ===========================================================================
 // Residuals: reconstruct, src/hevc/slicedec.rs:2004-2049 with dequant /
@@ -105,6 +112,11 @@ __global__ void __launch_bounds__(128) hevc_residual_kernel(HevcLaunch P) {
     int32_t *co = buf[w][0], *col = buf[w][1];
     for (int ti = blockIdx.x * 4 + w; ti < P.num_tus; ti += gridDim.x * 4) {
         const rc_hevc_tu t = P.tus[ti];
+        if (lane == 0) {  // the range of transform blocks of each CTB (contiguous in decode order)
+            const int c = tu_ctb(P, t);
+            if (ti == 0 || tu_ctb(P, P.tus[ti - 1]) != c) P.ctb_first[c] = ti;
+            if (ti == P.num_tus - 1 || tu_ctb(P, P.tus[ti + 1]) != c) P.ctb_end[c] = ti + 1;
+        }
         if (!(t.flags & RC_HEVC_TU_CBF) || (t.flags & RC_HEVC_TU_PCM)) continue;
         const int log2 = t.log2, n = 1 << log2, c = t.c, mx = t.max_x, my = t.max_y;
         const unsigned long long cnt = (unsigned long long)(mx + 1) * (my + 1);
@@ -291,6 +303,53 @@ __global__ void __launch_bounds__(64) hevc_inter_kernel(HevcLaunch P) {
 }
 
 // ===========================================================================
+// Intra task order.  Decode order would keep the persistent intra warps on
+// two or three CTBs at a time (an all-intra picture then runs CTB after
+// CTB); CTBs on one anti-diagonal cx + 2 cy depend on none of each other,
+// and every neighbour an intra block reads lies on an earlier anti-diagonal
+// or earlier in the same CTB, so this order keeps each wait on a block taken
+// before it.
+// ===========================================================================
+__global__ void __launch_bounds__(1024) hevc_order_scan_kernel(HevcLaunch P) {
+    __shared__ uint32_t keysum[2048];
+    const int nctb = P.wctb * P.hctb, nkeys = P.wctb + 2 * P.hctb;
+    for (int k = threadIdx.x; k < nkeys; k += blockDim.x) keysum[k] = 0;
+    __syncthreads();
+    for (int c = threadIdx.x; c < nctb; c += blockDim.x) {
+        const uint32_t n = P.ctb_end[c] - P.ctb_first[c];
+        if (n) atomicAdd(&keysum[c % P.wctb + 2 * (c / P.wctb)], n);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {  // exclusive prefix over anti-diagonals
+        uint32_t acc = 0;
+        for (int k = 0; k < nkeys; k++) {
+            const uint32_t v = keysum[k];
+            keysum[k] = acc;
+            acc += v;
+        }
+    }
+    __syncthreads();
+    for (int c = threadIdx.x; c < nctb; c += blockDim.x) {
+        const int cx = c % P.wctb, cy = c / P.wctb, key = cx + 2 * cy;
+        uint32_t base = keysum[key];
+        for (int y = 0; y < cy; y++) {  // CTBs of the same anti-diagonal above this one
+            const int x = key - 2 * y;
+            if (x >= 0 && x < P.wctb) base += P.ctb_end[y * P.wctb + x] - P.ctb_first[y * P.wctb + x];
+        }
+        P.ctb_base[c] = base;
+    }
+}
+
+__global__ void __launch_bounds__(256) hevc_order_fill_kernel(HevcLaunch P) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.num_tus) return;
+    const int c = tu_ctb(P, P.tus[i]);
+    const uint32_t f = P.ctb_first[c], e = P.ctb_end[c];
+    if ((uint32_t)i >= f && (uint32_t)i < e) P.order[P.ctb_base[c] + (i - f)] = i;
+    else atomicOr(P.error, RC_DEV_ERR_RECORD);  // a CTB's blocks are not contiguous in decode order
+}
+
+// ===========================================================================
 // Intra prediction in decode order (src/hevc/intra.rs, intra_predict of
 // src/hevc/slicedec.rs:1673-1738)
 // ===========================================================================
@@ -360,27 +419,40 @@ __device__ void intra_tu(const HevcLaunch &P, IntraSmem &S, const rc_hevc_tu &t,
         }
     }
     __syncwarp();
-    // ---- substitute, src/hevc/intra.rs:19-65 (sequential scan)
-    if (lane == 0) {
-        bool any = false;
-        for (int i = 0; i <= n2; i++) any |= S.al[i];
-        for (int i = 1; i <= n2; i++) any |= S.at[i];
-        if (!any) {
-            for (int i = 0; i <= n2; i++) S.left[i] = S.top[i] = (uint16_t)(1 << (bd - 1));
-        } else {
-            if (!S.al[n2]) {
-                int found = -1;
-                for (int y = n2 - 1; y >= 0 && found < 0; y--)
-                    if (S.al[y]) found = S.left[y];
-                for (int x = 1; x <= n2 && found < 0; x++)
-                    if (S.at[x]) found = S.top[x];
-                S.left[n2] = (uint16_t)(found < 0 ? 0 : found);
+    // ---- substitute, src/hevc/intra.rs:19-65.  In scan order (up the left
+    // column from the bottom, the corner, then along the top) an unavailable
+    // sample takes its predecessor's value and a leading run the first
+    // available sample's; availability is uniform per unit, so a ballot over
+    // the units (scan index k: 0..NL-1 left units bottom-up, NL the corner,
+    // NL+1.. top units) finds every sample's source at once.
+    {
+        const int NL = n2 / unit, nk = 2 * NL + 1;
+        auto unit_avail = [&](int k) -> bool {
+            return k < NL ? S.al[1 + (NL - 1 - k) * unit] : k == NL ? S.al[0] : S.at[1 + (k - NL - 1) * unit];
+        };
+        // the unit's first / last sample in scan order
+        auto unit_val = [&](int k, bool last) -> int {
+            if (k < NL) return S.left[last ? 1 + (NL - 1 - k) * unit : n2 - k * unit];
+            if (k == NL) return S.left[0];
+            return S.top[last ? (k - NL) * unit : 1 + (k - NL - 1) * unit];
+        };
+        const uint32_t m0 = __ballot_sync(0xffffffffu, lane < nk && unit_avail(lane));
+        const uint32_t m1 = __ballot_sync(0xffffffffu, lane + 32 < nk && unit_avail(lane + 32));
+        const unsigned long long mask = (unsigned long long)m1 << 32 | m0;
+        const int first = __ffsll((long long)mask) - 1;
+        for (int i = lane; i <= 2 * n2; i += 32) {
+            // sample i: 0 corner, 1..n2 left[i], n2+1..2 n2 top[i - n2]
+            const int k = i == 0 ? NL : i <= n2 ? NL - 1 - (i - 1) / unit : NL + 1 + (i - n2 - 1) / unit;
+            if (mask >> k & 1) continue;
+            int v;
+            if (!mask) v = 1 << (bd - 1);
+            else {
+                const unsigned long long below = mask & ((1ull << k) - 1);
+                v = below ? unit_val(63 - __clzll((long long)below), true) : unit_val(first, false);
             }
-            for (int y = n2 - 1; y >= 0; y--)
-                if (!S.al[y]) S.left[y] = S.left[y + 1];
-            S.top[0] = S.left[0];
-            for (int x = 1; x <= n2; x++)
-                if (!S.at[x]) S.top[x] = S.top[x - 1];
+            if (i == 0) S.left[0] = S.top[0] = (uint16_t)v;
+            else if (i <= n2) S.left[i] = (uint16_t)v;
+            else S.top[i - n2] = (uint16_t)v;
         }
     }
     __syncwarp();
@@ -497,12 +569,20 @@ __global__ void __launch_bounds__(128) hevc_intra_kernel(HevcLaunch P) {
     __shared__ IntraSmem sm[4];
     IntraSmem &S = sm[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31;
+    // transform blocks in the intra task order, one per counter step (each
+    // waits only for blocks earlier in that order, all of which are already
+    // taken by running warps; luma and chroma chains proceed side by side)
     for (;;) {
         unsigned ti = 0;
         if (lane == 0) ti = aborted(P.error) ? 0xffffffffu : atomicAdd(P.counter, 1u);
         ti = __shfl_sync(0xffffffffu, ti, 0);
         if (ti >= (unsigned)P.num_tus) return;
-        const rc_hevc_tu t = P.tus[ti];
+        const uint32_t oi = P.order[ti];
+        if (oi >= (uint32_t)P.num_tus) {
+            if (lane == 0) atomicOr(P.error, RC_DEV_ERR_RECORD);
+            continue;
+        }
+        const rc_hevc_tu t = P.tus[oi];
         if (!(t.flags & RC_HEVC_TU_INTRA)) continue;
         const int n = 1 << t.log2, sc = t.c ? 2 : 1;
         if (t.log2 < 2 || t.log2 > 5 || t.c > 2 || t.mode > 34 || (t.x0 + n) * sc > P.W || (t.y0 + n) * sc > P.H) {
@@ -512,12 +592,14 @@ __global__ void __launch_bounds__(128) hevc_intra_kernel(HevcLaunch P) {
         if (t.flags & RC_HEVC_TU_PCM) pcm_tu<T>(P, t, lane);
         else intra_tu<T>(P, S, t, lane);
         if (aborted(P.error)) return;
-        __threadfence();
+        // publish the 4x4 luma-grid blocks this TU covers: the warp's sample
+        // stores, then one fence per lane, then relaxed flag stores (a
+        // release pattern; readers acquire the flags)
         __syncwarp();
-        // publish the 4x4 luma-grid blocks this TU covers
+        __threadfence();
         const int bw = (n * sc) >> 2, bx0 = (t.x0 * sc) >> 2, by0 = (t.y0 * sc) >> 2;
         uint32_t *rdy = P.ready + (size_t)t.c * P.w4 * P.h4;
-        for (int i = lane; i < bw * bw; i += 32) st_release(rdy + (size_t)(by0 + i / bw) * P.w4 + bx0 + i % bw, P.epoch);
+        for (int i = lane; i < bw * bw; i += 32) st_relaxed(rdy + (size_t)(by0 + i / bw) * P.w4 + bx0 + i % bw, P.epoch);
     }
 }
 
@@ -757,6 +839,8 @@ void launch_all_deblock(const HevcLaunch &p, cudaStream_t st) {
 
 void rc_launch_hevc_residual(const HevcLaunch &p, cudaStream_t st) {
     cudaMemsetAsync(p.res, 0, ((size_t)p.W * p.H + 2 * (size_t)p.CW * p.CH) * sizeof(int16_t), st);
+    // CTBs without transform blocks keep first = end = 0
+    cudaMemsetAsync(p.ctb_first, 0, 2 * (size_t)p.wctb * p.hctb * sizeof(uint32_t), st);
     int blocks = (p.num_tus + 3) / 4;
     blocks = blocks < 1 ? 1 : blocks > 4096 ? 4096 : blocks;
     hevc_residual_kernel<<<blocks, 128, 0, st>>>(p);
@@ -769,6 +853,8 @@ void rc_launch_hevc_inter(const HevcLaunch &p, cudaStream_t st) {
 }
 
 void rc_launch_hevc_intra(const HevcLaunch &p, cudaStream_t st, int blocks) {
+    hevc_order_scan_kernel<<<1, 1024, 0, st>>>(p);
+    if (p.num_tus > 0) hevc_order_fill_kernel<<<(p.num_tus + 255) / 256, 256, 0, st>>>(p);
     cudaMemsetAsync(p.counter, 0, sizeof(uint32_t), st);
     if (p.bd > 8) hevc_intra_kernel<uint16_t><<<blocks, 128, 0, st>>>(p);
     else hevc_intra_kernel<uint8_t><<<blocks, 128, 0, st>>>(p);

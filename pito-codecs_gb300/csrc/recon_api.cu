@@ -68,6 +68,9 @@ struct rc_stream {
     uint8_t *work = nullptr;     // picture being reconstructed (pre-SAO)
     int16_t *res = nullptr;      // residual planes
     uint32_t *ready = nullptr;   // per 4x4 block and component
+    uint32_t *ctb_ord = nullptr; // ctb_first, ctb_end, ctb_base for the smallest CTB size
+    size_t nctb_max = 0;
+    DevBuf order;                // intra task order
     int w4 = 0, h4 = 0, log2ctb_alloc = 0;
     int bps = 1;
     DevBuf mbs, slices, weights, levels;
@@ -239,6 +242,8 @@ void destroy(rc_stream *s) {
     cudaFree(s->work);
     cudaFree(s->res);
     cudaFree(s->ready);
+    dev_free(s, s->ctb_ord, 3 * s->nctb_max * sizeof(uint32_t));
+    dev_free(s, s->order.p, s->order.cap);
     cudaFree(s->counter);
     cudaFree(s->error);
     cudaFree(s->ls);
@@ -412,7 +417,7 @@ int rc_stream_create(int codec, int width, int height, int bit_depth, int dpb_sl
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, dev);
-    s->wave_blocks = std::max(1, s->sms / 2);
+    s->wave_blocks = std::max(1, s->sms * 2);
     if (const char *e = getenv("PITO_RECON_WAVE_BLOCKS")) {
         int v = atoi(e);
         if (v > 0 && v <= 4096) s->wave_blocks = v;
@@ -438,6 +443,8 @@ int rc_stream_create(int codec, int width, int height, int bit_depth, int dpb_sl
         ok = ok && dev_alloc(s, (void **)&s->work, s->slot_bytes);
         ok = ok && dev_alloc(s, (void **)&s->res, nres * sizeof(int16_t));
         ok = ok && dev_alloc(s, (void **)&s->ready, 3 * (size_t)s->w4 * s->h4 * sizeof(uint32_t));
+        s->nctb_max = (size_t)((s->width + 15) / 16) * ((s->height + 15) / 16);
+        ok = ok && dev_alloc(s, (void **)&s->ctb_ord, 3 * s->nctb_max * sizeof(uint32_t));
         ok = ok && cudaMemsetAsync(s->ready, 0, 3 * (size_t)s->w4 * s->h4 * sizeof(uint32_t), s->st) == cudaSuccess;
         ok = ok && cudaMemsetAsync(s->work, 0, s->slot_bytes, s->st) == cudaSuccess;
     }
@@ -622,6 +629,12 @@ int rc_hevc_submit(rc_stream *s, const rc_hevc_picture *pic, int out_slot) {
     L.work = s->work;
     L.res = s->res;
     L.ready = s->ready;
+    if ((size_t)wctb * hctb > s->nctb_max || wctb + 2 * hctb > 2048) return RC_EINVAL;
+    if ((rc = ensure(s, s->order, sizeof(uint32_t) * std::max(1, pic->num_tus))) != 0) return rc;
+    L.ctb_first = s->ctb_ord;
+    L.ctb_end = s->ctb_ord + (size_t)wctb * hctb;
+    L.ctb_base = s->ctb_ord + 2 * s->nctb_max;
+    L.order = (uint32_t *)s->order.p;
     L.counter = s->counter;
     L.error = s->error;
     L.epoch = ++s->epoch;
@@ -631,7 +644,7 @@ int rc_hevc_submit(rc_stream *s, const rc_hevc_picture *pic, int out_slot) {
     timed(s, RC_KERNEL_HEVC_INTRA, [&] { rc_launch_hevc_intra(L, s->st, s->wave_blocks); });
     timed(s, RC_KERNEL_HEVC_DEBLOCK, [&] { rc_launch_hevc_deblock(L, s->st); });
     timed(s, RC_KERNEL_HEVC_SAO, [&] { rc_launch_hevc_sao(L, s->st); });
-    s->launches += 1;  // the deblocking step is two launches (vertical, horizontal edges)
+    s->launches += 3;  // deblocking is two launches (vertical, horizontal edges); the intra order two more
     s->submits++;
     if (cudaGetLastError() != cudaSuccess) return cuda_fail(s);
     return RC_OK;
