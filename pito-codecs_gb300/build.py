@@ -20,8 +20,7 @@ OUT = PKG / "_build"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["recon_api.cu", "h264_kernels.cu", "hevc_kernels.cu"]
 SYNTH_SOURCES = ["synth_h264.cpp", "synth_hevc.cpp"]
-HEADERS = (list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + [PKG.parent / "include" / "pito_recon.h"] +
-           [PKG.parent / "oracle" / "hevc_trans_matrix.inc"])
+HEADERS = list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + [PKG.parent / "include" / "pito_recon.h"]
 
 RECON_LIB = PKG / "libpito_recon.so"
 SYNTH_LIB = PKG / "libpito_synth.so"

@@ -30,9 +30,43 @@
 
 namespace {
 
-__constant__ int8_t cTRANS[32][32] = {
-#include "../../oracle/hevc_trans_matrix.inc"
+// The 32x32 inverse-transform matrix (TRANS_MATRIX, src/hevc/spec_tables.rs:107),
+// built at compile time from the standard's integer cosine sets: entry (k, n)
+// stands for 64 sqrt(2) cos((2n+1) k pi / 64); with k = 2^e o (o odd) the
+// angle is (2n+1) o pi / (64 >> e), folded into the first quadrant, where the
+// set of the (64 >> e)-point transform gives its value.
+struct TransMatrix {
+    int8_t m[32][32];
 };
+__host__ __device__ constexpr int trans_cos(int den, int j) {
+    // integer cos(j pi / den), j odd, 0 < j < den / 2 (per transform size)
+    constexpr int c4[1] = {64}, c8[2] = {83, 36}, c16[4] = {89, 75, 50, 18};
+    constexpr int c32[8] = {90, 87, 80, 70, 57, 43, 25, 9};
+    constexpr int c64[16] = {90, 90, 88, 85, 82, 78, 73, 67, 61, 54, 46, 38, 31, 22, 13, 4};
+    const int i = (j - 1) / 2;
+    return den == 4 ? c4[i] : den == 8 ? c8[i] : den == 16 ? c16[i] : den == 32 ? c32[i] : c64[i];
+}
+__host__ __device__ constexpr int trans_entry(int k, int n) {
+    if (k == 0) return 64;
+    int e = 0;
+    while (!((k >> e) & 1)) e++;
+    const int o = k >> e, den = 64 >> e;
+    int j = ((2 * n + 1) * o) % (2 * den), sign = 1;
+    if (j > den) j = 2 * den - j;  // cos(2 pi - a) = cos(a)
+    if (j > den / 2) {             // cos(pi - a) = -cos(a)
+        j = den - j;
+        sign = -1;
+    }
+    return sign * trans_cos(den, j);
+}
+__host__ __device__ constexpr TransMatrix make_trans_matrix() {
+    TransMatrix t{};
+    for (int k = 0; k < 32; k++)
+        for (int n = 0; n < 32; n++) t.m[k][n] = (int8_t)trans_entry(k, n);
+    return t;
+}
+__constant__ TransMatrix cTRANSM = make_trans_matrix();
+#define cTRANS (cTRANSM.m)
 __constant__ int8_t cDST[4][4] = {{29, 55, 74, 84}, {74, 74, 0, -74}, {84, -29, -74, 55}, {55, -84, 74, -29}};
 __constant__ int cLEVEL_SCALE[6] = {40, 45, 51, 57, 64, 72};
 __constant__ int8_t cANGLE[35] = {0,  0,  32, 26, 21, 17, 13, 9,  5,  2,   0,   -2,  -5,  -9,  -13, -17, -21, -26,
