@@ -1145,11 +1145,14 @@ __global__ void __launch_bounds__(128) h264_db_params_kernel(H264Launch P) {
 //   intra MB (x, y)    after intra row y-1 has reconstructed MBs 0..x+1;
 //   filter MB (x, y)   after rows y and y+1 have reconstructed MBs 0..x+2 and
 //                      0..x+1 (every intra MB that reads samples this step
-//                      changes, and MB x+2, which the step prefetches), and
-//                      after row y-1 has filtered and stored MBs 0..x+1 (MB
-//                      x+1's left edge is the last change to MB (x, y-1)).
+//                      changes, and MB x+2, which the step prefetches); its
+//                      horizontal edges, which read MB (x, y-1), also after
+//                      row y-1 has filtered MB x+1's vertical edges (the last
+//                      change to MB (x, y-1)) and stored MBs 0..x.
 // A filter row stores MB x-1 once MB x's left edge is filtered (its last
-// change in the row) and the three rows above MB x after MB x's top edge.
+// change in the row) and publishes its progress there, before MB x's
+// horizontal edges, and stores the three rows above MB x after MB x's top
+// edge.
 // ===========================================================================
 constexpr int BR = RC_H264_BAND_ROWS;
 constexpr int DRING = 8;  // ring slots between filter rows of a band
@@ -1402,18 +1405,22 @@ __device__ void band_luma_row(const H264Launch &P, BandSmem &B, int w, int my, i
         }
         cp_commit();
     };
+    // rows -4..-1 of MB x: the row above's ring, or (first row of a band) the
+    // picture; for the latter the next MB's rows are loaded one step early
+    // when the row above is already far enough
+    uint4 t4n = z4;
+    bool have_next = false;
+    auto top_rows = [&](int x) -> uint4 {
+        if (my == 0 || lane >= 4) return z4;
+        if (w > 0) return *(const uint4 *)(B.l[w - 1].ring[x % DRING] + lane * 16);
+        return __ldcg((const uint4 *)(Y + (size_t)(my * 16 - 4 + lane) * P.pitch + x * 16));
+    };
     if (!wait_ge(iown, min(2, P.mb_w), P, lane)) { band_fail(P, lane); return; }
     stage(0);
     stage(1);
     for (int x = 0; x < P.mb_w; x++) {
         if (!wait_ge(iown, min(x + 3, P.mb_w), P, lane)) { band_fail(P, lane); return; }
         if (below && !wait_ge(ibelow, min(x + 2, P.mb_w), P, lane)) { band_fail(P, lane); return; }
-        if (my > 0 && !wait_ge(dup, x + 1, P, lane)) { band_fail(P, lane); return; }
-        // rows -4..-1: the row above's ring, or the picture for the band's first row
-        uint4 t4 = z4;
-        if (my > 0 && lane < 4)
-            t4 = w > 0 ? *(const uint4 *)(B.l[w - 1].ring[x % DRING] + lane * 16)
-                       : __ldcg((const uint4 *)(Y + (size_t)(my * 16 - 4 + lane) * P.pitch + x * 16));
         stage(x + 2);
         cp_wait_all_but_1();
         const int sl = x % 3;
@@ -1445,9 +1452,25 @@ __device__ void band_luma_row(const H264Launch &P, BandSmem &B, int w, int my, i
                 if (act && r >= 12) *(uint4 *)(R.ring[(x - 1) % DRING] + (r - 12) * 16) = prev;
             }
         }
-        // ---- horizontal edges: lane r holds rows -4..15 of sample column r
         if (act) *(uint4 *)R.t[4 + r] = make_uint4(wd[1], wd[2], wd[3], wd[4]);
-        if (my > 0 && lane < 4) *(uint4 *)R.t[lane] = t4;
+        // MBs 0..x-1 are final and stored: the row below may take MB x-1's
+        // rows (its horizontal edges need nothing later of this row)
+        __syncwarp();
+        __threadfence_block();
+        if (lane == 0) *dmine = x;
+        // ---- horizontal edges: need MB (x, y-1) final, i.e. the row above past
+        // MB x+1's vertical edges
+        if (my > 0) {
+            if (!wait_ge(dup, x + 1, P, lane)) { band_fail(P, lane); return; }
+            const uint4 t4 = (w == 0 && have_next) ? t4n : top_rows(x);
+            have_next = false;
+            if (w == 0 && x + 1 < P.mb_w && __shfl_sync(0xffffffffu, *dup >= x + 2 ? 1 : 0, 0)) {
+                __threadfence_block();
+                t4n = top_rows(x + 1);
+                have_next = true;
+            }
+            if (lane < 4) *(uint4 *)R.t[lane] = t4;
+        }
         __syncwarp();
         const uint32_t eh[4] = {ph.x, ph.y, ph.z, ph.w};
         const bool top = my > 0 && __any_sync(0xffffffffu, eh[0] != 0);
@@ -1472,8 +1495,6 @@ __device__ void band_luma_row(const H264Launch &P, BandSmem &B, int w, int my, i
         if (top && lane < 3)
             *(uint4 *)(Y + (size_t)(my * 16 - 3 + lane) * P.pitch + x * 16) = *(const uint4 *)R.t[1 + lane];
         __syncwarp();
-        __threadfence_block();
-        if (lane == 0) *dmine = x;
     }
     // the row's last MB
     if (act) *(uint4 *)(Y + (size_t)(my * 16 + r) * P.pitch + (P.mb_w - 1) * 16) = prev;
@@ -1509,21 +1530,23 @@ __device__ void band_chroma_row(const H264Launch &P, BandSmem &B, int w, int my,
         }
         cp_commit();
     };
+    // rows -2..-1 of MB x per component (lanes 0..3: component lane >> 1, row
+    // lane & 1): the row above's ring, or (first row of a band) the picture,
+    // the next MB's one step early when the row above is far enough
+    uint2 t2n = z2;
+    bool have_next = false;
+    auto top_rows = [&](int x) -> uint2 {
+        if (my == 0 || lane >= 4) return z2;
+        const int cc = lane >> 1, rr = lane & 1;
+        if (w > 0) return *(const uint2 *)(B.c[w - 1].ring[x % DRING] + cc * 16 + rr * 8);
+        return __ldcg((const uint2 *)(Y + (cc ? P.v_off : P.u_off) + (size_t)(my * 8 - 2 + rr) * P.cpitch + x * 8));
+    };
     if (!wait_ge(iown, min(2, P.mb_w), P, lane)) { band_fail(P, lane); return; }
     stage(0);
     stage(1);
     for (int x = 0; x < P.mb_w; x++) {
         if (!wait_ge(iown, min(x + 3, P.mb_w), P, lane)) { band_fail(P, lane); return; }
         if (below && !wait_ge(ibelow, min(x + 2, P.mb_w), P, lane)) { band_fail(P, lane); return; }
-        if (my > 0 && !wait_ge(dup, x + 1, P, lane)) { band_fail(P, lane); return; }
-        // rows -2..-1 per component (lanes 0..3: component lane >> 1, row lane & 1)
-        uint2 t2 = z2;
-        if (my > 0 && lane < 4) {
-            const int cc = lane >> 1, rr = lane & 1;
-            t2 = w > 0 ? *(const uint2 *)(B.c[w - 1].ring[x % DRING] + cc * 16 + rr * 8)
-                       : __ldcg((const uint2 *)(Y + (cc ? P.v_off : P.u_off) + (size_t)(my * 8 - 2 + rr) * P.cpitch +
-                                                x * 8));
-        }
         stage(x + 2);
         cp_wait_all_but_1();
         const int sl = x % 3;
@@ -1550,9 +1573,24 @@ __device__ void band_chroma_row(const H264Launch &P, BandSmem &B, int w, int my,
                 if (act && r >= 6) *(uint2 *)(R.ring[(x - 1) % DRING] + c * 16 + (r - 6) * 8) = prev;
             }
         }
-        // ---- horizontal edges: lane holds rows -2..7 of its column
         if (act) *(uint2 *)R.t[c][2 + r] = make_uint2(wd[1], wd[2]);
-        if (my > 0 && lane < 4) *(uint2 *)R.t[lane >> 1][lane & 1] = t2;
+        // MBs 0..x-1 final and stored
+        __syncwarp();
+        __threadfence_block();
+        if (lane == 0) *dmine = x;
+        // ---- horizontal edges: lane holds rows -2..7 of its column; need the
+        // row above past MB x+1's vertical edges
+        if (my > 0) {
+            if (!wait_ge(dup, x + 1, P, lane)) { band_fail(P, lane); return; }
+            const uint2 t2 = (w == 0 && have_next) ? t2n : top_rows(x);
+            have_next = false;
+            if (w == 0 && x + 1 < P.mb_w && __shfl_sync(0xffffffffu, *dup >= x + 2 ? 1 : 0, 0)) {
+                __threadfence_block();
+                t2n = top_rows(x + 1);
+                have_next = true;
+            }
+            if (lane < 4) *(uint2 *)R.t[lane >> 1][lane & 1] = t2;
+        }
         __syncwarp();
         const bool top = my > 0 && __any_sync(0xffffffffu, ph.x != 0);
         if (__any_sync(0xffffffffu, (ph.x | ph.y) != 0)) {
@@ -1574,8 +1612,6 @@ __device__ void band_chroma_row(const H264Launch &P, BandSmem &B, int w, int my,
             *(uint2 *)(Y + (lane ? P.v_off : P.u_off) + (size_t)(my * 8 - 1) * P.cpitch + x * 8) =
                 *(const uint2 *)R.t[lane][1];
         __syncwarp();
-        __threadfence_block();
-        if (lane == 0) *dmine = x;
     }
     if (act) *(uint2 *)(Cp + (size_t)(my * 8 + r) * P.cpitch + (P.mb_w - 1) * 8) = prev;
     if (ring_out) {
