@@ -354,6 +354,99 @@ def run_reference(args, rank):
     print(json.dumps(line), flush=True)
 
 
+def run_multistream(args):
+    """The batched (64 mixed streams in flight together, against the plain
+    per-stream loop) and served (Poisson request traces through the request
+    loop, against the plain path serving the same trace) forms."""
+    import hashlib
+    import importlib
+    E = engine()
+    M = importlib.import_module("pito_codecs_gb300.multistream")
+    if E.lib().rc_device_select(0) != 0:
+        raise SystemExit("rc_device_select failed")
+    specs = M.mix_specs(args.streams, seed=SEED)
+    t0 = time.perf_counter()
+    tpl = {s.key: M.Templates(s) for s in specs}
+    import torch
+
+    def upload(raw):
+        d = torch.frombuffer(bytearray(raw), dtype=torch.uint8).cuda()
+        return d.data_ptr(), d
+
+    for t in tpl.values():  # records resident in HBM, as the plain line's value
+        t.to_device(upload)
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t0
+
+    def digest(st):
+        h = hashlib.sha256()
+        for slot in range(st.slots):
+            for plane in st.download(slot):
+                h.update(plane.tobytes())
+        return h.hexdigest()
+
+    def luma_samples(s, frames):
+        return s.width * s.height * frames
+
+    base = {"n_gpus": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8/u16",
+            "data": "synthetic (seeded syntax records; template pictures replayed per stream)"}
+    mix = (f"{args.streams} streams: resolutions uniform over 426x240..3840x2160, half H.264 8-bit, half HEVC "
+           "8/10-bit, 30-240 frames each")
+    if args.workload == "batched":
+        # warm-up: one frame per stream on separate streams
+        warm = {s.key: M.open_stream(s) for s in specs}
+        for s in specs:
+            M.submit(warm[s.key], s, *tpl[s.key].picture(0))
+        for st in warm.values():
+            st.sync()
+            st.close()
+        alone = {s.key: M.open_stream(s) for s in specs}
+        t_plain = M.run_plain(specs, tpl, alone)
+        mixed = {s.key: M.open_stream(s) for s in specs}
+        t_batch = M.run_batched(specs, tpl, mixed, depth=args.depth)
+        frames = sum(s.frames for s in specs)
+        check = specs[: args.parity_streams]
+        same = all(digest(alone[s.key]) == digest(mixed[s.key]) for s in check)
+        launches = sum(st.launches() for st in mixed.values())
+        for st in list(alone.values()) + list(mixed.values()):
+            st.close()
+        line = dict(base, metric="C4 batched recon frames/s", value=frames / t_batch, unit="frames/s",
+                    steps=1, warmup=1, ms_per_step=t_batch * 1000,
+                    config={"workload": "batched_c4: " + mix, "frames": frames, "depth": args.depth,
+                            "plain_loop_fps": frames / t_plain, "speedup_vs_plain": t_plain / t_batch,
+                            "luma_msamples_per_s": sum(luma_samples(s, s.frames) for s in specs) / t_batch / 1e6,
+                            "parity": f"{'identical' if same else 'DIFFERENT'} DPBs in the mix and alone for the "
+                                      f"first {len(check)} streams", "template_setup_s": setup_s},
+                    e2e={"value": frames / t_batch, "unit": "frames/s", "h2d_bytes_per_step": None,
+                         "d2h_bytes_per_step": 0},
+                    gpu_launches=launches)
+        print(json.dumps(line), flush=True)
+        return
+    # served
+    out = {}
+    for rate in args.rates:
+        count = max(20, int(rate * args.trace_seconds))
+        trace = M.poisson_trace(rate, count, len(specs), seed=SEED + int(rate))
+        srv = M.Server(specs, tpl, hbm_budget=args.hbm_budget_gb << 30, depth=args.depth)
+        srv.run(trace)
+        served = M.latency_stats(trace)
+        served["evictions"] = srv.evictions
+        srv.close()
+        trace2 = M.poisson_trace(rate, count, len(specs), seed=SEED + int(rate))
+        M.serve_plain(specs, tpl, trace2)
+        out[str(rate)] = {"served": served, "plain": M.latency_stats(trace2)}
+    top = out[str(args.rates[-1])]["served"]
+    line = dict(base, metric="C5 served recon: p50/p99 latency and frames/s", value=top["frames_per_s"],
+                unit="frames/s", steps=1, warmup=0, ms_per_step=None,
+                config={"workload": "served_c5: Poisson arrivals, requests of 1..12 frames (half single-frame) "
+                                    "on streams of the mix: " + mix,
+                        "hbm_budget_gb": args.hbm_budget_gb, "trace_seconds": args.trace_seconds,
+                        "rates": out},
+                e2e={"value": top["frames_per_s"], "unit": "frames/s", "h2d_bytes_per_step": None,
+                     "d2h_bytes_per_step": 0})
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -361,7 +454,14 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--frames", type=int, default=0, help="pictures per step (default: the workload's)")
     ap.add_argument("--workload", default="h264_1080p",
-                    choices=["h264_1080p", "hevc_1080p_8", "hevc_1080p_10", "hevc_2160p_8", "hevc_2160p_10"])
+                    choices=["h264_1080p", "hevc_1080p_8", "hevc_1080p_10", "hevc_2160p_8", "hevc_2160p_10",
+                             "batched", "served"])
+    ap.add_argument("--streams", type=int, default=64, help="batched / served: streams in the mix")
+    ap.add_argument("--depth", type=int, default=2, help="batched / served: pictures queued per stream")
+    ap.add_argument("--parity-streams", type=int, default=64, help="batched: streams whose DPBs are compared")
+    ap.add_argument("--rates", type=float, nargs="+", default=[50.0, 200.0, 800.0], help="served: requests/s")
+    ap.add_argument("--trace-seconds", type=float, default=3.0, help="served: trace length")
+    ap.add_argument("--hbm-budget-gb", type=int, default=120, help="served: DPB budget")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--ref-frames", type=int, default=6)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -371,6 +471,9 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         run_reference(args, rank)
+        return
+    if args.workload in ("batched", "served"):
+        run_multistream(args)
         return
 
     import torch

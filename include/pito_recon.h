@@ -401,6 +401,19 @@ long long rc_stream_launches(rc_stream *s);
 /* The CUDA stream (cudaStream_t) the stream's work is ordered on. */
 void *rc_stream_cuda_stream(rc_stream *s);
 
+/* Completion marks, for request loops that keep many streams busy without a
+ * host thread per stream (no counterpart in the reference, whose decoders
+ * return frames synchronously from Decoder::decode, src/h264/mod.rs:76).
+ * rc_stream_mark records a mark after all work submitted so far and returns
+ * its id (increasing from 1); rc_stream_mark_done returns 1 once the work
+ * before that mark has completed, 0 if not yet, or a negative RC_E* code.
+ * Not thread-safe per stream. */
+int rc_stream_mark(rc_stream *s, unsigned long long *mark);
+/* Device bytes the stream holds (DPB, scratch and record buffers), for
+ * admission control across streams. */
+size_t rc_stream_device_bytes(rc_stream *s);
+int rc_stream_mark_done(rc_stream *s, unsigned long long mark);
+
 #ifdef __cplusplus
 }
 #endif

@@ -222,6 +222,12 @@ def lib() -> ctypes.CDLL:
     L.rc_stream_launches.restype = ctypes.c_longlong
     L.rc_stream_cuda_stream.argtypes = [vp]
     L.rc_stream_cuda_stream.restype = vp
+    L.rc_stream_mark.argtypes = [vp, ctypes.POINTER(ctypes.c_ulonglong)]
+    L.rc_stream_mark.restype = i32
+    L.rc_stream_mark_done.argtypes = [vp, ctypes.c_ulonglong]
+    L.rc_stream_mark_done.restype = i32
+    L.rc_stream_device_bytes.argtypes = [vp]
+    L.rc_stream_device_bytes.restype = sz
     L.rc_h264_deblock_noalloc.argtypes = [vp, i32, i32, vp, vp, vp, i32, i32, vp, vp]
     L.rc_h264_deblock_noalloc.restype = i32
     return L
@@ -433,6 +439,21 @@ class ReconStream:
 
     def cuda_stream(self) -> int:
         return lib().rc_stream_cuda_stream(self._h)
+
+    def mark(self) -> int:
+        """A completion mark after all work submitted so far."""
+        m = ctypes.c_ulonglong()
+        _check(lib().rc_stream_mark(self._h, ctypes.byref(m)), "rc_stream_mark")
+        return m.value
+
+    def device_bytes(self) -> int:
+        return lib().rc_stream_device_bytes(self._h)
+
+    def mark_done(self, mark: int) -> bool:
+        r = lib().rc_stream_mark_done(self._h, mark)
+        if r < 0:
+            raise ReconError(r, "rc_stream_mark_done")
+        return r == 1
 
     def profile(self, enable: bool):
         _check(lib().rc_stream_profile(self._h, int(enable)), "rc_stream_profile")

@@ -28,6 +28,8 @@
 #include <stdint.h>
 #include <string.h>
 
+#include <mutex>
+
 #include "recon_internal.h"
 
 namespace {
@@ -1699,15 +1701,31 @@ void rc_launch_h264_mb(const H264Launch &p, cudaStream_t st) {
 
 size_t rc_h264_band_smem(int mb_w) { return (size_t)BR * mb_w * 32; }
 
+// The kernel's dynamic shared-memory limit is one attribute for every stream
+// of the process: raise it to the widest picture any stream needs (never
+// lower it, so a narrower stream created later cannot break a wider one).
+static std::mutex g_band_attr_mu;
+static int g_band_attr[64];
+
+static bool band_smem_attr(size_t dyn) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return false;
+    std::lock_guard<std::mutex> lock(g_band_attr_mu);
+    if ((int)dyn <= g_band_attr[dev]) return true;
+    if (cudaFuncSetAttribute(h264_band_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    g_band_attr[dev] = (int)dyn;
+    return true;
+}
+
 int rc_h264_band_capacity(int mb_w) {
     int dev = 0, sms = 0, per = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const size_t dyn = rc_h264_band_smem(mb_w);
-    if (cudaFuncSetAttribute(h264_band_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn) != cudaSuccess) {
-        cudaGetLastError();
-        return 0;
-    }
+    if (!band_smem_attr(dyn)) return 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, h264_band_kernel, BAND_THREADS, dyn) != cudaSuccess)
         return 0;
     return per * sms;
@@ -1715,6 +1733,7 @@ int rc_h264_band_capacity(int mb_w) {
 
 int rc_launch_h264_band(const H264Launch &p, cudaStream_t st) {
     const int bands = (p.mb_h + BR - 1) / BR;
+    if (!band_smem_attr(rc_h264_band_smem(p.mb_w))) return -1;
     H264Launch q = p;
     void *args[] = {&q};
     cudaError_t e = cudaLaunchCooperativeKernel((const void *)h264_band_kernel, dim3(bands), dim3(BAND_THREADS),
@@ -1736,7 +1755,6 @@ int rc_launch_h264_band(const H264Launch &p, cudaStream_t st) {
 #define RC_NOALLOC_DB_WORDS (RC_NOALLOC_MAX_MBS * (int)(sizeof(DbMb) / 4))
 static __device__ __align__(256) uint32_t g_noalloc_scratch[RC_NOALLOC_DB_WORDS + RC_NOALLOC_MAX_ROWS];
 
-#include <mutex>
 
 namespace {
 std::mutex g_noalloc_mu;

@@ -6,6 +6,7 @@
 #include <algorithm>
 #include <cstdlib>
 #include <cstring>
+#include <deque>
 #include <new>
 #include <vector>
 
@@ -90,6 +91,10 @@ struct rc_stream {
     // per-kernel CUDA-event timing
     bool profiling = false;
     std::vector<cudaEvent_t> ev_free;
+    // completion marks (rc_stream_mark): pending (id, event) in order
+    std::deque<std::pair<unsigned long long, cudaEvent_t>> marks;
+    std::vector<cudaEvent_t> mark_free;
+    unsigned long long next_mark = 0, marks_done = 0;
     std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> ev_pending;
     double prof_ms[RC_KERNEL_COUNT] = {0};
     long long prof_n[RC_KERNEL_COUNT] = {0};
@@ -235,6 +240,8 @@ void destroy(rc_stream *s) {
     if (s->st) cudaStreamSynchronize(s->st);
     drain_profile(s);
     for (cudaEvent_t e : s->ev_free) cudaEventDestroy(e);
+    for (auto &m : s->marks) cudaEventDestroy(m.second);
+    for (cudaEvent_t e : s->mark_free) cudaEventDestroy(e);
     dev_free(s, s->dpb, s->slot_bytes * s->slots);
     for (DevBuf *b : {&s->mbs, &s->slices, &s->weights, &s->levels, &s->ctbs, &s->blk, &s->mvf, &s->tus, &s->hslices,
                       &s->scaling})
@@ -417,7 +424,13 @@ int rc_stream_create(int codec, int width, int height, int bit_depth, int dpb_sl
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, dev);
-    s->wave_blocks = std::max(1, s->sms * 2);
+    // persistent HEVC intra CTAs: about one per two 64x64 CTBs (the intra
+    // wavefront's useful parallelism), at most two per SM, so that a small
+    // picture leaves the GPU to the other streams that run beside it
+    {
+        const int c64 = ((s->width + 63) / 64) * ((s->height + 63) / 64);
+        s->wave_blocks = std::max(8, std::min(s->sms * 2, c64 / 2));
+    }
     if (const char *e = getenv("PITO_RECON_WAVE_BLOCKS")) {
         int v = atoi(e);
         if (v > 0 && v <= 4096) s->wave_blocks = v;
@@ -480,15 +493,22 @@ int rc_h264_submit(rc_stream *s, const rc_h264_picture *pic, int out_slot) {
     if (pic->mem != RC_MEM_HOST && pic->mem != RC_MEM_DEVICE) return RC_EINVAL;
     const int n = s->mb_w * s->mb_h;
     int rc;
-    // level-scale tables (per PPS), uploaded only when they change
+    // level-scale tables (per PPS), uploaded only when they change.  The copy
+    // goes on the stream itself: the stream does not order with the legacy
+    // default stream, and a pageable cudaMemcpy may return before its DMA has
+    // landed.  Its source, ls_host, lives until the next change, which first
+    // waits for the stream.
     {
         std::vector<int32_t> ls(2304 + 2304 * 4);
         h264_level_scale(pic->scaling4, pic->scaling8, ls.data(), ls.data() + 2304);
         if (!s->ls_valid || ls != s->ls_host) {
             if (cudaStreamSynchronize(s->st) != cudaSuccess) return cuda_fail(s);
-            if (cudaMemcpy(s->ls, ls.data(), ls.size() * sizeof(int32_t), cudaMemcpyHostToDevice) != cudaSuccess)
-                return cuda_fail(s);
             s->ls_host.swap(ls);
+            if (cudaMemcpyAsync(s->ls, s->ls_host.data(), s->ls_host.size() * sizeof(int32_t), cudaMemcpyHostToDevice,
+                                s->st) != cudaSuccess) {
+                s->ls_valid = false;
+                return cuda_fail(s);
+            }
             s->ls_valid = true;
         }
     }
@@ -654,10 +674,13 @@ int rc_stream_sync(rc_stream *s) {
     if (!s) return RC_EINVAL;
     if (cudaStreamSynchronize(s->st) != cudaSuccess) return cuda_fail(s);
     uint32_t e = 0;
-    if (cudaMemcpy(&e, s->error, sizeof e, cudaMemcpyDeviceToHost) != cudaSuccess) return cuda_fail(s);
+    if (cudaMemcpyAsync(&e, s->error, sizeof e, cudaMemcpyDeviceToHost, s->st) != cudaSuccess ||
+        cudaStreamSynchronize(s->st) != cudaSuccess)
+        return cuda_fail(s);
     if (e) {
         if (!s->sticky) s->sticky = (e & RC_DEV_ERR_TIMEOUT) ? RC_ETIMEOUT : RC_EDEVICE;
-        cudaMemset(s->error, 0, sizeof e);
+        // on the stream, so that the next launch cannot overtake the reset
+        cudaMemsetAsync(s->error, 0, sizeof e, s->st);
     }
     return s->sticky;
 }
@@ -726,13 +749,15 @@ int rc_picture_upload(rc_stream *s, int slot, const void *py, const void *pu, co
     if (!s || slot < 0 || slot >= s->slots || !py || !pu || !pv) return RC_EINVAL;
     const int bps = s->bps;
     uint8_t *base = s->dpb + (size_t)slot * s->slot_bytes;
-    bool ok = cudaStreamSynchronize(s->st) == cudaSuccess &&
-              cudaMemcpy2D(base, s->pitch, py, (size_t)s->width * bps, (size_t)s->width * bps, s->height,
-                           cudaMemcpyHostToDevice) == cudaSuccess &&
-              cudaMemcpy2D(base + s->u_off, s->cpitch, pu, (size_t)s->cw * bps, (size_t)s->cw * bps, s->ch,
-                           cudaMemcpyHostToDevice) == cudaSuccess &&
-              cudaMemcpy2D(base + s->v_off, s->cpitch, pv, (size_t)s->cw * bps, (size_t)s->cw * bps, s->ch,
-                           cudaMemcpyHostToDevice) == cudaSuccess;
+    // stream-ordered copies (the stream does not order with the legacy default
+    // stream), complete before returning so that the caller may free its planes
+    bool ok = cudaMemcpy2DAsync(base, s->pitch, py, (size_t)s->width * bps, (size_t)s->width * bps, s->height,
+                                cudaMemcpyHostToDevice, s->st) == cudaSuccess &&
+              cudaMemcpy2DAsync(base + s->u_off, s->cpitch, pu, (size_t)s->cw * bps, (size_t)s->cw * bps, s->ch,
+                                cudaMemcpyHostToDevice, s->st) == cudaSuccess &&
+              cudaMemcpy2DAsync(base + s->v_off, s->cpitch, pv, (size_t)s->cw * bps, (size_t)s->cw * bps, s->ch,
+                                cudaMemcpyHostToDevice, s->st) == cudaSuccess &&
+              cudaStreamSynchronize(s->st) == cudaSuccess;
     return ok ? RC_OK : cuda_fail(s);
 }
 
@@ -757,5 +782,38 @@ int rc_picture_device_planes(rc_stream *s, int slot, void **y, void **u, void **
 long long rc_stream_launches(rc_stream *s) { return s ? s->launches : 0; }
 
 void *rc_stream_cuda_stream(rc_stream *s) { return s ? (void *)s->st : nullptr; }
+
+size_t rc_stream_device_bytes(rc_stream *s) { return s ? s->held : 0; }
+
+int rc_stream_mark(rc_stream *s, unsigned long long *mark) {
+    if (!s || !mark) return RC_EINVAL;
+    cudaEvent_t e = nullptr;
+    if (!s->mark_free.empty()) {
+        e = s->mark_free.back();
+        s->mark_free.pop_back();
+    } else if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
+        return cuda_fail(s);
+    }
+    if (cudaEventRecord(e, s->st) != cudaSuccess) {
+        s->mark_free.push_back(e);
+        return cuda_fail(s);
+    }
+    s->marks.push_back({++s->next_mark, e});
+    *mark = s->next_mark;
+    return RC_OK;
+}
+
+int rc_stream_mark_done(rc_stream *s, unsigned long long mark) {
+    if (!s || mark == 0 || mark > s->next_mark) return RC_EINVAL;
+    while (!s->marks.empty()) {
+        cudaError_t q = cudaEventQuery(s->marks.front().second);
+        if (q == cudaErrorNotReady) break;
+        if (q != cudaSuccess) return cuda_fail(s);
+        s->marks_done = s->marks.front().first;
+        s->mark_free.push_back(s->marks.front().second);
+        s->marks.pop_front();
+    }
+    return mark <= s->marks_done ? 1 : 0;
+}
 
 }  // extern "C"

@@ -139,3 +139,22 @@ def test_launch_count_and_profile(engine):
         assert st.launches() - n0 == 2
         prof = st.profile_read()
         assert all(prof[k][1] == 1 for k in (0, 1)) and prof[1][0] > 0
+
+
+def test_streams_of_different_widths_coexist(engine, oracle):
+    """A narrower stream created after a wider one must not break the wider
+    one's launches (the band kernel's shared-memory limit is per process)."""
+    wide = engine.ReconStream(engine.RC_CODEC_H264, 1920, 1088, 8, 2)
+    narrow = engine.ReconStream(engine.RC_CODEC_H264, 320, 192, 8, 2)
+    try:
+        for st, (mw, mh) in ((wide, (120, 68)), (narrow, (20, 12)), (wide, (120, 68))):
+            p = engine.SynthH264(seed=77 + mw, mb_w=mw, mb_h=mh, intra_only=1)
+            st.submit_h264(p, 0)
+            assert st.sync() == 0
+            dpb = oracle.H264Dpb(mw, mh, 2)
+            assert dpb.recon(p.ptr, 0) == 0
+            for g, w in zip(st.download(0), dpb.planes(0)):
+                assert np.array_equal(g, w)
+    finally:
+        wide.close()
+        narrow.close()
