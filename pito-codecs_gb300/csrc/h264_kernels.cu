@@ -456,74 +456,45 @@ struct __align__(16) WarpSmem {
     int16_t res[384];     // residual samples: 16x16 luma, then 8x8 Cb, 8x8 Cr
     uint8_t cy[17 * 32];  // luma canvas: rows -1..15, cols -1..30 -> [(r+1)*32 + c+1]
     uint8_t cc[2][9 * 12];  // chroma canvas: rows -1..7, cols -1..10
-    int32_t f[32];       // smoothed reference samples (8x8)
+    int32_t f[32];       // reference arrays: an 8x8 block's smoothed samples, or two 4x4 blocks'
 };
 
 __device__ __forceinline__ int cvy(const WarpSmem &S, int r, int c) { return S.cy[(r + 1) * 32 + c + 1]; }
 
-struct Avail {
-    bool left, top, tl, tr;
-};
-
-// Reference samples of an 8x8 block (load_edge, src/h264/dec/intra.rs:31-62:
-// 128 where unavailable, the last top sample where the top-right is) after
-// pred8x8's smoothing (intra.rs:199-231), into S.f: top 0..15, left 16..23,
-// corner 24.  Each lane reads the raw samples it needs straight from the
-// canvas.
-__device__ __forceinline__ void edge8(WarpSmem &S, int lane, int bx0, int by0, Avail a) {
-    auto ET = [&](int i) -> int { return a.top ? (int)cvy(S, by0 - 1, bx0 + ((i < 8 || a.tr) ? i : 7)) : 128; };
-    auto EL = [&](int j) -> int { return a.left ? (int)cvy(S, by0 + j, bx0 - 1) : 128; };
-    const int tl = a.tl ? (int)cvy(S, by0 - 1, bx0 - 1) : 128;
-    if (lane < 16) {
-        const int i = lane, c = ET(i);
-        int v = c;
-        if (a.top) {
-            if (i == 0) v = a.tl ? (tl + 2 * c + ET(1) + 2) >> 2 : (3 * c + ET(1) + 2) >> 2;
-            else if (i == 15) v = (ET(14) + 3 * c + 2) >> 2;
-            else v = (ET(i - 1) + 2 * c + ET(i + 1) + 2) >> 2;
-        }
-        S.f[i] = v;
-    } else if (lane < 24) {
-        const int j = lane - 16, c = EL(j);
-        int v = c;
-        if (a.left) {
-            if (j == 0) v = a.tl ? (tl + 2 * c + EL(1) + 2) >> 2 : (3 * c + EL(1) + 2) >> 2;
-            else if (j == 7) v = (EL(6) + 3 * c + 2) >> 2;
-            else v = (EL(j - 1) + 2 * c + EL(j + 1) + 2) >> 2;
-        }
-        S.f[lane] = v;
-    } else if (lane == 24) {
-        int v = tl;
-        if (a.tl) {
-            if (a.top && a.left) v = (ET(0) + 2 * tl + EL(0) + 2) >> 2;
-            else if (a.top) v = (3 * tl + ET(0) + 2) >> 2;
-            else if (a.left) v = (3 * tl + EL(0) + 2) >> 2;
-        }
-        S.f[24] = v;
-    }
-}
-
-// pred_nxn (src/h264/dec/intra.rs:64-192) as data: for every mode and
-// sample position of an n x n block (n = 4, 8) the reference samples the
-// prediction reads and how it combines them, so that a warp predicts samples
-// of different modes with one branch-free instruction sequence (a switch over
-// the mode costs several times the arithmetic).  Entry: taps i0, i1, i2 and
-// the kind k (bits 3n..): 0 copy i0; 1 (i0 + i1 + 1) >> 1; 2 (i0 + 2 i1 + i2
-// + 2) >> 2; 3 (i0 + 3 i1 + 2) >> 2; 4 DC.  Reference indices: 4x4 -- 0
-// corner, 1..8 top 0..7, 9..12 left 0..3 (4 bits); 8x8 -- the smoothed
-// samples of edge8: top 0..15, left 16..23, corner 24 (5 bits).
+// pred_nxn (src/h264/dec/intra.rs:64-192) and pred8x8 (intra.rs:194-238) as
+// data.  For every mode and sample position of an n x n block (n = 4, 8) the
+// table holds the three reference samples the prediction reads and the
+// weights it combines them with, (w0 r0 + w1 r1 + w2 r2 + rnd) >> 2:
+//   copy                        (4, 0, 0, 0)
+//   (r0 + r1 + 1) >> 1          (2, 2, 0, 2)
+//   (r0 + 2 r1 + r2 + 2) >> 2   (1, 2, 1, 2)
+//   (r0 + 3 r1 + 2) >> 2        (1, 3, 0, 2)
+// and DC copies the DC entry of the reference array.  A warp then predicts
+// samples of any mix of modes and positions with one instruction sequence:
+// no lane takes a branch of its own (divergent selects over the mode cost
+// several times the arithmetic).  Reference arrays: 4x4 -- 0 corner, 1..8
+// top 0..7, 9..12 left 0..3, 13 DC (4-bit indices); 8x8 -- the smoothed
+// samples top 0..15, left 16..23, corner 24, DC 25 (5-bit indices).
 template <int N>
 struct PredTab {
     uint32_t e[9][N * N];
 };
 template <int N>
+__host__ __device__ constexpr uint32_t ptS() { return N == 4 ? 4 : 5; }
+template <int N>
 __host__ __device__ constexpr int ptT(int i) { return N == 4 ? (i < 0 ? 0 : 1 + i) : (i < 0 ? 24 : i); }
 template <int N>
 __host__ __device__ constexpr int ptL(int j) { return N == 4 ? (j < 0 ? 0 : 9 + j) : (j < 0 ? 24 : 16 + j); }
 template <int N>
+__host__ __device__ constexpr int ptDC() { return N == 4 ? 13 : 25; }
+// k: 0 copy, 1 (r0 + r1 + 1) >> 1, 2 (r0 + 2 r1 + r2 + 2) >> 2, 3 (r0 + 3 r1 + 2) >> 2
+template <int N>
 __host__ __device__ constexpr uint32_t ptE(int k, int a, int b = 0, int c = 0) {
-    return (uint32_t)a | (uint32_t)b << (N == 4 ? 4 : 5) | (uint32_t)c << (N == 4 ? 8 : 10) |
-           (uint32_t)k << (N == 4 ? 12 : 15);
+    const uint32_t s = ptS<N>();
+    const uint32_t w0 = k == 0 ? 4 : k == 1 ? 2 : 1, w1 = k == 0 ? 0 : k == 3 ? 3 : 2, w2 = k == 2 ? 1 : 0,
+                   rnd = k == 0 ? 0 : 2;
+    return (uint32_t)a | (uint32_t)b << s | (uint32_t)c << (2 * s) | w0 << (3 * s) | w1 << (3 * s + 3) |
+           w2 << (3 * s + 5) | rnd << (3 * s + 6);
 }
 template <int N>
 __host__ __device__ constexpr uint32_t pt_entry(int mode, int x, int y) {
@@ -531,7 +502,7 @@ __host__ __device__ constexpr uint32_t pt_entry(int mode, int x, int y) {
     switch (mode) {
     case 0: return ptE<N>(0, ptT<N>(x));
     case 1: return ptE<N>(0, ptL<N>(y));
-    case 2: return ptE<N>(4, 0);
+    case 2: return ptE<N>(0, ptDC<N>());
     case 3:
         if (x == n - 1 && y == n - 1) return ptE<N>(3, ptT<N>(2 * n - 2), ptT<N>(2 * n - 1));
         return ptE<N>(2, ptT<N>(x + y), ptT<N>(x + y + 1), ptT<N>(x + y + 2));
@@ -577,38 +548,26 @@ __host__ __device__ constexpr PredTab<N> make_predtab() {
 __constant__ PredTab<4> cPRED4 = make_predtab<4>();
 __constant__ PredTab<8> cPRED8 = make_predtab<8>();
 
-// One sample of a 4x4 block at (bx0, by0) from its table entry; reference
-// samples straight from the canvas with load_edge's substitutions
-// (intra.rs:31-62): 128 where a neighbour is unavailable, the last top
-// sample where the top-right one is.
-__device__ __forceinline__ int tap4(const WarpSmem &S, int idx, int bx0, int by0, Avail a) {
-    const bool isT = (unsigned)(idx - 1) < 8u, isL = idx >= 9;
-    const int i = (idx - 1 < 4 || a.tr) ? idx - 1 : 3;
-    const int row = isL ? by0 + idx - 9 : by0 - 1;
-    const int col = isL ? bx0 - 1 : isT ? bx0 + i : bx0 - 1;
-    const bool ok = isL ? a.left : isT ? a.top : a.tl;
-    const int v = S.cy[(row + 1) * 32 + col + 1];
-    return ok ? v : 128;
+// Blocks of an Intra4x4 MB (raster index) whose top-right 4x4 block lies in
+// the MB and precedes them in decode (8x8 zig-zag) order.
+__host__ __device__ constexpr uint32_t tr_inside_mask() {
+    constexpr int dec[16] = {0, 1, 4, 5, 2, 3, 6, 7, 8, 9, 12, 13, 10, 11, 14, 15};
+    uint32_t m = 0;
+    for (int b = 4; b < 16; b++)
+        if ((b & 3) < 3 && dec[b - 3] < dec[b]) m |= 1u << b;
+    return m;
 }
-__device__ __forceinline__ int pred4(const WarpSmem &S, uint32_t e, int bx0, int by0, Avail a) {
-    const int k = e >> 12;
-    const int r0 = tap4(S, e & 15, bx0, by0, a), r1 = tap4(S, (e >> 4) & 15, bx0, by0, a),
-              r2 = tap4(S, (e >> 8) & 15, bx0, by0, a);
-    const uint8_t *tp = S.cy + by0 * 32 + bx0 + 1;  // row -1 of the block
-    const int st = tp[0] + tp[1] + tp[2] + tp[3];
-    const int sl = S.cy[(by0 + 1) * 32 + bx0] + S.cy[(by0 + 2) * 32 + bx0] + S.cy[(by0 + 3) * 32 + bx0] +
-                   S.cy[(by0 + 4) * 32 + bx0];
-    const int dc = (a.top && a.left) ? (st + sl + 4) >> 3 : a.left ? (sl + 2) >> 2 : a.top ? (st + 2) >> 2 : 128;
-    const int v1 = (r0 + r1 + 1) >> 1, v2 = (r0 + 2 * r1 + r2 + 2) >> 2, v3 = (r0 + 3 * r1 + 2) >> 2;
-    return k == 0 ? r0 : k == 1 ? v1 : k == 2 ? v2 : k == 3 ? v3 : dc;
-}
-// One sample of an 8x8 block from its table entry and the smoothed reference
-// samples in S.f.
-__device__ __forceinline__ int pred8(const WarpSmem &S, uint32_t e, int dc) {
-    const int k = e >> 15;
-    const int r0 = S.f[e & 31], r1 = S.f[(e >> 5) & 31], r2 = S.f[(e >> 10) & 31];
-    const int v1 = (r0 + r1 + 1) >> 1, v2 = (r0 + 2 * r1 + r2 + 2) >> 2, v3 = (r0 + 3 * r1 + 2) >> 2;
-    return k == 0 ? r0 : k == 1 ? v1 : k == 2 ? v2 : k == 3 ? v3 : dc;
+constexpr uint32_t kTR_INSIDE = tr_inside_mask();
+static_assert(kTR_INSIDE == 0x5750u, "top-right availability inside an Intra4x4 MB");
+
+// One predicted sample from its table entry and the block's reference array.
+template <int N>
+__device__ __forceinline__ int pt_apply(uint32_t e, const int *ref) {
+    constexpr uint32_t s = ptS<N>(), m = (1u << s) - 1;
+    const int r0 = ref[e & m], r1 = ref[(e >> s) & m], r2 = ref[(e >> (2 * s)) & m];
+    const int w0 = (e >> (3 * s)) & 7, w1 = (e >> (3 * s + 3)) & 3, w2 = (e >> (3 * s + 5)) & 1,
+              rnd = (e >> (3 * s + 6)) & 3;
+    return (w0 * r0 + w1 * r1 + w2 * r2 + rnd) >> 2;
 }
 
 // reconstruct_intra, src/h264/dec/slicedec.rs:1325-1388, one warp, on the
@@ -622,86 +581,131 @@ __device__ void intra_mb(WarpSmem &S, int lane, const bool nb[4], const uint32_t
         // top-left and top-right blocks), two blocks per step, 16 lanes each
         constexpr int8_t kA[10] = {0, 1, 2, 3, 6, 7, 10, 11, 14, 15};
         constexpr int8_t kB[10] = {-1, -1, 4, 5, 8, 9, 12, 13, -1, -1};
-        // raster block index -> decode (8x8 zig-zag) order, for the top-right rule
-        constexpr int8_t kDec[16] = {0, 1, 4, 5, 2, 3, 6, 7, 8, 9, 12, 13, 10, 11, 14, 15};
-        const int g = lane >> 4, px = lane & 3, py = (lane >> 2) & 3;
-        const uint2 m0 = *(const uint2 *)m.modes, m1 = *(const uint2 *)(m.modes + 8);
-        const uint32_t mword[4] = {m0.x, m0.y, m1.x, m1.y};
+        const int g = lane >> 4, l = lane & 15, px = lane & 3, py = (lane >> 2) & 3;
+        int *E = S.f + 16 * g;  // the reference array of this half-warp's block
+        // this lane's table entry and residual sample of every step (a half-warp
+        // without a block in a step shadows the other half's block, unstored)
+        uint32_t ent[10];
+        int rs[10];
 #pragma unroll
         for (int st = 0; st < 10; st++) {
-            const int ba = kA[st], bb = kB[st];
-            const int blk = g ? bb : ba;
-            if (blk >= 0) {
-                const int bx = blk & 3, by = blk >> 2;
-                Avail a;  // luma_avail4, slicedec.rs:1297-1323
-                a.left = bx > 0 ? true : nb[0];
-                a.top = by > 0 ? true : nb[1];
-                a.tl = (bx > 0 && by > 0) ? true : by > 0 ? nb[0] : bx > 0 ? nb[1] : nb[3];
-                const bool tr_a = (ba >> 2) == 0 ? ((ba & 3) < 3 ? nb[1] : nb[2])
-                                  : (ba & 3) == 3 ? false : kDec[ba - 3] < kDec[ba];
-                const bool tr_b = bb < 0 ? false : (bb >> 2) == 0 ? ((bb & 3) < 3 ? nb[1] : nb[2])
-                                  : (bb & 3) == 3 ? false : kDec[bb - 3] < kDec[bb];
-                a.tr = g ? tr_b : tr_a;
-                const int mode_a = (mword[ba >> 2] >> ((ba & 3) * 8)) & 255;
-                const int mode_b = bb < 0 ? 0 : (mword[bb >> 2] >> ((bb & 3) * 8)) & 255;
-                const uint32_t e = tab4[(g ? mode_b : mode_a) * 16 + py * 4 + px];
-                int v = pred4(S, e, bx * 4, by * 4, a);
-                v = clip255(v + S.res[(by * 4 + py) * 16 + bx * 4 + px]);
-                S.cy[(by * 4 + py + 1) * 32 + bx * 4 + px + 1] = (uint8_t)v;
+            const int b = (g && kB[st] >= 0) ? kB[st] : kA[st];
+            ent[st] = tab4[m.modes[b] * 16 + py * 4 + px];
+            rs[st] = S.res[((b >> 2) * 4 + py) * 16 + (b & 3) * 4 + px];
+        }
+#pragma unroll
+        for (int st = 0; st < 10; st++) {
+            const bool act = !g || kB[st] >= 0;
+            const int b = (g && kB[st] >= 0) ? kB[st] : kA[st];
+            const int bx = b & 3, by = b >> 2, bx0 = bx * 4, by0 = by * 4;
+            // luma_avail4, slicedec.rs:1297-1323
+            const bool aL = bx > 0 || nb[0], aT = by > 0 || nb[1];
+            const bool aTL = (bx > 0 && by > 0) || (by > 0 ? nb[0] : bx > 0 ? nb[1] : nb[3]);
+            const bool aTR = by == 0 ? (bx < 3 ? nb[1] : nb[2]) : (kTR_INSIDE >> b & 1);
+            // reference array (load_edge, intra.rs:31-62: 128 where unavailable,
+            // the last top sample for an unavailable top-right) and the DC
+            {
+                const bool isT = (unsigned)(l - 1) < 8u, isL = (unsigned)(l - 9) < 4u;
+                const int ti = (l - 1 < 4 || aTR) ? l - 1 : 3;
+                const int row = isL ? by0 + l - 9 : by0 - 1;
+                const int col = isT ? bx0 + ti : bx0 - 1;
+                const bool ok = isT ? aT : isL ? aL : aTL;
+                const int raw = S.cy[(row + 1) * 32 + col + 1];
+                const uint8_t *tp = S.cy + by0 * 32 + bx0 + 1;  // row -1 of the block
+                const uint8_t *lp = S.cy + (by0 + 1) * 32 + bx0;  // column -1, row 0
+                const int st4 = tp[0] + tp[1] + tp[2] + tp[3], sl4 = lp[0] + lp[32] + lp[64] + lp[96];
+                const int dc = (aT && aL) ? (st4 + sl4 + 4) >> 3 : aL ? (sl4 + 2) >> 2 : aT ? (st4 + 2) >> 2 : 128;
+                E[l] = l == 13 ? dc : ok ? raw : 128;
+            }
+            __syncwarp();
+            {
+                const int v = clip255(pt_apply<4>(ent[st], E) + rs[st]);
+                if (act) S.cy[(by0 + py + 1) * 32 + bx0 + px + 1] = (uint8_t)v;
             }
             __syncwarp();
         }
     } else if (m.kind == RC_H264_I8x8) {
+        uint32_t ent[4][2];
+        int rs[4][2];
+#pragma unroll
         for (int b8 = 0; b8 < 4; b8++) {
             const int bx = (b8 & 1) * 2, by = (b8 >> 1) * 2;
-            Avail a;
-            a.left = bx > 0 ? true : nb[0];
-            a.top = by > 0 ? true : nb[1];
-            a.tl = (bx > 0 && by > 0) ? true : by > 0 ? nb[0] : bx > 0 ? nb[1] : nb[3];
-            a.tr = b8 == 0 ? nb[1] : b8 == 1 ? nb[2] : b8 == 2;
-            edge8(S, lane, bx * 4, by * 4, a);
-            __syncwarp();
             const int mode = m.modes[by * 4 + bx];
-            int st = 0, sl = 0;
-#pragma unroll
-            for (int i = 0; i < 8; i++) { st += S.f[i]; sl += S.f[16 + i]; }
-            const int dc = (a.top && a.left) ? (st + sl + 8) >> 4 : a.left ? (sl + 4) >> 3 : a.top ? (st + 4) >> 3 : 128;
 #pragma unroll
             for (int h = 0; h < 2; h++) {
-                int idx = lane + 32 * h, x = idx & 7, y = idx >> 3;
-                int v = pred8(S, tab8[mode * 64 + idx], dc);
-                v = clip255(v + S.res[(by * 4 + y) * 16 + bx * 4 + x]);
-                S.cy[(by * 4 + y + 1) * 32 + bx * 4 + x + 1] = (uint8_t)v;
+                const int idx = lane + 32 * h, x = idx & 7, y = idx >> 3;
+                ent[b8][h] = tab8[mode * 64 + idx];
+                rs[b8][h] = S.res[(by * 4 + y) * 16 + bx * 4 + x];
+            }
+        }
+#pragma unroll
+        for (int b8 = 0; b8 < 4; b8++) {
+            const int bx = (b8 & 1) * 2, by = (b8 >> 1) * 2, bx0 = bx * 4, by0 = by * 4;
+            const bool aL = bx > 0 || nb[0], aT = by > 0 || nb[1];
+            const bool aTL = (bx > 0 && by > 0) || (by > 0 ? nb[0] : bx > 0 ? nb[1] : nb[3]);
+            const bool aTR = b8 == 0 ? nb[1] : b8 == 1 ? nb[2] : b8 == 2;
+            // reference samples (load_edge, intra.rs:31-62) smoothed by
+            // pred8x8's [1 2 1] filter (intra.rs:199-231).  On the line
+            // L7..L0, corner, T0..T15 (u = 0..24) a sample takes a neighbour
+            // only when both are available, else itself; lanes 25..31 the DC.
+            {
+                const int u = lane < 16 ? 9 + lane : lane < 24 ? 23 - lane : 8;
+                auto at = [&](int w, bool &av) -> int {
+                    av = w < 8 ? aL : w == 8 ? aTL : aT;
+                    const int i = w - 9, ti = (i < 8 || aTR) ? i : 7;
+                    const int row = w < 8 ? by0 + 7 - w : by0 - 1;
+                    const int col = w <= 8 ? bx0 - 1 : bx0 + ti;
+                    return S.cy[(row + 1) * 32 + col + 1];
+                };
+                bool ac, a1, a2;
+                const int rc = at(u, ac), r1 = at(u > 0 ? u - 1 : 0, a1), r2 = at(u < 24 ? u + 1 : 24, a2);
+                const int c = ac ? rc : 128;
+                const int n1 = (u > 0 && ac && a1) ? r1 : c, n2 = (u < 24 && ac && a2) ? r2 : c;
+                const int v = (n1 + 2 * c + n2 + 2) >> 2;
+                const int st = (int)__reduce_add_sync(0xffffffffu, (unsigned)(lane < 8 ? v : 0));
+                const int sl = (int)__reduce_add_sync(0xffffffffu, (unsigned)(lane >= 16 && lane < 24 ? v : 0));
+                const int dc =
+                    (aT && aL) ? (st + sl + 8) >> 4 : aL ? (sl + 4) >> 3 : aT ? (st + 4) >> 3 : 128;
+                S.f[lane] = lane < 25 ? v : dc;
+            }
+            __syncwarp();
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const int idx = lane + 32 * h, x = idx & 7, y = idx >> 3;
+                const int v = clip255(pt_apply<8>(ent[b8][h], S.f) + rs[b8][h]);
+                S.cy[(by0 + y + 1) * 32 + bx0 + x + 1] = (uint8_t)v;
             }
             __syncwarp();
         }
     } else {
-        // pred16x16, src/h264/dec/intra.rs:240-305
+        // pred16x16, src/h264/dec/intra.rs:240-305 (the DC sums and plane
+        // gradients only for their modes; the mode is uniform over the warp)
         const bool al = nb[0], at = nb[1], atl = nb[3];
         const int mode = m.i16_mode;
-        int topv = at ? cvy(S, -1, lane & 15) : 0, leftv = al ? cvy(S, lane & 15, -1) : 0;
-        int tl = atl ? cvy(S, -1, -1) : 128;
-        int st = __reduce_add_sync(0xffffffffu, (unsigned)(lane < 16 ? topv : 0));
-        int sl = __reduce_add_sync(0xffffffffu, (unsigned)(lane < 16 ? leftv : 0));
-        int hterm = 0, vterm = 0;
-        if (lane < 8) {
-            int k = lane;
-            int t8k = at ? cvy(S, -1, 8 + k) : 0;
-            int t6k = (6 - k) < 0 ? tl : (at ? cvy(S, -1, 6 - k) : 0);
-            int l8k = al ? cvy(S, 8 + k, -1) : 0;
-            int l6k = (6 - k) < 0 ? tl : (al ? cvy(S, 6 - k, -1) : 0);
-            hterm = (k + 1) * (t8k - t6k);
-            vterm = (k + 1) * (l8k - l6k);
+        int dc = 128, aa = 0, bb = 0, cc = 0;
+        if (mode == 2) {
+            const int topv = at ? cvy(S, -1, lane & 15) : 0, leftv = al ? cvy(S, lane & 15, -1) : 0;
+            const int st = (int)__reduce_add_sync(0xffffffffu, (unsigned)(lane < 16 ? topv : 0));
+            const int sl = (int)__reduce_add_sync(0xffffffffu, (unsigned)(lane < 16 ? leftv : 0));
+            dc = (at && al) ? (st + sl + 16) >> 5 : al ? (sl + 8) >> 4 : at ? (st + 8) >> 4 : 128;
+        } else if (mode == 3) {
+            const int tl = atl ? cvy(S, -1, -1) : 128;
+            int hterm = 0, vterm = 0;
+            if (lane < 8) {
+                const int kk = lane;
+                const int t8k = at ? cvy(S, -1, 8 + kk) : 0;
+                const int t6k = (6 - kk) < 0 ? tl : (at ? cvy(S, -1, 6 - kk) : 0);
+                const int l8k = al ? cvy(S, 8 + kk, -1) : 0;
+                const int l6k = (6 - kk) < 0 ? tl : (al ? cvy(S, 6 - kk, -1) : 0);
+                hterm = (kk + 1) * (t8k - t6k);
+                vterm = (kk + 1) * (l8k - l6k);
+            }
+            const int H = (int)__reduce_add_sync(0xffffffffu, (unsigned)hterm);
+            const int Vv = (int)__reduce_add_sync(0xffffffffu, (unsigned)vterm);
+            aa = 16 * ((al ? cvy(S, 15, -1) : 0) + (at ? cvy(S, -1, 15) : 0));
+            bb = (5 * H + 32) >> 6;
+            cc = (5 * Vv + 32) >> 6;
         }
-        int H = (int)__reduce_add_sync(0xffffffffu, (unsigned)hterm);
-        int Vv = (int)__reduce_add_sync(0xffffffffu, (unsigned)vterm);
-        int dc;
-        if (at && al) dc = (st + sl + 16) >> 5;
-        else if (al) dc = (sl + 8) >> 4;
-        else if (at) dc = (st + 8) >> 4;
-        else dc = 128;
-        int aa = 16 * ((al ? cvy(S, 15, -1) : 0) + (at ? cvy(S, -1, 15) : 0));
-        int bb = (5 * H + 32) >> 6, cc = (5 * Vv + 32) >> 6;
         // all reads of the canvas edge are done before any write below
         __syncwarp();
 #pragma unroll
@@ -717,49 +721,61 @@ __device__ void intra_mb(WarpSmem &S, int lane, const bool nb[4], const uint32_t
         }
         __syncwarp();
     }
-    // ---- chroma, pred_chroma, src/h264/dec/intra.rs:307-395
+    // ---- chroma, pred_chroma, src/h264/dec/intra.rs:307-395.  The per-block
+    // DC values (mode 0) or the per-component plane parameters (mode 3)
+    // first, into S.f, then every sample with one sequence.
     {
         const bool al = nb[0], at = nb[1], atl = nb[3];
         const int mode = m.chroma_mode;
+        if (mode == 0) {
+            // lane & 7: component (bit 2) and 4x4 block (bx bit 0, by bit 1)
+            const int c = (lane >> 2) & 1, bx = lane & 1, by = (lane >> 1) & 1;
+            const uint8_t *cv = S.cc[c];
+            int st = 0, sl = 0;
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                st += at ? (int)cv[bx * 4 + i + 1] : 0;
+                sl += al ? (int)cv[(by * 4 + i + 1) * 12] : 0;
+            }
+            const int both = (at && al) ? (st + sl + 4) >> 3 : al ? (sl + 2) >> 2 : at ? (st + 2) >> 2 : 128;
+            const int topf = at ? (st + 2) >> 2 : al ? (sl + 2) >> 2 : 128;
+            const int leftf = al ? (sl + 2) >> 2 : at ? (st + 2) >> 2 : 128;
+            if (lane < 8) S.f[lane] = bx == by ? both : bx ? topf : leftf;
+        } else if (mode == 3) {
+            const int c = lane & 1;
+            const uint8_t *cv = S.cc[c];
+            const int tl = atl ? cv[0] : 128;
+            int hh = 0, vv = 0;
+#pragma unroll
+            for (int kk = 0; kk < 4; kk++) {
+                const int tm = kk == 3 ? tl : (at ? (int)cv[2 - kk + 1] : 0);
+                const int lm = kk == 3 ? tl : (al ? (int)cv[(2 - kk + 1) * 12] : 0);
+                hh += (kk + 1) * ((at ? (int)cv[4 + kk + 1] : 0) - tm);
+                vv += (kk + 1) * ((al ? (int)cv[(4 + kk + 1) * 12] : 0) - lm);
+            }
+            if (lane < 2) {
+                S.f[8 + 3 * c] = 16 * ((al ? (int)cv[8 * 12] : 0) + (at ? (int)cv[8] : 0));
+                S.f[9 + 3 * c] = (34 * hh + 32) >> 6;
+                S.f[10 + 3 * c] = (34 * vv + 32) >> 6;
+            }
+        }
+        __syncwarp();
         int outv[4];
 #pragma unroll
         for (int h = 0; h < 4; h++) {
-            int idx = lane + 32 * h, c = idx >> 6, x = idx & 7, y = (idx >> 3) & 7;
+            const int idx = lane + 32 * h, c = idx >> 6, x = idx & 7, y = (idx >> 3) & 7;
             const uint8_t *cv = S.cc[c];
-#define CT(i) (at ? (int)cv[(i) + 1] : 0)
-#define CL(i) (al ? (int)cv[((i) + 1) * 12] : 0)
             int v;
-            if (mode == 0) {
-                int bx = x >> 2, by = y >> 2, st = 0, sl = 0;
-                for (int i = 0; i < 4; i++) { st += CT(bx * 4 + i); sl += CL(by * 4 + i); }
-                if ((bx == 0 && by == 0) || (bx > 0 && by > 0)) {
-                    v = (at && al) ? (st + sl + 4) >> 3 : al ? (sl + 2) >> 2 : at ? (st + 2) >> 2 : 128;
-                } else if (bx > 0) {
-                    v = at ? (st + 2) >> 2 : al ? (sl + 2) >> 2 : 128;
-                } else {
-                    v = al ? (sl + 2) >> 2 : at ? (st + 2) >> 2 : 128;
-                }
-            } else if (mode == 1) v = CL(y);
-            else if (mode == 2) v = CT(x);
-            else {
-                int tl = atl ? cv[0] : 128, hh = 0, vv = 0;
-                for (int k = 0; k < 4; k++) {
-                    int tm = (2 - k) < 0 ? tl : CT(2 - k), lm = (2 - k) < 0 ? tl : CL(2 - k);
-                    hh += (k + 1) * (CT(4 + k) - tm);
-                    vv += (k + 1) * (CL(4 + k) - lm);
-                }
-                int aa = 16 * (CL(7) + CT(7)), bb = (34 * hh + 32) >> 6, cc2 = (34 * vv + 32) >> 6;
-                v = clip255((aa + bb * (x - 3) + cc2 * (y - 3) + 16) >> 5);
-            }
-#undef CT
-#undef CL
-            v = clip255(v + S.res[256 + c * 64 + y * 8 + x]);
-            outv[h] = v;
+            if (mode == 0) v = S.f[c * 4 + (y >> 2) * 2 + (x >> 2)];
+            else if (mode == 1) v = al ? (int)cv[(y + 1) * 12] : 0;
+            else if (mode == 2) v = at ? (int)cv[x + 1] : 0;
+            else v = clip255((S.f[8 + 3 * c] + S.f[9 + 3 * c] * (x - 3) + S.f[10 + 3 * c] * (y - 3) + 16) >> 5);
+            outv[h] = clip255(v + S.res[256 + c * 64 + y * 8 + x]);
         }
         __syncwarp();
 #pragma unroll
         for (int h = 0; h < 4; h++) {
-            int idx = lane + 32 * h, c = idx >> 6, x = idx & 7, y = (idx >> 3) & 7;
+            const int idx = lane + 32 * h, c = idx >> 6, x = idx & 7, y = (idx >> 3) & 7;
             S.cc[c][(y + 1) * 12 + x + 1] = (uint8_t)outv[h];
         }
     }
@@ -1159,6 +1175,12 @@ __global__ void __launch_bounds__(128) h264_db_params_kernel(H264Launch P) {
 constexpr int BR = RC_H264_BAND_ROWS;
 constexpr int DRING = 8;  // ring slots between filter rows of a band
 constexpr int BAND_THREADS = (3 * BR + 1) * 32;
+// an intra warp's staging: parameters (32 B) and residual (768 B), then one
+// 4-byte word per lane holding the next MB's column -1 sample (luma rows
+// 0..15, Cb rows 0..7, Cr rows 0..7)
+constexpr int RC_BAND_STG_LEFT = 800;
+constexpr int RC_BAND_STG = RC_BAND_STG_LEFT + 32 * 4;
+static_assert(RC_BAND_STG % 16 == 0, "staging areas stay 16-byte aligned");
 
 struct __align__(16) LumaRow {
     uint8_t t[20][16];        // rows -4..15 of the MB being filtered (horizontal edges)
@@ -1275,15 +1297,26 @@ __device__ __forceinline__ void cp_async8(void *dst, const void *src) {
     asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src)
                  : "memory");
 }
+__device__ __forceinline__ void cp_async4(void *dst, const void *src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src)
+                 : "memory");
+}
 __device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 __device__ __forceinline__ void cp_wait_all_but_1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
 
 // Intra warp of band row w (picture row my).  `lines` holds, per band row,
 // the row's unfiltered bottom samples (luma row 15, then Cb and Cr row 7):
 // filled from the picture at the start (inter MBs are final already) and
 // updated as the row's intra MBs are reconstructed, so that the row below
-// reads its top neighbours from shared memory.
-__device__ void band_intra_row(const H264Launch &P, BandSmem &B, uint8_t *lines, int w, int my, int lane) {
+// reads its top neighbours from shared memory.  `stg` stages the next intra
+// MB's parameters, residual and (when its left neighbour is an inter MB) the
+// words holding its column -1, loaded with cp.async while the current MB is
+// reconstructed.  All of these are final before the kernel starts and stay
+// unchanged until this warp reports the MB after them reconstructed (the
+// filter warps wait for that), so they may be read early.
+__device__ void band_intra_row(const H264Launch &P, BandSmem &B, uint8_t *lines, uint8_t *stg, int w, int my,
+                               int lane) {
     WarpSmem &S = B.iw[w];
     uint8_t *Y = P.dpb + (size_t)P.out_slot * P.slot_bytes;
     uint8_t *U = Y + P.u_off, *V = Y + P.v_off;
@@ -1291,6 +1324,49 @@ __device__ void band_intra_row(const H264Launch &P, BandSmem &B, uint8_t *lines,
     uint8_t *ly = lines + (size_t)w * LW, *lu = ly + P.mb_w * 16, *lv = lu + P.mb_w * 8;
     const uint8_t *ay = ly - LW, *au = lu - LW, *av = lv - LW;  // the row above (w > 0)
     volatile int *above = &B.iprog[w], *mine = &B.iprog[w + 1];
+    // the row's intra MBs: lane j holds the bits of MBs 32 j .. 32 j + 31 (rows
+    // of up to 1024 MBs, see rc_h264_band_capacity)
+    const int nwords = (P.mb_w + 31) >> 5;
+    uint32_t word = 0;
+    for (int j0 = 0; j0 < nwords; j0 += 4) {
+        int kinds[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const int xl = (j0 + u) * 32 + lane;
+            kinds[u] = xl < P.mb_w ? __ldg(&P.mbs[my * P.mb_w + xl].kind) : RC_H264_NONE;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const uint32_t b = __ballot_sync(0xffffffffu, wave_intra(kinds[u]));
+            if (lane == j0 + u) word = b;
+        }
+    }
+    auto next_intra = [&](int from) -> int {  // the first intra MB at or after `from`, else mb_w
+        for (int j = from >> 5; j < nwords; j++) {
+            uint32_t b = __shfl_sync(0xffffffffu, word, j);
+            if (j == (from >> 5)) b &= ~0u << (from & 31);
+            if (b) return j * 32 + __ffs(b) - 1;
+        }
+        return P.mb_w;
+    };
+    auto prefetch = [&](int nx) {
+        if (nx < P.mb_w) {
+            const int addr = my * P.mb_w + nx;
+            const uint8_t *q = (const uint8_t *)(P.iinfo + addr), *res = (const uint8_t *)(P.ires + (size_t)addr * 384);
+            // 16-byte chunks 0..1 parameters, 2..49 residual
+            cp_async16(stg + lane * 16, lane < 2 ? q + lane * 16 : res + (lane - 2) * 16);
+            if (lane < 18) cp_async16(stg + (32 + lane) * 16, res + (30 + lane) * 16);
+            if (nx > 0) {
+                const uint8_t *src = lane < 16 ? Y + (size_t)(my * 16 + lane) * P.pitch + nx * 16 - 4
+                                               : ((lane >> 3) & 1 ? V : U) + (size_t)(my * 8 + (lane & 7)) * P.cpitch +
+                                                     nx * 8 - 4;
+                cp_async4(stg + RC_BAND_STG_LEFT + lane * 4, src);
+            }
+        }
+        cp_commit();
+    };
+    int mx = next_intra(0);
+    prefetch(mx);
     {
         const uint32_t *gy = (const uint32_t *)(Y + (size_t)(my * 16 + 15) * P.pitch);
         const uint32_t *gu = (const uint32_t *)(U + (size_t)(my * 8 + 7) * P.cpitch);
@@ -1304,81 +1380,80 @@ __device__ void band_intra_row(const H264Launch &P, BandSmem &B, uint8_t *lines,
         __threadfence_block();
     }
     int last = -2;  // the MB reconstructed last (its right column is still in the canvas)
-    for (int x0 = 0; x0 < P.mb_w; x0 += 32) {
-        const int xl = x0 + lane;
-        const int kind = xl < P.mb_w ? __ldg(&P.mbs[my * P.mb_w + xl].kind) : RC_H264_NONE;
-        uint32_t todo = __ballot_sync(0xffffffffu, wave_intra(kind));
-        while (todo) {
-            const int mx = x0 + __ffs(todo) - 1;
-            todo &= todo - 1;
-            const int addr = my * P.mb_w + mx;
-            // the MBs before mx are reconstructed (inter ones by h264_mb_kernel)
-            if (lane == 0 && *mine < mx) *mine = mx;
-            // prediction parameters and residual (independent of the neighbours)
-            if (lane < 8) ((uint32_t *)&S.q)[lane] = __ldcg((const uint32_t *)(P.iinfo + addr) + lane);
-            {
-                const uint4 *src = (const uint4 *)(P.ires + (size_t)addr * 384);
-                uint4 *dst = (uint4 *)S.res;
-                dst[lane] = __ldcg(src + lane);
-                if (lane < 16) dst[32 + lane] = __ldcg(src + 32 + lane);
-            }
-            // canvas column -1: MB mx-1's right column, from the canvas when this
-            // warp reconstructed it, else from the picture (an inter MB)
+    while (mx < P.mb_w) {
+        const int nx = next_intra(mx + 1);
+        // the MBs before mx are reconstructed (inter ones by h264_mb_kernel)
+        if (lane == 0 && *mine < mx) *mine = mx;
+        // the staged parameters and residual; canvas column -1: MB mx-1's right
+        // column, from the canvas when this warp reconstructed it, else staged
+        cp_wait_all();
+        __syncwarp();
+        {
+            const uint4 *sg = (const uint4 *)stg;
+            uint4 *dq = (uint4 *)&S.q, *dr = (uint4 *)S.res;
+            if (lane < 2) dq[lane] = sg[lane];
+            else dr[lane - 2] = sg[lane];
+            if (lane < 18) dr[30 + lane] = sg[32 + lane];
             if (mx > 0) {
                 const int c = (lane >> 3) & 1, rr = lane & 7;
-                if (last == mx - 1) {
-                    if (lane < 16) S.cy[(lane + 1) * 32] = S.cy[(lane + 1) * 32 + 16];
-                    else S.cc[c][(rr + 1) * 12] = S.cc[c][(rr + 1) * 12 + 8];
-                } else {
-                    if (lane < 16) S.cy[(lane + 1) * 32] = __ldcg(Y + (size_t)(my * 16 + lane) * P.pitch + mx * 16 - 1);
-                    else S.cc[c][(rr + 1) * 12] = __ldcg((c ? V : U) + (size_t)(my * 8 + rr) * P.cpitch + mx * 8 - 1);
-                }
+                const uint8_t v = last == mx - 1 ? (lane < 16 ? S.cy[(lane + 1) * 32 + 16] : S.cc[c][(rr + 1) * 12 + 8])
+                                                 : stg[RC_BAND_STG_LEFT + lane * 4 + 3];
+                if (lane < 16) S.cy[(lane + 1) * 32] = v;
+                else S.cc[c][(rr + 1) * 12] = v;
             }
-            if (my > 0 && !wait_ge(above, min(mx + 2, P.mb_w), P, lane)) { band_fail(P, lane); return; }
-            // canvas row -1: the row above's bottom samples, columns -1..30 (chroma -1..8)
-            if (my > 0) {
-                const int gx = mx * 16 + lane - 1;
-                uint8_t v = 0;
-                if (gx >= 0 && gx < P.W) v = w > 0 ? ay[gx] : __ldcg(Y + (size_t)(my * 16 - 1) * P.pitch + gx);
-                S.cy[lane] = v;
-                if (lane < 20) {
-                    const int c = lane / 10, gxc = mx * 8 + lane % 10 - 1;
-                    uint8_t u = 0;
-                    if (gxc >= 0 && gxc < P.CW)
-                        u = w > 0 ? (c ? av : au)[gxc] : __ldcg((c ? V : U) + (size_t)(my * 8 - 1) * P.cpitch + gxc);
-                    S.cc[c][lane % 10] = u;
-                }
-            }
-            __syncwarp();
-            bool nb[4];
-#pragma unroll
-            for (int n = 0; n < 4; n++) nb[n] = S.q.nb >> n & 1;
-            intra_mb(S, lane, nb, B.tab4, B.tab8);
-            // store the MB; its bottom samples into this row's line
-            {
-                const int r = lane >> 1, half = lane & 1;
-                const uint8_t *q = S.cy + (r + 1) * 32 + 1 + half * 8;
-                const uint32_t lo = q[0] | q[1] << 8 | q[2] << 16 | (uint32_t)q[3] << 24;
-                const uint32_t hi = q[4] | q[5] << 8 | q[6] << 16 | (uint32_t)q[7] << 24;
-                *(uint2 *)(Y + (size_t)(my * 16 + r) * P.pitch + mx * 16 + half * 8) = make_uint2(lo, hi);
-                if (lane < 16) {
-                    const int c = lane >> 3, rr = lane & 7;
-                    const uint8_t *t = S.cc[c] + (rr + 1) * 12 + 1;
-                    const uint32_t a0 = t[0] | t[1] << 8 | t[2] << 16 | (uint32_t)t[3] << 24;
-                    const uint32_t a1 = t[4] | t[5] << 8 | t[6] << 16 | (uint32_t)t[7] << 24;
-                    *(uint2 *)((c ? V : U) + (size_t)(my * 8 + rr) * P.cpitch + mx * 8) = make_uint2(a0, a1);
-                    ly[mx * 16 + lane] = S.cy[16 * 32 + lane + 1];
-                } else {
-                    const int c = (lane >> 3) & 1, i = lane & 7;
-                    (c ? lv : lu)[mx * 8 + i] = S.cc[c][8 * 12 + i + 1];
-                }
-            }
-            last = mx;
-            __syncwarp();
-            __threadfence_block();
-            if (lane == 0) *mine = mx + 1;
         }
+        __syncwarp();
+        prefetch(nx);
+        if (my > 0 && !wait_ge(above, min(mx + 2, P.mb_w), P, lane)) {
+            cp_wait_all();
+            band_fail(P, lane);
+            return;
+        }
+        // canvas row -1: the row above's bottom samples, columns -1..30 (chroma -1..8)
+        if (my > 0) {
+            const int gx = mx * 16 + lane - 1;
+            uint8_t v = 0;
+            if (gx >= 0 && gx < P.W) v = w > 0 ? ay[gx] : __ldcg(Y + (size_t)(my * 16 - 1) * P.pitch + gx);
+            S.cy[lane] = v;
+            if (lane < 20) {
+                const int c = lane / 10, gxc = mx * 8 + lane % 10 - 1;
+                uint8_t u = 0;
+                if (gxc >= 0 && gxc < P.CW)
+                    u = w > 0 ? (c ? av : au)[gxc] : __ldcg((c ? V : U) + (size_t)(my * 8 - 1) * P.cpitch + gxc);
+                S.cc[c][lane % 10] = u;
+            }
+        }
+        __syncwarp();
+        bool nb[4];
+#pragma unroll
+        for (int n = 0; n < 4; n++) nb[n] = S.q.nb >> n & 1;
+        intra_mb(S, lane, nb, B.tab4, B.tab8);
+        // store the MB; its bottom samples into this row's line
+        {
+            const int r = lane >> 1, half = lane & 1;
+            const uint8_t *q = S.cy + (r + 1) * 32 + 1 + half * 8;
+            const uint32_t lo = q[0] | q[1] << 8 | q[2] << 16 | (uint32_t)q[3] << 24;
+            const uint32_t hi = q[4] | q[5] << 8 | q[6] << 16 | (uint32_t)q[7] << 24;
+            *(uint2 *)(Y + (size_t)(my * 16 + r) * P.pitch + mx * 16 + half * 8) = make_uint2(lo, hi);
+            if (lane < 16) {
+                const int c = lane >> 3, rr = lane & 7;
+                const uint8_t *t = S.cc[c] + (rr + 1) * 12 + 1;
+                const uint32_t a0 = t[0] | t[1] << 8 | t[2] << 16 | (uint32_t)t[3] << 24;
+                const uint32_t a1 = t[4] | t[5] << 8 | t[6] << 16 | (uint32_t)t[7] << 24;
+                *(uint2 *)((c ? V : U) + (size_t)(my * 8 + rr) * P.cpitch + mx * 8) = make_uint2(a0, a1);
+                ly[mx * 16 + lane] = S.cy[16 * 32 + lane + 1];
+            } else {
+                const int c = (lane >> 3) & 1, i = lane & 7;
+                (c ? lv : lu)[mx * 8 + i] = S.cc[c][8 * 12 + i + 1];
+            }
+        }
+        last = mx;
+        __syncwarp();
+        __threadfence_block();
+        if (lane == 0) *mine = mx + 1;
+        mx = nx;
     }
+    cp_wait_all();
     __syncwarp();
     if (lane == 0) *mine = P.mb_w;
 }
@@ -1674,7 +1749,9 @@ __device__ void band_helper(const H264Launch &P, BandSmem &B, int y0, int rows, 
 
 __global__ void __launch_bounds__(BAND_THREADS, 1) h264_band_kernel(H264Launch P) {
     __shared__ BandSmem B;
-    extern __shared__ __align__(16) uint8_t band_lines[];  // BR rows x mb_w x 32 bytes
+    // dynamic: per band row the intra warp's staging (RC_BAND_STG bytes), then
+    // per band row its line of bottom samples (mb_w x 32 bytes)
+    extern __shared__ __align__(16) uint8_t band_dyn[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int y0 = blockIdx.x * BR, rows = min(BR, P.mb_h - y0);
     for (int i = threadIdx.x; i < 9 * 16; i += blockDim.x) B.tab4[i] = (&cPRED4.e[0][0])[i];
@@ -1688,7 +1765,7 @@ __global__ void __launch_bounds__(BAND_THREADS, 1) h264_band_kernel(H264Launch P
     if (warp == 3 * BR) { band_helper(P, B, y0, rows, lane); return; }
     const int role = warp / BR, w = warp % BR;
     if (w >= rows) return;
-    if (role == 0) band_intra_row(P, B, band_lines, w, y0 + w, lane);
+    if (role == 0) band_intra_row(P, B, band_dyn + BR * RC_BAND_STG, band_dyn + w * RC_BAND_STG, w, y0 + w, lane);
     else if (role == 1) band_luma_row(P, B, w, y0 + w, rows, lane);
     else band_chroma_row(P, B, w, y0 + w, rows, lane);
 }
@@ -1699,7 +1776,7 @@ void rc_launch_h264_mb(const H264Launch &p, cudaStream_t st) {
     h264_mb_kernel<<<p.mb_w * p.mb_h, 256, 0, st>>>(p);
 }
 
-size_t rc_h264_band_smem(int mb_w) { return (size_t)BR * mb_w * 32; }
+size_t rc_h264_band_smem(int mb_w) { return (size_t)BR * (RC_BAND_STG + (size_t)mb_w * 32); }
 
 // The kernel's dynamic shared-memory limit is one attribute for every stream
 // of the process: raise it to the widest picture any stream needs (never
@@ -1724,6 +1801,7 @@ int rc_h264_band_capacity(int mb_w) {
     int dev = 0, sms = 0, per = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (mb_w <= 0 || mb_w > 1024) return 0;  // the intra warps' row bitmaps
     const size_t dyn = rc_h264_band_smem(mb_w);
     if (!band_smem_attr(dyn)) return 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, h264_band_kernel, BAND_THREADS, dyn) != cudaSuccess)
