@@ -115,7 +115,11 @@ void rc_launch_hevc_sao(const HevcLaunch &p, cudaStream_t st);
 void rc_launch_h264_mb(const H264Launch &p, cudaStream_t st);
 // Intra reconstruction and the loop filter in one cooperative launch, one
 // CTA per band of RC_H264_BAND_ROWS MB rows; returns 0 or -1 (launch failed).
-#define RC_H264_BAND_ROWS 7
+// Four rows per band: more rows share one SM's issue slots among more busy
+// warps, fewer put more hand-overs through global memory on the critical
+// path (1080p P+I sequence on GB300: 7 rows 1237, 5 1350, 4 1395, 3 1396,
+// 2 1340, 1 1033 frames/s).
+#define RC_H264_BAND_ROWS 4
 int rc_launch_h264_band(const H264Launch &p, cudaStream_t st);
 // Band CTAs that can be resident at once for pictures mb_w MBs wide (0 if
 // unknown); the band kernel's dynamic shared memory for that width.
