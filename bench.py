@@ -78,7 +78,7 @@ class H264Workload:
     crop = (0, 0, 1920, 1080)
     description = ("h264_1080p_plain: 1920x1080 High 8-bit 4:2:0, 120 frames, I then P with 2 refs, 30% intra, "
                    "20% explicit WP, 80% zero blocks, QP 20-40, deblocking on")
-    kernels = {0: ("h264_mb_kernel", "mb"), 1: ("h264_band_kernel", "band")}
+    kernels = {2: ("h264_edge_kernel", "edge"), 0: ("h264_mb_kernel", "mb"), 1: ("h264_band_kernel", "band")}
     buffer_keys = ("mbs", "slices", "weights", "levels")
 
     def __init__(self, E, frames=None):
@@ -125,14 +125,17 @@ class H264Workload:
         out_frame = self.MB_W * 16 * self.MB_H * 16 * 3 // 2
         n = len(kind)
         edges = 256  # loop-filter edge words per MB
-        # h264_mb_kernel: every record (176 B) and its left/top neighbours' (L2), its
-        # levels, the edge words out; inter/PCM samples out with their reference
-        # samples in; intra MBs' residuals (768 B) and parameters (32 B) out
-        mb = int(n * (176 + edges) + lv_bytes.sum() + mbk.sum() * 384 + ref_bytes + intra.sum() * (768 + 32))
+        # h264_edge_kernel: every record (176 B; its left/top neighbours' come
+        # from L2) in, the edge words out
+        edge = int(n * (176 + edges))
+        # h264_mb_kernel: every record and its levels in; inter/PCM samples out
+        # with their reference samples in; intra MBs' residuals (768 B) and
+        # parameters (32 B) out
+        mb = int(n * 176 + lv_bytes.sum() + mbk.sum() * 384 + ref_bytes + intra.sum() * (768 + 32))
         # h264_band_kernel: intra MBs' parameters and residuals in; the picture
         # read and written once by the loop filter with the edge words in
         band = int(intra.sum() * (32 + 768) + 2 * out_frame + n * edges)
-        return {"mb": mb, "band": band, "job": out_frame + ref_bytes + p.nbytes, "syntax": p.nbytes}
+        return {"edge": edge, "mb": mb, "band": band, "job": out_frame + ref_bytes + p.nbytes, "syntax": p.nbytes}
 
     def oracle_dpb(self, O):
         return O.H264Dpb(self.MB_W, self.MB_H, self.slots)

@@ -357,6 +357,7 @@ int rc_picture_device_planes(rc_stream *s, int slot, void **y, void **u,
  * profiling was enabled; returns the number of kernel ids filled. */
 #define RC_KERNEL_H264_MB 0
 #define RC_KERNEL_H264_BAND 1
+#define RC_KERNEL_H264_EDGE 2
 #define RC_KERNEL_HEVC_RESIDUAL 3
 #define RC_KERNEL_HEVC_INTER 4
 #define RC_KERNEL_HEVC_INTRA 5

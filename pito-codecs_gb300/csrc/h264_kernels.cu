@@ -211,6 +211,33 @@ __device__ void compute_db(const H264Launch &P, const rc_h264_mb &q, const rc_h2
 __device__ void edge_words(const DbMb &d, int lane, uint32_t *out);
 
 // ===========================================================================
+// Kernel 0: the loop filter's parameters of every MB -- boundary strengths,
+// QPs, alpha / beta / tc0 -- as the 64 edge words the band kernel's filter
+// warps read (deblock.rs:7-124, 302-371).  One warp per MB: the derivation
+// is a short serial chain per MB, so all MBs of a picture are in flight at
+// once instead of holding up the CTA of h264_mb_kernel.
+// ===========================================================================
+constexpr int EDGE_MBS = 8;  // MBs (warps) per CTA
+__global__ void __launch_bounds__(32 * EDGE_MBS) h264_edge_kernel(H264Launch P) {
+    __shared__ __align__(16) rc_h264_mb rec[EDGE_MBS][3];  // the MB, its left and top neighbours
+    __shared__ DbMb dbm[EDGE_MBS];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int addr = blockIdx.x * EDGE_MBS + w;
+    if (addr >= P.mb_w * P.mb_h) return;  // whole warps only
+    const int mbx = addr % P.mb_w, mby = addr / P.mb_w;
+    constexpr int RW = (int)(sizeof(rc_h264_mb) / 4);
+    for (int i = lane; i < 3 * RW; i += 32) {
+        const int which = i / RW, j = i - which * RW;
+        const int src = which == 0 ? addr : which == 1 ? (mbx > 0 ? addr - 1 : -1) : (mby > 0 ? addr - P.mb_w : -1);
+        if (src >= 0) ((uint32_t *)&rec[w][which])[j] = __ldg((const uint32_t *)(P.mbs + src) + j);
+    }
+    __syncwarp();
+    compute_db(P, rec[w][0], rec[w][1], rec[w][2], addr, lane, &dbm[w]);
+    __syncwarp();
+    edge_words(dbm[w], lane, P.edges + (size_t)addr * RC_EDGE_WORDS);
+}
+
+// ===========================================================================
 // Kernel 1: inter MBs (prediction + residual) and I_PCM, one CTA per MB.
 // ===========================================================================
 __global__ void __launch_bounds__(256) h264_mb_kernel(H264Launch P) {
@@ -219,27 +246,15 @@ __global__ void __launch_bounds__(256) h264_mb_kernel(H264Launch P) {
     __shared__ int32_t coefc[128];
     __shared__ uint8_t predy[256];
     __shared__ uint8_t predc[128];
-    __shared__ __align__(16) rc_h264_mb nbr[2];  // left, top (loop-filter parameters)
     __shared__ uint32_t nzl, nzc;
     const int t = threadIdx.x, addr = blockIdx.x;
     const int mbx = addr % P.mb_w, mby = addr / P.mb_w;
     constexpr int RW = (int)(sizeof(rc_h264_mb) / 4);
     if (t < RW) ((uint32_t *)&m)[t] = __ldg((const uint32_t *)(P.mbs + addr) + t);
-    else if (t < 2 * RW) {
-        if (mbx > 0) ((uint32_t *)&nbr[0])[t - RW] = __ldg((const uint32_t *)(P.mbs + addr - 1) + t - RW);
-    } else if (t < 3 * RW) {
-        if (mby > 0) ((uint32_t *)&nbr[1])[t - 2 * RW] = __ldg((const uint32_t *)(P.mbs + addr - P.mb_w) + t - 2 * RW);
-    }
     if (t == 0) { nzl = 0; nzc = 0; }
     coef[t] = 0;
     if (t < 128) coefc[t] = 0;
     __syncthreads();
-    if (t < 32) {
-        __shared__ DbMb dbm;
-        compute_db(P, m, nbr[0], nbr[1], addr, t, &dbm);
-        __syncwarp();
-        edge_words(dbm, t, P.edges + (size_t)addr * RC_EDGE_WORDS);
-    }
     const int kind = m.kind;
     if (kind == RC_H264_NONE || kind > RC_H264_INTER) return;
     uint8_t *Y = P.dpb + (size_t)P.out_slot * P.slot_bytes;
@@ -1771,6 +1786,11 @@ __global__ void __launch_bounds__(BAND_THREADS, 1) h264_band_kernel(H264Launch P
 }
 
 }  // namespace
+
+void rc_launch_h264_edge(const H264Launch &p, cudaStream_t st) {
+    const int n = p.mb_w * p.mb_h;
+    h264_edge_kernel<<<(n + EDGE_MBS - 1) / EDGE_MBS, 32 * EDGE_MBS, 0, st>>>(p);
+}
 
 void rc_launch_h264_mb(const H264Launch &p, cudaStream_t st) {
     h264_mb_kernel<<<p.mb_w * p.mb_h, 256, 0, st>>>(p);

@@ -562,6 +562,7 @@ int rc_h264_submit(rc_stream *s, const rc_h264_picture *pic, int out_slot) {
     L.irowprog = s->irowprog;
     L.iinfo = s->iinfo;
     L.ires = s->ires;
+    timed(s, RC_KERNEL_H264_EDGE, [&] { rc_launch_h264_edge(L, s->st); });
     timed(s, RC_KERNEL_H264_MB, [&] { rc_launch_h264_mb(L, s->st); });
     int lrc = 0;
     timed(s, RC_KERNEL_H264_BAND, [&] { lrc = rc_launch_h264_band(L, s->st); });

@@ -112,6 +112,7 @@ void rc_launch_hevc_deblock(const HevcLaunch &p, cudaStream_t st);
 void rc_launch_hevc_sao(const HevcLaunch &p, cudaStream_t st);
 
 // Launchers (h264_kernels.cu).
+void rc_launch_h264_edge(const H264Launch &p, cudaStream_t st);
 void rc_launch_h264_mb(const H264Launch &p, cudaStream_t st);
 // Intra reconstruction and the loop filter in one cooperative launch, one
 // CTA per band of RC_H264_BAND_ROWS MB rows; returns 0 or -1 (launch failed).

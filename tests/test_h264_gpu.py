@@ -136,9 +136,9 @@ def test_launch_count_and_profile(engine):
         p = engine.SynthH264(seed=3, mb_w=4, mb_h=4, intra_only=1)
         n0 = st.launches()
         st.submit_h264(p, 0)
-        assert st.launches() - n0 == 2
+        assert st.launches() - n0 == 3  # edge words, MB kernel, band kernel
         prof = st.profile_read()
-        assert all(prof[k][1] == 1 for k in (0, 1)) and prof[1][0] > 0
+        assert all(prof[k][1] == 1 for k in (0, 1, 2)) and prof[1][0] > 0
 
 
 def test_streams_of_different_widths_coexist(engine, oracle):
