@@ -79,6 +79,9 @@ __device__ __forceinline__ uint32_t ld_acquire(const uint32_t *p) {
 __device__ __forceinline__ void st_release(uint32_t *p, uint32_t v) {
     asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
+__device__ __forceinline__ void st_relaxed(uint32_t *p, uint32_t v) {
+    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
 __device__ __forceinline__ bool aborted(const uint32_t *err) {
     return (*(const volatile uint32_t *)err & RC_DEV_ERR_TIMEOUT) != 0;
 }
@@ -1176,12 +1179,15 @@ __global__ void __launch_bounds__(128) h264_db_params_kernel(H264Launch P) {
 //
 // Order (every wait is capped, see wait_ge):
 //   intra MB (x, y)    after intra row y-1 has reconstructed MBs 0..x+1;
-//   filter MB (x, y)   after rows y and y+1 have reconstructed MBs 0..x+2 and
-//                      0..x+1 (every intra MB that reads samples this step
-//                      changes, and MB x+2, which the step prefetches); its
-//                      horizontal edges, which read MB (x, y-1), also after
-//                      row y-1 has filtered MB x+1's vertical edges (the last
-//                      change to MB (x, y-1)) and stored MBs 0..x.
+//   filter MB (x, y)   after row y has reconstructed MBs 0..x+2 (every intra
+//                      MB whose samples the step reads or changes, and MB
+//                      x+2, which the step prefetches) and, for a band's last
+//                      row, row y+1 MBs 0..x+1 (the next band's intra warps
+//                      read row y's unfiltered samples from the picture;
+//                      inside a band they read the intra warp's line copy);
+//                      its horizontal edges, which read MB (x, y-1), also
+//                      after row y-1 has filtered MB x+1's vertical edges
+//                      (the last change to MB (x, y-1)) and stored MBs 0..x.
 // A filter row stores MB x-1 once MB x's left edge is filtered (its last
 // change in the row) and publishes its progress there, before MB x's
 // horizontal edges, and stores the three rows above MB x after MB x's top
@@ -1480,7 +1486,10 @@ __device__ void band_luma_row(const H264Launch &P, BandSmem &B, int w, int my, i
     uint8_t *Y = P.dpb + (size_t)P.out_slot * P.slot_bytes;
     const bool act = lane < 16;
     const int r = lane & 15, k = r >> 2;
-    const bool below = my + 1 < P.mb_h, ring_out = w + 1 < rows;
+    // the row below reads this row's unfiltered samples from the picture
+    // only when it starts the next band (inside a band it reads the intra
+    // warp's line copy), so only then must the filter wait for its intra
+    const bool below = w + 1 == rows && my + 1 < P.mb_h, ring_out = w + 1 < rows;
     volatile int *iown = &B.iprog[w + 1], *ibelow = &B.iprog[w + 2];
     volatile int *dup = &B.lprog[w], *dmine = &B.lprog[w + 1], *ddown = &B.lprog[min(w + 2, BR)];
     const uint4 *E = (const uint4 *)(P.edges + (size_t)my * P.mb_w * RC_EDGE_WORDS);
@@ -1607,7 +1616,10 @@ __device__ void band_chroma_row(const H264Launch &P, BandSmem &B, int w, int my,
     const bool act = lane < 16;
     const int c = (lane >> 3) & 1, r = lane & 7, k = r >> 1;
     uint8_t *Cp = Y + (c ? P.v_off : P.u_off);
-    const bool below = my + 1 < P.mb_h, ring_out = w + 1 < rows;
+    // the row below reads this row's unfiltered samples from the picture
+    // only when it starts the next band (inside a band it reads the intra
+    // warp's line copy), so only then must the filter wait for its intra
+    const bool below = w + 1 == rows && my + 1 < P.mb_h, ring_out = w + 1 < rows;
     volatile int *iown = &B.iprog[w + 1], *ibelow = &B.iprog[w + 2];
     volatile int *dup = &B.cprog[w], *dmine = &B.cprog[w + 1], *ddown = &B.cprog[min(w + 2, BR)];
     const uint2 *E = (const uint2 *)(P.edges + (size_t)my * P.mb_w * RC_EDGE_WORDS);
@@ -1717,7 +1729,7 @@ __device__ void band_chroma_row(const H264Launch &P, BandSmem &B, int w, int my,
 
 // Helper warp: lanes 0..2 mirror the progress of the neighbouring bands'
 // rows (global, acquire) into shared memory; lanes 3..5 publish this band's
-// boundary rows (release).  Each lane runs its own loop.
+// boundary rows (a fence, then the flag).  Each lane runs its own loop.
 __device__ void band_helper(const H264Launch &P, BandSmem &B, int y0, int rows, int lane) {
     const uint32_t tag = (P.epoch & 0xffffu) << 16;
     const bool above = y0 > 0, below = y0 + rows < P.mb_h;
@@ -1748,8 +1760,12 @@ __device__ void band_helper(const H264Launch &P, BandSmem &B, int y0, int rows, 
                 else if (lane == 1) B.iprog[0] = seen;
                 else B.iprog[rows + 1] = seen;
             } else {
+                // the fence orders every store the band's warps made before
+                // the progress this lane read (they fenced before publishing
+                // it in shared memory) ahead of the flag; the flag itself can
+                // then be relaxed (a release store costs about a fence more)
                 __threadfence();
-                st_release(dst, tag | (uint32_t)seen);
+                st_relaxed(dst, tag | (uint32_t)seen);
             }
             it = 0;
             continue;
@@ -1758,7 +1774,7 @@ __device__ void band_helper(const H264Launch &P, BandSmem &B, int y0, int rows, 
             set_error(P.error, RC_DEV_ERR_TIMEOUT);
             return;
         }
-        __nanosleep(src ? 256 : 64);
+        __nanosleep(32);
     }
 }
 
