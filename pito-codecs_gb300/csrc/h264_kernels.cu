@@ -1516,6 +1516,17 @@ __device__ void band_luma_row(const H264Launch &P, BandSmem &B, int w, int my, i
         if (w > 0) return *(const uint4 *)(B.l[w - 1].ring[x % DRING] + lane * 16);
         return __ldcg((const uint4 *)(Y + (size_t)(my * 16 - 4 + lane) * P.pitch + x * 16));
     };
+    // a band's first row: load MB x+1's top rows as soon as the row above has
+    // stored MB x+1 (checked at several points of step x), so that the load
+    // overlaps work instead of stalling the horizontal edges of step x+1
+    auto try_next = [&](int x) {
+        if (w == 0 && my > 0 && !have_next && x + 1 < P.mb_w &&
+            __shfl_sync(0xffffffffu, *dup >= x + 2 ? 1 : 0, 0)) {
+            __threadfence_block();
+            t4n = top_rows(x + 1);
+            have_next = true;
+        }
+    };
     if (!wait_ge(iown, min(2, P.mb_w), P, lane)) { band_fail(P, lane); return; }
     stage(0);
     stage(1);
@@ -1523,6 +1534,7 @@ __device__ void band_luma_row(const H264Launch &P, BandSmem &B, int w, int my, i
         if (!wait_ge(iown, min(x + 3, P.mb_w), P, lane)) { band_fail(P, lane); return; }
         if (below && !wait_ge(ibelow, min(x + 2, P.mb_w), P, lane)) { band_fail(P, lane); return; }
         stage(x + 2);
+        try_next(x - 1);
         cp_wait_all_but_1();
         const int sl = x % 3;
         const uint4 cur = act ? R.st[sl][0][r] : z4, pv = act ? R.st[sl][1][r] : z4,
@@ -1565,11 +1577,7 @@ __device__ void band_luma_row(const H264Launch &P, BandSmem &B, int w, int my, i
             if (!wait_ge(dup, x + 1, P, lane)) { band_fail(P, lane); return; }
             const uint4 t4 = (w == 0 && have_next) ? t4n : top_rows(x);
             have_next = false;
-            if (w == 0 && x + 1 < P.mb_w && __shfl_sync(0xffffffffu, *dup >= x + 2 ? 1 : 0, 0)) {
-                __threadfence_block();
-                t4n = top_rows(x + 1);
-                have_next = true;
-            }
+            try_next(x);
             if (lane < 4) *(uint4 *)R.t[lane] = t4;
         }
         __syncwarp();
@@ -1645,6 +1653,15 @@ __device__ void band_chroma_row(const H264Launch &P, BandSmem &B, int w, int my,
         if (w > 0) return *(const uint2 *)(B.c[w - 1].ring[x % DRING] + cc * 16 + rr * 8);
         return __ldcg((const uint2 *)(Y + (cc ? P.v_off : P.u_off) + (size_t)(my * 8 - 2 + rr) * P.cpitch + x * 8));
     };
+    // a band's first row: MB x+1's top rows as early as the row above allows
+    auto try_next = [&](int x) {
+        if (w == 0 && my > 0 && !have_next && x + 1 < P.mb_w &&
+            __shfl_sync(0xffffffffu, *dup >= x + 2 ? 1 : 0, 0)) {
+            __threadfence_block();
+            t2n = top_rows(x + 1);
+            have_next = true;
+        }
+    };
     if (!wait_ge(iown, min(2, P.mb_w), P, lane)) { band_fail(P, lane); return; }
     stage(0);
     stage(1);
@@ -1652,6 +1669,7 @@ __device__ void band_chroma_row(const H264Launch &P, BandSmem &B, int w, int my,
         if (!wait_ge(iown, min(x + 3, P.mb_w), P, lane)) { band_fail(P, lane); return; }
         if (below && !wait_ge(ibelow, min(x + 2, P.mb_w), P, lane)) { band_fail(P, lane); return; }
         stage(x + 2);
+        try_next(x - 1);
         cp_wait_all_but_1();
         const int sl = x % 3;
         const uint2 cur = act ? R.st[sl][0][lane] : z2, pv = act ? R.st[sl][1][lane] : z2,
@@ -1688,11 +1706,7 @@ __device__ void band_chroma_row(const H264Launch &P, BandSmem &B, int w, int my,
             if (!wait_ge(dup, x + 1, P, lane)) { band_fail(P, lane); return; }
             const uint2 t2 = (w == 0 && have_next) ? t2n : top_rows(x);
             have_next = false;
-            if (w == 0 && x + 1 < P.mb_w && __shfl_sync(0xffffffffu, *dup >= x + 2 ? 1 : 0, 0)) {
-                __threadfence_block();
-                t2n = top_rows(x + 1);
-                have_next = true;
-            }
+            try_next(x);
             if (lane < 4) *(uint2 *)R.t[lane >> 1][lane & 1] = t2;
         }
         __syncwarp();
