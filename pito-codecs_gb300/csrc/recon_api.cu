@@ -77,6 +77,8 @@ struct rc_stream {
     DevBuf mbs, slices, weights, levels;
     int32_t *ls = nullptr;            // device ls4 (2304 ints) + ls8 (2304*4 ints)
     std::vector<int32_t> ls_host;     // last uploaded tables
+    uint8_t ls_key[2 + 96 + 384] = {0};  // the scaling lists they were made from (flat: flag 0)
+    std::vector<uint8_t> scal_host;      // HEVC: the scaling factors last uploaded
     bool ls_valid = false;
     void *staging[2] = {nullptr, nullptr};
     size_t staging_cap[2] = {0, 0};
@@ -499,10 +501,17 @@ int rc_h264_submit(rc_stream *s, const rc_h264_picture *pic, int out_slot) {
     // landed.  Its source, ls_host, lives until the next change, which first
     // waits for the stream.
     {
-        std::vector<int32_t> ls(2304 + 2304 * 4);
-        h264_level_scale(pic->scaling4, pic->scaling8, ls.data(), ls.data() + 2304);
-        if (!s->ls_valid || ls != s->ls_host) {
+        // compare the scaling lists (480 bytes), not the tables made from them
+        uint8_t key[sizeof s->ls_key] = {0};
+        key[0] = pic->scaling4 != nullptr;
+        key[1] = pic->scaling8 != nullptr;
+        if (pic->scaling4) memcpy(key + 2, pic->scaling4, 96);
+        if (pic->scaling8) memcpy(key + 2 + 96, pic->scaling8, 384);
+        if (!s->ls_valid || memcmp(key, s->ls_key, sizeof key) != 0) {
+            std::vector<int32_t> ls(2304 + 2304 * 4);
+            h264_level_scale(pic->scaling4, pic->scaling8, ls.data(), ls.data() + 2304);
             if (cudaStreamSynchronize(s->st) != cudaSuccess) return cuda_fail(s);
+            memcpy(s->ls_key, key, sizeof key);
             s->ls_host.swap(ls);
             if (cudaMemcpyAsync(s->ls, s->ls_host.data(), s->ls_host.size() * sizeof(int32_t), cudaMemcpyHostToDevice,
                                 s->st) != cudaSuccess) {
@@ -591,9 +600,16 @@ int rc_hevc_submit(rc_stream *s, const rc_hevc_picture *pic, int out_slot) {
     const size_t b_scal = 6 * (16 + 64 + 256 + 1024);
     HevcLaunch L;
     memset(&L, 0, sizeof L);
-    if (pic->scaling) {  // scaling factors are host memory in both modes
-        Part sp{&s->scaling, pic->scaling, b_scal};
-        if ((rc = upload(s, &sp, 1)) != 0) return rc;
+    if (pic->scaling) {  // scaling factors are host memory in both modes; uploaded when they change
+        const uint8_t *sf = (const uint8_t *)pic->scaling;
+        if (s->scal_host.size() != b_scal || memcmp(s->scal_host.data(), sf, b_scal) != 0) {
+            Part sp{&s->scaling, pic->scaling, b_scal};
+            if ((rc = upload(s, &sp, 1)) != 0) {
+                s->scal_host.clear();
+                return rc;
+            }
+            s->scal_host.assign(sf, sf + b_scal);
+        }
         L.scaling = (const uint8_t *)s->scaling.p;
     }
     if (pic->mem == RC_MEM_HOST) {
