@@ -1175,7 +1175,7 @@ __global__ void __launch_bounds__(128) h264_db_params_kernel(H264Launch P) {
 // (reconstruct_intra of the row's intra MBs), a luma and a chroma loop-filter
 // warp (deblock_mb: an MB's vertical edges, then its horizontal edges).  Rows
 // of a band hand over through shared memory, bands through per-row progress
-// words in global memory that the band's helper warp mirrors and publishes.
+// words in global memory that the band's two helper warps mirror and publish.
 //
 // Order (every wait is capped, see wait_ge):
 //   intra MB (x, y)    after intra row y-1 has reconstructed MBs 0..x+1;
@@ -1195,7 +1195,7 @@ __global__ void __launch_bounds__(128) h264_db_params_kernel(H264Launch P) {
 // ===========================================================================
 constexpr int BR = RC_H264_BAND_ROWS;
 constexpr int DRING = 8;  // ring slots between filter rows of a band
-constexpr int BAND_THREADS = (3 * BR + 1) * 32;
+constexpr int BAND_THREADS = (3 * BR + 2) * 32;  // intra, luma, chroma per row; mirror and publish warps
 // an intra warp's staging: parameters (32 B) and residual (768 B), then one
 // 4-byte word per lane holding the next MB's column -1 sample (luma rows
 // 0..15, Cb rows 0..7, Cr rows 0..7)
@@ -1207,11 +1207,13 @@ struct __align__(16) LumaRow {
     uint8_t t[20][16];        // rows -4..15 of the MB being filtered (horizontal edges)
     uint8_t ring[DRING][64];  // final rows 12..15 of this row's MBs, for the row below
     uint4 st[3][3][16];       // staged MBs x..x+2 (slot x % 3): sample rows, vertical and horizontal edge words
+    uint8_t tn[2][4][16];     // a band's first row: the next MB's rows -4..-1 (slot x & 1), copied ahead
 };
 struct __align__(16) ChromaRow {
     uint8_t t[2][10][8];      // per component, rows -2..7
     uint8_t ring[DRING][32];  // final rows 6..7 per component, for the row below
     uint2 st[3][3][16];       // staged MBs, as LumaRow::st
+    uint8_t tn[2][4][16];     // a band's first row: the 16-byte chunks holding the next MB's rows -2..-1
 };
 struct __align__(16) BandSmem {
     uint32_t tab4[9 * 16];  // copies of cPRED4 / cPRED8
@@ -1509,21 +1511,23 @@ __device__ void band_luma_row(const H264Launch &P, BandSmem &B, int w, int my, i
     // rows -4..-1 of MB x: the row above's ring, or (first row of a band) the
     // picture; for the latter the next MB's rows are loaded one step early
     // when the row above is already far enough
-    uint4 t4n = z4;
     bool have_next = false;
     auto top_rows = [&](int x) -> uint4 {
         if (my == 0 || lane >= 4) return z4;
         if (w > 0) return *(const uint4 *)(B.l[w - 1].ring[x % DRING] + lane * 16);
         return __ldcg((const uint4 *)(Y + (size_t)(my * 16 - 4 + lane) * P.pitch + x * 16));
     };
-    // a band's first row: load MB x+1's top rows as soon as the row above has
-    // stored MB x+1 (checked at several points of step x), so that the load
-    // overlaps work instead of stalling the horizontal edges of step x+1
+    // a band's first row: copy MB x+1's top rows into shared memory as soon
+    // as the row above has stored MB x+1, with cp.async, whose group the next
+    // step's cp_wait_all_but_1 completes (a register load here stalled the
+    // warp until it returned); the group precedes that step's stage group
     auto try_next = [&](int x) {
         if (w == 0 && my > 0 && !have_next && x + 1 < P.mb_w &&
             __shfl_sync(0xffffffffu, *dup >= x + 2 ? 1 : 0, 0)) {
             __threadfence_block();
-            t4n = top_rows(x + 1);
+            if (lane < 4)
+                cp_async16(&R.tn[(x + 1) & 1][lane][0], Y + (size_t)(my * 16 - 4 + lane) * P.pitch + (x + 1) * 16);
+            cp_commit();
             have_next = true;
         }
     };
@@ -1533,8 +1537,8 @@ __device__ void band_luma_row(const H264Launch &P, BandSmem &B, int w, int my, i
     for (int x = 0; x < P.mb_w; x++) {
         if (!wait_ge(iown, min(x + 3, P.mb_w), P, lane)) { band_fail(P, lane); return; }
         if (below && !wait_ge(ibelow, min(x + 2, P.mb_w), P, lane)) { band_fail(P, lane); return; }
-        stage(x + 2);
         try_next(x - 1);
+        stage(x + 2);
         cp_wait_all_but_1();
         const int sl = x % 3;
         const uint4 cur = act ? R.st[sl][0][r] : z4, pv = act ? R.st[sl][1][r] : z4,
@@ -1575,7 +1579,7 @@ __device__ void band_luma_row(const H264Launch &P, BandSmem &B, int w, int my, i
         // MB x+1's vertical edges
         if (my > 0) {
             if (!wait_ge(dup, x + 1, P, lane)) { band_fail(P, lane); return; }
-            const uint4 t4 = (w == 0 && have_next) ? t4n : top_rows(x);
+            const uint4 t4 = (w == 0 && have_next) ? *(const uint4 *)&R.tn[x & 1][lane & 3][0] : top_rows(x);
             have_next = false;
             try_next(x);
             if (lane < 4) *(uint4 *)R.t[lane] = t4;
@@ -1645,7 +1649,6 @@ __device__ void band_chroma_row(const H264Launch &P, BandSmem &B, int w, int my,
     // rows -2..-1 of MB x per component (lanes 0..3: component lane >> 1, row
     // lane & 1): the row above's ring, or (first row of a band) the picture,
     // the next MB's one step early when the row above is far enough
-    uint2 t2n = z2;
     bool have_next = false;
     auto top_rows = [&](int x) -> uint2 {
         if (my == 0 || lane >= 4) return z2;
@@ -1653,12 +1656,17 @@ __device__ void band_chroma_row(const H264Launch &P, BandSmem &B, int w, int my,
         if (w > 0) return *(const uint2 *)(B.c[w - 1].ring[x % DRING] + cc * 16 + rr * 8);
         return __ldcg((const uint2 *)(Y + (cc ? P.v_off : P.u_off) + (size_t)(my * 8 - 2 + rr) * P.cpitch + x * 8));
     };
-    // a band's first row: MB x+1's top rows as early as the row above allows
+    // a band's first row: MB x+1's top rows copied ahead, as for luma (the
+    // 16-byte aligned chunk holding the MB's 8 bytes: cp.async from L2)
     auto try_next = [&](int x) {
         if (w == 0 && my > 0 && !have_next && x + 1 < P.mb_w &&
             __shfl_sync(0xffffffffu, *dup >= x + 2 ? 1 : 0, 0)) {
             __threadfence_block();
-            t2n = top_rows(x + 1);
+            if (lane < 4)
+                cp_async16(&R.tn[(x + 1) & 1][lane][0], Y + ((lane >> 1) ? P.v_off : P.u_off) +
+                                                            (size_t)(my * 8 - 2 + (lane & 1)) * P.cpitch +
+                                                            ((x + 1) & ~1) * 8);
+            cp_commit();
             have_next = true;
         }
     };
@@ -1668,8 +1676,8 @@ __device__ void band_chroma_row(const H264Launch &P, BandSmem &B, int w, int my,
     for (int x = 0; x < P.mb_w; x++) {
         if (!wait_ge(iown, min(x + 3, P.mb_w), P, lane)) { band_fail(P, lane); return; }
         if (below && !wait_ge(ibelow, min(x + 2, P.mb_w), P, lane)) { band_fail(P, lane); return; }
-        stage(x + 2);
         try_next(x - 1);
+        stage(x + 2);
         cp_wait_all_but_1();
         const int sl = x % 3;
         const uint2 cur = act ? R.st[sl][0][lane] : z2, pv = act ? R.st[sl][1][lane] : z2,
@@ -1704,7 +1712,7 @@ __device__ void band_chroma_row(const H264Launch &P, BandSmem &B, int w, int my,
         // row above past MB x+1's vertical edges
         if (my > 0) {
             if (!wait_ge(dup, x + 1, P, lane)) { band_fail(P, lane); return; }
-            const uint2 t2 = (w == 0 && have_next) ? t2n : top_rows(x);
+            const uint2 t2 = (w == 0 && have_next) ? *(const uint2 *)&R.tn[x & 1][lane & 3][(x & 1) * 8] : top_rows(x);
             have_next = false;
             try_next(x);
             if (lane < 4) *(uint2 *)R.t[lane >> 1][lane & 1] = t2;
@@ -1741,52 +1749,73 @@ __device__ void band_chroma_row(const H264Launch &P, BandSmem &B, int w, int my,
     if (lane == 0) *dmine = P.mb_w;
 }
 
-// Helper warp: lanes 0..2 mirror the progress of the neighbouring bands'
-// rows (global, acquire) into shared memory; lanes 3..5 publish this band's
-// boundary rows (a fence, then the flag).  Each lane runs its own loop.
-__device__ void band_helper(const H264Launch &P, BandSmem &B, int y0, int rows, int lane) {
+// The hand-over to the neighbouring bands runs on two helper warps whose
+// lanes poll together, so that one lane's fence or global load never holds
+// up another's turn (lanes of one warp with loops of their own take turns).
+//
+// Mirror warp: lane 0 copies the row above's filter progress, lane 1 its
+// intra progress, lane 2 the row below's intra progress (global, acquire)
+// into shared memory.
+__device__ void band_mirror(const H264Launch &P, BandSmem &B, int y0, int rows, int lane) {
     const uint32_t tag = (P.epoch & 0xffffu) << 16;
     const bool above = y0 > 0, below = y0 + rows < P.mb_h;
-    const uint32_t *src = nullptr;
-    uint32_t *dst = nullptr;
-    if (lane == 0) { if (!above) { B.lprog[0] = P.mb_w; B.cprog[0] = P.mb_w; return; } src = P.rowprog + y0 - 1; }
-    else if (lane == 1) { if (!above) { B.iprog[0] = P.mb_w; return; } src = P.irowprog + y0 - 1; }
-    else if (lane == 2) { if (!below) { B.iprog[rows + 1] = P.mb_w; return; } src = P.irowprog + y0 + rows; }
-    else if (lane == 3) { if (!below) return; dst = P.rowprog + y0 + rows - 1; }
-    else if (lane == 4) { if (!below) return; dst = P.irowprog + y0 + rows - 1; }
-    else if (lane == 5) { if (!above) return; dst = P.irowprog + y0; }
-    else return;
-    int seen = 0;
+    const uint32_t *src = lane == 0 ? (above ? P.rowprog + y0 - 1 : nullptr)
+                          : lane == 1 ? (above ? P.irowprog + y0 - 1 : nullptr)
+                          : lane == 2 ? (below ? P.irowprog + y0 + rows : nullptr)
+                                      : nullptr;
+    if (lane == 0 && !above) { B.lprog[0] = P.mb_w; B.cprog[0] = P.mb_w; }
+    if (lane == 1 && !above) B.iprog[0] = P.mb_w;
+    if (lane == 2 && !below) B.iprog[rows + 1] = P.mb_w;
+    int seen = src ? 0 : P.mb_w;
     uint32_t it = 0;
-    while (seen < P.mb_w) {
-        int n;
-        if (src) {
+    while (!__all_sync(0xffffffffu, seen >= P.mb_w)) {
+        if (src && seen < P.mb_w) {
             const uint32_t v = ld_acquire(src);
-            n = (v & 0xffff0000u) == tag ? (int)(v & 0xffffu) : 0;
-        } else {
-            n = lane == 3 ? min(B.lprog[rows], B.cprog[rows]) : lane == 4 ? B.iprog[rows] : B.iprog[1];
-        }
-        if (n > seen) {
-            seen = n;
-            if (src) {
+            const int n = (v & 0xffff0000u) == tag ? (int)(v & 0xffffu) : 0;
+            if (n > seen) {
+                seen = n;
                 __threadfence_block();
                 if (lane == 0) { B.lprog[0] = seen; B.cprog[0] = seen; }
                 else if (lane == 1) B.iprog[0] = seen;
                 else B.iprog[rows + 1] = seen;
-            } else {
-                // the fence orders every store the band's warps made before
-                // the progress this lane read (they fenced before publishing
-                // it in shared memory) ahead of the flag; the flag itself can
-                // then be relaxed (a release store costs about a fence more)
-                __threadfence();
-                st_relaxed(dst, tag | (uint32_t)seen);
+                it = 0;
+            } else if (++it > P.wait_limit || ((it & 63) == 0 && aborted(P.error))) {
+                set_error(P.error, RC_DEV_ERR_TIMEOUT);
+                seen = P.mb_w;  // give up; the waiting warps see the error
+            }
+        }
+        __nanosleep(32);
+    }
+}
+
+// Publish warp: lane 0 publishes this band's last row's filter progress,
+// lane 1 its intra progress (for the band below), lane 2 its first row's
+// intra progress (for the band above).  One fence per round orders every
+// store the band's warps made before the progress the lanes read (they
+// fenced before publishing it in shared memory) ahead of the flags, which
+// can then be relaxed stores (a release store costs about a fence more).
+__device__ void band_publish(const H264Launch &P, BandSmem &B, int y0, int rows, int lane) {
+    const uint32_t tag = (P.epoch & 0xffffu) << 16;
+    const bool above = y0 > 0, below = y0 + rows < P.mb_h;
+    uint32_t *dst = lane == 0 ? (below ? P.rowprog + y0 + rows - 1 : nullptr)
+                    : lane == 1 ? (below ? P.irowprog + y0 + rows - 1 : nullptr)
+                    : lane == 2 ? (above ? P.irowprog + y0 : nullptr)
+                                : nullptr;
+    int seen = dst ? 0 : P.mb_w;
+    uint32_t it = 0;
+    while (!__all_sync(0xffffffffu, seen >= P.mb_w)) {
+        const int n = !dst ? seen : lane == 0 ? min(B.lprog[rows], B.cprog[rows]) : lane == 1 ? B.iprog[rows] : B.iprog[1];
+        const bool moved = n > seen;
+        if (__any_sync(0xffffffffu, moved)) {
+            __threadfence();
+            if (moved) {
+                st_relaxed(dst, tag | (uint32_t)n);
+                seen = n;
             }
             it = 0;
-            continue;
-        }
-        if (++it > P.wait_limit || ((it & 63) == 0 && aborted(P.error))) {
-            set_error(P.error, RC_DEV_ERR_TIMEOUT);
-            return;
+        } else if (++it > P.wait_limit || ((it & 63) == 0 && aborted(P.error))) {
+            if (lane == 0) set_error(P.error, RC_DEV_ERR_TIMEOUT);
+            break;
         }
         __nanosleep(32);
     }
@@ -1807,7 +1836,8 @@ __global__ void __launch_bounds__(BAND_THREADS, 1) h264_band_kernel(H264Launch P
         B.cprog[threadIdx.x] = 0;
     }
     __syncthreads();
-    if (warp == 3 * BR) { band_helper(P, B, y0, rows, lane); return; }
+    if (warp == 3 * BR) { band_mirror(P, B, y0, rows, lane); return; }
+    if (warp == 3 * BR + 1) { band_publish(P, B, y0, rows, lane); return; }
     const int role = warp / BR, w = warp % BR;
     if (w >= rows) return;
     if (role == 0) band_intra_row(P, B, band_dyn + BR * RC_BAND_STG, band_dyn + w * RC_BAND_STG, w, y0 + w, lane);
