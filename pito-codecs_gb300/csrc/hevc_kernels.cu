@@ -150,6 +150,7 @@ __global__ void __launch_bounds__(128) hevc_residual_kernel(HevcLaunch P) {
             const int c = tu_ctb(P, t);
             if (ti == 0 || tu_ctb(P, P.tus[ti - 1]) != c) P.ctb_first[c] = ti;
             if (ti == P.num_tus - 1 || tu_ctb(P, P.tus[ti + 1]) != c) P.ctb_end[c] = ti + 1;
+            if (t.flags & RC_HEVC_TU_INTRA) atomicAdd(&P.ctb_nintra[c], 1u);
         }
         if (!(t.flags & RC_HEVC_TU_CBF) || (t.flags & RC_HEVC_TU_PCM)) continue;
         const int log2 = t.log2, n = 1 << log2, c = t.c, mx = t.max_x, my = t.max_y;
@@ -342,7 +343,9 @@ __global__ void __launch_bounds__(64) hevc_inter_kernel(HevcLaunch P) {
 // CTB); CTBs on one anti-diagonal cx + 2 cy depend on none of each other,
 // and every neighbour an intra block reads lies on an earlier anti-diagonal
 // or earlier in the same CTB, so this order keeps each wait on a block taken
-// before it.
+// before it.  Only intra (and PCM) blocks are listed: the others are done by
+// the residual and inter kernels, and every listed task costs the intra
+// warps a turn at one global counter.
 // ===========================================================================
 __global__ void __launch_bounds__(1024) hevc_order_scan_kernel(HevcLaunch P) {
     __shared__ uint32_t keysum[2048];
@@ -350,7 +353,7 @@ __global__ void __launch_bounds__(1024) hevc_order_scan_kernel(HevcLaunch P) {
     for (int k = threadIdx.x; k < nkeys; k += blockDim.x) keysum[k] = 0;
     __syncthreads();
     for (int c = threadIdx.x; c < nctb; c += blockDim.x) {
-        const uint32_t n = P.ctb_end[c] - P.ctb_first[c];
+        const uint32_t n = P.ctb_nintra[c];
         if (n) atomicAdd(&keysum[c % P.wctb + 2 * (c / P.wctb)], n);
     }
     __syncthreads();
@@ -361,6 +364,7 @@ __global__ void __launch_bounds__(1024) hevc_order_scan_kernel(HevcLaunch P) {
             keysum[k] = acc;
             acc += v;
         }
+        P.counter[1] = acc;  // the number of intra tasks
     }
     __syncthreads();
     for (int c = threadIdx.x; c < nctb; c += blockDim.x) {
@@ -368,19 +372,36 @@ __global__ void __launch_bounds__(1024) hevc_order_scan_kernel(HevcLaunch P) {
         uint32_t base = keysum[key];
         for (int y = 0; y < cy; y++) {  // CTBs of the same anti-diagonal above this one
             const int x = key - 2 * y;
-            if (x >= 0 && x < P.wctb) base += P.ctb_end[y * P.wctb + x] - P.ctb_first[y * P.wctb + x];
+            if (x >= 0 && x < P.wctb) base += P.ctb_nintra[y * P.wctb + x];
         }
         P.ctb_base[c] = base;
     }
 }
 
+// One warp per CTB: its intra blocks, in decode order, from the CTB's base.
 __global__ void __launch_bounds__(256) hevc_order_fill_kernel(HevcLaunch P) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= P.num_tus) return;
-    const int c = tu_ctb(P, P.tus[i]);
+    const int c = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (c >= P.wctb * P.hctb) return;
     const uint32_t f = P.ctb_first[c], e = P.ctb_end[c];
-    if ((uint32_t)i >= f && (uint32_t)i < e) P.order[P.ctb_base[c] + (i - f)] = i;
-    else atomicOr(P.error, RC_DEV_ERR_RECORD);  // a CTB's blocks are not contiguous in decode order
+    uint32_t base = P.ctb_base[c], placed = 0;
+    bool bad = false;
+    for (uint32_t i0 = f; i0 < e; i0 += 32) {
+        const uint32_t i = i0 + lane;
+        bool intra = false;
+        if (i < e) {
+            const rc_hevc_tu t = P.tus[i];
+            intra = (t.flags & RC_HEVC_TU_INTRA) != 0;
+            bad = bad || tu_ctb(P, t) != c;  // a CTB's blocks are not contiguous in decode order
+        }
+        const uint32_t b = __ballot_sync(0xffffffffu, intra);
+        if (intra && placed + __popc(b & ((1u << lane) - 1)) < P.ctb_nintra[c])
+            P.order[base + __popc(b & ((1u << lane) - 1))] = i;
+        base += __popc(b);
+        placed += __popc(b);
+    }
+    if (__any_sync(0xffffffffu, bad) || (lane == 0 && placed != P.ctb_nintra[c])) {
+        if (lane == 0) atomicOr(P.error, RC_DEV_ERR_RECORD);
+    }
 }
 
 // ===========================================================================
@@ -606,11 +627,12 @@ __global__ void __launch_bounds__(128) hevc_intra_kernel(HevcLaunch P) {
     // transform blocks in the intra task order, one per counter step (each
     // waits only for blocks earlier in that order, all of which are already
     // taken by running warps; luma and chroma chains proceed side by side)
+    const unsigned ntasks = *(volatile const unsigned *)(P.counter + 1);
     for (;;) {
         unsigned ti = 0;
         if (lane == 0) ti = aborted(P.error) ? 0xffffffffu : atomicAdd(P.counter, 1u);
         ti = __shfl_sync(0xffffffffu, ti, 0);
-        if (ti >= (unsigned)P.num_tus) return;
+        if (ti >= ntasks || ti >= (unsigned)P.num_tus) return;
         const uint32_t oi = P.order[ti];
         if (oi >= (uint32_t)P.num_tus) {
             if (lane == 0) atomicOr(P.error, RC_DEV_ERR_RECORD);
@@ -873,8 +895,9 @@ void launch_all_deblock(const HevcLaunch &p, cudaStream_t st) {
 
 void rc_launch_hevc_residual(const HevcLaunch &p, cudaStream_t st) {
     cudaMemsetAsync(p.res, 0, ((size_t)p.W * p.H + 2 * (size_t)p.CW * p.CH) * sizeof(int16_t), st);
-    // CTBs without transform blocks keep first = end = 0
+    // CTBs without transform blocks keep first = end = 0 and no intra blocks
     cudaMemsetAsync(p.ctb_first, 0, 2 * (size_t)p.wctb * p.hctb * sizeof(uint32_t), st);
+    cudaMemsetAsync(p.ctb_nintra, 0, (size_t)p.wctb * p.hctb * sizeof(uint32_t), st);
     int blocks = (p.num_tus + 3) / 4;
     blocks = blocks < 1 ? 1 : blocks > 4096 ? 4096 : blocks;
     hevc_residual_kernel<<<blocks, 128, 0, st>>>(p);
@@ -888,7 +911,7 @@ void rc_launch_hevc_inter(const HevcLaunch &p, cudaStream_t st) {
 
 void rc_launch_hevc_intra(const HevcLaunch &p, cudaStream_t st, int blocks) {
     hevc_order_scan_kernel<<<1, 1024, 0, st>>>(p);
-    if (p.num_tus > 0) hevc_order_fill_kernel<<<(p.num_tus + 255) / 256, 256, 0, st>>>(p);
+    hevc_order_fill_kernel<<<(p.wctb * p.hctb + 7) / 8, 256, 0, st>>>(p);
     cudaMemsetAsync(p.counter, 0, sizeof(uint32_t), st);
     if (p.bd > 8) hevc_intra_kernel<uint16_t><<<blocks, 128, 0, st>>>(p);
     else hevc_intra_kernel<uint8_t><<<blocks, 128, 0, st>>>(p);

@@ -69,7 +69,7 @@ struct rc_stream {
     uint8_t *work = nullptr;     // picture being reconstructed (pre-SAO)
     int16_t *res = nullptr;      // residual planes
     uint32_t *ready = nullptr;   // per 4x4 block and component
-    uint32_t *ctb_ord = nullptr; // ctb_first, ctb_end, ctb_base for the smallest CTB size
+    uint32_t *ctb_ord = nullptr; // ctb_first, ctb_end, ctb_base, ctb_nintra for the smallest CTB size
     size_t nctb_max = 0;
     DevBuf order;                // intra task order
     int w4 = 0, h4 = 0, log2ctb_alloc = 0;
@@ -251,7 +251,7 @@ void destroy(rc_stream *s) {
     cudaFree(s->work);
     cudaFree(s->res);
     cudaFree(s->ready);
-    dev_free(s, s->ctb_ord, 3 * s->nctb_max * sizeof(uint32_t));
+    dev_free(s, s->ctb_ord, 4 * s->nctb_max * sizeof(uint32_t));
     dev_free(s, s->order.p, s->order.cap);
     cudaFree(s->counter);
     cudaFree(s->error);
@@ -459,7 +459,7 @@ int rc_stream_create(int codec, int width, int height, int bit_depth, int dpb_sl
         ok = ok && dev_alloc(s, (void **)&s->res, nres * sizeof(int16_t));
         ok = ok && dev_alloc(s, (void **)&s->ready, 3 * (size_t)s->w4 * s->h4 * sizeof(uint32_t));
         s->nctb_max = (size_t)((s->width + 15) / 16) * ((s->height + 15) / 16);
-        ok = ok && dev_alloc(s, (void **)&s->ctb_ord, 3 * s->nctb_max * sizeof(uint32_t));
+        ok = ok && dev_alloc(s, (void **)&s->ctb_ord, 4 * s->nctb_max * sizeof(uint32_t));
         ok = ok && cudaMemsetAsync(s->ready, 0, 3 * (size_t)s->w4 * s->h4 * sizeof(uint32_t), s->st) == cudaSuccess;
         ok = ok && cudaMemsetAsync(s->work, 0, s->slot_bytes, s->st) == cudaSuccess;
     }
@@ -671,6 +671,7 @@ int rc_hevc_submit(rc_stream *s, const rc_hevc_picture *pic, int out_slot) {
     L.ctb_first = s->ctb_ord;
     L.ctb_end = s->ctb_ord + (size_t)wctb * hctb;
     L.ctb_base = s->ctb_ord + 2 * s->nctb_max;
+    L.ctb_nintra = s->ctb_ord + 3 * s->nctb_max;
     L.order = (uint32_t *)s->order.p;
     L.counter = s->counter;
     L.error = s->error;
