@@ -71,7 +71,6 @@ struct rc_stream {
     uint32_t *ready = nullptr;   // per 4x4 block and component
     uint32_t *ctb_ord = nullptr; // ctb_first, ctb_end, ctb_base, ctb_nintra for the smallest CTB size
     size_t nctb_max = 0;
-    DevBuf order;                // intra task order
     int w4 = 0, h4 = 0, log2ctb_alloc = 0;
     int bps = 1;
     DevBuf mbs, slices, weights, levels;
@@ -252,7 +251,6 @@ void destroy(rc_stream *s) {
     cudaFree(s->res);
     cudaFree(s->ready);
     dev_free(s, s->ctb_ord, 4 * s->nctb_max * sizeof(uint32_t));
-    dev_free(s, s->order.p, s->order.cap);
     cudaFree(s->counter);
     cudaFree(s->error);
     cudaFree(s->ls);
@@ -667,12 +665,10 @@ int rc_hevc_submit(rc_stream *s, const rc_hevc_picture *pic, int out_slot) {
     L.res = s->res;
     L.ready = s->ready;
     if ((size_t)wctb * hctb > s->nctb_max || wctb + 2 * hctb > 2048) return RC_EINVAL;
-    if ((rc = ensure(s, s->order, sizeof(uint32_t) * std::max(1, pic->num_tus))) != 0) return rc;
     L.ctb_first = s->ctb_ord;
     L.ctb_end = s->ctb_ord + (size_t)wctb * hctb;
     L.ctb_base = s->ctb_ord + 2 * s->nctb_max;
     L.ctb_nintra = s->ctb_ord + 3 * s->nctb_max;
-    L.order = (uint32_t *)s->order.p;
     L.counter = s->counter;
     L.error = s->error;
     L.epoch = ++s->epoch;
@@ -682,7 +678,7 @@ int rc_hevc_submit(rc_stream *s, const rc_hevc_picture *pic, int out_slot) {
     timed(s, RC_KERNEL_HEVC_INTRA, [&] { rc_launch_hevc_intra(L, s->st, s->wave_blocks); });
     timed(s, RC_KERNEL_HEVC_DEBLOCK, [&] { rc_launch_hevc_deblock(L, s->st); });
     timed(s, RC_KERNEL_HEVC_SAO, [&] { rc_launch_hevc_sao(L, s->st); });
-    s->launches += 3;  // deblocking is two launches (vertical, horizontal edges); the intra order two more
+    s->launches += 2;  // deblocking is two launches (vertical, horizontal edges); the intra task order one more
     s->submits++;
     if (cudaGetLastError() != cudaSuccess) return cuda_fail(s);
     return RC_OK;

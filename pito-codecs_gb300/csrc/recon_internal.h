@@ -94,12 +94,10 @@ struct HevcLaunch {
     uint8_t *work;                // pre-SAO picture, same layout as a slot
     int16_t *res;                 // residual planes: luma W*H, then Cb, Cr CW*CH
     uint32_t *ready;              // 3 planes of w4*h4 flags: epoch when reconstructed
-    // intra task order: CTBs by anti-diagonal (cx + 2 cy), each CTB's intra
-    // transform blocks in decode order.  Per CTB (wctb * hctb): first block,
-    // one past its last (0, 0 for a CTB without blocks), start in the order,
-    // number of intra blocks.
+    // per CTB (wctb * hctb): its first transform block, one past its last
+    // (0, 0 for a CTB without blocks), its number of intra blocks; ctb_base:
+    // the CTBs in the intra task order (anti-diagonal cx + 2 cy, then cy)
     uint32_t *ctb_first, *ctb_end, *ctb_base, *ctb_nintra;
-    uint32_t *order;              // the intra transform-block indices
     uint32_t *counter;
     uint32_t *error;
     uint32_t epoch, wait_limit;
