@@ -11,11 +11,14 @@
 //  hevc_inter_kernel     one thread per sample of every inter block: 8-tap /
 //                        4-tap interpolation with i16 intermediates, default
 //                        or explicit weighted prediction, residual add, clip.
-//  hevc_intra_kernel     persistent; one warp per intra transform block taken
-//                        in decode order; waits (acquire loads, capped spin)
-//                        only for the intra neighbour blocks it reads,
-//                        substitutes / smooths the reference samples and
-//                        predicts (planar, DC, 33 angles + edge filters).
+//  hevc_intra_kernel     persistent CTAs of 16 warps take CTBs in anti-diagonal
+//                        order and reconstruct a CTB's intra blocks in shared
+//                        memory, one warp per block in decode order: waits
+//                        (capped) only for the intra neighbour blocks it
+//                        reads -- shared-memory flags inside the CTB, global
+//                        ready flags across CTBs -- then substitutes / smooths
+//                        the reference samples and predicts (planar, DC, 33
+//                        angles + edge filters).
 //  hevc_deblock_kernel   vertical edges, then (second launch) horizontal
 //                        edges, one thread per 4-sample edge segment: edges
 //                        8 samples apart never interact within a direction.
