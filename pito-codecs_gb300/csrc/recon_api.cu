@@ -58,14 +58,27 @@ struct rc_stream {
     int pitch = 0, cpitch = 0, cw = 0, ch = 0;
     size_t slot_bytes = 0, u_off = 0, v_off = 0;
     size_t budget = 0, held = 0;
-    cudaStream_t st = nullptr;
+    cudaStream_t st = nullptr;   // kernels
+    // host <-> device copies run beside the kernels, uploads and downloads on
+    // streams of their own (a download waits for the kernels before it, and
+    // an upload queued behind it would too): records upload into one of two
+    // sets (by submit parity) while the kernels read the other, and a submit
+    // that writes a slot waits for that slot's download
+    cudaStream_t cst = nullptr;  // uploads
+    cudaStream_t dst = nullptr;  // downloads
+    cudaEvent_t set_used[2] = {nullptr, nullptr};  // kernels of the last submit that read record set i
+    cudaEvent_t set_ready[2] = {nullptr, nullptr}; // record set i uploaded
+    bool set_busy[2] = {false, false};
+    cudaEvent_t kernels_done = nullptr;            // recorded before each download
+    std::vector<cudaEvent_t> slot_dl;              // per DPB slot: its last download
+    std::vector<char> slot_dl_pending;
     uint8_t *dpb = nullptr;
     uint32_t *counter = nullptr, *error = nullptr;
     uint32_t *rowprog = nullptr, *irowprog = nullptr, *edges = nullptr;
     IntraInfo *iinfo = nullptr;
     int16_t *ires = nullptr;
     // HEVC
-    DevBuf ctbs, blk, mvf, tus, hslices, scaling;
+    DevBuf ctbs[2], blk[2], mvf[2], tus[2], hslices[2], scaling;
     uint8_t *work = nullptr;     // picture being reconstructed (pre-SAO)
     int16_t *res = nullptr;      // residual planes
     uint32_t *ready = nullptr;   // per 4x4 block and component
@@ -73,7 +86,7 @@ struct rc_stream {
     size_t nctb_max = 0;
     int w4 = 0, h4 = 0, log2ctb_alloc = 0;
     int bps = 1;
-    DevBuf mbs, slices, weights, levels;
+    DevBuf mbs[2], slices[2], weights[2], levels[2];
     int32_t *ls = nullptr;            // device ls4 (2304 ints) + ls8 (2304*4 ints)
     std::vector<int32_t> ls_host;     // last uploaded tables
     uint8_t ls_key[2 + 96 + 384] = {0};  // the scaling lists they were made from (flat: flag 0)
@@ -163,7 +176,9 @@ void dev_free(rc_stream *s, void *p, size_t n) {
 // Grow a device buffer (waits for in-flight work that may read it).
 int ensure(rc_stream *s, DevBuf &b, size_t n) {
     if (n <= b.cap) return 0;
-    if (cudaStreamSynchronize(s->st) != cudaSuccess) return cuda_fail(s);
+    if (cudaStreamSynchronize(s->st) != cudaSuccess || cudaStreamSynchronize(s->cst) != cudaSuccess ||
+        cudaStreamSynchronize(s->dst) != cudaSuccess)
+        return cuda_fail(s);
     size_t want = std::max(n, b.cap + b.cap / 2);
     want = align_up(std::max<size_t>(want, 4096), 4096);
     dev_free(s, b.p, b.cap);
@@ -239,14 +254,18 @@ int validate_h264(const Geo *s, const rc_h264_picture *p) {
 void destroy(rc_stream *s) {
     if (!s) return;
     if (s->st) cudaStreamSynchronize(s->st);
+    if (s->cst) cudaStreamSynchronize(s->cst);
+    if (s->dst) cudaStreamSynchronize(s->dst);
     drain_profile(s);
     for (cudaEvent_t e : s->ev_free) cudaEventDestroy(e);
     for (auto &m : s->marks) cudaEventDestroy(m.second);
     for (cudaEvent_t e : s->mark_free) cudaEventDestroy(e);
     dev_free(s, s->dpb, s->slot_bytes * s->slots);
-    for (DevBuf *b : {&s->mbs, &s->slices, &s->weights, &s->levels, &s->ctbs, &s->blk, &s->mvf, &s->tus, &s->hslices,
-                      &s->scaling})
-        dev_free(s, b->p, b->cap);
+    for (int i = 0; i < 2; i++)
+        for (DevBuf *b : {&s->mbs[i], &s->slices[i], &s->weights[i], &s->levels[i], &s->ctbs[i], &s->blk[i], &s->mvf[i],
+                          &s->tus[i], &s->hslices[i]})
+            dev_free(s, b->p, b->cap);
+    dev_free(s, s->scaling.p, s->scaling.cap);
     cudaFree(s->work);
     cudaFree(s->res);
     cudaFree(s->ready);
@@ -263,6 +282,15 @@ void destroy(rc_stream *s) {
         if (s->staging[i]) cudaFreeHost(s->staging[i]);
         if (s->staged[i]) cudaEventDestroy(s->staged[i]);
     }
+    for (int i = 0; i < 2; i++) {
+        if (s->set_used[i]) cudaEventDestroy(s->set_used[i]);
+        if (s->set_ready[i]) cudaEventDestroy(s->set_ready[i]);
+    }
+    if (s->kernels_done) cudaEventDestroy(s->kernels_done);
+    for (cudaEvent_t e : s->slot_dl)
+        if (e) cudaEventDestroy(e);
+    if (s->cst) cudaStreamDestroy(s->cst);
+    if (s->dst) cudaStreamDestroy(s->dst);
     if (s->st) cudaStreamDestroy(s->st);
     delete s;
 }
@@ -273,9 +301,9 @@ struct Part {
     size_t n;
 };
 
-// Copy host buffers to device buffers on the stream: directly when every
+// Copy host buffers to device buffers on stream `on`: directly when every
 // source is pinned, else through the stream's double-buffered pinned staging.
-int upload(rc_stream *s, Part *parts, int np) {
+int upload(rc_stream *s, Part *parts, int np, cudaStream_t on) {
     int rc;
     for (int i = 0; i < np; i++)
         if ((rc = ensure(s, *parts[i].dst, std::max<size_t>(parts[i].n, 64)))) return rc;
@@ -284,7 +312,7 @@ int upload(rc_stream *s, Part *parts, int np) {
     if (pinned) {
         for (int i = 0; i < np; i++)
             if (parts[i].n &&
-                cudaMemcpyAsync(parts[i].dst->p, parts[i].src, parts[i].n, cudaMemcpyHostToDevice, s->st) != cudaSuccess)
+                cudaMemcpyAsync(parts[i].dst->p, parts[i].src, parts[i].n, cudaMemcpyHostToDevice, on) != cudaSuccess)
                 return cuda_fail(s);
         return 0;
     }
@@ -305,11 +333,38 @@ int upload(rc_stream *s, Part *parts, int np) {
     for (int i = 0; i < np; i++) {
         if (!parts[i].n) continue;
         memcpy(stage + off, parts[i].src, parts[i].n);
-        if (cudaMemcpyAsync(parts[i].dst->p, stage + off, parts[i].n, cudaMemcpyHostToDevice, s->st) != cudaSuccess)
+        if (cudaMemcpyAsync(parts[i].dst->p, stage + off, parts[i].n, cudaMemcpyHostToDevice, on) != cudaSuccess)
             return cuda_fail(s);
         off += align_up(parts[i].n, 256);
     }
-    if (cudaEventRecord(s->staged[k], s->st) != cudaSuccess) return cuda_fail(s);
+    if (cudaEventRecord(s->staged[k], on) != cudaSuccess) return cuda_fail(s);
+    return 0;
+}
+
+// Before uploading record set k on the copy stream: the kernels that last
+// read it are done.  After: the kernels wait for the upload.
+int set_begin(rc_stream *s, int k) {
+    if (s->set_busy[k] && cudaStreamWaitEvent(s->cst, s->set_used[k], 0) != cudaSuccess) return cuda_fail(s);
+    return 0;
+}
+int set_end(rc_stream *s, int k) {
+    if (cudaEventRecord(s->set_ready[k], s->cst) != cudaSuccess ||
+        cudaStreamWaitEvent(s->st, s->set_ready[k], 0) != cudaSuccess)
+        return cuda_fail(s);
+    return 0;
+}
+// Before a picture's kernels write slot `slot`: its pending download is done.
+int slot_begin(rc_stream *s, int slot) {
+    if (s->slot_dl_pending[slot]) {
+        if (cudaStreamWaitEvent(s->st, s->slot_dl[slot], 0) != cudaSuccess) return cuda_fail(s);
+        s->slot_dl_pending[slot] = 0;
+    }
+    return 0;
+}
+// After the kernels of a submit that read record set k.
+int set_release(rc_stream *s, int k) {
+    if (cudaEventRecord(s->set_used[k], s->st) != cudaSuccess) return cuda_fail(s);
+    s->set_busy[k] = true;
     return 0;
 }
 
@@ -338,17 +393,27 @@ int validate_hevc(const HGeo *g, const rc_hevc_picture *p) {
     }
     for (int i = 0; i < wctb * hctb; i++)
         if (p->ctbs[i].slice >= p->num_slices) return RC_EINVAL;
-    for (int by = 0; by < h4; by++)
-        for (int bx = 0; bx < w4; bx++) {
-            const rc_hevc_blk &b = p->blk[by * w4 + bx];
-            if (b.qp < -6 * (g->bd - 8) || b.qp > 51) return RC_EINVAL;
-            if (!(b.flags & RC_HEVC_F_CODED) || (b.flags & RC_HEVC_F_INTRA)) continue;
-            const rc_hevc_mvf &f = p->mvf[by * w4 + bx];
-            const rc_hevc_slice &sl = p->slices[p->ctbs[(by * 4 / ctb) * wctb + bx * 4 / ctb].slice];
-            if (f.ref_idx[0] < 0 && f.ref_idx[1] < 0) return RC_EINVAL;
-            for (int l = 0; l < 2; l++)
-                if (f.ref_idx[l] < -1 || f.ref_idx[l] >= sl.num_ref[l]) return RC_EINVAL;
+    // per 4x4 block: the QP range, and an inter block's reference indices
+    // against its slice's lists (walked one CTB-wide run at a time, so that
+    // the slice is looked up once per run: a 2160p picture has 518400 blocks)
+    const int qmin = -6 * (g->bd - 8), run = ctb / 4;
+    for (int by = 0; by < h4; by++) {
+        const rc_hevc_ctb *crow = p->ctbs + (size_t)((by * 4) >> p->log2_ctb) * wctb;
+        const rc_hevc_blk *brow = p->blk + (size_t)by * w4;
+        const rc_hevc_mvf *frow = p->mvf + (size_t)by * w4;
+        for (int cx = 0; cx < wctb; cx++) {
+            const rc_hevc_slice &sl = p->slices[crow[cx].slice];
+            const int n0 = sl.num_ref[0], n1 = sl.num_ref[1];
+            const int bx1 = std::min(w4, (cx + 1) * run);
+            for (int bx = cx * run; bx < bx1; bx++) {
+                const rc_hevc_blk &b = brow[bx];
+                if (b.qp < qmin || b.qp > 51) return RC_EINVAL;
+                if (!(b.flags & RC_HEVC_F_CODED) || (b.flags & RC_HEVC_F_INTRA)) continue;
+                const int r0 = frow[bx].ref_idx[0], r1 = frow[bx].ref_idx[1];
+                if ((r0 < 0 && r1 < 0) || r0 < -1 || r1 < -1 || r0 >= n0 || r1 >= n1) return RC_EINVAL;
+            }
         }
+    }
     for (int i = 0; i < p->num_tus; i++) {
         const rc_hevc_tu &t = p->tus[i];
         if (t.log2 < 2 || t.log2 > 5 || t.c > 2 || t.mode > 34) return RC_EINVAL;
@@ -436,7 +501,17 @@ int rc_stream_create(int codec, int width, int height, int bit_depth, int dpb_sl
         if (v > 0 && v <= 4096) s->wave_blocks = v;
     }
     const int n = s->mb_w * s->mb_h;
-    bool ok = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking) == cudaSuccess;
+    bool ok = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaStreamCreateWithFlags(&s->cst, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaStreamCreateWithFlags(&s->dst, cudaStreamNonBlocking) == cudaSuccess;
+    for (int i = 0; i < 2 && ok; i++)
+        ok = cudaEventCreateWithFlags(&s->set_used[i], cudaEventDisableTiming) == cudaSuccess &&
+             cudaEventCreateWithFlags(&s->set_ready[i], cudaEventDisableTiming) == cudaSuccess;
+    ok = ok && cudaEventCreateWithFlags(&s->kernels_done, cudaEventDisableTiming) == cudaSuccess;
+    s->slot_dl.assign(s->slots, nullptr);
+    s->slot_dl_pending.assign(s->slots, 0);
+    for (int i = 0; i < s->slots && ok; i++)
+        ok = cudaEventCreateWithFlags(&s->slot_dl[i], cudaEventDisableTiming) == cudaSuccess;
     ok = ok && dev_alloc(s, (void **)&s->dpb, s->slot_bytes * s->slots);
     ok = ok && cudaMalloc(&s->counter, 64) == cudaSuccess;
     ok = ok && cudaMalloc(&s->error, 64) == cudaSuccess;
@@ -526,13 +601,15 @@ int rc_h264_submit(rc_stream *s, const rc_h264_picture *pic, int out_slot) {
         if ((rc = validate_h264(&g, pic)) != 0) return rc;
         const size_t b_mbs = sizeof(rc_h264_mb) * n, b_sl = sizeof(rc_h264_slice) * pic->num_slices;
         const size_t b_w = sizeof(rc_h264_weight) * pic->num_weights, b_lv = sizeof(int16_t) * pic->num_levels;
-        Part parts[4] = {{&s->mbs, pic->mbs, b_mbs}, {&s->slices, pic->slices, b_sl},
-                         {&s->weights, pic->weights, b_w}, {&s->levels, pic->levels, b_lv}};
-        if ((rc = upload(s, parts, 4)) != 0) return rc;
-        L.mbs = (const rc_h264_mb *)s->mbs.p;
-        L.slices = (const rc_h264_slice *)s->slices.p;
-        L.weights = (const rc_h264_weight *)s->weights.p;
-        L.levels = (const int16_t *)s->levels.p;
+        const int k = s->submits & 1;
+        Part parts[4] = {{&s->mbs[k], pic->mbs, b_mbs}, {&s->slices[k], pic->slices, b_sl},
+                         {&s->weights[k], pic->weights, b_w}, {&s->levels[k], pic->levels, b_lv}};
+        if ((rc = set_begin(s, k)) != 0 || (rc = upload(s, parts, 4, s->cst)) != 0 || (rc = set_end(s, k)) != 0)
+            return rc;
+        L.mbs = (const rc_h264_mb *)s->mbs[k].p;
+        L.slices = (const rc_h264_slice *)s->slices[k].p;
+        L.weights = (const rc_h264_weight *)s->weights[k].p;
+        L.levels = (const int16_t *)s->levels[k].p;
     } else {
         if (!pic->mbs || !pic->slices || pic->num_slices <= 0) return RC_EINVAL;
         L.mbs = pic->mbs;
@@ -569,11 +646,13 @@ int rc_h264_submit(rc_stream *s, const rc_h264_picture *pic, int out_slot) {
     L.irowprog = s->irowprog;
     L.iinfo = s->iinfo;
     L.ires = s->ires;
+    if ((rc = slot_begin(s, out_slot)) != 0) return rc;
     timed(s, RC_KERNEL_H264_EDGE, [&] { rc_launch_h264_edge(L, s->st); });
     timed(s, RC_KERNEL_H264_MB, [&] { rc_launch_h264_mb(L, s->st); });
     int lrc = 0;
     timed(s, RC_KERNEL_H264_BAND, [&] { lrc = rc_launch_h264_band(L, s->st); });
     if (lrc != 0) return cuda_fail(s);
+    if (pic->mem == RC_MEM_HOST && (rc = set_release(s, s->submits & 1)) != 0) return rc;
     s->submits++;
     if (cudaGetLastError() != cudaSuccess) return cuda_fail(s);
     return RC_OK;
@@ -601,8 +680,8 @@ int rc_hevc_submit(rc_stream *s, const rc_hevc_picture *pic, int out_slot) {
     if (pic->scaling) {  // scaling factors are host memory in both modes; uploaded when they change
         const uint8_t *sf = (const uint8_t *)pic->scaling;
         if (s->scal_host.size() != b_scal || memcmp(s->scal_host.data(), sf, b_scal) != 0) {
-            Part sp{&s->scaling, pic->scaling, b_scal};
-            if ((rc = upload(s, &sp, 1)) != 0) {
+            Part sp{&s->scaling, pic->scaling, b_scal};  // on the kernels' stream: they read the previous factors
+            if ((rc = upload(s, &sp, 1, s->st)) != 0) {
                 s->scal_host.clear();
                 return rc;
             }
@@ -613,19 +692,21 @@ int rc_hevc_submit(rc_stream *s, const rc_hevc_picture *pic, int out_slot) {
     if (pic->mem == RC_MEM_HOST) {
         HGeo g{s->width, s->height, s->bit_depth, s->slots};
         if ((rc = validate_hevc(&g, pic)) != 0) return rc;
-        Part parts[6] = {{&s->ctbs, pic->ctbs, sizeof(rc_hevc_ctb) * wctb * hctb},
-                         {&s->blk, pic->blk, sizeof(rc_hevc_blk) * nblk},
-                         {&s->mvf, pic->mvf, sizeof(rc_hevc_mvf) * nblk},
-                         {&s->tus, pic->tus, sizeof(rc_hevc_tu) * pic->num_tus},
-                         {&s->hslices, pic->slices, sizeof(rc_hevc_slice) * pic->num_slices},
-                         {&s->levels, pic->levels, sizeof(int16_t) * pic->num_levels}};
-        if ((rc = upload(s, parts, 6)) != 0) return rc;
-        L.ctbs = (const rc_hevc_ctb *)s->ctbs.p;
-        L.blk = (const rc_hevc_blk *)s->blk.p;
-        L.mvf = (const rc_hevc_mvf *)s->mvf.p;
-        L.tus = (const rc_hevc_tu *)s->tus.p;
-        L.slices = (const rc_hevc_slice *)s->hslices.p;
-        L.levels = (const int16_t *)s->levels.p;
+        const int k = s->submits & 1;
+        Part parts[6] = {{&s->ctbs[k], pic->ctbs, sizeof(rc_hevc_ctb) * wctb * hctb},
+                         {&s->blk[k], pic->blk, sizeof(rc_hevc_blk) * nblk},
+                         {&s->mvf[k], pic->mvf, sizeof(rc_hevc_mvf) * nblk},
+                         {&s->tus[k], pic->tus, sizeof(rc_hevc_tu) * pic->num_tus},
+                         {&s->hslices[k], pic->slices, sizeof(rc_hevc_slice) * pic->num_slices},
+                         {&s->levels[k], pic->levels, sizeof(int16_t) * pic->num_levels}};
+        if ((rc = set_begin(s, k)) != 0 || (rc = upload(s, parts, 6, s->cst)) != 0 || (rc = set_end(s, k)) != 0)
+            return rc;
+        L.ctbs = (const rc_hevc_ctb *)s->ctbs[k].p;
+        L.blk = (const rc_hevc_blk *)s->blk[k].p;
+        L.mvf = (const rc_hevc_mvf *)s->mvf[k].p;
+        L.tus = (const rc_hevc_tu *)s->tus[k].p;
+        L.slices = (const rc_hevc_slice *)s->hslices[k].p;
+        L.levels = (const int16_t *)s->levels[k].p;
     } else {
         if (!pic->ctbs || !pic->blk || !pic->mvf || !pic->slices || pic->num_slices <= 0) return RC_EINVAL;
         L.ctbs = pic->ctbs;
@@ -673,12 +754,14 @@ int rc_hevc_submit(rc_stream *s, const rc_hevc_picture *pic, int out_slot) {
     L.error = s->error;
     L.epoch = ++s->epoch;
     L.wait_limit = s->wait_limit;
+    if ((rc = slot_begin(s, out_slot)) != 0) return rc;
     timed(s, RC_KERNEL_HEVC_RESIDUAL, [&] { rc_launch_hevc_residual(L, s->st); });
     timed(s, RC_KERNEL_HEVC_INTER, [&] { rc_launch_hevc_inter(L, s->st); });
     timed(s, RC_KERNEL_HEVC_INTRA, [&] { rc_launch_hevc_intra(L, s->st, s->wave_blocks); });
     timed(s, RC_KERNEL_HEVC_DEBLOCK, [&] { rc_launch_hevc_deblock(L, s->st); });
     timed(s, RC_KERNEL_HEVC_SAO, [&] { rc_launch_hevc_sao(L, s->st); });
     s->launches += 2;  // deblocking is two launches (vertical, horizontal edges); the intra task order one more
+    if (pic->mem == RC_MEM_HOST && (rc = set_release(s, s->submits & 1)) != 0) return rc;
     s->submits++;
     if (cudaGetLastError() != cudaSuccess) return cuda_fail(s);
     return RC_OK;
@@ -686,7 +769,9 @@ int rc_hevc_submit(rc_stream *s, const rc_hevc_picture *pic, int out_slot) {
 
 int rc_stream_sync(rc_stream *s) {
     if (!s) return RC_EINVAL;
-    if (cudaStreamSynchronize(s->st) != cudaSuccess) return cuda_fail(s);
+    if (cudaStreamSynchronize(s->st) != cudaSuccess || cudaStreamSynchronize(s->cst) != cudaSuccess ||
+        cudaStreamSynchronize(s->dst) != cudaSuccess)
+        return cuda_fail(s);
     uint32_t e = 0;
     if (cudaMemcpyAsync(&e, s->error, sizeof e, cudaMemcpyDeviceToHost, s->st) != cudaSuccess ||
         cudaStreamSynchronize(s->st) != cudaSuccess)
@@ -716,13 +801,20 @@ static int download(rc_stream *s, int slot, int x, int y, int w, int h, void *ou
         return RC_EINVAL;
     const int bps = s->bps;
     const uint8_t *base = s->dpb + (size_t)slot * s->slot_bytes;
-    bool ok = cudaMemcpy2DAsync(out_y, (size_t)w * bps, base + (size_t)y * s->pitch + (size_t)x * bps, s->pitch,
-                                (size_t)w * bps, h, cudaMemcpyDeviceToHost, s->st) == cudaSuccess &&
+    // on the download stream, after every kernel submitted so far; later
+    // submits that write this slot wait for it
+    cudaStream_t c = s->dst;
+    bool ok = cudaEventRecord(s->kernels_done, s->st) == cudaSuccess &&
+              cudaStreamWaitEvent(c, s->kernels_done, 0) == cudaSuccess &&
+              cudaMemcpy2DAsync(out_y, (size_t)w * bps, base + (size_t)y * s->pitch + (size_t)x * bps, s->pitch,
+                                (size_t)w * bps, h, cudaMemcpyDeviceToHost, c) == cudaSuccess &&
               cudaMemcpy2DAsync(out_u, (size_t)ccw * bps, base + s->u_off + (size_t)cy * s->cpitch + (size_t)cx * bps,
-                                s->cpitch, (size_t)ccw * bps, cch, cudaMemcpyDeviceToHost, s->st) == cudaSuccess &&
+                                s->cpitch, (size_t)ccw * bps, cch, cudaMemcpyDeviceToHost, c) == cudaSuccess &&
               cudaMemcpy2DAsync(out_v, (size_t)ccw * bps, base + s->v_off + (size_t)cy * s->cpitch + (size_t)cx * bps,
-                                s->cpitch, (size_t)ccw * bps, cch, cudaMemcpyDeviceToHost, s->st) == cudaSuccess &&
-              (!wait || cudaStreamSynchronize(s->st) == cudaSuccess);
+                                s->cpitch, (size_t)ccw * bps, cch, cudaMemcpyDeviceToHost, c) == cudaSuccess &&
+              cudaEventRecord(s->slot_dl[slot], c) == cudaSuccess;
+    if (ok) s->slot_dl_pending[slot] = 1;
+    ok = ok && (!wait || cudaStreamSynchronize(c) == cudaSuccess);
     return ok ? RC_OK : cuda_fail(s);
 }
 
@@ -763,6 +855,7 @@ int rc_picture_upload(rc_stream *s, int slot, const void *py, const void *pu, co
     if (!s || slot < 0 || slot >= s->slots || !py || !pu || !pv) return RC_EINVAL;
     const int bps = s->bps;
     uint8_t *base = s->dpb + (size_t)slot * s->slot_bytes;
+    if (slot_begin(s, slot) != 0) return cuda_fail(s);
     // stream-ordered copies (the stream does not order with the legacy default
     // stream), complete before returning so that the caller may free its planes
     bool ok = cudaMemcpy2DAsync(base, s->pitch, py, (size_t)s->width * bps, (size_t)s->width * bps, s->height,
