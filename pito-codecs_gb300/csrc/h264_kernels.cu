@@ -1247,6 +1247,33 @@ __device__ __forceinline__ bool wait_ge(volatile int *c, int need, const H264Lau
     return ok;
 }
 
+// wait_ge that remembers the largest progress it has observed: progress only
+// grows, so a value seen (and ordered by the fence) at an earlier wait
+// answers later ones without another round through shared memory.
+__device__ __forceinline__ bool wait_seen(volatile int *c, int &seen, int need, const H264Launch &P, int lane) {
+    if (seen >= need) return true;
+    bool ok = true;
+    int v = 0;
+    if (lane == 0) {
+        v = *c;
+        if (v < need) {
+            uint32_t it = 0, ns = 16;
+            do {
+                if (++it > P.wait_limit || ((it & 63) == 0 && aborted(P.error))) { ok = false; break; }
+                __nanosleep(ns);
+                ns = min(ns * 2, 128u);
+                v = *c;
+            } while (v < need);
+        }
+    }
+    ok = __shfl_sync(0xffffffffu, ok, 0);
+    v = __shfl_sync(0xffffffffu, v, 0);
+    __syncwarp();
+    __threadfence_block();
+    if (ok) seen = v;
+    return ok;
+}
+
 // filter_lanes (deblock.rs:146-229) for one luma line s[0..7] = p3..q3 and
 // one edge word (alpha | beta << 8 | tc0 << 16 | bS << 24), without
 // branches: every candidate is computed and the results selected, so that a
@@ -1512,6 +1539,7 @@ __device__ void band_luma_row(const H264Launch &P, BandSmem &B, int w, int my, i
     // picture; for the latter the next MB's rows are loaded one step early
     // when the row above is already far enough
     bool have_next = false;
+    int iown_seen = 0, ibelow_seen = 0, dup_seen = 0, ddown_seen = 0;  // progress observed so far
     auto top_rows = [&](int x) -> uint4 {
         if (my == 0 || lane >= 4) return z4;
         if (w > 0) return *(const uint4 *)(B.l[w - 1].ring[x % DRING] + lane * 16);
@@ -1531,12 +1559,12 @@ __device__ void band_luma_row(const H264Launch &P, BandSmem &B, int w, int my, i
             have_next = true;
         }
     };
-    if (!wait_ge(iown, min(2, P.mb_w), P, lane)) { band_fail(P, lane); return; }
+    if (!wait_seen(iown, iown_seen, min(2, P.mb_w), P, lane)) { band_fail(P, lane); return; }
     stage(0);
     stage(1);
     for (int x = 0; x < P.mb_w; x++) {
-        if (!wait_ge(iown, min(x + 3, P.mb_w), P, lane)) { band_fail(P, lane); return; }
-        if (below && !wait_ge(ibelow, min(x + 2, P.mb_w), P, lane)) { band_fail(P, lane); return; }
+        if (!wait_seen(iown, iown_seen, min(x + 3, P.mb_w), P, lane)) { band_fail(P, lane); return; }
+        if (below && !wait_seen(ibelow, ibelow_seen, min(x + 2, P.mb_w), P, lane)) { band_fail(P, lane); return; }
         try_next(x - 1);
         stage(x + 2);
         cp_wait_all_but_1();
@@ -1565,7 +1593,7 @@ __device__ void band_luma_row(const H264Launch &P, BandSmem &B, int w, int my, i
             prev.w = wd[0];
             if (act) *(uint4 *)(Y + (size_t)(my * 16 + r) * P.pitch + (x - 1) * 16) = prev;
             if (ring_out) {
-                if (x - DRING > 0 && !wait_ge(ddown, x - DRING, P, lane)) { band_fail(P, lane); return; }
+                if (x - DRING > 0 && !wait_seen(ddown, ddown_seen, x - DRING, P, lane)) { band_fail(P, lane); return; }
                 if (act && r >= 12) *(uint4 *)(R.ring[(x - 1) % DRING] + (r - 12) * 16) = prev;
             }
         }
@@ -1578,7 +1606,7 @@ __device__ void band_luma_row(const H264Launch &P, BandSmem &B, int w, int my, i
         // ---- horizontal edges: need MB (x, y-1) final, i.e. the row above past
         // MB x+1's vertical edges
         if (my > 0) {
-            if (!wait_ge(dup, x + 1, P, lane)) { band_fail(P, lane); return; }
+            if (!wait_seen(dup, dup_seen, x + 1, P, lane)) { band_fail(P, lane); return; }
             const uint4 t4 = (w == 0 && have_next) ? *(const uint4 *)&R.tn[x & 1][lane & 3][0] : top_rows(x);
             have_next = false;
             try_next(x);
@@ -1612,7 +1640,7 @@ __device__ void band_luma_row(const H264Launch &P, BandSmem &B, int w, int my, i
     // the row's last MB
     if (act) *(uint4 *)(Y + (size_t)(my * 16 + r) * P.pitch + (P.mb_w - 1) * 16) = prev;
     if (ring_out) {
-        if (P.mb_w - DRING > 0 && !wait_ge(ddown, P.mb_w - DRING, P, lane)) { band_fail(P, lane); return; }
+        if (P.mb_w - DRING > 0 && !wait_seen(ddown, ddown_seen, P.mb_w - DRING, P, lane)) { band_fail(P, lane); return; }
         if (act && r >= 12) *(uint4 *)(R.ring[(P.mb_w - 1) % DRING] + (r - 12) * 16) = prev;
     }
     __syncwarp();
@@ -1650,6 +1678,7 @@ __device__ void band_chroma_row(const H264Launch &P, BandSmem &B, int w, int my,
     // lane & 1): the row above's ring, or (first row of a band) the picture,
     // the next MB's one step early when the row above is far enough
     bool have_next = false;
+    int iown_seen = 0, ibelow_seen = 0, dup_seen = 0, ddown_seen = 0;  // progress observed so far
     auto top_rows = [&](int x) -> uint2 {
         if (my == 0 || lane >= 4) return z2;
         const int cc = lane >> 1, rr = lane & 1;
@@ -1670,12 +1699,12 @@ __device__ void band_chroma_row(const H264Launch &P, BandSmem &B, int w, int my,
             have_next = true;
         }
     };
-    if (!wait_ge(iown, min(2, P.mb_w), P, lane)) { band_fail(P, lane); return; }
+    if (!wait_seen(iown, iown_seen, min(2, P.mb_w), P, lane)) { band_fail(P, lane); return; }
     stage(0);
     stage(1);
     for (int x = 0; x < P.mb_w; x++) {
-        if (!wait_ge(iown, min(x + 3, P.mb_w), P, lane)) { band_fail(P, lane); return; }
-        if (below && !wait_ge(ibelow, min(x + 2, P.mb_w), P, lane)) { band_fail(P, lane); return; }
+        if (!wait_seen(iown, iown_seen, min(x + 3, P.mb_w), P, lane)) { band_fail(P, lane); return; }
+        if (below && !wait_seen(ibelow, ibelow_seen, min(x + 2, P.mb_w), P, lane)) { band_fail(P, lane); return; }
         try_next(x - 1);
         stage(x + 2);
         cp_wait_all_but_1();
@@ -1699,7 +1728,7 @@ __device__ void band_chroma_row(const H264Launch &P, BandSmem &B, int w, int my,
             prev.y = wd[0];
             if (act) *(uint2 *)(Cp + (size_t)(my * 8 + r) * P.cpitch + (x - 1) * 8) = prev;
             if (ring_out) {
-                if (x - DRING > 0 && !wait_ge(ddown, x - DRING, P, lane)) { band_fail(P, lane); return; }
+                if (x - DRING > 0 && !wait_seen(ddown, ddown_seen, x - DRING, P, lane)) { band_fail(P, lane); return; }
                 if (act && r >= 6) *(uint2 *)(R.ring[(x - 1) % DRING] + c * 16 + (r - 6) * 8) = prev;
             }
         }
@@ -1711,7 +1740,7 @@ __device__ void band_chroma_row(const H264Launch &P, BandSmem &B, int w, int my,
         // ---- horizontal edges: lane holds rows -2..7 of its column; need the
         // row above past MB x+1's vertical edges
         if (my > 0) {
-            if (!wait_ge(dup, x + 1, P, lane)) { band_fail(P, lane); return; }
+            if (!wait_seen(dup, dup_seen, x + 1, P, lane)) { band_fail(P, lane); return; }
             const uint2 t2 = (w == 0 && have_next) ? *(const uint2 *)&R.tn[x & 1][lane & 3][(x & 1) * 8] : top_rows(x);
             have_next = false;
             try_next(x);
@@ -1741,7 +1770,7 @@ __device__ void band_chroma_row(const H264Launch &P, BandSmem &B, int w, int my,
     }
     if (act) *(uint2 *)(Cp + (size_t)(my * 8 + r) * P.cpitch + (P.mb_w - 1) * 8) = prev;
     if (ring_out) {
-        if (P.mb_w - DRING > 0 && !wait_ge(ddown, P.mb_w - DRING, P, lane)) { band_fail(P, lane); return; }
+        if (P.mb_w - DRING > 0 && !wait_seen(ddown, ddown_seen, P.mb_w - DRING, P, lane)) { band_fail(P, lane); return; }
         if (act && r >= 6) *(uint2 *)(R.ring[(P.mb_w - 1) % DRING] + c * 16 + (r - 6) * 8) = prev;
     }
     __syncwarp();
