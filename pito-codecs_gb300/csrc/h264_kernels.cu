@@ -1430,6 +1430,7 @@ __device__ void band_intra_row(const H264Launch &P, BandSmem &B, uint8_t *lines,
         __threadfence_block();
     }
     int last = -2;  // the MB reconstructed last (its right column is still in the canvas)
+    int above_seen = 0;  // the row above's intra progress observed so far
     while (mx < P.mb_w) {
         const int nx = next_intra(mx + 1);
         // the MBs before mx are reconstructed (inter ones by h264_mb_kernel)
@@ -1454,7 +1455,7 @@ __device__ void band_intra_row(const H264Launch &P, BandSmem &B, uint8_t *lines,
         }
         __syncwarp();
         prefetch(nx);
-        if (my > 0 && !wait_ge(above, min(mx + 2, P.mb_w), P, lane)) {
+        if (my > 0 && !wait_seen(above, above_seen, min(mx + 2, P.mb_w), P, lane)) {
             cp_wait_all();
             band_fail(P, lane);
             return;
