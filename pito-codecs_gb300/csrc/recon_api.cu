@@ -74,7 +74,15 @@ struct rc_stream {
     std::vector<char> slot_dl_pending;
     uint8_t *dpb = nullptr;
     uint32_t *counter = nullptr, *error = nullptr;
-    uint32_t *rowprog = nullptr, *irowprog = nullptr, *edges = nullptr;
+    uint32_t *rowprog = nullptr, *irowprog = nullptr;
+    // H.264 edge words, two sets by submit parity: h264_edge_kernel runs on
+    // its own stream as soon as the picture's records are in, beside the
+    // previous picture's band kernel (it reads only records)
+    uint32_t *edges[2] = {nullptr, nullptr};
+    cudaStream_t est = nullptr;
+    cudaEvent_t edges_used[2] = {nullptr, nullptr};  // band kernel that last read set i
+    cudaEvent_t edges_ready = nullptr;
+    bool edges_busy[2] = {false, false};
     IntraInfo *iinfo = nullptr;
     int16_t *ires = nullptr;
     // HEVC
@@ -129,16 +137,17 @@ cudaEvent_t take_event(rc_stream *s) {
 
 // Launch one kernel through `fn`, bracketed by timing events when profiling.
 template <class F>
-void timed(rc_stream *s, int kernel, F fn) {
+void timed(rc_stream *s, int kernel, F fn, cudaStream_t on = nullptr) {
+    if (!on) on = s->st;
     if (!s->profiling) {
         fn();
         s->launches++;
         return;
     }
     cudaEvent_t a = take_event(s), b = take_event(s);
-    cudaEventRecord(a, s->st);
+    cudaEventRecord(a, on);
     fn();
-    cudaEventRecord(b, s->st);
+    cudaEventRecord(b, on);
     s->ev_pending.push_back({kernel, {a, b}});
     s->launches++;
 }
@@ -177,7 +186,7 @@ void dev_free(rc_stream *s, void *p, size_t n) {
 int ensure(rc_stream *s, DevBuf &b, size_t n) {
     if (n <= b.cap) return 0;
     if (cudaStreamSynchronize(s->st) != cudaSuccess || cudaStreamSynchronize(s->cst) != cudaSuccess ||
-        cudaStreamSynchronize(s->dst) != cudaSuccess)
+        cudaStreamSynchronize(s->dst) != cudaSuccess || (s->est && cudaStreamSynchronize(s->est) != cudaSuccess))
         return cuda_fail(s);
     size_t want = std::max(n, b.cap + b.cap / 2);
     want = align_up(std::max<size_t>(want, 4096), 4096);
@@ -275,7 +284,15 @@ void destroy(rc_stream *s) {
     cudaFree(s->ls);
     cudaFree(s->rowprog);
     cudaFree(s->irowprog);
-    dev_free(s, s->edges, (size_t)s->mb_w * s->mb_h * RC_EDGE_WORDS * sizeof(uint32_t));
+    for (int i = 0; i < 2; i++) {
+        dev_free(s, s->edges[i], (size_t)s->mb_w * s->mb_h * RC_EDGE_WORDS * sizeof(uint32_t));
+        if (s->edges_used[i]) cudaEventDestroy(s->edges_used[i]);
+    }
+    if (s->edges_ready) cudaEventDestroy(s->edges_ready);
+    if (s->est) {
+        cudaStreamSynchronize(s->est);
+        cudaStreamDestroy(s->est);
+    }
     dev_free(s, s->iinfo, (size_t)s->mb_w * s->mb_h * sizeof(IntraInfo));
     dev_free(s, s->ires, (size_t)s->mb_w * s->mb_h * 384 * sizeof(int16_t));
     for (int i = 0; i < 2; i++) {
@@ -519,7 +536,12 @@ int rc_stream_create(int codec, int width, int height, int bit_depth, int dpb_sl
     ok = ok && cudaMalloc(&s->rowprog, (size_t)s->mb_h * sizeof(uint32_t)) == cudaSuccess;
     ok = ok && cudaMalloc(&s->irowprog, (size_t)s->mb_h * sizeof(uint32_t)) == cudaSuccess;
     if (codec == RC_CODEC_H264) {
-        ok = ok && dev_alloc(s, (void **)&s->edges, (size_t)n * RC_EDGE_WORDS * sizeof(uint32_t));
+        for (int i = 0; i < 2; i++) {
+            ok = ok && dev_alloc(s, (void **)&s->edges[i], (size_t)n * RC_EDGE_WORDS * sizeof(uint32_t));
+            ok = ok && cudaEventCreateWithFlags(&s->edges_used[i], cudaEventDisableTiming) == cudaSuccess;
+        }
+        ok = ok && cudaStreamCreateWithFlags(&s->est, cudaStreamNonBlocking) == cudaSuccess &&
+             cudaEventCreateWithFlags(&s->edges_ready, cudaEventDisableTiming) == cudaSuccess;
         ok = ok && dev_alloc(s, (void **)&s->iinfo, (size_t)n * sizeof(IntraInfo));
         ok = ok && dev_alloc(s, (void **)&s->ires, (size_t)n * 384 * sizeof(int16_t));
         // band kernel: one CTA per RC_H264_BAND_ROWS MB rows, all resident (cooperative launch)
@@ -641,17 +663,30 @@ int rc_h264_submit(rc_stream *s, const rc_h264_picture *pic, int out_slot) {
     L.error = s->error;
     L.wait_limit = s->wait_limit;
     L.db = nullptr;
-    L.edges = s->edges;
+    const int ek = s->submits & 1;
+    L.edges = s->edges[ek];
     L.rowprog = s->rowprog;
     L.irowprog = s->irowprog;
     L.iinfo = s->iinfo;
     L.ires = s->ires;
     if ((rc = slot_begin(s, out_slot)) != 0) return rc;
-    timed(s, RC_KERNEL_H264_EDGE, [&] { rc_launch_h264_edge(L, s->st); });
+    // the edge kernel: after the picture's records (host records: their
+    // upload) and after the band kernel that last read this set of edge words
+    {
+        bool ok = true;
+        if (pic->mem == RC_MEM_HOST) ok = cudaStreamWaitEvent(s->est, s->set_ready[s->submits & 1], 0) == cudaSuccess;
+        if (s->edges_busy[ek]) ok = ok && cudaStreamWaitEvent(s->est, s->edges_used[ek], 0) == cudaSuccess;
+        if (!ok) return cuda_fail(s);
+    }
+    timed(s, RC_KERNEL_H264_EDGE, [&] { rc_launch_h264_edge(L, s->est); }, s->est);
+    if (cudaEventRecord(s->edges_ready, s->est) != cudaSuccess) return cuda_fail(s);
     timed(s, RC_KERNEL_H264_MB, [&] { rc_launch_h264_mb(L, s->st); });
+    if (cudaStreamWaitEvent(s->st, s->edges_ready, 0) != cudaSuccess) return cuda_fail(s);
     int lrc = 0;
     timed(s, RC_KERNEL_H264_BAND, [&] { lrc = rc_launch_h264_band(L, s->st); });
     if (lrc != 0) return cuda_fail(s);
+    if (cudaEventRecord(s->edges_used[ek], s->st) != cudaSuccess) return cuda_fail(s);
+    s->edges_busy[ek] = true;
     if (pic->mem == RC_MEM_HOST && (rc = set_release(s, s->submits & 1)) != 0) return rc;
     s->submits++;
     if (cudaGetLastError() != cudaSuccess) return cuda_fail(s);
@@ -770,7 +805,7 @@ int rc_hevc_submit(rc_stream *s, const rc_hevc_picture *pic, int out_slot) {
 int rc_stream_sync(rc_stream *s) {
     if (!s) return RC_EINVAL;
     if (cudaStreamSynchronize(s->st) != cudaSuccess || cudaStreamSynchronize(s->cst) != cudaSuccess ||
-        cudaStreamSynchronize(s->dst) != cudaSuccess)
+        cudaStreamSynchronize(s->dst) != cudaSuccess || (s->est && cudaStreamSynchronize(s->est) != cudaSuccess))
         return cuda_fail(s);
     uint32_t e = 0;
     if (cudaMemcpyAsync(&e, s->error, sizeof e, cudaMemcpyDeviceToHost, s->st) != cudaSuccess ||
@@ -829,7 +864,8 @@ int rc_picture_download_async(rc_stream *s, int slot, int x, int y, int w, int h
 
 int rc_stream_profile(rc_stream *s, int enable) {
     if (!s) return RC_EINVAL;
-    if (cudaStreamSynchronize(s->st) != cudaSuccess) return cuda_fail(s);
+    if (cudaStreamSynchronize(s->st) != cudaSuccess || (s->est && cudaStreamSynchronize(s->est) != cudaSuccess))
+        return cuda_fail(s);
     drain_profile(s);
     for (int k = 0; k < RC_KERNEL_COUNT; k++) {
         s->prof_ms[k] = 0;
@@ -841,7 +877,8 @@ int rc_stream_profile(rc_stream *s, int enable) {
 
 int rc_stream_profile_read(rc_stream *s, double *ms, long long *launches, int max_kernels) {
     if (!s || max_kernels < 0) return RC_EINVAL;
-    if (cudaStreamSynchronize(s->st) != cudaSuccess) return cuda_fail(s);
+    if (cudaStreamSynchronize(s->st) != cudaSuccess || (s->est && cudaStreamSynchronize(s->est) != cudaSuccess))
+        return cuda_fail(s);
     drain_profile(s);
     int n = std::min(max_kernels, RC_KERNEL_COUNT);
     for (int k = 0; k < n; k++) {
