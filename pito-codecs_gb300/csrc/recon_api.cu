@@ -75,22 +75,23 @@ struct rc_stream {
     uint8_t *dpb = nullptr;
     uint32_t *counter = nullptr, *error = nullptr;
     uint32_t *rowprog = nullptr, *irowprog = nullptr;
-    // H.264 edge words, two sets by submit parity: h264_edge_kernel runs on
-    // its own stream as soon as the picture's records are in, beside the
-    // previous picture's band kernel (it reads only records)
+    // The first kernel of a picture reads only its records (H.264 edge
+    // words, HEVC residuals and CTB ranges): it runs on a side stream as soon
+    // as the records are in, beside the previous picture's wavefront kernels,
+    // writing one of two sets of these buffers by submit parity.
     uint32_t *edges[2] = {nullptr, nullptr};
     cudaStream_t est = nullptr;
-    cudaEvent_t edges_used[2] = {nullptr, nullptr};  // band kernel that last read set i
-    cudaEvent_t edges_ready = nullptr;
-    bool edges_busy[2] = {false, false};
+    cudaEvent_t aux_used[2] = {nullptr, nullptr};  // the kernels that last read set i
+    cudaEvent_t aux_ready = nullptr;
+    bool aux_busy[2] = {false, false};
     IntraInfo *iinfo = nullptr;
     int16_t *ires = nullptr;
     // HEVC
     DevBuf ctbs[2], blk[2], mvf[2], tus[2], hslices[2], scaling;
     uint8_t *work = nullptr;     // picture being reconstructed (pre-SAO)
-    int16_t *res = nullptr;      // residual planes
+    int16_t *res[2] = {nullptr, nullptr};  // residual planes (two sets by submit parity)
     uint32_t *ready = nullptr;   // per 4x4 block and component
-    uint32_t *ctb_ord = nullptr; // ctb_first, ctb_end, ctb_base, ctb_nintra for the smallest CTB size
+    uint32_t *ctb_ord[2] = {nullptr, nullptr};  // ctb_first, ctb_end, ctb_base, ctb_nintra (smallest CTB size)
     size_t nctb_max = 0;
     int w4 = 0, h4 = 0, log2ctb_alloc = 0;
     int bps = 1;
@@ -276,19 +277,19 @@ void destroy(rc_stream *s) {
             dev_free(s, b->p, b->cap);
     dev_free(s, s->scaling.p, s->scaling.cap);
     cudaFree(s->work);
-    cudaFree(s->res);
+    for (int i = 0; i < 2; i++) cudaFree(s->res[i]);
     cudaFree(s->ready);
-    dev_free(s, s->ctb_ord, 4 * s->nctb_max * sizeof(uint32_t));
+    for (int i = 0; i < 2; i++) dev_free(s, s->ctb_ord[i], 4 * s->nctb_max * sizeof(uint32_t));
     cudaFree(s->counter);
     cudaFree(s->error);
     cudaFree(s->ls);
     cudaFree(s->rowprog);
     cudaFree(s->irowprog);
     for (int i = 0; i < 2; i++) {
-        dev_free(s, s->edges[i], (size_t)s->mb_w * s->mb_h * RC_EDGE_WORDS * sizeof(uint32_t));
-        if (s->edges_used[i]) cudaEventDestroy(s->edges_used[i]);
+        if (s->edges[i]) dev_free(s, s->edges[i], (size_t)s->mb_w * s->mb_h * RC_EDGE_WORDS * sizeof(uint32_t));
+        if (s->aux_used[i]) cudaEventDestroy(s->aux_used[i]);
     }
-    if (s->edges_ready) cudaEventDestroy(s->edges_ready);
+    if (s->aux_ready) cudaEventDestroy(s->aux_ready);
     if (s->est) {
         cudaStreamSynchronize(s->est);
         cudaStreamDestroy(s->est);
@@ -524,7 +525,10 @@ int rc_stream_create(int codec, int width, int height, int bit_depth, int dpb_sl
     for (int i = 0; i < 2 && ok; i++)
         ok = cudaEventCreateWithFlags(&s->set_used[i], cudaEventDisableTiming) == cudaSuccess &&
              cudaEventCreateWithFlags(&s->set_ready[i], cudaEventDisableTiming) == cudaSuccess;
-    ok = ok && cudaEventCreateWithFlags(&s->kernels_done, cudaEventDisableTiming) == cudaSuccess;
+    ok = ok && cudaEventCreateWithFlags(&s->kernels_done, cudaEventDisableTiming) == cudaSuccess &&
+         cudaStreamCreateWithFlags(&s->est, cudaStreamNonBlocking) == cudaSuccess &&
+         cudaEventCreateWithFlags(&s->aux_ready, cudaEventDisableTiming) == cudaSuccess;
+    for (int i = 0; i < 2 && ok; i++) ok = cudaEventCreateWithFlags(&s->aux_used[i], cudaEventDisableTiming) == cudaSuccess;
     s->slot_dl.assign(s->slots, nullptr);
     s->slot_dl_pending.assign(s->slots, 0);
     for (int i = 0; i < s->slots && ok; i++)
@@ -536,12 +540,8 @@ int rc_stream_create(int codec, int width, int height, int bit_depth, int dpb_sl
     ok = ok && cudaMalloc(&s->rowprog, (size_t)s->mb_h * sizeof(uint32_t)) == cudaSuccess;
     ok = ok && cudaMalloc(&s->irowprog, (size_t)s->mb_h * sizeof(uint32_t)) == cudaSuccess;
     if (codec == RC_CODEC_H264) {
-        for (int i = 0; i < 2; i++) {
+        for (int i = 0; i < 2; i++)
             ok = ok && dev_alloc(s, (void **)&s->edges[i], (size_t)n * RC_EDGE_WORDS * sizeof(uint32_t));
-            ok = ok && cudaEventCreateWithFlags(&s->edges_used[i], cudaEventDisableTiming) == cudaSuccess;
-        }
-        ok = ok && cudaStreamCreateWithFlags(&s->est, cudaStreamNonBlocking) == cudaSuccess &&
-             cudaEventCreateWithFlags(&s->edges_ready, cudaEventDisableTiming) == cudaSuccess;
         ok = ok && dev_alloc(s, (void **)&s->iinfo, (size_t)n * sizeof(IntraInfo));
         ok = ok && dev_alloc(s, (void **)&s->ires, (size_t)n * 384 * sizeof(int16_t));
         // band kernel: one CTA per RC_H264_BAND_ROWS MB rows, all resident (cooperative launch)
@@ -551,10 +551,10 @@ int rc_stream_create(int codec, int width, int height, int bit_depth, int dpb_sl
     if (codec == RC_CODEC_HEVC) {
         const size_t nres = (size_t)s->width * s->height + 2 * (size_t)s->cw * s->ch;
         ok = ok && dev_alloc(s, (void **)&s->work, s->slot_bytes);
-        ok = ok && dev_alloc(s, (void **)&s->res, nres * sizeof(int16_t));
+        for (int i = 0; i < 2; i++) ok = ok && dev_alloc(s, (void **)&s->res[i], nres * sizeof(int16_t));
         ok = ok && dev_alloc(s, (void **)&s->ready, 3 * (size_t)s->w4 * s->h4 * sizeof(uint32_t));
         s->nctb_max = (size_t)((s->width + 15) / 16) * ((s->height + 15) / 16);
-        ok = ok && dev_alloc(s, (void **)&s->ctb_ord, 4 * s->nctb_max * sizeof(uint32_t));
+        for (int i = 0; i < 2; i++) ok = ok && dev_alloc(s, (void **)&s->ctb_ord[i], 4 * s->nctb_max * sizeof(uint32_t));
         ok = ok && cudaMemsetAsync(s->ready, 0, 3 * (size_t)s->w4 * s->h4 * sizeof(uint32_t), s->st) == cudaSuccess;
         ok = ok && cudaMemsetAsync(s->work, 0, s->slot_bytes, s->st) == cudaSuccess;
     }
@@ -675,18 +675,18 @@ int rc_h264_submit(rc_stream *s, const rc_h264_picture *pic, int out_slot) {
     {
         bool ok = true;
         if (pic->mem == RC_MEM_HOST) ok = cudaStreamWaitEvent(s->est, s->set_ready[s->submits & 1], 0) == cudaSuccess;
-        if (s->edges_busy[ek]) ok = ok && cudaStreamWaitEvent(s->est, s->edges_used[ek], 0) == cudaSuccess;
+        if (s->aux_busy[ek]) ok = ok && cudaStreamWaitEvent(s->est, s->aux_used[ek], 0) == cudaSuccess;
         if (!ok) return cuda_fail(s);
     }
     timed(s, RC_KERNEL_H264_EDGE, [&] { rc_launch_h264_edge(L, s->est); }, s->est);
-    if (cudaEventRecord(s->edges_ready, s->est) != cudaSuccess) return cuda_fail(s);
+    if (cudaEventRecord(s->aux_ready, s->est) != cudaSuccess) return cuda_fail(s);
     timed(s, RC_KERNEL_H264_MB, [&] { rc_launch_h264_mb(L, s->st); });
-    if (cudaStreamWaitEvent(s->st, s->edges_ready, 0) != cudaSuccess) return cuda_fail(s);
+    if (cudaStreamWaitEvent(s->st, s->aux_ready, 0) != cudaSuccess) return cuda_fail(s);
     int lrc = 0;
     timed(s, RC_KERNEL_H264_BAND, [&] { lrc = rc_launch_h264_band(L, s->st); });
     if (lrc != 0) return cuda_fail(s);
-    if (cudaEventRecord(s->edges_used[ek], s->st) != cudaSuccess) return cuda_fail(s);
-    s->edges_busy[ek] = true;
+    if (cudaEventRecord(s->aux_used[ek], s->st) != cudaSuccess) return cuda_fail(s);
+    s->aux_busy[ek] = true;
     if (pic->mem == RC_MEM_HOST && (rc = set_release(s, s->submits & 1)) != 0) return rc;
     s->submits++;
     if (cudaGetLastError() != cudaSuccess) return cuda_fail(s);
@@ -715,8 +715,8 @@ int rc_hevc_submit(rc_stream *s, const rc_hevc_picture *pic, int out_slot) {
     if (pic->scaling) {  // scaling factors are host memory in both modes; uploaded when they change
         const uint8_t *sf = (const uint8_t *)pic->scaling;
         if (s->scal_host.size() != b_scal || memcmp(s->scal_host.data(), sf, b_scal) != 0) {
-            Part sp{&s->scaling, pic->scaling, b_scal};  // on the kernels' stream: they read the previous factors
-            if ((rc = upload(s, &sp, 1, s->st)) != 0) {
+            Part sp{&s->scaling, pic->scaling, b_scal};  // on the side stream, after the residual kernels before
+            if ((rc = upload(s, &sp, 1, s->est)) != 0) {
                 s->scal_host.clear();
                 return rc;
             }
@@ -778,21 +778,34 @@ int rc_hevc_submit(rc_stream *s, const rc_hevc_picture *pic, int out_slot) {
     L.pitch = s->pitch;
     L.cpitch = s->cpitch;
     L.work = s->work;
-    L.res = s->res;
+    const int ak = s->submits & 1;
+    L.res = s->res[ak];
     L.ready = s->ready;
     if ((size_t)wctb * hctb > s->nctb_max || wctb + 2 * hctb > 2048) return RC_EINVAL;
-    L.ctb_first = s->ctb_ord;
-    L.ctb_end = s->ctb_ord + (size_t)wctb * hctb;
-    L.ctb_base = s->ctb_ord + 2 * s->nctb_max;
-    L.ctb_nintra = s->ctb_ord + 3 * s->nctb_max;
+    L.ctb_first = s->ctb_ord[ak];
+    L.ctb_end = s->ctb_ord[ak] + (size_t)wctb * hctb;
+    L.ctb_base = s->ctb_ord[0] + 2 * s->nctb_max;  // written and read on the kernels' stream
+    L.ctb_nintra = s->ctb_ord[ak] + 3 * s->nctb_max;
     L.counter = s->counter;
     L.error = s->error;
     L.epoch = ++s->epoch;
     L.wait_limit = s->wait_limit;
     if ((rc = slot_begin(s, out_slot)) != 0) return rc;
-    timed(s, RC_KERNEL_HEVC_RESIDUAL, [&] { rc_launch_hevc_residual(L, s->st); });
+    // the residual kernel: after the picture's records (host records: their
+    // upload) and after the intra kernel that last read this set
+    {
+        bool ok = true;
+        if (pic->mem == RC_MEM_HOST) ok = cudaStreamWaitEvent(s->est, s->set_ready[s->submits & 1], 0) == cudaSuccess;
+        if (s->aux_busy[ak]) ok = ok && cudaStreamWaitEvent(s->est, s->aux_used[ak], 0) == cudaSuccess;
+        if (!ok) return cuda_fail(s);
+    }
+    timed(s, RC_KERNEL_HEVC_RESIDUAL, [&] { rc_launch_hevc_residual(L, s->est); }, s->est);
+    if (cudaEventRecord(s->aux_ready, s->est) != cudaSuccess || cudaStreamWaitEvent(s->st, s->aux_ready, 0) != cudaSuccess)
+        return cuda_fail(s);
     timed(s, RC_KERNEL_HEVC_INTER, [&] { rc_launch_hevc_inter(L, s->st); });
     timed(s, RC_KERNEL_HEVC_INTRA, [&] { rc_launch_hevc_intra(L, s->st, s->wave_blocks); });
+    if (cudaEventRecord(s->aux_used[ak], s->st) != cudaSuccess) return cuda_fail(s);
+    s->aux_busy[ak] = true;
     timed(s, RC_KERNEL_HEVC_DEBLOCK, [&] { rc_launch_hevc_deblock(L, s->st); });
     timed(s, RC_KERNEL_HEVC_SAO, [&] { rc_launch_hevc_sao(L, s->st); });
     s->launches += 2;  // deblocking is two launches (vertical, horizontal edges); the intra task order one more
