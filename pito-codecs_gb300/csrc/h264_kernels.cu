@@ -1,27 +1,30 @@
 // h264_kernels.cu — H.264 block reconstruction on sm_103a.
 //
-// Three launches per picture:
+// Per picture:
 //
+//  h264_edge_kernel     one warp per macroblock: boundary strengths and QPs
+//                       of the MB's edges (deblock.rs) as 64 ready-to-use
+//                       filter words; reads only syntax, so it runs on a side
+//                       stream beside the previous picture's band kernel.
 //  h264_mb_kernel       one CTA (256 threads) per macroblock, all in parallel.
 //                       Inter MBs: dequantisation (scale4/scale8, chroma DC
 //                       Hadamard), 4x4/8x8 inverse transforms, 6-tap luma and
 //                       bilinear chroma motion compensation with edge
 //                       extension by coordinate clamp, default / explicit
 //                       weighted prediction, residual add and clip, fused.
-//                       I_PCM MBs are copied.  Every MB also gets its
-//                       loop-filter parameters (boundary strengths, QPs),
-//                       which depend on syntax only.
-//  h264_intra_kernel    persistent; one warp per intra MB in anti-diagonal
-//                       order (key x + 2y); a warp waits (acquire loads,
-//                       capped spin) for its intra neighbours L, T, TR, TL,
-//                       then predicts and adds the residual block by block
-//                       in decode order on a shared-memory canvas.
-//  h264_deblock_kernel  one warp per MB row, walking the row left to right
-//                       on a shared-memory tile (the reference's MB-raster
-//                       filter order, src/h264/dec/slicedec.rs:184-208): row
-//                       y filters MB x once row y-1 has published MBs 0..x,
-//                       so every edge sees exactly the samples it would in
-//                       raster order.
+//                       I_PCM MBs are copied.  Intra MBs are dequantised and
+//                       transformed; their residuals wait for the band kernel.
+//  h264_band_kernel     one cooperative launch, a CTA per band of MB rows:
+//                       per row an intra warp (prediction block by block in
+//                       decode order on a shared-memory canvas) and two
+//                       loop-filter warps (luma, chroma) walking the row in
+//                       the reference's MB-raster filter order
+//                       (src/h264/dec/slicedec.rs:184-208) behind the intra
+//                       warps; rows hand over through shared memory, bands
+//                       through progress words in global memory.
+//
+// rc_h264_deblock_noalloc filters a reconstructed picture without allocating
+// (h264_db_params_kernel, then h264_deblock_kernel: one warp per MB row).
 //
 // Arithmetic follows src/h264/dec/{transform,intra,inter,deblock}.rs and the
 // reconstruction half of slicedec.rs; citations at each function.
