@@ -437,11 +437,13 @@ __device__ bool wait_local(volatile uint8_t &f, uint32_t limit, const uint32_t *
 // the picture, after their global ready flags.
 template <class T>
 __device__ void intra_tu(const HevcLaunch &P, IntraSmem &S, const CtbCanvas<T> &C, const rc_hevc_tu &t, int lane) {
-    const int log2 = t.log2, n = 1 << log2, c = t.c, sc = c ? 2 : 1, unit = 4 / sc;
+    // reference units: 4 luma samples, 2 chroma samples (shifts by lu, not
+    // divisions by a run-time unit size)
+    const int log2 = t.log2, n = 1 << log2, c = t.c, sc = c ? 2 : 1, lu = c ? 1 : 2, unit = 1 << lu;
     const int x0 = t.x0, y0 = t.y0, xl = x0 * sc, yl = y0 * sc, bd = P.bd, max = (1 << bd) - 1;
     T *pl = plane_ptr<T>(P.work, P, c);
     const int pitch = pitch_el(P, c, sizeof(T));
-    const int n2 = 2 * n, nunits = 1 + 2 * (n2 / unit);
+    const int n2 = 2 * n, nunits = 1 + 2 * (n2 >> lu);
     // a reference sample (plane coordinates) from the CTB copy or the picture
     auto ref = [&](int x, int y) -> uint16_t {
         return C.inside(x * sc, y * sc) ? (uint16_t)C.at(c, x, y) : (uint16_t)__ldcg(pl + (size_t)y * pitch + x);
@@ -451,8 +453,8 @@ __device__ void intra_tu(const HevcLaunch &P, IntraSmem &S, const CtbCanvas<T> &
     for (int u = lane; u < nunits; u += 32) {
         int xn, yn;
         if (u == 0) { xn = xl - 1; yn = yl - 1; }
-        else if (u <= n2 / unit) { xn = xl - 1; yn = (y0 + (u - 1) * unit) * sc; }
-        else { xn = (x0 + (u - 1 - n2 / unit) * unit) * sc; yn = yl - 1; }
+        else if (u <= (n2 >> lu)) { xn = xl - 1; yn = (y0 + ((u - 1) << lu)) * sc; }
+        else { xn = (x0 + ((u - 1 - (n2 >> lu)) << lu)) * sc; yn = yl - 1; }
         bool a = zavail(P, xl, yl, xn, yn);
         const bool in = C.inside(xn, yn);
         uint8_t bf = !a ? 0 : in ? C.blkf[((yn - C.y0) >> 2) * 16 + ((xn - C.x0) >> 2)] : P.blk[(yn >> 2) * P.w4 + (xn >> 2)].flags;
@@ -464,8 +466,8 @@ __device__ void intra_tu(const HevcLaunch &P, IntraSmem &S, const CtbCanvas<T> &
                                      P.wait_limit, P.error);
         }
         if (u == 0) S.al[0] = S.at[0] = a;
-        else if (u <= n2 / unit) for (int i = 0; i < unit; i++) S.al[1 + (u - 1) * unit + i] = a;
-        else for (int i = 0; i < unit; i++) S.at[1 + (u - 1 - n2 / unit) * unit + i] = a;
+        else if (u <= (n2 >> lu)) for (int i = 0; i < unit; i++) S.al[1 + ((u - 1) << lu) + i] = a;
+        else for (int i = 0; i < unit; i++) S.at[1 + ((u - 1 - (n2 >> lu)) << lu) + i] = a;
     }
     if (!__all_sync(0xffffffffu, ok)) {
         if (lane == 0) atomicOr(P.error, RC_DEV_ERR_TIMEOUT);
@@ -491,23 +493,25 @@ __device__ void intra_tu(const HevcLaunch &P, IntraSmem &S, const CtbCanvas<T> &
     // the units (scan index k: 0..NL-1 left units bottom-up, NL the corner,
     // NL+1.. top units) finds every sample's source at once.
     {
-        const int NL = n2 / unit, nk = 2 * NL + 1;
+        const int NL = n2 >> lu, nk = 2 * NL + 1;
         auto unit_avail = [&](int k) -> bool {
-            return k < NL ? S.al[1 + (NL - 1 - k) * unit] : k == NL ? S.al[0] : S.at[1 + (k - NL - 1) * unit];
+            return k < NL ? S.al[1 + ((NL - 1 - k) << lu)] : k == NL ? S.al[0] : S.at[1 + ((k - NL - 1) << lu)];
         };
         // the unit's first / last sample in scan order
         auto unit_val = [&](int k, bool last) -> int {
-            if (k < NL) return S.left[last ? 1 + (NL - 1 - k) * unit : n2 - k * unit];
+            if (k < NL) return S.left[last ? 1 + ((NL - 1 - k) << lu) : n2 - (k << lu)];
             if (k == NL) return S.left[0];
-            return S.top[last ? (k - NL) * unit : 1 + (k - NL - 1) * unit];
+            return S.top[last ? (k - NL) << lu : 1 + ((k - NL - 1) << lu)];
         };
         const uint32_t m0 = __ballot_sync(0xffffffffu, lane < nk && unit_avail(lane));
         const uint32_t m1 = __ballot_sync(0xffffffffu, lane + 32 < nk && unit_avail(lane + 32));
         const unsigned long long mask = (unsigned long long)m1 << 32 | m0;
         const int first = __ffsll((long long)mask) - 1;
-        for (int i = lane; i <= 2 * n2; i += 32) {
+        const unsigned long long all = nk >= 64 ? ~0ull : (1ull << nk) - 1;
+        // every unit available (the common case inside a picture): nothing to substitute
+        for (int i = lane; i <= 2 * n2 && mask != all; i += 32) {
             // sample i: 0 corner, 1..n2 left[i], n2+1..2 n2 top[i - n2]
-            const int k = i == 0 ? NL : i <= n2 ? NL - 1 - (i - 1) / unit : NL + 1 + (i - n2 - 1) / unit;
+            const int k = i == 0 ? NL : i <= n2 ? NL - 1 - ((i - 1) >> lu) : NL + 1 + ((i - n2 - 1) >> lu);
             if (mask >> k & 1) continue;
             int v;
             if (!mask) v = 1 << (bd - 1);
