@@ -4,10 +4,15 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
+#include <condition_variable>
 #include <cstdlib>
 #include <cstring>
 #include <deque>
+#include <functional>
+#include <mutex>
 #include <new>
+#include <thread>
 #include <vector>
 
 #include "recon_internal.h"
@@ -390,6 +395,83 @@ struct HGeo {
     int W, H, bd, slots;
 };
 
+// A few host threads for the validation of large pictures: a 2160p HEVC
+// picture has 518400 4x4 blocks and tens of thousands of transform blocks,
+// which take one host thread about as long as the GPU takes for the picture.
+// One job at a time; a caller that finds the pool busy (another stream's
+// thread validating) does its job alone.
+class HostPool {
+public:
+    static HostPool &get() {
+        static HostPool pool;
+        return pool;
+    }
+    // f(0) .. f(n - 1), on the workers and the calling thread
+    void run(int n, const std::function<void(int)> &f) {
+        std::unique_lock<std::mutex> one(call_, std::try_to_lock);
+        if (!one.owns_lock() || th_.empty()) {
+            for (int i = 0; i < n; i++) f(i);
+            return;
+        }
+        {
+            std::unique_lock<std::mutex> lk(m_);
+            // a worker still inside the previous job (woken after its items
+            // were all taken) leaves it before the job changes
+            done_.wait(lk, [&] { return active_ == 0; });
+            job_ = &f;
+            n_ = n;
+            next_.store(0);
+            gen_++;
+        }
+        go_.notify_all();
+        for (int i; (i = next_.fetch_add(1)) < n;) f(i);
+        std::unique_lock<std::mutex> lk(m_);
+        done_.wait(lk, [&] { return active_ == 0; });
+    }
+    ~HostPool() {
+        {
+            std::lock_guard<std::mutex> lk(m_);
+            quit_ = true;
+        }
+        go_.notify_all();
+        for (auto &t : th_) t.join();
+    }
+
+private:
+    HostPool() {
+        const unsigned hw = std::thread::hardware_concurrency();
+        const int workers = std::min(7, (int)(hw > 1 ? hw - 1 : 0));
+        for (int i = 0; i < workers; i++) th_.emplace_back([this] { loop(); });
+    }
+    void loop() {
+        unsigned long long seen = 0;
+        for (;;) {
+            const std::function<void(int)> *f;
+            int n;
+            {
+                std::unique_lock<std::mutex> lk(m_);
+                go_.wait(lk, [&] { return quit_ || gen_ != seen; });
+                if (quit_) return;
+                seen = gen_;
+                f = job_;
+                n = n_;
+                active_++;
+            }
+            for (int i; (i = next_.fetch_add(1)) < n;) (*f)(i);
+            std::lock_guard<std::mutex> lk(m_);
+            if (--active_ == 0) done_.notify_all();
+        }
+    }
+    std::mutex call_, m_;
+    std::condition_variable go_, done_;
+    std::vector<std::thread> th_;
+    const std::function<void(int)> *job_ = nullptr;
+    int n_ = 0, active_ = 0;
+    std::atomic<int> next_{0};
+    unsigned long long gen_ = 0;
+    bool quit_ = false;
+};
+
 // Host-side validation of an HEVC picture (ranges, reference indices,
 // payload bounds; src/hevc/slicedec.rs:2153-2160 rejects bad ref_idx).
 int validate_hevc(const HGeo *g, const rc_hevc_picture *p) {
@@ -411,42 +493,63 @@ int validate_hevc(const HGeo *g, const rc_hevc_picture *p) {
     }
     for (int i = 0; i < wctb * hctb; i++)
         if (p->ctbs[i].slice >= p->num_slices) return RC_EINVAL;
-    // per 4x4 block: the QP range, and an inter block's reference indices
-    // against its slice's lists (walked one CTB-wide run at a time, so that
-    // the slice is looked up once per run: a 2160p picture has 518400 blocks)
+    // per 4x4 block, rows [y0, y1): the QP range, and an inter block's
+    // reference indices against its slice's lists (walked one CTB-wide run
+    // at a time, so that the slice is looked up once per run).  The checks
+    // are OR-ed without branches and tested once per row.
     const int qmin = -6 * (g->bd - 8), run = ctb / 4;
-    for (int by = 0; by < h4; by++) {
-        const rc_hevc_ctb *crow = p->ctbs + (size_t)((by * 4) >> p->log2_ctb) * wctb;
-        const rc_hevc_blk *brow = p->blk + (size_t)by * w4;
-        const rc_hevc_mvf *frow = p->mvf + (size_t)by * w4;
-        for (int cx = 0; cx < wctb; cx++) {
-            const rc_hevc_slice &sl = p->slices[crow[cx].slice];
-            const int n0 = sl.num_ref[0], n1 = sl.num_ref[1];
-            const int bx1 = std::min(w4, (cx + 1) * run);
-            for (int bx = cx * run; bx < bx1; bx++) {
-                const rc_hevc_blk &b = brow[bx];
-                if (b.qp < qmin || b.qp > 51) return RC_EINVAL;
-                if (!(b.flags & RC_HEVC_F_CODED) || (b.flags & RC_HEVC_F_INTRA)) continue;
-                const int r0 = frow[bx].ref_idx[0], r1 = frow[bx].ref_idx[1];
-                if ((r0 < 0 && r1 < 0) || r0 < -1 || r1 < -1 || r0 >= n0 || r1 >= n1) return RC_EINVAL;
+    auto blocks = [&](int y0, int y1) -> bool {
+        for (int by = y0; by < y1; by++) {
+            const rc_hevc_ctb *crow = p->ctbs + (size_t)((by * 4) >> p->log2_ctb) * wctb;
+            const rc_hevc_blk *brow = p->blk + (size_t)by * w4;
+            const rc_hevc_mvf *frow = p->mvf + (size_t)by * w4;
+            unsigned bad = 0;
+            for (int cx = 0; cx < wctb; cx++) {
+                const rc_hevc_slice &sl = p->slices[crow[cx].slice];
+                const int n0 = sl.num_ref[0], n1 = sl.num_ref[1];
+                const int bx1 = std::min(w4, (cx + 1) * run);
+                for (int bx = cx * run; bx < bx1; bx++) {
+                    const int qp = brow[bx].qp, fl = brow[bx].flags;
+                    const int r0 = frow[bx].ref_idx[0], r1 = frow[bx].ref_idx[1];
+                    const unsigned inter = (fl & (RC_HEVC_F_CODED | RC_HEVC_F_INTRA)) == RC_HEVC_F_CODED;
+                    const unsigned refs = ((r0 < 0) & (r1 < 0)) | (r0 < -1) | (r1 < -1) | (r0 >= n0) | (r1 >= n1);
+                    bad |= (qp < qmin) | (qp > 51) | (inter & refs);
+                }
             }
+            if (bad) return false;
         }
-    }
-    for (int i = 0; i < p->num_tus; i++) {
-        const rc_hevc_tu &t = p->tus[i];
-        if (t.log2 < 2 || t.log2 > 5 || t.c > 2 || t.mode > 34) return RC_EINVAL;
-        const int n = 1 << t.log2, pw = t.c ? CW : g->W, ph = t.c ? CH : g->H;
-        if (t.x0 + n > pw || t.y0 + n > ph) return RC_EINVAL;
-        if (t.flags & RC_HEVC_TU_PCM) {
-            if ((size_t)t.coef_off + (size_t)n * n > p->num_levels) return RC_EINVAL;
-            continue;
+        return true;
+    };
+    // per transform block, [i0, i1): its size, component, mode and position,
+    // and the levels it reads; OR-ed the same way
+    const size_t nlev = (size_t)p->num_levels;
+    const int qmax = 51 + 6 * (g->bd - 8);
+    auto tus = [&](int i0, int i1) -> bool {
+        unsigned bad = 0;
+        for (int i = i0; i < i1; i++) {
+            const rc_hevc_tu &t = p->tus[i];
+            const int l2 = t.log2, n = 1 << (l2 & 7), pw = t.c ? CW : g->W, ph = t.c ? CH : g->H;
+            const unsigned shape = (l2 < 2) | (l2 > 5) | (t.c > 2) | (t.mode > 34) | (t.x0 + n > pw) | (t.y0 + n > ph);
+            const unsigned pcm = (size_t)t.coef_off + (size_t)n * n > nlev;
+            const unsigned cbf = (t.max_x >= n) | (t.max_y >= n) |
+                                 (((t.flags & RC_HEVC_TU_BYPASS) == 0) & ((t.qp < 0) | (t.qp > qmax))) |
+                                 ((size_t)t.coef_off + (size_t)(t.max_x + 1) * (t.max_y + 1) > nlev);
+            bad |= shape | ((t.flags & RC_HEVC_TU_PCM) ? pcm : ((t.flags & RC_HEVC_TU_CBF) != 0) & cbf);
         }
-        if (!(t.flags & RC_HEVC_TU_CBF)) continue;
-        if (t.max_x >= n || t.max_y >= n) return RC_EINVAL;
-        if (!(t.flags & RC_HEVC_TU_BYPASS) && (t.qp < 0 || t.qp > 51 + 6 * (g->bd - 8))) return RC_EINVAL;
-        if ((size_t)t.coef_off + (size_t)(t.max_x + 1) * (t.max_y + 1) > p->num_levels) return RC_EINVAL;
-    }
-    return 0;
+        return bad == 0;
+    };
+    // pictures above 1080p in pieces of 32 block rows and 8192 transform
+    // blocks on the host pool
+    constexpr int kRows = 32, kTus = 8192;
+    if ((size_t)w4 * h4 <= (size_t)480 * 272) return blocks(0, h4) && tus(0, p->num_tus) ? 0 : RC_EINVAL;
+    const int nr = (h4 + kRows - 1) / kRows, nt = (p->num_tus + kTus - 1) / kTus;
+    std::atomic<bool> ok{true};
+    HostPool::get().run(nr + nt, [&](int i) {
+        const bool good = i < nr ? blocks(i * kRows, std::min(h4, (i + 1) * kRows))
+                                 : tus((i - nr) * kTus, std::min(p->num_tus, (i - nr + 1) * kTus));
+        if (!good) ok.store(false, std::memory_order_relaxed);
+    });
+    return ok.load() ? 0 : RC_EINVAL;
 }
 
 }  // namespace

@@ -135,3 +135,125 @@ def test_hevc_validate(engine):
     pic = engine.HevcPicture.from_buffer_copy(bytes(engine.HevcPicture.from_address(p.ptr)))
     pic.tus = ctypes.addressof(keep)
     assert L.rc_hevc_validate(64, 64, 8, 2, ctypes.addressof(pic)) == engine.RC_EINVAL
+
+
+# record flags of include/pito_recon.h
+TU_CBF, TU_BYPASS, TU_PCM = 2, 8, 16
+F_INTRA, F_CODED = 1, 16
+
+
+def test_hevc_validate_each_check(engine):
+    """Every host-side check of rc_hevc_validate rejects its bad field, and
+    the limits themselves (QP 51, a block ending on the picture edge, levels
+    ending on the last one) are accepted."""
+    L = engine.lib()
+    W = H = 64
+    p = engine.SynthHevc(seed=21, width=W, height=H, log2_ctb=5, refs=[(0, 1, 1)], intra_permille=300)
+    base = engine.HevcPicture.from_buffer_copy(bytes(engine.HevcPicture.from_address(p.ptr)))
+    bufs = p.buffers()
+    keep = []
+
+    def arr(key, cls):
+        return np.frombuffer(bufs[key], dtype=np.dtype(cls)).copy()
+
+    def check(**recs):
+        pic = engine.HevcPicture.from_buffer_copy(bytes(base))
+        for key, a in recs.items():
+            b = ctypes.create_string_buffer(a.tobytes(), a.nbytes)
+            keep.append(b)
+            setattr(pic, key, ctypes.addressof(b))
+        return L.rc_hevc_validate(W, H, 8, 2, ctypes.addressof(pic))
+
+    tus, blk, mvf, ctbs = arr("tus", engine.HevcTu), arr("blk", engine.HevcBlk), arr("mvf", engine.HevcMvf), arr(
+        "ctbs", engine.HevcCtb)
+    assert check() == 0
+    nlev = base.num_levels
+    luma = int(np.flatnonzero((tus["c"] == 0) & ((tus["flags"] & (TU_CBF | TU_BYPASS | TU_PCM)) == TU_CBF))[0])
+    n = 1 << int(tus[luma]["log2"])
+
+    def tu(field, value, i=luma, flags=None):
+        t = tus.copy()
+        t[i][field] = value
+        if flags is not None:
+            t[i]["flags"] = flags
+        return check(tus=t)
+
+    for field, value in (("log2", 1), ("log2", 6), ("c", 3), ("mode", 35), ("x0", W - n + 4), ("y0", H - n + 4),
+                         ("max_x", n), ("max_y", n), ("qp", -1), ("qp", 52), ("coef_off", nlev)):
+        assert tu(field, value) == engine.RC_EINVAL, (field, value)
+    for field, value in (("x0", W - n), ("y0", H - n), ("qp", 51), ("qp", 0)):
+        assert tu(field, value) == 0, (field, value)
+    # transquant bypass: the QP is not used
+    assert tu("qp", 60, flags=TU_CBF | TU_BYPASS) == 0
+    # PCM: n x n levels from coef_off, the last one included
+    assert tu("coef_off", nlev - n * n, flags=TU_PCM) == 0
+    assert tu("coef_off", nlev - n * n + 1, flags=TU_PCM) == engine.RC_EINVAL
+    # no coefficients: the level range is not read
+    assert tu("coef_off", nlev + 1000, flags=0) == 0
+
+    inter = int(np.flatnonzero((blk["flags"] & (F_CODED | F_INTRA)) == F_CODED)[0])
+    intra = int(np.flatnonzero((blk["flags"] & (F_CODED | F_INTRA)) == (F_CODED | F_INTRA))[0])
+
+    def blk_qp(i, qp):
+        b = blk.copy()
+        b[i]["qp"] = qp
+        return check(blk=b)
+
+    assert blk_qp(inter, 52) == engine.RC_EINVAL and blk_qp(intra, -1) == engine.RC_EINVAL
+    assert blk_qp(inter, 51) == 0 and blk_qp(intra, 0) == 0
+
+    def refs(i, r0, r1):
+        m = mvf.copy()
+        m[i]["ref_idx"][0], m[i]["ref_idx"][1] = r0, r1
+        return check(mvf=m)
+
+    for r0, r1 in ((1, -1), (-1, -1), (-2, 0), (0, -2), (0, 0)):  # one reference in list 0, none in list 1
+        assert refs(inter, r0, r1) == engine.RC_EINVAL, (r0, r1)
+    assert refs(inter, 0, -1) == 0
+    assert refs(intra, 5, 5) == 0  # an intra block's motion field is not read
+    c = ctbs.copy()
+    c[len(c) - 1]["slice"] = base.num_slices
+    assert check(ctbs=c) == engine.RC_EINVAL
+
+
+def test_hevc_validate_large_picture_in_pieces(engine):
+    """A 2160p picture is validated in pieces on host threads: a bad record in
+    the last piece of block rows or of transform blocks is still found, also
+    while other threads validate at the same time."""
+    import threading
+    L = engine.lib()
+    W, H = 3840, 2160
+    p = engine.SynthHevc(seed=22, width=W, height=H, bit_depth=10, refs=[(0, 1, 1)], frame_id=1)
+    base = engine.HevcPicture.from_buffer_copy(bytes(engine.HevcPicture.from_address(p.ptr)))
+    bufs = p.buffers()
+    blk = np.frombuffer(bufs["blk"], dtype=np.dtype(engine.HevcBlk)).copy()
+    tus = np.frombuffer(bufs["tus"], dtype=np.dtype(engine.HevcTu)).copy()
+    blk[-1]["qp"] = 70
+    tus[-1]["mode"] = 40
+    keep = []
+
+    def pic_with(key, a):
+        pic = engine.HevcPicture.from_buffer_copy(bytes(base))
+        b = ctypes.create_string_buffer(a.tobytes(), a.nbytes)
+        keep.append((pic, b))
+        setattr(pic, key, ctypes.addressof(b))
+        return ctypes.addressof(pic)
+
+    cases = [(p.ptr, 0), (pic_with("blk", blk), engine.RC_EINVAL), (pic_with("tus", tus), engine.RC_EINVAL)]
+    for ptr, want in cases:
+        assert L.rc_hevc_validate(W, H, 10, 2, ptr) == want
+    errors = []
+
+    def worker(k):
+        for j in range(6):
+            ptr, want = cases[(k + j) % 3]
+            got = L.rc_hevc_validate(W, H, 10, 2, ptr)
+            if got != want:
+                errors.append((k, j, got, want))
+
+    threads = [threading.Thread(target=worker, args=(k,)) for k in range(4)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors
