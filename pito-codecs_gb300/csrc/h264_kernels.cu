@@ -1377,23 +1377,44 @@ __device__ void band_intra_row(const H264Launch &P, BandSmem &B, uint8_t *lines,
     uint8_t *ly = lines + (size_t)w * LW, *lu = ly + P.mb_w * 16, *lv = lu + P.mb_w * 8;
     const uint8_t *ay = ly - LW, *au = lu - LW, *av = lv - LW;  // the row above (w > 0)
     volatile int *above = &B.iprog[w], *mine = &B.iprog[w + 1];
-    // the row's intra MBs: lane j holds the bits of MBs 32 j .. 32 j + 31 (rows
-    // of up to 1024 MBs, see rc_h264_band_capacity)
+    // the intra MBs of this row (word) and of the row above (aword): lane j
+    // holds the bits of MBs 32 j .. 32 j + 31 (rows of up to 1024 MBs, see
+    // rc_h264_band_capacity)
     const int nwords = (P.mb_w + 31) >> 5;
-    uint32_t word = 0;
+    uint32_t word = 0, aword = 0;
     for (int j0 = 0; j0 < nwords; j0 += 4) {
-        int kinds[4];
+        int kinds[4], akinds[4];
 #pragma unroll
         for (int u = 0; u < 4; u++) {
             const int xl = (j0 + u) * 32 + lane;
             kinds[u] = xl < P.mb_w ? __ldg(&P.mbs[my * P.mb_w + xl].kind) : RC_H264_NONE;
+            akinds[u] = xl < P.mb_w && my > 0 ? __ldg(&P.mbs[(my - 1) * P.mb_w + xl].kind) : RC_H264_NONE;
         }
 #pragma unroll
         for (int u = 0; u < 4; u++) {
             const uint32_t b = __ballot_sync(0xffffffffu, wave_intra(kinds[u]));
-            if (lane == j0 + u) word = b;
+            const uint32_t a = __ballot_sync(0xffffffffu, wave_intra(akinds[u]));
+            if (lane == j0 + u) {
+                word = b;
+                aword = a;
+            }
         }
     }
+    auto above_intra = [&](int x) -> bool {  // MB (x, my - 1) is intra
+        const uint32_t b = __shfl_sync(0xffffffffu, aword, (x >> 5) & 31);
+        return x >= 0 && x < P.mb_w && (b >> (x & 31) & 1);
+    };
+    // the progress of the row above that MB x's prediction needs: its intra
+    // neighbours among MBs x-1, x, x+1 of that row reconstructed (inter ones
+    // are final from the start: in the line copy, which the row above fills
+    // before its first report, or in the picture for a band's first row)
+    auto above_need = [&](int x) -> int {
+        const int base = w > 0 ? 1 : 0;
+        if (above_intra(x + 1)) return min(x + 2, P.mb_w);
+        if (above_intra(x)) return x + 1;
+        if (above_intra(x - 1)) return max(x, base);
+        return base;
+    };
     auto next_intra = [&](int from) -> int {  // the first intra MB at or after `from`, else mb_w
         for (int j = from >> 5; j < nwords; j++) {
             uint32_t b = __shfl_sync(0xffffffffu, word, j);
@@ -1458,7 +1479,7 @@ __device__ void band_intra_row(const H264Launch &P, BandSmem &B, uint8_t *lines,
         }
         __syncwarp();
         prefetch(nx);
-        if (my > 0 && !wait_seen(above, above_seen, min(mx + 2, P.mb_w), P, lane)) {
+        if (my > 0 && !wait_seen(above, above_seen, above_need(mx), P, lane)) {
             cp_wait_all();
             band_fail(P, lane);
             return;
@@ -1582,11 +1603,11 @@ __device__ void band_luma_row(const H264Launch &P, BandSmem &B, int w, int my, i
             int sv[20];
 #pragma unroll
             for (int i = 0; i < 20; i++) sv[i] = (wd[i >> 2] >> (8 * (i & 3))) & 255;
-            if (__any_sync(0xffffffffu, (ev[0] >> 24) >= 4)) lf_luma<true>(sv, ev[0]);
-            else if (__any_sync(0xffffffffu, ev[0] != 0)) lf_luma<false>(sv, ev[0]);
+            // every edge, without a vote per edge: an edge with bS 0 leaves its
+            // samples unchanged, and the bS-4 form equals the other below bS 4
+            lf_luma<true>(sv, ev[0]);
 #pragma unroll
-            for (int e = 1; e < 4; e++)
-                if (__any_sync(0xffffffffu, ev[e] != 0)) lf_luma<false>(sv + 4 * e, ev[e]);
+            for (int e = 1; e < 4; e++) lf_luma<false>(sv + 4 * e, ev[e]);
 #pragma unroll
             for (int j = 0; j < 5; j++)
                 wd[j] = (uint32_t)sv[4 * j] | (uint32_t)sv[4 * j + 1] << 8 | (uint32_t)sv[4 * j + 2] << 16 |
@@ -1623,11 +1644,9 @@ __device__ void band_luma_row(const H264Launch &P, BandSmem &B, int w, int my, i
             int sv[20];
 #pragma unroll
             for (int i = 0; i < 20; i++) sv[i] = R.t[i][r];
-            if (__any_sync(0xffffffffu, (eh[0] >> 24) >= 4)) lf_luma<true>(sv, eh[0]);
-            else if (__any_sync(0xffffffffu, eh[0] != 0)) lf_luma<false>(sv, eh[0]);
+            lf_luma<true>(sv, eh[0]);
 #pragma unroll
-            for (int e = 1; e < 4; e++)
-                if (__any_sync(0xffffffffu, eh[e] != 0)) lf_luma<false>(sv + 4 * e, eh[e]);
+            for (int e = 1; e < 4; e++) lf_luma<false>(sv + 4 * e, eh[e]);
             __syncwarp();
             if (act) {
 #pragma unroll
@@ -1721,8 +1740,8 @@ __device__ void band_chroma_row(const H264Launch &P, BandSmem &B, int w, int my,
             int sv[12];
 #pragma unroll
             for (int i = 0; i < 12; i++) sv[i] = (wd[i >> 2] >> (8 * (i & 3))) & 255;
-            if (__any_sync(0xffffffffu, pv.x != 0)) lf_chroma(sv + 2, pv.x);
-            if (__any_sync(0xffffffffu, pv.y != 0)) lf_chroma(sv + 6, pv.y);
+            lf_chroma(sv + 2, pv.x);  // bS 0: unchanged
+            lf_chroma(sv + 6, pv.y);
 #pragma unroll
             for (int j = 0; j < 3; j++)
                 wd[j] = (uint32_t)sv[4 * j] | (uint32_t)sv[4 * j + 1] << 8 | (uint32_t)sv[4 * j + 2] << 16 |
@@ -1756,8 +1775,8 @@ __device__ void band_chroma_row(const H264Launch &P, BandSmem &B, int w, int my,
             int sv[10];
 #pragma unroll
             for (int i = 0; i < 10; i++) sv[i] = R.t[c][i][r];
-            if (__any_sync(0xffffffffu, ph.x != 0)) lf_chroma(sv + 0, ph.x);
-            if (__any_sync(0xffffffffu, ph.y != 0)) lf_chroma(sv + 4, ph.y);
+            lf_chroma(sv + 0, ph.x);
+            lf_chroma(sv + 4, ph.y);
             __syncwarp();
             if (act) {
 #pragma unroll
