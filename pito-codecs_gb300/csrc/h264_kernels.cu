@@ -1599,21 +1599,18 @@ __device__ void band_luma_row(const H264Launch &P, BandSmem &B, int w, int my, i
         // ---- vertical edges: lane r holds columns -4..15 of sample row r
         uint32_t wd[5] = {prev.w, cur.x, cur.y, cur.z, cur.w};
         const uint32_t ev[4] = {pv.x, pv.y, pv.z, pv.w};
-        if (__any_sync(0xffffffffu, (ev[0] | ev[1] | ev[2] | ev[3]) != 0)) {
-            int sv[20];
+        const bool vfilt = __any_sync(0xffffffffu, (ev[0] | ev[1] | ev[2] | ev[3]) != 0);
+        int sv[20];
+        if (vfilt) {
 #pragma unroll
             for (int i = 0; i < 20; i++) sv[i] = (wd[i >> 2] >> (8 * (i & 3))) & 255;
-            // every edge, without a vote per edge: an edge with bS 0 leaves its
-            // samples unchanged, and the bS-4 form equals the other below bS 4
+            // the MB edge; the bS-4 form equals the other below bS 4, and an
+            // edge with bS 0 leaves its samples unchanged
             lf_luma<true>(sv, ev[0]);
-#pragma unroll
-            for (int e = 1; e < 4; e++) lf_luma<false>(sv + 4 * e, ev[e]);
-#pragma unroll
-            for (int j = 0; j < 5; j++)
-                wd[j] = (uint32_t)sv[4 * j] | (uint32_t)sv[4 * j + 1] << 8 | (uint32_t)sv[4 * j + 2] << 16 |
-                        (uint32_t)sv[4 * j + 3] << 24;
+            wd[0] = (uint32_t)sv[0] | (uint32_t)sv[1] << 8 | (uint32_t)sv[2] << 16 | (uint32_t)sv[3] << 24;
         }
-        // ---- MB x-1 is final in this row: store it, and its rows 12..15 for the row below
+        // ---- MB x-1 is final once this MB's left edge is filtered (the inner
+        // edges start at column 1): store it, and its rows 12..15 for the row below
         if (x > 0) {
             prev.w = wd[0];
             if (act) *(uint4 *)(Y + (size_t)(my * 16 + r) * P.pitch + (x - 1) * 16) = prev;
@@ -1622,12 +1619,22 @@ __device__ void band_luma_row(const H264Launch &P, BandSmem &B, int w, int my, i
                 if (act && r >= 12) *(uint4 *)(R.ring[(x - 1) % DRING] + (r - 12) * 16) = prev;
             }
         }
-        if (act) *(uint4 *)R.t[4 + r] = make_uint4(wd[1], wd[2], wd[3], wd[4]);
         // MBs 0..x-1 are final and stored: the row below may take MB x-1's
         // rows (its horizontal edges need nothing later of this row)
         __syncwarp();
         __threadfence_block();
         if (lane == 0) *dmine = x;
+        // the inner vertical edges, without a vote per edge
+        if (vfilt) {
+#pragma unroll
+            for (int e = 1; e < 4; e++) lf_luma<false>(sv + 4 * e, ev[e]);
+#pragma unroll
+            for (int j = 1; j < 5; j++)
+                wd[j] = (uint32_t)sv[4 * j] | (uint32_t)sv[4 * j + 1] << 8 | (uint32_t)sv[4 * j + 2] << 16 |
+                        (uint32_t)sv[4 * j + 3] << 24;
+        }
+        if (act) *(uint4 *)R.t[4 + r] = make_uint4(wd[1], wd[2], wd[3], wd[4]);
+        __syncwarp();
         // ---- horizontal edges: need MB (x, y-1) final, i.e. the row above past
         // MB x+1's vertical edges
         if (my > 0) {
