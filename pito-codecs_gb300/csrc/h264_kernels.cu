@@ -1357,6 +1357,7 @@ __device__ __forceinline__ void cp_async4(void *dst, const void *src) {
 __device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 __device__ __forceinline__ void cp_wait_all_but_1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+__device__ __forceinline__ void cp_wait_all_but_4() { asm volatile("cp.async.wait_group 4;" ::: "memory"); }
 
 // Intra warp of band row w (picture row my).  `lines` holds, per band row,
 // the row's unfiltered bottom samples (luma row 15, then Cb and Cr row 7):
@@ -1571,28 +1572,39 @@ __device__ void band_luma_row(const H264Launch &P, BandSmem &B, int w, int my, i
         return __ldcg((const uint4 *)(Y + (size_t)(my * 16 - 4 + lane) * P.pitch + x * 16));
     };
     // a band's first row: copy MB x+1's top rows into shared memory as soon
-    // as the row above has stored MB x+1, with cp.async, whose group the next
-    // step's cp_wait_all_but_1 completes (a register load here stalled the
-    // warp until it returned); the group precedes that step's stage group
+    // as the row above has stored MB x+1, with cp.async (a register load here
+    // stalled the warp until it returned).  Commits a group in every case.
     auto try_next = [&](int x) {
         if (w == 0 && my > 0 && !have_next && x + 1 < P.mb_w &&
             __shfl_sync(0xffffffffu, *dup >= x + 2 ? 1 : 0, 0)) {
             __threadfence_block();
             if (lane < 4)
                 cp_async16(&R.tn[(x + 1) & 1][lane][0], Y + (size_t)(my * 16 - 4 + lane) * P.pitch + (x + 1) * 16);
-            cp_commit();
             have_next = true;
         }
+        cp_commit();
     };
-    if (!wait_seen(iown, iown_seen, min(2, P.mb_w), P, lane)) { band_fail(P, lane); return; }
+    auto fail = [&]() {
+        cp_wait_all();
+        band_fail(P, lane);
+    };
+    // Groups: step x commits try_next(x-1) and stage(x+2) right after it
+    // reports MB x-1 (off the path that the row below waits on), then
+    // try_next(x) at its horizontal edges.  Before the loop, the same pattern
+    // for steps -2 and -1 (empty try_next groups).  So at the top of step x
+    // four groups are younger than stage(x)'s, and at step x's horizontal
+    // edges one is younger than the last group that can hold MB x's top rows.
+    if (!wait_seen(iown, iown_seen, min(2, P.mb_w), P, lane)) { fail(); return; }
+    cp_commit();
     stage(0);
+    cp_commit();
+    cp_commit();
     stage(1);
+    cp_commit();
     for (int x = 0; x < P.mb_w; x++) {
-        if (!wait_seen(iown, iown_seen, min(x + 3, P.mb_w), P, lane)) { band_fail(P, lane); return; }
-        if (below && !wait_seen(ibelow, ibelow_seen, min(x + 2, P.mb_w), P, lane)) { band_fail(P, lane); return; }
-        try_next(x - 1);
-        stage(x + 2);
-        cp_wait_all_but_1();
+        if (below && !wait_seen(ibelow, ibelow_seen, min(x + 2, P.mb_w), P, lane)) { fail(); return; }
+        cp_wait_all_but_4();
+        __syncwarp();
         const int sl = x % 3;
         const uint4 cur = act ? R.st[sl][0][r] : z4, pv = act ? R.st[sl][1][r] : z4,
                     ph = act ? R.st[sl][2][r] : z4;
@@ -1615,7 +1627,7 @@ __device__ void band_luma_row(const H264Launch &P, BandSmem &B, int w, int my, i
             prev.w = wd[0];
             if (act) *(uint4 *)(Y + (size_t)(my * 16 + r) * P.pitch + (x - 1) * 16) = prev;
             if (ring_out) {
-                if (x - DRING > 0 && !wait_seen(ddown, ddown_seen, x - DRING, P, lane)) { band_fail(P, lane); return; }
+                if (x - DRING > 0 && !wait_seen(ddown, ddown_seen, x - DRING, P, lane)) { fail(); return; }
                 if (act && r >= 12) *(uint4 *)(R.ring[(x - 1) % DRING] + (r - 12) * 16) = prev;
             }
         }
@@ -1624,6 +1636,11 @@ __device__ void band_luma_row(const H264Launch &P, BandSmem &B, int w, int my, i
         __syncwarp();
         __threadfence_block();
         if (lane == 0) *dmine = x;
+        // MB x+2 reconstructed (also orders this step's horizontal edges after
+        // this row's intra prediction, which reads the row above): stage it
+        if (!wait_seen(iown, iown_seen, min(x + 3, P.mb_w), P, lane)) { fail(); return; }
+        try_next(x - 1);
+        stage(x + 2);
         // the inner vertical edges, without a vote per edge
         if (vfilt) {
 #pragma unroll
@@ -1637,13 +1654,19 @@ __device__ void band_luma_row(const H264Launch &P, BandSmem &B, int w, int my, i
         __syncwarp();
         // ---- horizontal edges: need MB (x, y-1) final, i.e. the row above past
         // MB x+1's vertical edges
+        uint4 t4 = z4;
         if (my > 0) {
-            if (!wait_seen(dup, dup_seen, x + 1, P, lane)) { band_fail(P, lane); return; }
-            const uint4 t4 = (w == 0 && have_next) ? *(const uint4 *)&R.tn[x & 1][lane & 3][0] : top_rows(x);
+            if (!wait_seen(dup, dup_seen, x + 1, P, lane)) { fail(); return; }
+            if (w == 0 && have_next) {
+                cp_wait_all_but_1();  // the top rows' group, whichever try_next committed it
+                t4 = *(const uint4 *)&R.tn[x & 1][lane & 3][0];
+            } else {
+                t4 = top_rows(x);
+            }
             have_next = false;
-            try_next(x);
-            if (lane < 4) *(uint4 *)R.t[lane] = t4;
         }
+        try_next(x);
+        if (my > 0 && lane < 4) *(uint4 *)R.t[lane] = t4;
         __syncwarp();
         const uint32_t eh[4] = {ph.x, ph.y, ph.z, ph.w};
         const bool top = my > 0 && __any_sync(0xffffffffu, eh[0] != 0);
@@ -1667,6 +1690,7 @@ __device__ void band_luma_row(const H264Launch &P, BandSmem &B, int w, int my, i
             *(uint4 *)(Y + (size_t)(my * 16 - 3 + lane) * P.pitch + x * 16) = *(const uint4 *)R.t[1 + lane];
         __syncwarp();
     }
+    cp_wait_all();
     // the row's last MB
     if (act) *(uint4 *)(Y + (size_t)(my * 16 + r) * P.pitch + (P.mb_w - 1) * 16) = prev;
     if (ring_out) {
