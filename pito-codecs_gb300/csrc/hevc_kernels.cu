@@ -386,7 +386,6 @@ __device__ bool zavail(const HevcLaunch &P, int xc, int yc, int xn, int yn) {
 struct __align__(16) IntraSmem {
     uint16_t left[136], top[136];   // reference samples (index 0 = corner)
     uint16_t fleft[136], ftop[136]; // smoothed copy
-    uint8_t al[136], at[136];
     int refa[200];
 };
 
@@ -443,21 +442,28 @@ __device__ void intra_tu(const HevcLaunch &P, IntraSmem &S, const CtbCanvas<T> &
     const int x0 = t.x0, y0 = t.y0, xl = x0 * sc, yl = y0 * sc, bd = P.bd, max = (1 << bd) - 1;
     T *pl = plane_ptr<T>(P.work, P, c);
     const int pitch = pitch_el(P, c, sizeof(T));
-    const int n2 = 2 * n, nunits = 1 + 2 * (n2 >> lu);
+    const int n2 = 2 * n;
     // a reference sample (plane coordinates) from the CTB copy or the picture
     auto ref = [&](int x, int y) -> uint16_t {
         return C.inside(x * sc, y * sc) ? (uint16_t)C.at(c, x, y) : (uint16_t)__ldcg(pl + (size_t)y * pitch + x);
     };
-    // ---- availability of each reference unit; wait for intra neighbours
-    bool ok = true;
-    for (int u = lane; u < nunits; u += 32) {
+    // Reference units in the substitution scan order of src/hevc/intra.rs:
+    // 19-65 (k: 0..NL-1 the left column's units bottom-up, NL the corner,
+    // NL+1..2 NL the top row's units left to right).  Lane k decides unit k's
+    // availability (and waits for it when it is an intra block); a ballot
+    // gives the mask of available units.
+    const int NL = n2 >> lu, nk = 2 * NL + 1;
+    auto unit_xy = [&](int k, int &xn, int &yn) {  // the unit's first luma sample
+        if (k < NL) { xn = xl - 1; yn = (y0 + ((NL - 1 - k) << lu)) * sc; }
+        else if (k == NL) { xn = xl - 1; yn = yl - 1; }
+        else { xn = (x0 + ((k - NL - 1) << lu)) * sc; yn = yl - 1; }
+    };
+    auto unit_avail = [&](int k, bool &ok) -> bool {
         int xn, yn;
-        if (u == 0) { xn = xl - 1; yn = yl - 1; }
-        else if (u <= (n2 >> lu)) { xn = xl - 1; yn = (y0 + ((u - 1) << lu)) * sc; }
-        else { xn = (x0 + ((u - 1 - (n2 >> lu)) << lu)) * sc; yn = yl - 1; }
+        unit_xy(k, xn, yn);
         bool a = zavail(P, xl, yl, xn, yn);
         const bool in = C.inside(xn, yn);
-        uint8_t bf = !a ? 0 : in ? C.blkf[((yn - C.y0) >> 2) * 16 + ((xn - C.x0) >> 2)] : P.blk[(yn >> 2) * P.w4 + (xn >> 2)].flags;
+        const uint8_t bf = !a ? 0 : in ? C.blkf[((yn - C.y0) >> 2) * 16 + ((xn - C.x0) >> 2)] : P.blk[(yn >> 2) * P.w4 + (xn >> 2)].flags;
         if (a && P.constrained_intra && !(bf & RC_HEVC_F_INTRA)) a = false;
         if (a && (bf & RC_HEVC_F_INTRA)) {
             if (in) ok = ok && wait_local(C.flag(c, xn, yn), P.wait_limit, P.error);
@@ -465,63 +471,46 @@ __device__ void intra_tu(const HevcLaunch &P, IntraSmem &S, const CtbCanvas<T> &
                 ok = ok && wait_flag(P.ready + (size_t)c * P.w4 * P.h4 + (yn >> 2) * P.w4 + (xn >> 2), P.epoch,
                                      P.wait_limit, P.error);
         }
-        if (u == 0) S.al[0] = S.at[0] = a;
-        else if (u <= (n2 >> lu)) for (int i = 0; i < unit; i++) S.al[1 + ((u - 1) << lu) + i] = a;
-        else for (int i = 0; i < unit; i++) S.at[1 + ((u - 1 - (n2 >> lu)) << lu) + i] = a;
-    }
+        return a;
+    };
+    bool ok = true;
+    const bool a0 = lane < nk && unit_avail(lane, ok);
+    const bool a1 = lane + 32 < nk && unit_avail(lane + 32, ok);  // a 32x32 luma block's last top unit
+    const unsigned long long mask =
+        (unsigned long long)__ballot_sync(0xffffffffu, a1) << 32 | __ballot_sync(0xffffffffu, a0);
     if (!__all_sync(0xffffffffu, ok)) {
         if (lane == 0) atomicOr(P.error, RC_DEV_ERR_TIMEOUT);
         return;
     }
-    __syncwarp();
     __threadfence_block();
-    // ---- reference samples (pre-deblock picture)
-    for (int i = lane; i <= n2; i += 32) {
-        if (i == 0) {
-            const uint16_t v = S.al[0] ? ref(x0 - 1, y0 - 1) : 0;
-            S.left[0] = S.top[0] = v;
-        } else {
-            S.left[i] = S.al[i] ? ref(x0 - 1, y0 + i - 1) : 0;
-            S.top[i] = S.at[i] ? ref(x0 + i - 1, y0 - 1) : 0;
-        }
-    }
-    __syncwarp();
-    // ---- substitute, src/hevc/intra.rs:19-65.  In scan order (up the left
-    // column from the bottom, the corner, then along the top) an unavailable
-    // sample takes its predecessor's value and a leading run the first
-    // available sample's; availability is uniform per unit, so a ballot over
-    // the units (scan index k: 0..NL-1 left units bottom-up, NL the corner,
-    // NL+1.. top units) finds every sample's source at once.
+    // ---- reference samples with substitution in one pass: scan-order
+    // sample j (0..n2-1 left bottom-up, n2 the corner, n2+1.. top) reads
+    // itself when its unit is available, else the last sample of the nearest
+    // available unit before it, else (a leading run) the first available
+    // sample; none available: 1 << (bd - 1)
     {
-        const int NL = n2 >> lu, nk = 2 * NL + 1;
-        auto unit_avail = [&](int k) -> bool {
-            return k < NL ? S.al[1 + ((NL - 1 - k) << lu)] : k == NL ? S.al[0] : S.at[1 + ((k - NL - 1) << lu)];
-        };
-        // the unit's first / last sample in scan order
-        auto unit_val = [&](int k, bool last) -> int {
-            if (k < NL) return S.left[last ? 1 + ((NL - 1 - k) << lu) : n2 - (k << lu)];
-            if (k == NL) return S.left[0];
-            return S.top[last ? (k - NL) << lu : 1 + ((k - NL - 1) << lu)];
-        };
-        const uint32_t m0 = __ballot_sync(0xffffffffu, lane < nk && unit_avail(lane));
-        const uint32_t m1 = __ballot_sync(0xffffffffu, lane + 32 < nk && unit_avail(lane + 32));
-        const unsigned long long mask = (unsigned long long)m1 << 32 | m0;
         const int first = __ffsll((long long)mask) - 1;
-        const unsigned long long all = nk >= 64 ? ~0ull : (1ull << nk) - 1;
-        // every unit available (the common case inside a picture): nothing to substitute
-        for (int i = lane; i <= 2 * n2 && mask != all; i += 32) {
-            // sample i: 0 corner, 1..n2 left[i], n2+1..2 n2 top[i - n2]
-            const int k = i == 0 ? NL : i <= n2 ? NL - 1 - ((i - 1) >> lu) : NL + 1 + ((i - n2 - 1) >> lu);
-            if (mask >> k & 1) continue;
-            int v;
-            if (!mask) v = 1 << (bd - 1);
-            else {
+        auto unit_first = [&](int k) -> int { return k < NL ? k << lu : k == NL ? n2 : n2 + 1 + ((k - NL - 1) << lu); };
+        for (int j = lane; j <= 2 * n2; j += 32) {
+            const int k = j < n2 ? j >> lu : j == n2 ? NL : NL + 1 + ((j - n2 - 1) >> lu);
+            int src = j;
+            if (!(mask >> k & 1)) {
                 const unsigned long long below = mask & ((1ull << k) - 1);
-                v = below ? unit_val(63 - __clzll((long long)below), true) : unit_val(first, false);
+                if (below) {
+                    const int kb = 63 - __clzll((long long)below);
+                    src = unit_first(kb) + (kb == NL ? 0 : unit - 1);
+                } else {
+                    src = unit_first(first);
+                }
             }
-            if (i == 0) S.left[0] = S.top[0] = (uint16_t)v;
-            else if (i <= n2) S.left[i] = (uint16_t)v;
-            else S.top[i - n2] = (uint16_t)v;
+            uint16_t v = (uint16_t)(1 << (bd - 1));
+            if (mask) {
+                const int x = src < n2 ? x0 - 1 : src == n2 ? x0 - 1 : x0 + src - n2 - 1;
+                const int y = src < n2 ? y0 + n2 - 1 - src : y0 - 1;
+                v = ref(x, y);
+            }
+            if (j <= n2) S.left[n2 - j] = v;
+            if (j >= n2) S.top[j - n2] = v;
         }
     }
     __syncwarp();
@@ -587,8 +576,6 @@ __device__ void intra_tu(const HevcLaunch &P, IntraSmem &S, const CtbCanvas<T> &
         }
         __syncwarp();
     }
-    const int16_t *rp = res_plane(P, c);
-    const int rpitch = c ? P.CW : P.W;
     for (int i = lane; i < n * n; i += 32) {
         const int y = i >> log2, x = i & (n - 1);
         int v;
