@@ -657,7 +657,11 @@ __global__ void __launch_bounds__(32 * INTRA_WARPS) hevc_intra_kernel(HevcLaunch
     C.rdy = rdy;
     for (;;) {
         __syncthreads();  // the previous CTB is finished with the shared state
-        if (tid == 0) task = aborted(P.error) ? nctb : (int)atomicAdd(P.counter, 1u);
+        if (tid == 0) {  // the error word and the next task, both requests in flight at once
+            const uint32_t er = *(const volatile uint32_t *)P.error;
+            const int tk = (int)atomicAdd(P.counter, 1u);
+            task = (er & RC_DEV_ERR_TIMEOUT) ? nctb : tk;
+        }
         __syncthreads();
         if (task >= nctb) return;
         const int cb = P.ctb_base[task];
@@ -726,9 +730,12 @@ __global__ void __launch_bounds__(32 * INTRA_WARPS) hevc_intra_kernel(HevcLaunch
                 if (lane == 0) atomicOr(P.error, RC_DEV_ERR_RECORD);
                 continue;
             }
+            // the error word, read as the block starts and tested once its
+            // flags are out (a global read there would delay every waiting
+            // block by a round trip)
+            const uint32_t err0 = *(const volatile uint32_t *)P.error;
             if (t.flags & RC_HEVC_TU_PCM) pcm_tu<T>(P, C, t, lane);
             else intra_tu<T>(P, S, C, t, lane);
-            if (aborted(P.error)) break;
             // the block's luma-grid 4x4 units, for the warps of this CTA
             __syncwarp();
             __threadfence_block();
@@ -743,6 +750,7 @@ __global__ void __launch_bounds__(32 * INTRA_WARPS) hevc_intra_kernel(HevcLaunch
                 for (int i = lane; i < bw * bw; i += 32)
                     st_relaxed(gr + (size_t)(((t.y0 * sc) >> 2) + i / bw) * P.w4 + ((t.x0 * sc) >> 2) + i % bw, P.epoch);
             }
+            if (err0 & RC_DEV_ERR_TIMEOUT) break;
         }
     }
 }
