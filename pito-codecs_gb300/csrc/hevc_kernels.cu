@@ -386,7 +386,6 @@ __device__ bool zavail(const HevcLaunch &P, int xc, int yc, int xn, int yn) {
 struct __align__(16) IntraSmem {
     uint16_t left[136], top[136];   // reference samples (index 0 = corner)
     uint16_t fleft[136], ftop[136]; // smoothed copy
-    int refa[200];
 };
 
 // The CTB a CTA reconstructs: its luma origin and size, a shared-memory copy
@@ -560,22 +559,14 @@ __device__ void intra_tu(const HevcLaunch &P, IntraSmem &S, const CtbCanvas<T> &
         for (int i = lane; i < n; i += 32) s += Tp[1 + i] + L[1 + i];
         s = __reduce_add_sync(0xffffffffu, (unsigned)s);
         dc = (s + n) >> (log2 + 1);
-    } else if (mode >= 2) {
-        const int angle = cANGLE[mode], base = n;
-        const uint16_t *mn = mode >= 18 ? Tp : L, *sd = mode >= 18 ? L : Tp;
-        for (int x = lane; x <= 2 * n; x += 32) {
-            if (x <= n) S.refa[base + x] = mn[x];
-            else if (angle >= 0) S.refa[base + x] = mn[x];
-        }
-        if (angle < 0) {
-            const int lim = (n * angle) >> 5;
-            if (lim < -1) {
-                const int inv = cINV_ANGLE[mode - 11];
-                for (int x = lim + lane; x <= -1; x += 32) S.refa[base + x] = sd[-1 + ((x * inv + 128) >> 8) + 1];
-            }
-        }
-        __syncwarp();
     }
+    // angular: ref[r] of src/hevc/intra.rs is read where it is needed, the
+    // main side's sample r for r >= 0, else (a negative angle) the side
+    // reference projected onto it, p[-1][-1 + ((r * invAngle + 128) >> 8)];
+    // r < 0 only occurs when (n * angle) >> 5 < -1, as the standard has it
+    const int angle = mode >= 2 ? cANGLE[mode] : 0, inv = angle < 0 ? cINV_ANGLE[mode - 11] : 0;
+    const uint16_t *mn = mode >= 18 ? Tp : L, *sd = mode >= 18 ? L : Tp;
+    auto refv = [&](int r) -> int { return r >= 0 ? mn[r] : sd[(r * inv + 128) >> 8]; };
     for (int i = lane; i < n * n; i += 32) {
         const int y = i >> log2, x = i & (n - 1);
         int v;
@@ -590,13 +581,12 @@ __device__ void intra_tu(const HevcLaunch &P, IntraSmem &S, const CtbCanvas<T> &
                 else if (x == 0) v = (L[1 + y] + 3 * dc + 2) >> 2;
             }
         } else {
-            const int angle = cANGLE[mode];
             const bool horizontal = mode < 18;
             // output (x, y): horizontal modes run j along x, vertical along y
             const int j = horizontal ? x : y, ii = horizontal ? y : x;
             const int pos = (j + 1) * angle, idx = pos >> 5, fact = pos & 31;
-            const int k = n + ii + idx + 1;
-            v = fact ? ((32 - fact) * S.refa[k] + fact * S.refa[k + 1] + 16) >> 5 : S.refa[k];
+            const int r = ii + idx + 1;
+            v = fact ? ((32 - fact) * refv(r) + fact * refv(r + 1) + 16) >> 5 : refv(r);
             if (edge) {
                 if (mode == 26 && x == 0) v = clampi(Tp[1] + ((L[1 + y] - L[0]) >> 1), 0, max);
                 else if (mode == 10 && y == 0) v = clampi(L[1] + ((Tp[1 + x] - Tp[0]) >> 1), 0, max);
