@@ -907,8 +907,8 @@ __global__ void __launch_bounds__(128) hevc_deblock_kernel(HevcLaunch P) {
 }
 
 // ===========================================================================
-// SAO, src/hevc/filter.rs:521-894: one thread per sample, deblocked work
-// picture -> DPB slot
+// SAO, src/hevc/filter.rs:521-894: four samples per thread, deblocked
+// work picture -> DPB slot
 // ===========================================================================
 // cross_ok, filter.rs:605-632
 __device__ bool cross_ok(const HevcLaunch &P, int rs, int nrs) {
@@ -922,51 +922,100 @@ __device__ bool cross_ok(const HevcLaunch &P, int rs, int nrs) {
     return P.lf_across_tiles || n.tile == q.tile;
 }
 
+// Four horizontally adjacent samples of a plane row (x a multiple of 4: the
+// planes' widths and pitches keep such groups aligned)
+template <class T> struct Quad;
+template <> struct Quad<uint8_t> {
+    __device__ static void load(const uint8_t *p, int v[4]) {
+        const uint32_t w = *(const uint32_t *)p;
+        for (int i = 0; i < 4; i++) v[i] = (w >> (8 * i)) & 255;
+    }
+    __device__ static void store(uint8_t *p, const int v[4]) {
+        *(uint32_t *)p = (uint32_t)v[0] | (uint32_t)v[1] << 8 | (uint32_t)v[2] << 16 | (uint32_t)v[3] << 24;
+    }
+};
+template <> struct Quad<uint16_t> {
+    __device__ static void load(const uint16_t *p, int v[4]) {
+        const uint2 w = *(const uint2 *)p;
+        v[0] = w.x & 0xffff; v[1] = w.x >> 16; v[2] = w.y & 0xffff; v[3] = w.y >> 16;
+    }
+    __device__ static void store(uint16_t *p, const int v[4]) {
+        *(uint2 *)p = make_uint2((uint32_t)v[0] | (uint32_t)v[1] << 16, (uint32_t)v[2] | (uint32_t)v[3] << 16);
+    }
+};
+
+// SAO, src/hevc/filter.rs sao: four samples per thread, which share a CTB
+// (its parameters and slice are read once) and whose neighbours are read
+// together
 template <class T>
 __global__ void __launch_bounds__(256) hevc_sao_kernel(HevcLaunch P) {
     const int c = blockIdx.z, sc = c ? 1 : 0;
     const int w = c ? P.CW : P.W, h = c ? P.CH : P.H;
-    const int x = blockIdx.x * 32 + (threadIdx.x & 31), y = blockIdx.y * 8 + (threadIdx.x >> 5);
-    if (x >= w || y >= h) return;
+    const int x0 = (blockIdx.x * 32 + (threadIdx.x & 31)) * 4, y = blockIdx.y * 8 + (threadIdx.x >> 5);
+    if (x0 >= w || y >= h) return;
     const long pitch = pitch_el(P, c, sizeof(T));
     const T *in = plane_ptr<T>(P.work, P, c);
     T *out = plane_ptr<T>(P.dpb + (size_t)P.out_slot * P.slot_bytes, P, c);
-    const int v = in[(size_t)y * pitch + x];
-    int res = v;
+    int v[4], res[4];
+    Quad<T>::load(in + (size_t)y * pitch + x0, v);
     const int s = P.log2ctb - sc;
-    const int rs = (y >> s) * P.wctb + (x >> s);
+    const int rs = (y >> s) * P.wctb + (x0 >> s);
     const rc_hevc_ctb &ct = P.ctbs[rs];
     const rc_hevc_slice *sl = slice_of_ctb(P, rs);
     const int type = ct.sao.type_idx[c];
-    const bool nof = P.blk[((y << sc) >> 2) * P.w4 + ((x << sc) >> 2)].flags & RC_HEVC_F_NOFILTER;
-    if ((c ? sl->sao_chroma : sl->sao_luma) && type != 0 && !nof && ct.slice < P.num_slices) {
+    // the 4x4 luma units' no-filter flags (one unit for luma, two for chroma)
+    const rc_hevc_blk *brow = P.blk + (size_t)((y << sc) >> 2) * P.w4;
+    bool nof[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) nof[i] = brow[((x0 + i) << sc) >> 2].flags & RC_HEVC_F_NOFILTER;
+#pragma unroll
+    for (int i = 0; i < 4; i++) res[i] = v[i];
+    if ((c ? sl->sao_chroma : sl->sao_luma) && type != 0 && ct.slice < P.num_slices) {
         const int bd = P.bd, max = (1 << bd) - 1;
         if (type == 1) {
-            const int band = v >> (bd - 5), k = (band - ct.sao.band_pos[c]) & 31;
-            if (k < 4) res = clampi(v + ct.sao.offsets[c][k], 0, max);
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                const int band = v[i] >> (bd - 5), k = (band - ct.sao.band_pos[c]) & 31;
+                if (k < 4) res[i] = clampi(v[i] + ct.sao.offsets[c][k], 0, max);
+            }
         } else {
             const int cls = ct.sao.eo_class[c] & 3;
             const int hp0 = cls == 1 ? 0 : cls == 3 ? 1 : -1, hp1 = -hp0;
             const int vp0 = cls == 0 ? 0 : -1, vp1 = -vp0;
-            bool ok = true;
-            int sum = 0;
+            // the two neighbours of every sample: read first, all of them
+            int nv[2][4];
+            bool ok[4];
 #pragma unroll
-            for (int j = 0; j < 2; j++) {
-                const int xn = x + (j ? hp1 : hp0), yn = y + (j ? vp1 : vp0);
-                if (xn < 0 || yn < 0 || xn >= w || yn >= h) { ok = false; break; }
-                const int nrs = (yn >> s) * P.wctb + (xn >> s);
-                if (!cross_ok(P, rs, nrs)) { ok = false; break; }
-                const int nv = in[(size_t)yn * pitch + xn];
-                sum += (v > nv) - (v < nv);
+            for (int i = 0; i < 4; i++) {
+                ok[i] = true;
+#pragma unroll
+                for (int j = 0; j < 2; j++) {
+                    const int xn = x0 + i + (j ? hp1 : hp0), yn = y + (j ? vp1 : vp0);
+                    const bool in_pic = xn >= 0 && yn >= 0 && xn < w && yn < h;
+                    nv[j][i] = in_pic ? (int)in[(size_t)yn * pitch + xn] : 0;
+                    ok[i] = ok[i] && in_pic;
+                }
             }
-            if (ok) {
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                bool good = ok[i];
+#pragma unroll
+                for (int j = 0; j < 2 && good; j++) {
+                    const int xn = x0 + i + (j ? hp1 : hp0), yn = y + (j ? vp1 : vp0);
+                    good = cross_ok(P, rs, (yn >> s) * P.wctb + (xn >> s));
+                }
+                if (!good) continue;
+                const int sum = (v[i] > nv[0][i]) - (v[i] < nv[0][i]) + (v[i] > nv[1][i]) - (v[i] < nv[1][i]);
                 // edge_map [1, 2, 0, 3, 4]: sum -2 -> offsets[0], -1 -> [1], 0 -> none, 1 -> [2], 2 -> [3]
                 const int e = sum == -2 ? 0 : sum == -1 ? 1 : sum == 1 ? 2 : sum == 2 ? 3 : -1;
-                if (e >= 0) res = clampi(v + ct.sao.offsets[c][e], 0, max);
+                if (e >= 0) res[i] = clampi(v[i] + ct.sao.offsets[c][e], 0, max);
             }
         }
     }
-    out[(size_t)y * pitch + x] = (T)res;
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+        if (nof[i]) res[i] = v[i];
+    Quad<T>::store(out + (size_t)y * pitch + x0, res);
 }
 
 template <class T>
@@ -1017,7 +1066,7 @@ void rc_launch_hevc_deblock(const HevcLaunch &p, cudaStream_t st) {
 }
 
 void rc_launch_hevc_sao(const HevcLaunch &p, cudaStream_t st) {
-    dim3 grid((p.W + 31) / 32, (p.H + 7) / 8, 3);
+    dim3 grid((p.W / 4 + 31) / 32, (p.H + 7) / 8, 3);
     if (p.bd > 8) hevc_sao_kernel<uint16_t><<<grid, 256, 0, st>>>(p);
     else hevc_sao_kernel<uint8_t><<<grid, 256, 0, st>>>(p);
 }
