@@ -347,7 +347,8 @@ def serve_plain(specs, templates, trace, clock=time.perf_counter, open_fn=open_s
     t0 = clock()
     for req in sorted(trace, key=lambda r: r.arrival):
         while clock() - t0 < req.arrival:
-            time.sleep(min(1e-3, req.arrival - (clock() - t0)))
+            # the arrival may pass between the test and this read of the clock
+            time.sleep(max(0.0, min(1e-3, req.arrival - (clock() - t0))))
         key = req.stream
         if key not in streams:
             streams[key] = open_fn(specs[key])
