@@ -232,46 +232,99 @@ __device__ __forceinline__ int rsamp(const T *p, int pitch, int w, int h, int x,
     return __ldg(p + (size_t)clampi(y, 0, h - 1) * pitch + clampi(x, 0, w - 1));
 }
 
-// interpolate, inter.rs:86-133, one sample at integer position (xi, yi)
-template <class T, int TAPS>
-__device__ int interp(const T *p, int pitch, int w, int h, int xi, int yi, int fx, int fy, int bd) {
-    constexpr int m = TAPS / 2 - 1;
+// Four horizontally adjacent samples of a plane row (x a multiple of 4: the
+// planes' widths and pitches keep such groups aligned)
+template <class T> struct Quad;
+template <> struct Quad<uint8_t> {
+    __device__ static void load(const uint8_t *p, int v[4]) {
+        const uint32_t w = *(const uint32_t *)p;
+        for (int i = 0; i < 4; i++) v[i] = (w >> (8 * i)) & 255;
+    }
+    __device__ static void store(uint8_t *p, const int v[4]) {
+        *(uint32_t *)p = (uint32_t)v[0] | (uint32_t)v[1] << 8 | (uint32_t)v[2] << 16 | (uint32_t)v[3] << 24;
+    }
+};
+template <> struct Quad<uint16_t> {
+    __device__ static void load(const uint16_t *p, int v[4]) {
+        const uint2 w = *(const uint2 *)p;
+        v[0] = w.x & 0xffff; v[1] = w.x >> 16; v[2] = w.y & 0xffff; v[3] = w.y >> 16;
+    }
+    __device__ static void store(uint16_t *p, const int v[4]) {
+        *(uint2 *)p = make_uint2((uint32_t)v[0] | (uint32_t)v[1] << 16, (uint32_t)v[2] | (uint32_t)v[3] << 16);
+    }
+};
+
+// interpolate, inter.rs:86-133, for N horizontally adjacent samples from
+// integer position (xi, yi) with one motion vector: each reference row's
+// N + TAPS - 1 samples are read once for the N outputs
+template <class T, int TAPS, int N>
+__device__ void interp_n(const T *p, int pitch, int w, int h, int xi, int yi, int fx, int fy, int bd, int out[N]) {
+    constexpr int m = TAPS / 2 - 1, W = N + TAPS - 1;
     const int shift1 = min(bd, 12) - 8, shift3 = 14 - bd;
-    if (fx == 0 && fy == 0) return (int16_t)(rsamp(p, pitch, w, h, xi, yi) << shift3);
+    if (fx == 0 && fy == 0) {
+#pragma unroll
+        for (int i = 0; i < N; i++) out[i] = (int16_t)(rsamp(p, pitch, w, h, xi + i, yi) << shift3);
+        return;
+    }
     const int8_t *hf = TAPS == 8 ? cLUMA_F[fx] : cCHROMA_F[fx];
     const int8_t *vf = TAPS == 8 ? cLUMA_F[fy] : cCHROMA_F[fy];
     if (fy == 0) {
-        int s = 0;
+        int s[W];
 #pragma unroll
-        for (int k = 0; k < TAPS; k++) s += hf[k] * rsamp(p, pitch, w, h, xi - m + k, yi);
-        return (int16_t)(s >> shift1);
+        for (int j = 0; j < W; j++) s[j] = rsamp(p, pitch, w, h, xi - m + j, yi);
+#pragma unroll
+        for (int i = 0; i < N; i++) {
+            int a = 0;
+#pragma unroll
+            for (int k = 0; k < TAPS; k++) a += hf[k] * s[i + k];
+            out[i] = (int16_t)(a >> shift1);
+        }
+        return;
     }
     if (fx == 0) {
-        int s = 0;
+        int a[N];
 #pragma unroll
-        for (int k = 0; k < TAPS; k++) s += vf[k] * rsamp(p, pitch, w, h, xi, yi - m + k);
-        return (int16_t)(s >> shift1);
+        for (int i = 0; i < N; i++) a[i] = 0;
+#pragma unroll
+        for (int k = 0; k < TAPS; k++)
+#pragma unroll
+            for (int i = 0; i < N; i++) a[i] += vf[k] * rsamp(p, pitch, w, h, xi + i, yi - m + k);
+#pragma unroll
+        for (int i = 0; i < N; i++) out[i] = (int16_t)(a[i] >> shift1);
+        return;
     }
-    int v = 0;
+    int v[N];
+#pragma unroll
+    for (int i = 0; i < N; i++) v[i] = 0;
 #pragma unroll
     for (int r = 0; r < TAPS; r++) {
-        int s = 0;
+        int s[W];
 #pragma unroll
-        for (int k = 0; k < TAPS; k++) s += hf[k] * rsamp(p, pitch, w, h, xi - m + k, yi - m + r);
-        v += vf[r] * (int16_t)(s >> shift1);
+        for (int j = 0; j < W; j++) s[j] = rsamp(p, pitch, w, h, xi - m + j, yi - m + r);
+#pragma unroll
+        for (int i = 0; i < N; i++) {
+            int a = 0;
+#pragma unroll
+            for (int k = 0; k < TAPS; k++) a += hf[k] * s[i + k];
+            v[i] += vf[r] * (int16_t)(a >> shift1);
+        }
     }
-    return (int16_t)(v >> 6);
+#pragma unroll
+    for (int i = 0; i < N; i++) out[i] = (int16_t)(v[i] >> 6);
 }
 
-// motion_compensate + put_uni / put_bi / put_weighted_*, for one sample
-template <class T>
-__device__ int mc_sample(const HevcLaunch &P, int c, int x, int y, const rc_hevc_mvf &f, const rc_hevc_slice *sl) {
+// motion_compensate + put_uni / put_bi / put_weighted_*, for N horizontally
+// adjacent samples of one motion field
+template <class T, int N>
+__device__ void mc_n(const HevcLaunch &P, int c, int x, int y, const rc_hevc_mvf &f, const rc_hevc_slice *sl, int out[N]) {
     const int bd = P.bd, max = (1 << bd) - 1;
-    int pv[2] = {0, 0};
+    int pv[2][N];
     bool use[2] = {false, false};
     const int pw = c ? P.CW : P.W, ph = c ? P.CH : P.H, pitch = pitch_el(P, c, sizeof(T));
 #pragma unroll
     for (int l = 0; l < 2; l++) {
+#pragma unroll
+        for (int i = 0; i < N; i++) pv[l][i] = 0;
         int ri = f.ref_idx[l];
         if (ri < 0) continue;
         int slot = ri < min(sl->num_ref[l], RC_HEVC_MAX_REFS) ? sl->ref_slot[l][ri] : -1;
@@ -279,17 +332,21 @@ __device__ int mc_sample(const HevcLaunch &P, int c, int x, int y, const rc_hevc
         use[l] = true;
         const T *p = plane_ptr<T>(P.dpb + (size_t)slot * P.slot_bytes, P, c);
         int mvx = f.mv[l][0], mvy = f.mv[l][1];
-        if (c == 0) pv[l] = interp<T, 8>(p, pitch, pw, ph, x + (mvx >> 2), y + (mvy >> 2), mvx & 3, mvy & 3, bd);
-        else pv[l] = interp<T, 4>(p, pitch, pw, ph, x + (mvx >> 3), y + (mvy >> 3), mvx & 7, mvy & 7, bd);
+        if (c == 0) interp_n<T, 8, N>(p, pitch, pw, ph, x + (mvx >> 2), y + (mvy >> 2), mvx & 3, mvy & 3, bd, pv[l]);
+        else interp_n<T, 4, N>(p, pitch, pw, ph, x + (mvx >> 3), y + (mvy >> 3), mvx & 7, mvy & 7, bd, pv[l]);
     }
     const bool bi = use[0] && use[1];
     if (!sl->weighted) {
         if (bi) {
             const int shift = 15 - bd;
-            return clampi((pv[0] + pv[1] + (1 << (shift - 1))) >> shift, 0, max);
+#pragma unroll
+            for (int i = 0; i < N; i++) out[i] = clampi((pv[0][i] + pv[1][i] + (1 << (shift - 1))) >> shift, 0, max);
+            return;
         }
         const int shift = 14 - bd, off = shift > 0 ? 1 << (shift - 1) : 0;
-        return clampi((pv[use[0] ? 0 : 1] + off) >> shift, 0, max);
+#pragma unroll
+        for (int i = 0; i < N; i++) out[i] = clampi(((use[0] ? pv[0][i] : pv[1][i]) + off) >> shift, 0, max);
+        return;
     }
     const int log2wd = (c ? sl->chroma_log2_denom : sl->luma_log2_denom) + 14 - bd;
     int w[2] = {0, 0}, o[2] = {0, 0};
@@ -300,42 +357,61 @@ __device__ int mc_sample(const HevcLaunch &P, int c, int x, int y, const rc_hevc
         w[l] = c ? sl->chroma_w[l][ri][c - 1] : sl->luma_w[l][ri];
         o[l] = (c ? sl->chroma_o[l][ri][c - 1] : sl->luma_o[l][ri]) * (1 << (bd - 8));
     }
-    if (bi) return clampi((pv[0] * w[0] + pv[1] * w[1] + ((o[0] + o[1] + 1) << log2wd)) >> (log2wd + 1), 0, max);
+    if (bi) {
+#pragma unroll
+        for (int i = 0; i < N; i++)
+            out[i] = clampi((pv[0][i] * w[0] + pv[1][i] * w[1] + ((o[0] + o[1] + 1) << log2wd)) >> (log2wd + 1), 0, max);
+        return;
+    }
     const int l = use[0] ? 0 : 1;
-    int v = pv[l] * w[l];
-    v = log2wd >= 1 ? ((v + (1 << (log2wd - 1))) >> log2wd) + o[l] : v + o[l];
-    return clampi(v, 0, max);
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+        int v = (l ? pv[1][i] : pv[0][i]) * w[l];
+        v = log2wd >= 1 ? ((v + (1 << (log2wd - 1))) >> log2wd) + o[l] : v + o[l];
+        out[i] = clampi(v, 0, max);
+    }
 }
 
-// One CTA per 8x8 luma block: 64 luma samples + 2x16 chroma samples.
+// One CTA per 16x16 luma area: a thread reconstructs four adjacent luma
+// samples of one 4x4 unit, then two adjacent chroma samples (of one unit
+// too), each group with its motion field read once
 template <class T>
 __global__ void __launch_bounds__(64) hevc_inter_kernel(HevcLaunch P) {
     const int t = threadIdx.x;
-    const int bx8 = blockIdx.x, by8 = blockIdx.y;
     uint8_t *work = P.work;
     const int max = (1 << P.bd) - 1;
     {
-        const int x = bx8 * 8 + (t & 7), y = by8 * 8 + (t >> 3);
-        const int bi = (y >> 2) * P.w4 + (x >> 2);
-        const rc_hevc_blk b = P.blk[bi];
-        if ((b.flags & RC_HEVC_F_CODED) && !(b.flags & RC_HEVC_F_INTRA)) {
-            const rc_hevc_mvf f = P.mvf[bi];
-            const rc_hevc_slice *sl = slice_of_ctb(P, ctb_of(P, x, y));
-            int v = mc_sample<T>(P, 0, x, y, f, sl);
-            v = clampi(v + res_plane(P, 0)[(size_t)y * P.W + x], 0, max);
-            plane_ptr<T>(work, P, 0)[(size_t)y * pitch_el(P, 0, sizeof(T)) + x] = (T)v;
+        const int x = blockIdx.x * 16 + (t & 3) * 4, y = blockIdx.y * 16 + (t >> 2);
+        if (x < P.W && y < P.H) {  // W is a multiple of 8: the group lies inside
+            const int bi = (y >> 2) * P.w4 + (x >> 2);
+            const rc_hevc_blk b = P.blk[bi];
+            if ((b.flags & RC_HEVC_F_CODED) && !(b.flags & RC_HEVC_F_INTRA)) {
+                const rc_hevc_mvf f = P.mvf[bi];
+                const rc_hevc_slice *sl = slice_of_ctb(P, ctb_of(P, x, y));
+                int v[4];
+                mc_n<T, 4>(P, 0, x, y, f, sl, v);
+                const int16_t *r = res_plane(P, 0) + (size_t)y * P.W + x;
+#pragma unroll
+                for (int i = 0; i < 4; i++) v[i] = clampi(v[i] + r[i], 0, max);
+                Quad<T>::store(plane_ptr<T>(work, P, 0) + (size_t)y * pitch_el(P, 0, sizeof(T)) + x, v);
+            }
         }
     }
-    if (t < 32) {
-        const int c = 1 + (t >> 4), x = bx8 * 4 + (t & 3), y = by8 * 4 + ((t >> 2) & 3);
-        const int bi = ((2 * y) >> 2) * P.w4 + ((2 * x) >> 2);
-        const rc_hevc_blk b = P.blk[bi];
-        if ((b.flags & RC_HEVC_F_CODED) && !(b.flags & RC_HEVC_F_INTRA)) {
-            const rc_hevc_mvf f = P.mvf[bi];
-            const rc_hevc_slice *sl = slice_of_ctb(P, ctb_of(P, 2 * x, 2 * y));
-            int v = mc_sample<T>(P, c, x, y, f, sl);
-            v = clampi(v + res_plane(P, c)[(size_t)y * P.CW + x], 0, max);
-            plane_ptr<T>(work, P, c)[(size_t)y * pitch_el(P, c, sizeof(T)) + x] = (T)v;
+    {
+        const int c = 1 + (t >> 5), x = blockIdx.x * 8 + (t & 3) * 2, y = blockIdx.y * 8 + ((t >> 2) & 7);
+        if (x < P.CW && y < P.CH) {  // CW is a multiple of 4
+            const int bi = ((2 * y) >> 2) * P.w4 + ((2 * x) >> 2);
+            const rc_hevc_blk b = P.blk[bi];
+            if ((b.flags & RC_HEVC_F_CODED) && !(b.flags & RC_HEVC_F_INTRA)) {
+                const rc_hevc_mvf f = P.mvf[bi];
+                const rc_hevc_slice *sl = slice_of_ctb(P, ctb_of(P, 2 * x, 2 * y));
+                int v[2];
+                mc_n<T, 2>(P, c, x, y, f, sl, v);
+                const int16_t *r = res_plane(P, c) + (size_t)y * P.CW + x;
+                T *o = plane_ptr<T>(work, P, c) + (size_t)y * pitch_el(P, c, sizeof(T)) + x;
+#pragma unroll
+                for (int i = 0; i < 2; i++) o[i] = (T)clampi(v[i] + r[i], 0, max);
+            }
         }
     }
 }
@@ -922,28 +998,6 @@ __device__ bool cross_ok(const HevcLaunch &P, int rs, int nrs) {
     return P.lf_across_tiles || n.tile == q.tile;
 }
 
-// Four horizontally adjacent samples of a plane row (x a multiple of 4: the
-// planes' widths and pitches keep such groups aligned)
-template <class T> struct Quad;
-template <> struct Quad<uint8_t> {
-    __device__ static void load(const uint8_t *p, int v[4]) {
-        const uint32_t w = *(const uint32_t *)p;
-        for (int i = 0; i < 4; i++) v[i] = (w >> (8 * i)) & 255;
-    }
-    __device__ static void store(uint8_t *p, const int v[4]) {
-        *(uint32_t *)p = (uint32_t)v[0] | (uint32_t)v[1] << 8 | (uint32_t)v[2] << 16 | (uint32_t)v[3] << 24;
-    }
-};
-template <> struct Quad<uint16_t> {
-    __device__ static void load(const uint16_t *p, int v[4]) {
-        const uint2 w = *(const uint2 *)p;
-        v[0] = w.x & 0xffff; v[1] = w.x >> 16; v[2] = w.y & 0xffff; v[3] = w.y >> 16;
-    }
-    __device__ static void store(uint16_t *p, const int v[4]) {
-        *(uint2 *)p = make_uint2((uint32_t)v[0] | (uint32_t)v[1] << 16, (uint32_t)v[2] | (uint32_t)v[3] << 16);
-    }
-};
-
 // SAO, src/hevc/filter.rs sao: four samples per thread, which share a CTB
 // (its parameters and slice are read once) and whose neighbours are read
 // together
@@ -1039,7 +1093,7 @@ void rc_launch_hevc_residual(const HevcLaunch &p, cudaStream_t st) {
 }
 
 void rc_launch_hevc_inter(const HevcLaunch &p, cudaStream_t st) {
-    dim3 grid(p.W / 8, p.H / 8);
+    dim3 grid((p.W + 15) / 16, (p.H + 15) / 16);
     if (p.bd > 8) hevc_inter_kernel<uint16_t><<<grid, 64, 0, st>>>(p);
     else hevc_inter_kernel<uint8_t><<<grid, 64, 0, st>>>(p);
 }
