@@ -500,7 +500,7 @@ __device__ bool wait_local(volatile uint8_t &f, uint32_t limit, const uint32_t *
     while (!f) {
         if (++it > limit) return false;
         if ((it & 63) == 0 && aborted(err)) return false;
-        if (it > 16) __nanosleep(32);
+        if (it > 256) __nanosleep(32);  // a neighbour block is usually done within a few hundred polls
     }
     return true;
 }
@@ -669,8 +669,27 @@ __device__ void intra_tu(const HevcLaunch &P, IntraSmem &S, const CtbCanvas<T> &
             }
         }
         if (t.flags & RC_HEVC_TU_CBF) v = clampi(v + C.resid(c, x0 + x, y0 + y), 0, max);
-        pl[(size_t)(y0 + y) * pitch + x0 + x] = (T)v;
-        C.at(c, x0 + x, y0 + y) = (T)v;
+        C.at(c, x0 + x, y0 + y) = (T)v;  // the picture gets the block after its ready flags (copy_out)
+    }
+}
+
+// A reconstructed block's rows from the CTB copy to the picture, in 16-,
+// 8- or 4-byte pieces (a block's rows are whole pieces: n * sizeof(T) is
+// 4..64 bytes, and its x is a multiple of n)
+template <class T>
+__device__ void copy_out(const HevcLaunch &P, const CtbCanvas<T> &C, int c, int x0, int y0, int n, int lane) {
+    T *pl = plane_ptr<T>(P.work, P, c);
+    const int pitch = pitch_el(P, c, sizeof(T)), bytes = n * (int)sizeof(T);
+    if (bytes >= 16) {
+        const int q = bytes / 16;
+        for (int i = lane; i < n * q; i += 32) {
+            const int y = i / q, j = i % q;
+            *((uint4 *)(pl + (size_t)(y0 + y) * pitch + x0) + j) = *((const uint4 *)&C.at(c, x0, y0 + y) + j);
+        }
+    } else if (bytes == 8) {
+        if (lane < n) *(uint2 *)(pl + (size_t)(y0 + lane) * pitch + x0) = *(const uint2 *)&C.at(c, x0, y0 + lane);
+    } else if (lane < n) {
+        *(uint32_t *)(pl + (size_t)(y0 + lane) * pitch + x0) = *(const uint32_t *)&C.at(c, x0, y0 + lane);
     }
 }
 
@@ -807,6 +826,9 @@ __global__ void __launch_bounds__(32 * INTRA_WARPS) hevc_intra_kernel(HevcLaunch
             __threadfence_block();
             const int bw = (n * sc) >> 2;
             for (int i = lane; i < bw * bw; i += 32) C.flag(t.c, t.x0 * sc + (i % bw) * 4, t.y0 * sc + (i / bw) * 4) = 1;
+            // then the picture's copy (blocks in this CTB read the CTB copy;
+            // later CTBs read the picture after the global flags below)
+            if (!(t.flags & RC_HEVC_TU_PCM)) copy_out<T>(P, C, t.c, t.x0, t.y0, n, lane);
             // a block on the CTB's right column or bottom row is read by later
             // CTBs: after a fence, its global ready flags (the shared ones are
             // set first, so this CTB's next blocks do not wait for the fence)
