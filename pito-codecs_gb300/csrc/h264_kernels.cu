@@ -21,7 +21,10 @@
 //                       the reference's MB-raster filter order
 //                       (src/h264/dec/slicedec.rs:184-208) behind the intra
 //                       warps; rows hand over through shared memory, bands
-//                       through progress words in global memory.
+//                       through progress words in global memory.  An intra
+//                       MB waits only for its intra neighbours in the row
+//                       above; the luma filter reports MB x-1 to the row
+//                       below as soon as MB x's left edge is filtered.
 //
 // rc_h264_deblock_noalloc filters a reconstructed picture without allocating
 // (h264_db_params_kernel, then h264_deblock_kernel: one warp per MB row).

@@ -8,22 +8,30 @@
 //                        shared memory (clamp between), transform skip, the
 //                        DC-only shortcut, transquant bypass -> int16 residual
 //                        planes.
-//  hevc_inter_kernel     one thread per sample of every inter block: 8-tap /
-//                        4-tap interpolation with i16 intermediates, default
-//                        or explicit weighted prediction, residual add, clip.
+//  hevc_inter_kernel     one 64-thread CTA per 16x16 luma area; a thread
+//                        takes four adjacent luma samples (two chroma) of one
+//                        motion field and reads each reference row once for
+//                        them: 8-tap / 4-tap interpolation with i16
+//                        intermediates, default or explicit weighted
+//                        prediction, residual add, clip.
 //  hevc_intra_kernel     persistent CTAs of 16 warps take CTBs in anti-diagonal
 //                        order and reconstruct a CTB's intra blocks in shared
-//                        memory, one warp per block in decode order: waits
-//                        (capped) only for the intra neighbour blocks it
-//                        reads -- shared-memory flags inside the CTB, global
-//                        ready flags across CTBs -- then substitutes / smooths
-//                        the reference samples and predicts (planar, DC, 33
-//                        angles + edge filters).
+//                        memory, one warp per block in decode order: one lane
+//                        per reference unit decides availability and waits
+//                        (capped) only for intra neighbour blocks --
+//                        shared-memory flags inside the CTB, global ready
+//                        flags across CTBs -- a ballot gives the available
+//                        units, the reference samples are gathered with
+//                        substitution in one pass, smoothed, and predicted
+//                        (planar, DC, 33 angles read straight from the
+//                        references + edge filters) into the CTB copy; the
+//                        block reaches the picture after its ready flags.
 //  hevc_deblock_kernel   vertical edges, then (second launch) horizontal
 //                        edges, one thread per 4-sample edge segment: edges
 //                        8 samples apart never interact within a direction.
-//  hevc_sao_kernel       one thread per sample: band / edge offsets from the
-//                        deblocked picture into the DPB slot.
+//  hevc_sao_kernel       four samples of one CTB per thread: band / edge
+//                        offsets from the deblocked picture into the DPB
+//                        slot.
 //
 // Arithmetic follows src/hevc/{transform,intra,inter,filter}.rs and the
 // reconstruction half of src/hevc/slicedec.rs; citations at each function.
