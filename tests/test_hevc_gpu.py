@@ -88,6 +88,13 @@ def test_dense_residual_and_far_motion(engine, oracle):
     run_sequence(engine, oracle, 64, 64, 3, seed=9, log2_ctb=6, zero_tu_permille=100, mv_range=300)
 
 
+def test_tiny_pictures_partial_groups(engine, oracle):
+    """Pictures smaller than one 16x16 inter area in a dimension, and chroma
+    rows of 20 and 12 samples: every thread group at a picture edge is partial."""
+    run_sequence(engine, oracle, 40, 24, 3, seed=14, log2_ctb=4)
+    run_sequence(engine, oracle, 24, 40, 3, seed=15, bit_depth=10, log2_ctb=4, mv_range=40)
+
+
 def test_1080p_8bit_and_10bit(engine, oracle):
     run_sequence(engine, oracle, 1920, 1080, 3, seed=10)
     run_sequence(engine, oracle, 1920, 1080, 2, seed=11, bit_depth=10)
