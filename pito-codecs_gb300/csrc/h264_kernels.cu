@@ -1183,7 +1183,7 @@ __global__ void __launch_bounds__(128) h264_db_params_kernel(H264Launch P) {
 // of a band hand over through shared memory, bands through per-row progress
 // words in global memory that the band's two helper warps mirror and publish.
 //
-// Order (every wait is capped, see wait_ge):
+// Order (every wait is capped, see wait_seen):
 //   intra MB (x, y)    after intra row y-1 has reconstructed MBs 0..x+1;
 //   filter MB (x, y)   after row y has reconstructed MBs 0..x+2 (every intra
 //                      MB whose samples the step reads or changes, and MB
@@ -1234,28 +1234,14 @@ struct __align__(16) BandSmem {
     volatile int cprog[BR + 1];  // same for chroma
 };
 
-// Warp-wide wait until *c >= need.  Lane 0 polls shared memory and sleeps
-// between polls (16 ns doubling to 128 ns): a band CTA holds about twenty
-// warps, and waiting ones must leave the issue slots to the working ones.
-// False after the iteration cap or once another warp has reported an error.
-__device__ __forceinline__ bool wait_ge(volatile int *c, int need, const H264Launch &P, int lane) {
-    bool ok = true;
-    if (lane == 0 && *c < need) {
-        uint32_t it = 0, ns = 16;
-        do {
-            if (++it > P.wait_limit || ((it & 63) == 0 && aborted(P.error))) { ok = false; break; }
-            __nanosleep(ns);
-            ns = min(ns * 2, 128u);
-        } while (*c < need);
-    }
-    ok = __shfl_sync(0xffffffffu, ok, 0);
-    __threadfence_block();
-    return ok;
-}
 
-// wait_ge that remembers the largest progress it has observed: progress only
-// grows, so a value seen (and ordered by the fence) at an earlier wait
-// answers later ones without another round through shared memory.
+// Warp-wide wait until *c >= need.  Lane 0 polls shared memory and sleeps
+// between polls (16 ns doubling to 128 ns): a band CTA holds fourteen warps,
+// and waiting ones must leave the issue slots to the working ones.  False
+// after the iteration cap or once another warp has reported an error.  The
+// largest progress observed is remembered: progress only grows, so a value
+// seen (and ordered by the fence) at an earlier wait answers later ones
+// without another round through shared memory.
 __device__ __forceinline__ bool wait_seen(volatile int *c, int &seen, int need, const H264Launch &P, int lane) {
     if (seen >= need) return true;
     bool ok = true;
