@@ -405,8 +405,16 @@ def run_multistream(args):
             st.close()
         alone = {s.key: M.open_stream(s) for s in specs}
         t_plain = M.run_plain(specs, tpl, alone)
+        # the schedule: the autotuner's choice for this mix (each candidate
+        # runs the first 16 pictures of every stream, so that predicted
+        # pictures outweigh the intra one as in the full streams), unless given
+        if args.depth > 0:
+            schedule, rates = M.Schedule(args.depth, 1.0), {}
+        else:
+            schedule, rates = M.autotune(specs, tpl, frames=16)
         mixed = {s.key: M.open_stream(s) for s in specs}
-        t_batch = M.run_batched(specs, tpl, mixed, depth=args.depth)
+        M.apply_schedule(mixed, specs, schedule)
+        t_batch = M.run_batched(specs, tpl, mixed, depth=schedule.depth)
         frames = sum(s.frames for s in specs)
         check = specs[: args.parity_streams]
         same = all(digest(alone[s.key]) == digest(mixed[s.key]) for s in check)
@@ -415,7 +423,10 @@ def run_multistream(args):
             st.close()
         line = dict(base, metric="C4 batched recon frames/s", value=frames / t_batch, unit="frames/s",
                     steps=1, warmup=1, ms_per_step=t_batch * 1000,
-                    config={"workload": "batched_c4: " + mix, "frames": frames, "depth": args.depth,
+                    config={"workload": "batched_c4: " + mix, "frames": frames, "depth": schedule.depth,
+                            "intra_cta_scale": schedule.intra_scale,
+                            "autotune_fps": {f"depth {s.depth}, intra x{s.intra_scale}": round(v, 1)
+                                             for s, v in rates.items()},
                             "plain_loop_fps": frames / t_plain, "speedup_vs_plain": t_plain / t_batch,
                             "luma_msamples_per_s": sum(luma_samples(s, s.frames) for s in specs) / t_batch / 1e6,
                             "parity": f"{'identical' if same else 'DIFFERENT'} DPBs in the mix and alone for the "
@@ -430,7 +441,7 @@ def run_multistream(args):
     for rate in args.rates:
         count = max(20, int(rate * args.trace_seconds))
         trace = M.poisson_trace(rate, count, len(specs), seed=SEED + int(rate))
-        srv = M.Server(specs, tpl, hbm_budget=args.hbm_budget_gb << 30, depth=args.depth)
+        srv = M.Server(specs, tpl, hbm_budget=args.hbm_budget_gb << 30, depth=args.depth or 2)
         srv.run(trace)
         served = M.latency_stats(trace)
         served["evictions"] = srv.evictions
@@ -460,7 +471,8 @@ def main():
                     choices=["h264_1080p", "hevc_1080p_8", "hevc_1080p_10", "hevc_2160p_8", "hevc_2160p_10",
                              "batched", "served"])
     ap.add_argument("--streams", type=int, default=64, help="batched / served: streams in the mix")
-    ap.add_argument("--depth", type=int, default=2, help="batched / served: pictures queued per stream")
+    ap.add_argument("--depth", type=int, default=0,
+                    help="batched: pictures queued per stream (0: the autotuner's schedule); served: 0 means 2")
     ap.add_argument("--parity-streams", type=int, default=64, help="batched: streams whose DPBs are compared")
     ap.add_argument("--rates", type=float, nargs="+", default=[50.0, 200.0, 800.0], help="served: requests/s")
     ap.add_argument("--trace-seconds", type=float, default=3.0, help="served: trace length")

@@ -365,6 +365,14 @@ int rc_picture_device_planes(rc_stream *s, int slot, void **y, void **u,
 #define RC_KERNEL_HEVC_SAO 7
 #define RC_KERNEL_COUNT 8
 int rc_stream_profile(rc_stream *s, int enable);
+/* Schedule knob for many streams sharing one GPU: the HEVC intra kernel's
+ * persistent CTAs per launch (default: about one per two 64x64 CTBs, at
+ * least 8, at most two per SM).  ctas <= 0 restores the default; more than
+ * 4096 is RC_EINVAL.  Takes effect from the next submit.  The arithmetic,
+ * and so the output, does not depend on it. */
+int rc_stream_set_intra_ctas(rc_stream *s, int ctas);
+/* The current value (0 for an H.264 stream, which has no such kernel). */
+int rc_stream_intra_ctas(rc_stream *s);
 int rc_stream_profile_read(rc_stream *s, double *ms, long long *launches,
                            int max_kernels);
 

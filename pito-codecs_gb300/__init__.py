@@ -201,6 +201,10 @@ def lib() -> ctypes.CDLL:
     L.rc_hevc_validate.argtypes = [i32, i32, i32, i32, vp]
     L.rc_hevc_validate.restype = i32
     L.rc_stream_sync.argtypes = [vp]
+    L.rc_stream_set_intra_ctas.argtypes = [vp, i32]
+    L.rc_stream_set_intra_ctas.restype = i32
+    L.rc_stream_intra_ctas.argtypes = [vp]
+    L.rc_stream_intra_ctas.restype = i32
     L.rc_stream_sync.restype = i32
     L.rc_stream_error.argtypes = [vp]
     L.rc_stream_error.restype = i32
@@ -457,6 +461,13 @@ class ReconStream:
 
     def profile(self, enable: bool):
         _check(lib().rc_stream_profile(self._h, int(enable)), "rc_stream_profile")
+
+    def set_intra_ctas(self, ctas: int):
+        """HEVC intra kernel CTAs per launch (0: the default); a schedule knob."""
+        _check(lib().rc_stream_set_intra_ctas(self._h, int(ctas)), "rc_stream_set_intra_ctas")
+
+    def intra_ctas(self) -> int:
+        return lib().rc_stream_intra_ctas(self._h)
 
     def profile_read(self) -> dict:
         ms = (ctypes.c_double * RC_KERNEL_COUNT)()

@@ -113,7 +113,7 @@ struct rc_stream {
     uint32_t epoch = 0;
     long long launches = 0;
     int sticky = 0;
-    int wave_blocks = 0;
+    int wave_blocks = 0, wave_default = 0;  // HEVC intra CTAs per launch, and its default
     int sms = 0;
     uint32_t wait_limit = RC_WAIT_LIMIT;
     // per-kernel CUDA-event timing
@@ -616,6 +616,7 @@ int rc_stream_create(int codec, int width, int height, int bit_depth, int dpb_sl
     {
         const int c64 = ((s->width + 63) / 64) * ((s->height + 63) / 64);
         s->wave_blocks = std::max(8, std::min(s->sms * 2, c64 / 2));
+        s->wave_default = s->wave_blocks;
     }
     if (const char *e = getenv("PITO_RECON_WAVE_BLOCKS")) {
         int v = atoi(e);
@@ -977,6 +978,14 @@ int rc_picture_download_async(rc_stream *s, int slot, int x, int y, int w, int h
                               void *out_v) {
     return download(s, slot, x, y, w, h, out_y, out_u, out_v, false);
 }
+
+int rc_stream_set_intra_ctas(rc_stream *s, int ctas) {
+    if (!s || ctas > 4096) return RC_EINVAL;
+    s->wave_blocks = ctas <= 0 ? s->wave_default : ctas;
+    return RC_OK;
+}
+
+int rc_stream_intra_ctas(rc_stream *s) { return s && s->codec == RC_CODEC_HEVC ? s->wave_blocks : 0; }
 
 int rc_stream_profile(rc_stream *s, int enable) {
     if (!s) return RC_EINVAL;

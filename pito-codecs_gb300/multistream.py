@@ -7,7 +7,9 @@ decode order; a picture's bytes do not depend on what else runs beside it.
 
 * Batched form: a mix of streams of uneven resolution, codec and bit depth
   (``mix_specs``) kept in flight together -- ``run_batched`` submits the
-  streams' pictures round-robin, ``run_plain`` one stream after the other.
+  streams' pictures round-robin, ``run_plain`` one stream after the other;
+  ``autotune`` picks its schedule (pictures queued per stream, HEVC intra
+  CTAs per launch) for a mix by timing the candidates.
 * Served form: ``Server`` admits decode requests (a stream and a number of
   frames) as they arrive, while the device bytes of the resident streams
   stay within an HBM budget; streams stay resident between requests and idle
@@ -25,6 +27,9 @@ from __future__ import annotations
 
 import collections
 import dataclasses
+import hashlib
+import json
+import os
 import random
 import time
 
@@ -191,6 +196,71 @@ def run_batched(specs, templates, streams, depth: int = 2):
         if streams[spec.key].sync() != 0:
             raise RuntimeError(f"stream {spec.key}: device error")
     return time.perf_counter() - t0
+
+
+# ---------------------------------------------------------------------------
+# Schedule autotuner for the batched form
+# ---------------------------------------------------------------------------
+@dataclasses.dataclass(frozen=True)
+class Schedule:
+    depth: int = 2            # pictures queued per stream ahead of its completed work
+    intra_scale: float = 1.0  # HEVC intra CTAs per launch, times each stream's default
+
+
+def mix_signature(specs) -> str:
+    """A key for a stream mix: the codec, coded size and bit depth of its streams."""
+    items = sorted((s.codec, *s.coded, s.bit_depth) for s in specs)
+    return hashlib.sha256(repr(items).encode()).hexdigest()[:16]
+
+
+def apply_schedule(streams, specs, schedule: Schedule):
+    """Set every HEVC stream's intra CTAs per launch for `schedule`."""
+    for s in specs:
+        if s.codec == RC_CODEC_HEVC:
+            st = streams[s.key]
+            st.set_intra_ctas(0)
+            st.set_intra_ctas(max(1, int(round(st.intra_ctas() * schedule.intra_scale))))
+
+
+def autotune(specs, templates, depths=(1, 2, 3, 4), intra_scales=(0.5, 1.0, 2.0), frames: int = 8,
+             open_fn=open_stream, runner=None, cache_path=None):
+    """Choose the batched form's schedule for a stream mix.
+
+    Every candidate (pictures queued per stream x HEVC intra CTAs per launch)
+    runs the first `frames` pictures of every stream of the mix on fresh
+    streams and is timed; the fastest wins.  The schedule changes only the
+    order and overlap of the work, never a picture's bytes.  With
+    `cache_path` the choice is kept per mix signature (JSON) and reused.
+    Returns (schedule, {schedule: frames/s}); the dict is empty when the
+    schedule came from the cache."""
+    runner = runner or run_batched
+    key = mix_signature(specs)
+    cache = {}
+    if cache_path and os.path.exists(cache_path):
+        with open(cache_path) as f:
+            cache = json.load(f)
+        if key in cache:
+            return Schedule(**cache[key]["schedule"]), {}
+    prefix = [dataclasses.replace(s, frames=min(s.frames, frames)) for s in specs]
+    total = sum(s.frames for s in prefix)
+    rates = {}
+    for depth in depths:
+        for scale in intra_scales:
+            schedule = Schedule(depth, scale)
+            streams = {s.key: open_fn(s) for s in prefix}
+            try:
+                apply_schedule(streams, prefix, schedule)
+                seconds = runner(prefix, templates, streams, depth=depth)
+            finally:
+                for st in streams.values():
+                    st.close()
+            rates[schedule] = total / seconds
+    best = max(rates, key=rates.get)
+    if cache_path:
+        cache[key] = {"schedule": dataclasses.asdict(best), "frames_per_s": rates[best]}
+        with open(cache_path, "w") as f:
+            json.dump(cache, f, indent=1)
+    return best, rates
 
 
 # ---------------------------------------------------------------------------

@@ -114,6 +114,28 @@ def test_batched_equals_alone(engine):
 
 
 @pytest.mark.gpu
+def test_schedule_changes_no_bytes(engine):
+    """The autotuner's knobs (pictures queued per stream, HEVC intra CTAs per
+    launch) change the order and overlap of the work only."""
+    M = ms(engine)
+    specs = [s for s in M.mix_specs(8, min_frames=4, max_frames=7, seed=21) if s.codec == engine.RC_CODEC_HEVC]
+    for s in specs:
+        s.width, s.height = 854, 480
+    tpl = {s.key: M.Templates(s) for s in specs}
+    digests = []
+    for schedule in (M.Schedule(1, 1.0), M.Schedule(3, 0.25), M.Schedule(2, 4.0)):
+        streams = {s.key: M.open_stream(s) for s in specs}
+        try:
+            M.apply_schedule(streams, specs, schedule)
+            M.run_batched(specs, tpl, streams, depth=schedule.depth)
+            digests.append([_dpb_digest(streams[s.key]) for s in specs])
+        finally:
+            for st in streams.values():
+                st.close()
+    assert digests[0] == digests[1] == digests[2]
+
+
+@pytest.mark.gpu
 def test_batched_device_records_equal_alone(engine):
     """Many streams with device-resident records run far ahead of the GPU:
     every per-stream upload (level-scale tables included) must be ordered on
