@@ -418,10 +418,10 @@ void *rc_stream_cuda_stream(rc_stream *s);
  * before that mark has completed, 0 if not yet, or a negative RC_E* code.
  * Not thread-safe per stream. */
 int rc_stream_mark(rc_stream *s, unsigned long long *mark);
+int rc_stream_mark_done(rc_stream *s, unsigned long long mark);
 /* Device bytes the stream holds (DPB, scratch and record buffers), for
  * admission control across streams. */
 size_t rc_stream_device_bytes(rc_stream *s);
-int rc_stream_mark_done(rc_stream *s, unsigned long long mark);
 
 #ifdef __cplusplus
 }
