@@ -1,5 +1,6 @@
-"""The batched form's schedule autotuner (pito-codecs_gb300/multistream.py),
-on fake streams and a fake runner: no GPU needed."""
+"""Host logic of pito-codecs_gb300/multistream.py on fake streams (no GPU
+needed): the batched form's schedule autotuner, and the plain server's wait
+for arrivals."""
 from __future__ import annotations
 
 import importlib
@@ -67,3 +68,38 @@ def test_apply_schedule_restores_each_default_first(engine):
     M.apply_schedule(streams, specs, M.Schedule(2, 0.5))  # relative to the default, not to the last value
     for s in specs:
         assert streams[s.key].ctas == (15 if s.codec == engine.RC_CODEC_HEVC else 30)
+
+
+def test_plain_server_wait_survives_an_arrival_passing_mid_wait(engine):
+    """serve_plain waits for each request's arrival; the clock may pass the
+    arrival between the loop's test and the read that sizes the sleep, which
+    must then sleep zero, not a negative time."""
+    M = ms(engine)
+    spec = M.StreamSpec(0, engine.RC_CODEC_H264, 64, 48, 8, 4, 1)
+
+    class Tpl:
+        def picture(self, n):
+            return None, n % spec.slots
+
+    class Stream:
+        def __init__(self, s):
+            self.n = 0
+
+        def submit_h264(self, pic, slot):
+            self.n += 1
+
+        def mark(self):
+            return self.n
+
+        def mark_done(self, m):
+            return True
+
+        def close(self):
+            pass
+
+    # t0, then the loop's test (before the arrival), then the sleep's read
+    # (after it), then everything later
+    times = iter([0.0, 0.4, 0.6] + [0.7 + 0.01 * i for i in range(100)])
+    trace = [M.Request(0, 0.5, 0, 2)]
+    M.serve_plain([spec], {0: Tpl()}, trace, clock=lambda: next(times), open_fn=Stream)
+    assert trace[0].admitted >= 0.5 and len(trace[0].done) == 2
