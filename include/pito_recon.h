@@ -373,6 +373,14 @@ int rc_stream_profile(rc_stream *s, int enable);
 int rc_stream_set_intra_ctas(rc_stream *s, int ctas);
 /* The current value (0 for an H.264 stream, which has no such kernel). */
 int rc_stream_intra_ctas(rc_stream *s);
+/* Iteration cap of every device-side wait in this stream's kernels (no
+ * counterpart in the reference, whose rayon jobs block on condition
+ * variables).  A wait that polls `limit` times without progress records
+ * RC_ETIMEOUT in the sticky error word and its launch unwinds, leaving the
+ * context usable.  For tests of that failure path and for callers that want
+ * a shorter bound; 0 restores the default (about a second of polling).
+ * Takes effect from the next submit. */
+int rc_stream_set_wait_limit(rc_stream *s, unsigned int limit);
 int rc_stream_profile_read(rc_stream *s, double *ms, long long *launches,
                            int max_kernels);
 
@@ -390,7 +398,10 @@ int rc_stream_profile_read(rc_stream *s, double *ms, long long *launches,
  * device that loads it, sized for RC_NOALLOC_MAX_MBS macroblocks (8704:
  * up to 2048x1088) and RC_NOALLOC_MAX_ROWS MB rows; larger pictures get
  * RC_EINVAL.  The first call on a device looks up that array's device
- * address, so make the first call before any stream capture.  Every call
+ * address in the current CUDA context, so make the first call before any
+ * stream capture.  A device reset (cudaDeviceReset) or a new context moves
+ * the array; the first call in the new context looks it up again, and it too
+ * belongs before any capture.  Every call
  * shares the one array: calls whose work overlaps on the GPU (on different
  * streams, or on different host threads) race and must be serialised by the
  * caller.  *status (device memory, 4 bytes) receives 0 or RC_DEV_* error bits

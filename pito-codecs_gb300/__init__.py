@@ -205,6 +205,8 @@ def lib() -> ctypes.CDLL:
     L.rc_stream_set_intra_ctas.restype = i32
     L.rc_stream_intra_ctas.argtypes = [vp]
     L.rc_stream_intra_ctas.restype = i32
+    L.rc_stream_set_wait_limit.argtypes = [vp, ctypes.c_uint]
+    L.rc_stream_set_wait_limit.restype = i32
     L.rc_stream_sync.restype = i32
     L.rc_stream_error.argtypes = [vp]
     L.rc_stream_error.restype = i32
@@ -397,6 +399,28 @@ class PictureBuffers:
         self.ptr = ctypes.addressof(p)
 
 
+class HevcPictureBuffers:
+    """An rc_hevc_picture rebuilt from raw buffers (fixture files, parsed
+    streams, edited records), keeping the buffers alive.  `header` holds the
+    scalar fields of rc_hevc_picture (log2_ctb, num_slices, num_tus, ...)."""
+
+    HEADER = ("log2_ctb", "constrained_intra_pred", "strong_intra_smoothing", "loop_filter_across_tiles",
+              "cb_qp_offset", "cr_qp_offset", "num_slices", "num_tus", "frame_id")
+
+    def __init__(self, bufs: dict, header: dict):
+        self._keep = {k: ctypes.create_string_buffer(v, len(v)) if v else None for k, v in bufs.items()}
+        p = HevcPicture()
+        p.mem = RC_MEM_HOST
+        for k in self.HEADER:
+            setattr(p, k, int(header.get(k, 0)))
+        p.num_levels = len(bufs.get("levels", b"")) // 2
+        addr = lambda k: ctypes.addressof(self._keep[k]) if self._keep.get(k) is not None else None
+        for k in ("ctbs", "blk", "mvf", "tus", "slices", "levels", "scaling"):
+            setattr(p, k, addr(k))
+        self.pic = p
+        self.ptr = ctypes.addressof(p)
+
+
 # ---- the stream -------------------------------------------------------------
 def _check(rc: int, what: str):
     if rc != RC_OK:
@@ -468,6 +492,10 @@ class ReconStream:
 
     def intra_ctas(self) -> int:
         return lib().rc_stream_intra_ctas(self._h)
+
+    def set_wait_limit(self, limit: int):
+        """Iteration cap of the device-side waits (0: the default)."""
+        _check(lib().rc_stream_set_wait_limit(self._h, int(limit)), "rc_stream_set_wait_limit")
 
     def profile_read(self) -> dict:
         ms = (ctypes.c_double * RC_KERNEL_COUNT)()

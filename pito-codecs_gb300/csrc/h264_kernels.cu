@@ -31,6 +31,7 @@
 //
 // Arithmetic follows src/h264/dec/{transform,intra,inter,deblock}.rs and the
 // reconstruction half of slicedec.rs; citations at each function.
+#include <cuda.h>  // CUcontext and CUresult: driver calls reached through cudaGetDriverEntryPointByVersion
 #include <stdint.h>
 #include <string.h>
 
@@ -1987,26 +1988,76 @@ static __device__ __align__(256) uint32_t g_noalloc_scratch[RC_NOALLOC_DB_WORDS 
 
 
 namespace {
+// The array's device address belongs to the CUDA context the module was
+// loaded into, not to the device number: after cudaDeviceReset (or after the
+// primary context is released and created again) the module loads into a new
+// context and the array moves.  Addresses are therefore remembered per
+// context, keyed by the context's id (cuCtxGetId), which the driver never
+// gives to two contexts of one process, so a recreated context -- even one
+// whose handle value repeats -- is looked up afresh.  The two driver calls
+// are reached through the runtime's entry-point query, so the library does
+// not link the driver library itself.
+typedef CUresult (*CtxCurrentFn)(CUcontext *);
+typedef CUresult (*CtxIdFn)(CUcontext, unsigned long long *);
 std::mutex g_noalloc_mu;
-uint32_t *g_noalloc_addr[64];
-bool g_noalloc_ready[64];
+CtxCurrentFn g_ctx_current = nullptr;
+CtxIdFn g_ctx_id = nullptr;
+bool g_ctx_fns_looked_up = false;
+struct NoallocEntry {
+    unsigned long long ctx_id;
+    uint32_t *addr;
+};
+NoallocEntry g_noalloc_seen[64];
+int g_noalloc_count = 0, g_noalloc_next = 0;
 
-// Device address of the static scratch for the current device; looked up once
-// per device (the host-side name is not a device address).
-int noalloc_scratch(uint32_t **out) {
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return RC_ENODEV;
-    std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_ready[dev]) {
-        void *p = nullptr;
-        if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) {
+// Id of the context current on this thread, or 0 if there is none yet.
+bool current_ctx_id(unsigned long long *id) {
+    *id = 0;
+    if (!g_ctx_fns_looked_up) {
+        cudaDriverEntryPointQueryResult q1, q2;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", (void **)&g_ctx_current, 4000, cudaEnableDefault,
+                                             &q1) != cudaSuccess || q1 != cudaDriverEntryPointSuccess ||
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", (void **)&g_ctx_id, 12000, cudaEnableDefault, &q2) !=
+                cudaSuccess || q2 != cudaDriverEntryPointSuccess) {
             cudaGetLastError();
-            return RC_ECUDA;
+            g_ctx_current = nullptr;
+            g_ctx_id = nullptr;
+            return false;
         }
-        g_noalloc_addr[dev] = (uint32_t *)p;
-        g_noalloc_ready[dev] = true;
+        g_ctx_fns_looked_up = true;
     }
-    *out = g_noalloc_addr[dev];
+    CUcontext c = nullptr;
+    if (g_ctx_current(&c) != CUDA_SUCCESS) return false;
+    if (!c) return true;
+    return g_ctx_id(c, id) == CUDA_SUCCESS;
+}
+
+// Device address of the static scratch in the current context.  The first
+// call in a context looks it up with cudaGetSymbolAddress (the host-side name
+// of a __device__ array is not a device address); later calls in the same
+// context reuse it.
+int noalloc_scratch(uint32_t **out) {
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    unsigned long long id = 0;
+    if (!current_ctx_id(&id)) return RC_ECUDA;
+    if (id)
+        for (int i = 0; i < g_noalloc_count; i++)
+            if (g_noalloc_seen[i].ctx_id == id) {
+                *out = g_noalloc_seen[i].addr;
+                return RC_OK;
+            }
+    // not seen in this context (or no context yet: the lookup creates the
+    // device's primary context and makes it current)
+    void *p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) {
+        cudaGetLastError();
+        return RC_ECUDA;
+    }
+    if (!id && (!current_ctx_id(&id) || !id)) return RC_ECUDA;
+    NoallocEntry &e = g_noalloc_seen[g_noalloc_count < 64 ? g_noalloc_count++ : (g_noalloc_next++ & 63)];
+    e.ctx_id = id;
+    e.addr = (uint32_t *)p;
+    *out = e.addr;
     return RC_OK;
 }
 }  // namespace
@@ -2051,7 +2102,12 @@ extern "C" int rc_h264_deblock_noalloc(const rc_h264_picture *pic, int mb_w, int
     L.error = status;
     L.epoch = 1;
     L.wait_limit = RC_WAIT_LIMIT;
-    h264_db_params_kernel<<<(mb_w * mb_h + 3) / 4, 128, 0, st>>>(L);
-    h264_deblock_kernel<<<mb_h, 32, 0, st>>>(L);
-    return cudaGetLastError() == cudaSuccess ? RC_OK : RC_ECUDA;
+    // each launch checked on its own return code: an error the caller left
+    // pending from earlier work is neither reported here nor cleared
+    void *args[] = {&L};
+    if (cudaLaunchKernel((const void *)h264_db_params_kernel, dim3((mb_w * mb_h + 3) / 4), dim3(128), args, 0, st) !=
+            cudaSuccess ||
+        cudaLaunchKernel((const void *)h264_deblock_kernel, dim3(mb_h), dim3(32), args, 0, st) != cudaSuccess)
+        return RC_ECUDA;
+    return RC_OK;
 }

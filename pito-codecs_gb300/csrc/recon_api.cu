@@ -987,6 +987,12 @@ int rc_stream_set_intra_ctas(rc_stream *s, int ctas) {
 
 int rc_stream_intra_ctas(rc_stream *s) { return s && s->codec == RC_CODEC_HEVC ? s->wave_blocks : 0; }
 
+int rc_stream_set_wait_limit(rc_stream *s, unsigned int limit) {
+    if (!s) return RC_EINVAL;
+    s->wait_limit = limit ? limit : RC_WAIT_LIMIT;
+    return RC_OK;
+}
+
 int rc_stream_profile(rc_stream *s, int enable) {
     if (!s) return RC_EINVAL;
     if (cudaStreamSynchronize(s->st) != cudaSuccess || (s->est && cudaStreamSynchronize(s->est) != cudaSuccess))

@@ -13,8 +13,10 @@ engine.  Run here, where the reference checkout exists:
 """
 from __future__ import annotations
 
+import argparse
 import hashlib
 import json
+import os
 import pathlib
 import re
 import sys
@@ -23,7 +25,7 @@ import numpy as np
 
 HERE = pathlib.Path(__file__).resolve().parent
 REPO = HERE.parents[1]
-REFS = pathlib.Path("/root/reference/tests/refs/h264")
+REFS = None  # <reference checkout>/tests/refs/h264, set by main()
 sys.path.insert(0, str(REPO / "tests"))
 sys.path.insert(0, str(HERE))
 
@@ -82,4 +84,12 @@ def main(names):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1:] or ["baseline"])
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--reference", default=os.environ.get("PITO_REFERENCE"),
+                    help="root of the reference checkout (default: $PITO_REFERENCE)")
+    ap.add_argument("names", nargs="*", default=["baseline"])
+    a = ap.parse_args()
+    if not a.reference:
+        raise SystemExit("name the reference checkout with --reference or PITO_REFERENCE")
+    REFS = pathlib.Path(a.reference) / "tests" / "refs" / "h264"
+    main(a.names)

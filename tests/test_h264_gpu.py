@@ -158,3 +158,38 @@ def test_streams_of_different_widths_coexist(engine, oracle):
     finally:
         wide.close()
         narrow.close()
+
+
+def _bench():
+    import importlib.util
+    import pathlib
+    import sys
+    if "bench" in sys.modules:
+        return sys.modules["bench"]
+    path = pathlib.Path(__file__).resolve().parent.parent / "bench.py"
+    spec = importlib.util.spec_from_file_location("bench", path)
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules["bench"] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def test_benched_1080p_sequence_first_30_frames(engine, oracle):
+    """The bench's own workload (same generator, seed, references and DPB
+    slots), its first 30 frames at 1920x1088, every plane against the oracle."""
+    B = _bench()
+    wl = B.H264Workload(engine)
+    pics = wl.sequence(B.SEED, 30)
+    st = engine.ReconStream(engine.RC_CODEC_H264, wl.W, wl.H, 8, wl.slots)
+    dpb = wl.oracle_dpb(oracle)
+    try:
+        for n, p in enumerate(pics):
+            slot = n % wl.slots
+            st.submit_h264(p, slot)
+            assert dpb.recon(p.ptr, slot) == 0
+            assert st.sync() == 0
+            for name, g, w, blk in zip("YUV", st.download(slot), dpb.planes(slot), (16, 8, 8)):
+                msg = first_diff(g, w, blk)
+                assert msg is None, f"frame {n} plane {name}: {msg}"
+    finally:
+        st.close()

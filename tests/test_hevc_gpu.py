@@ -122,3 +122,33 @@ def test_invalid_hevc_rejected(engine):
         assert st.sync() == 0
     with pytest.raises(engine.ReconError):
         engine.ReconStream(engine.RC_CODEC_HEVC, 100, 64, 8, 2)  # width not a multiple of 8
+
+
+def test_benched_1080p_sequences_first_frames(engine, oracle):
+    """The bench's own HEVC workloads (same generator, seed, references and
+    DPB slots), the first 8 frames at 8 and 10 bit, against the oracle."""
+    import importlib.util
+    import pathlib
+    import sys
+    if "bench" not in sys.modules:
+        spec = importlib.util.spec_from_file_location("bench", pathlib.Path(__file__).resolve().parent.parent / "bench.py")
+        mod = importlib.util.module_from_spec(spec)
+        sys.modules["bench"] = mod
+        spec.loader.exec_module(mod)
+    B = sys.modules["bench"]
+    for name in ("hevc_1080p_8", "hevc_1080p_10"):
+        wl = B.workload(engine, name)
+        pics = wl.sequence(B.SEED, 8)
+        st = engine.ReconStream(engine.RC_CODEC_HEVC, wl.W, wl.H, wl.bd, wl.slots)
+        dpb = wl.oracle_dpb(oracle)
+        try:
+            for n, p in enumerate(pics):
+                slot = n % wl.slots
+                st.submit_hevc(p, slot)
+                assert dpb.recon(p.ptr, slot, 3) == 0
+                assert st.sync() == 0
+                for pn, g, w in zip("YUV", st.download(slot), dpb.planes(slot)):
+                    msg = first_diff(g.astype(np.uint16), w)
+                    assert msg is None, f"{name} frame {n} plane {pn}: {msg}"
+        finally:
+            st.close()
