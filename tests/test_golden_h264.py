@@ -1,12 +1,23 @@
-"""End-to-end parity against the reference's golden H.264 stream.
+"""End-to-end parity against the reference's golden H.264 streams.
 
-tests/golden/h264_baseline.npz holds the syntax records of the reference's
-tests/refs/h264/baseline.h264 (x264 Baseline, 10 frames, 2 slices per
-picture, I and P with 3 reference frames, deblocking on), parsed by
-tests/golden/h264_cavlc.py, and the sha256 the reference's manifest records
-for the stream's reconstruction (tests/refs/h264/manifest.toml, kind
-bit-exact; digest of every frame's cropped Y, Cb, Cr rows as in
-src/testref.rs:570-578).  The oracle and the engine must both reproduce it.
+tests/golden/h264_<name>.npz holds the syntax records of the reference's x264
+stream tests/refs/h264/<name>.h264 (made by tests/golden/make_h264_golden.py:
+h264_cavlc.py parses the Baseline stream, h264_cabac.py the Main and High
+ones), with each picture's DPB slot, picture order count and crop.  EXPECTED
+below is the sha256 the reference's manifest records for the stream's
+reconstruction (tests/refs/h264/manifest.toml, the "<name>.yuv" entry, kind
+bit-exact: the reconstruction x264 dumped while encoding).  The digest
+covers the pictures in output order, each cropped, Y then Cb then Cr row by
+row (src/testref.rs:570-578).  The oracle (CPU) and the engine (GPU, through
+the C ABI) must both reproduce it.
+
+  baseline          Baseline, CAVLC, 2 slices, I and P with 3 references
+  main_cabac_b      Main, CABAC, B pictures (spatial direct, implicit
+                    weights), explicit P weights with duplicated references
+  high_bpyramid     High, 8x8 transform and I8x8, B pyramid, temporal
+                    direct, explicit weights, 4 references
+  high_crop_slices  High, JVT scaling matrices (PPS, fall-back rule A), 4
+                    slices, B pictures, 238x158 cropped from 240x160
 """
 from __future__ import annotations
 
@@ -17,17 +28,25 @@ import pathlib
 import numpy as np
 import pytest
 
-GOLDEN = pathlib.Path(__file__).resolve().parent / "golden" / "h264_baseline.npz"
+GOLDEN = pathlib.Path(__file__).resolve().parent / "golden"
+EXPECTED = {
+    "baseline": "5a978004cf205415f059349e9fa14714e1d7578b1c5165c48520fca71a11ef00",
+    "main_cabac_b": "9f7179ab822f155adc7cbe0586f3d7447cf78f3863cb720335cbf927cc5b33a7",
+    "high_bpyramid": "25379e94ff635e93d66808405de5fbbad27595ab1b32e3ea6e7b0259ea92b21e",
+    "high_crop_slices": "6da5d2d112e7128e7a88af29d226fc4c300a95c4b795f0d0162ee9053fb901fc",
+}
+KEYS = ("mbs", "slices", "weights", "levels", "scaling4", "scaling8")
+DPB_SLOTS = 16
 
 
-def load_fixture(engine):
-    z = np.load(GOLDEN)
+def load_fixture(engine, name):
+    z = np.load(GOLDEN / f"h264_{name}.npz")
     meta = json.loads(bytes(z["meta"]).decode())
     pics = []
     for i, m in enumerate(meta["pictures"]):
-        bufs = {k: z[f"{k}_{i}"].tobytes() for k in ("mbs", "slices", "levels")}
-        bufs["weights"] = b""
-        pics.append((m, engine.PictureBuffers(bufs, m["num_slices"], 0, m["constrained_intra"], m["frame_id"])))
+        bufs = {k: z[f"{k}_{i}"].tobytes() for k in KEYS}
+        pics.append((m, engine.PictureBuffers(bufs, m["num_slices"], m["num_weights"], m["constrained_intra"],
+                                              m["frame_id"])))
     return meta, pics
 
 
@@ -40,34 +59,50 @@ def cropped(planes, crop):
     return [np.ascontiguousarray(p) for p in out]
 
 
-def test_fixture_is_the_reference_stream(engine):
-    meta, pics = load_fixture(engine)
-    assert len(pics) == 10
-    assert meta["expected_sha256"] == "5a978004cf205415f059349e9fa14714e1d7578b1c5165c48520fca71a11ef00"
-
-
-def test_oracle_reproduces_reference_digest(engine, oracle):
-    meta, pics = load_fixture(engine)
-    m0 = meta["pictures"][0]
-    dpb = oracle.H264Dpb(m0["mb_w"], m0["mb_h"], 8)
+def output_digest(metas, planes_after) -> str:
+    outs = {}
+    for i, m in enumerate(metas):
+        outs[(m["period"], m["poc"])] = [np.array(p, copy=True) for p in planes_after(i)]
     h = hashlib.sha256()
-    for m, p in pics:
+    for k in sorted(outs):
+        for pl in outs[k]:
+            h.update(pl.tobytes())
+    return h.hexdigest()
+
+
+def test_every_fixture_is_a_reference_stream():
+    assert sorted(p.stem[5:] for p in GOLDEN.glob("h264_*.npz")) == sorted(EXPECTED)
+    for name, want in EXPECTED.items():
+        z = np.load(GOLDEN / f"h264_{name}.npz")
+        meta = json.loads(bytes(z["meta"]).decode())
+        assert meta["expected_sha256"] == want and meta["stream"] == f"tests/refs/h264/{name}.h264"
+
+
+@pytest.mark.parametrize("name", sorted(EXPECTED))
+def test_oracle_reproduces_reference_digest(engine, oracle, name):
+    meta, pics = load_fixture(engine, name)
+    m0 = meta["pictures"][0]
+    dpb = oracle.H264Dpb(m0["mb_w"], m0["mb_h"], DPB_SLOTS)
+
+    def planes_after(i):
+        m, p = pics[i]
         assert dpb.recon(p.ptr, m["slot"]) == 0
-        for plane in cropped(dpb.planes(m["slot"]), m["crop"]):
-            h.update(plane.tobytes())
-    assert h.hexdigest() == meta["expected_sha256"]
+        return cropped(dpb.planes(m["slot"]), m["crop"])
+
+    assert output_digest([m for m, _ in pics], planes_after) == EXPECTED[name]
 
 
 @pytest.mark.gpu
-def test_engine_reproduces_reference_digest(engine):
-    meta, pics = load_fixture(engine)
+@pytest.mark.parametrize("name", sorted(EXPECTED))
+def test_engine_reproduces_reference_digest(engine, name):
+    meta, pics = load_fixture(engine, name)
     m0 = meta["pictures"][0]
     W, H = m0["mb_w"] * 16, m0["mb_h"] * 16
-    h = hashlib.sha256()
-    with engine.ReconStream(engine.RC_CODEC_H264, W, H, 8, 8) as st:
-        for m, p in pics:
+    with engine.ReconStream(engine.RC_CODEC_H264, W, H, 8, DPB_SLOTS) as st:
+        def planes_after(i):
+            m, p = pics[i]
             st.submit_h264(p, m["slot"])
             assert st.sync() == 0
-            for plane in cropped(st.download(m["slot"]), m["crop"]):
-                h.update(plane.tobytes())
-    assert h.hexdigest() == meta["expected_sha256"]
+            return cropped(st.download(m["slot"]), m["crop"])
+
+        assert output_digest([m for m, _ in pics], planes_after) == EXPECTED[name]
