@@ -434,6 +434,55 @@ int rc_stream_mark_done(rc_stream *s, unsigned long long mark);
  * admission control across streams. */
 size_t rc_stream_device_bytes(rc_stream *s);
 
+/* ======================================================================== */
+/*  Output order (DPB bumping)                                               */
+/* ======================================================================== */
+/*
+ * The engine reconstructs pictures into the DPB slots it is given, in
+ * decoding order.  These calls give the order in which a decoder hands them
+ * to its caller: the picture output process of the reference's DPBs
+ * (src/syntax/hevc/dpb.rs:76-160 bump / bump_before_decode / insert;
+ * src/syntax/h264/dpb.rs:73-132, 391-478 bump / idr / store_picture), after
+ * H.265 C.5.2.2-C.5.2.4 and H.264 C.4.5.3.  A bump outputs the waiting
+ * picture with the smallest POC.  Pictures are named by caller ids (e.g. DPB
+ * slot << 32 | frame number).  Host-only; needs no GPU.
+ *
+ * Every call that can output pictures writes their ids, in output order,
+ * to out_ids (room for cap ids, which must be at least rc_output_count + 1;
+ * RC_EINVAL before any change otherwise) and their number to *n_out.
+ */
+typedef struct rc_output_dpb rc_output_dpb;
+
+/* capacity: DPB size in pictures (sps_max_dec_pic_buffering_minus1 + 1, or
+ * H.264 max_dec_frame_buffering); max_num_reorder: pictures that may wait
+ * for output (sps_max_num_reorder_pics / max_num_reorder_frames);
+ * max_latency_pictures: SpsMaxLatencyPictures, 0 for none. */
+int rc_output_create(int capacity, int max_num_reorder, int max_latency_pictures, rc_output_dpb **out);
+void rc_output_destroy(rc_output_dpb *d);
+
+/* Before a picture is decoded.  new_sequence (an HEVC IRAP picture with
+ * NoRaslOutputFlag, an H.264 IDR): every waiting picture is output in POC
+ * order (none if no_output_of_prior_pics) and the DPB empties.  Otherwise
+ * pictures neither waiting nor used for reference leave, and the DPB bumps
+ * while it is over the reorder or latency limit or at capacity. */
+int rc_output_begin(rc_output_dpb *d, int new_sequence, int no_output_of_prior_pics, uint64_t *out_ids, int cap,
+                    int *n_out);
+
+/* A picture is no longer used for reference (reference marking). */
+int rc_output_unref(rc_output_dpb *d, uint64_t id);
+
+/* After a picture is decoded: it enters the DPB (waiting for output when
+ * output_flag is set, kept as a reference when is_reference is set); the
+ * DPB bumps while over the reorder or latency limit. */
+int rc_output_insert(rc_output_dpb *d, uint64_t id, int32_t poc, int output_flag, int is_reference,
+                     uint64_t *out_ids, int cap, int *n_out);
+
+/* End of the stream: every waiting picture in POC order; the DPB empties. */
+int rc_output_flush(rc_output_dpb *d, uint64_t *out_ids, int cap, int *n_out);
+
+/* Pictures the DPB holds (waiting for output or used for reference). */
+int rc_output_count(rc_output_dpb *d);
+
 #ifdef __cplusplus
 }
 #endif

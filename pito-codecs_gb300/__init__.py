@@ -236,6 +236,21 @@ def lib() -> ctypes.CDLL:
     L.rc_stream_device_bytes.restype = sz
     L.rc_h264_deblock_noalloc.argtypes = [vp, i32, i32, vp, vp, vp, i32, i32, vp, vp]
     L.rc_h264_deblock_noalloc.restype = i32
+    u64p = ctypes.POINTER(ctypes.c_uint64)
+    L.rc_output_create.argtypes = [i32, i32, i32, ctypes.POINTER(vp)]
+    L.rc_output_create.restype = i32
+    L.rc_output_destroy.argtypes = [vp]
+    L.rc_output_destroy.restype = None
+    L.rc_output_begin.argtypes = [vp, i32, i32, u64p, i32, ctypes.POINTER(i32)]
+    L.rc_output_begin.restype = i32
+    L.rc_output_unref.argtypes = [vp, ctypes.c_uint64]
+    L.rc_output_unref.restype = i32
+    L.rc_output_insert.argtypes = [vp, ctypes.c_uint64, ctypes.c_int32, i32, i32, u64p, i32, ctypes.POINTER(i32)]
+    L.rc_output_insert.restype = i32
+    L.rc_output_flush.argtypes = [vp, u64p, i32, ctypes.POINTER(i32)]
+    L.rc_output_flush.restype = i32
+    L.rc_output_count.argtypes = [vp]
+    L.rc_output_count.restype = i32
     return L
 
 
@@ -419,6 +434,50 @@ class HevcPictureBuffers:
             setattr(p, k, addr(k))
         self.pic = p
         self.ptr = ctypes.addressof(p)
+
+
+class OutputOrder:
+    """Output order of decoded pictures (rc_output_*: DPB bumping).  Each
+    call returns the ids it outputs, in order."""
+
+    def __init__(self, capacity: int, max_num_reorder: int, max_latency_pictures: int = 0):
+        h = ctypes.c_void_p()
+        _check(lib().rc_output_create(capacity, max_num_reorder, max_latency_pictures, ctypes.byref(h)),
+               "rc_output_create")
+        self._h = h
+
+    def _call(self, fn, *args):
+        cap = lib().rc_output_count(self._h) + 1
+        ids = (ctypes.c_uint64 * cap)()
+        n = ctypes.c_int()
+        _check(fn(self._h, *args, ids, cap, ctypes.byref(n)), fn.__name__)
+        return [ids[i] for i in range(n.value)]
+
+    def begin(self, new_sequence: bool = False, no_output_of_prior_pics: bool = False):
+        return self._call(lib().rc_output_begin, int(new_sequence), int(no_output_of_prior_pics))
+
+    def unref(self, pic_id: int):
+        _check(lib().rc_output_unref(self._h, pic_id), "rc_output_unref")
+
+    def insert(self, pic_id: int, poc: int, output: bool = True, reference: bool = True):
+        return self._call(lib().rc_output_insert, pic_id, poc, int(output), int(reference))
+
+    def flush(self):
+        return self._call(lib().rc_output_flush)
+
+    def count(self) -> int:
+        return lib().rc_output_count(self._h)
+
+    def close(self):
+        if self._h:
+            lib().rc_output_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 # ---- the stream -------------------------------------------------------------

@@ -18,7 +18,7 @@ PKG = pathlib.Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
 OUT = PKG / "_build"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["recon_api.cu", "h264_kernels.cu", "hevc_kernels.cu"]
+CU_SOURCES = ["recon_api.cu", "h264_kernels.cu", "hevc_kernels.cu", "output_order.cpp"]
 SYNTH_SOURCES = ["synth_h264.cpp", "synth_hevc.cpp"]
 HEADERS = list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + [PKG.parent / "include" / "pito_recon.h"]
 

@@ -452,8 +452,11 @@ def parse_sps(b: Bits) -> dict:
         raise NotImplementedError("luma and chroma bit depths differ")
     s["log2_max_poc_lsb"] = b.ue() + 4
     sub_info = b.u(1)
-    for _ in range(0 if sub_info else msl, msl + 1):
-        b.ue(), b.ue(), b.ue()
+    for _ in range(0 if sub_info else msl, msl + 1):  # the highest sub-layer's values are kept
+        s["max_dec_pic_buffering"] = b.ue() + 1
+        s["max_num_reorder"] = b.ue()
+        plus1 = b.ue()
+        s["max_latency"] = s["max_num_reorder"] + plus1 - 1 if plus1 else 0
     s["log2_min_cb"] = b.ue() + 3
     s["log2_ctb"] = s["log2_min_cb"] + b.ue()
     s["log2_min_tb"] = b.ue() + 2
@@ -541,8 +544,7 @@ TRAIL_N, TRAIL_R, RASL_N, RASL_R, BLA_W_LP, IDR_W_RADL, IDR_N_LP, CRA = 0, 1, 8,
 def parse_slice_header(b: Bits, nal_type: int, spss: dict, ppss: dict, prev: dict | None) -> dict:
     h = {"nal_type": nal_type}
     h["first"] = b.u(1)
-    if BLA_W_LP <= nal_type <= 23:
-        b.u(1)  # no_output_of_prior_pics_flag
+    h["no_output_of_prior_pics"] = b.u(1) if BLA_W_LP <= nal_type <= 23 else 0
     pps = ppss[b.ue()]
     sps = spss[pps["sps_id"]]
     h["pps"], h["sps"] = pps, sps
@@ -812,7 +814,9 @@ class Decoder:
         poc = msb + lsb
         if h["tid"] == 0 and not (nt in (RASL_N, RASL_R, 6, 7) or (nt <= 14 and nt % 2 == 0)):
             self.prev_tid0_poc = poc
-        if irap and no_rasl_output:
+        self.new_sequence = bool(irap and no_rasl_output)
+        self.unref = []
+        if self.new_sequence:
             self.cvs += 1
             for p in self.dpb:
                 p.ref = False
@@ -822,6 +826,7 @@ class Decoder:
         for p in self.dpb:
             if p.ref and p.poc not in keep:
                 p.ref = False
+                self.unref.append(p.ident)
         self.dpb = [p for p in self.dpb if p.ref]
         self.st_before = [self._by_poc(poc + d) for d, u in rps["s0"] if u]
         self.st_after = [self._by_poc(poc + d) for d, u in rps["s1"] if u]
@@ -940,6 +945,10 @@ class Decoder:
         self.pics.append({
             "W": self.W, "H": self.H, "bit_depth": self.bd, "slot": pic.slot, "poc": pic.poc, "cvs": self.cvs,
             "output": self.pic_hdr["output"], "crop": crop, "frame_id": pic.ident,
+            # the output process (DPB bumping): sequence start, the references
+            # this picture's RPS dropped, and the SPS limits
+            "new_sequence": self.new_sequence, "no_output_of_prior_pics": self.pic_hdr["no_output_of_prior_pics"],
+            "unref": self.unref, "dpb": [sps["max_dec_pic_buffering"], sps["max_num_reorder"], sps["max_latency"]],
             "header": {"log2_ctb": self.log2ctb, "constrained_intra_pred": pps["constrained_intra"],
                        "strong_intra_smoothing": sps["strong_intra"], "loop_filter_across_tiles": pps["lf_across_tiles"],
                        "cb_qp_offset": pps["cb_qp_offset"], "cr_qp_offset": pps["cr_qp_offset"],

@@ -103,7 +103,8 @@ def main(refs: pathlib.Path, names):
             for k in KEYS:
                 arrays[f"{k}_{i}"] = np.frombuffer(p["bufs"][k], np.uint8)
             meta["pictures"].append({k: p[k] for k in ("W", "H", "bit_depth", "slot", "poc", "cvs", "output", "crop",
-                                                        "header")})
+                                                        "header", "frame_id", "new_sequence",
+                                                        "no_output_of_prior_pics", "unref", "dpb")})
         arrays["meta"] = np.frombuffer(json.dumps(meta).encode(), np.uint8)
         np.savez_compressed(HERE / f"hevc_{name}.npz", **arrays)
         print(f"wrote tests/golden/hevc_{name}.npz")
