@@ -363,7 +363,8 @@ int rc_picture_device_planes(rc_stream *s, int slot, void **y, void **u,
 #define RC_KERNEL_HEVC_INTRA 5
 #define RC_KERNEL_HEVC_DEBLOCK 6
 #define RC_KERNEL_HEVC_SAO 7
-#define RC_KERNEL_COUNT 8
+#define RC_KERNEL_H264_GROUP 8
+#define RC_KERNEL_COUNT 9
 int rc_stream_profile(rc_stream *s, int enable);
 /* Schedule knob for many streams sharing one GPU: the HEVC intra kernel's
  * persistent CTAs per launch (default: about one per two 64x64 CTBs, at
@@ -381,6 +382,25 @@ int rc_stream_intra_ctas(rc_stream *s);
  * a shorter bound; 0 restores the default (about a second of polling).
  * Takes effect from the next submit. */
 int rc_stream_set_wait_limit(rc_stream *s, unsigned int limit);
+/* H.264 only: reconstruct up to `pictures` consecutive pictures in one
+ * launch (no counterpart in the reference, which decodes one picture at a
+ * time per thread and overlaps pictures only across its worker threads).
+ * The launch runs every picture's intra + loop-filter wavefront side by side
+ * with the MB phase of all of them, each inter MB waiting only for the rows
+ * of the pictures in the launch that its motion vectors reach; the output is
+ * the same as one launch per picture.  rc_h264_submit then queues a picture
+ * and launches when the group is full, when the next picture writes a DPB
+ * slot that a queued picture writes or reads, when the scaling lists change,
+ * before a picture whose records are in device memory, and in every call
+ * that waits for or orders after the submitted work (rc_stream_sync,
+ * rc_stream_error, rc_picture_download*, rc_picture_upload,
+ * rc_picture_device_planes, rc_stream_mark, rc_stream_cuda_stream,
+ * rc_stream_profile*).  1 launches each picture at its submit (the default);
+ * 0 picks the library's default group; at most 4.  The group is lowered
+ * until the pictures' band CTAs fit in two thirds of one launch.  Returns
+ * the pictures per launch now in effect, or RC_EINVAL (HEVC stream, out of
+ * range) / RC_ENOMEM (the per-picture scratch: about 1.2 KB per MB). */
+int rc_stream_set_h264_group(rc_stream *s, int pictures);
 int rc_stream_profile_read(rc_stream *s, double *ms, long long *launches,
                            int max_kernels);
 

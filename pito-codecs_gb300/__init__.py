@@ -33,8 +33,9 @@ ERROR_NAMES = {RC_EINVAL: "RC_EINVAL", RC_ENOMEM: "RC_ENOMEM", RC_ECUDA: "RC_ECU
 
 RC_H264_NONE, RC_H264_I4x4, RC_H264_I8x8, RC_H264_I16x16, RC_H264_IPCM, RC_H264_INTER = range(6)
 RC_KERNEL_NAMES = {0: "h264_mb_kernel", 1: "h264_band_kernel", 2: "h264_edge_kernel", 3: "hevc_residual_kernel",
-                   4: "hevc_inter_kernel", 5: "hevc_intra_kernel", 6: "hevc_deblock_kernel", 7: "hevc_sao_kernel"}
-RC_KERNEL_COUNT = 8
+                   4: "hevc_inter_kernel", 5: "hevc_intra_kernel", 6: "hevc_deblock_kernel", 7: "hevc_sao_kernel",
+                   8: "h264_group_kernel"}
+RC_KERNEL_COUNT = 9
 
 
 class ReconError(RuntimeError):
@@ -207,6 +208,8 @@ def lib() -> ctypes.CDLL:
     L.rc_stream_intra_ctas.restype = i32
     L.rc_stream_set_wait_limit.argtypes = [vp, ctypes.c_uint]
     L.rc_stream_set_wait_limit.restype = i32
+    L.rc_stream_set_h264_group.argtypes = [vp, i32]
+    L.rc_stream_set_h264_group.restype = i32
     L.rc_stream_sync.restype = i32
     L.rc_stream_error.argtypes = [vp]
     L.rc_stream_error.restype = i32
@@ -555,6 +558,14 @@ class ReconStream:
     def set_wait_limit(self, limit: int):
         """Iteration cap of the device-side waits (0: the default)."""
         _check(lib().rc_stream_set_wait_limit(self._h, int(limit)), "rc_stream_set_wait_limit")
+
+    def set_h264_group(self, pictures: int) -> int:
+        """H.264: pictures reconstructed per launch (1: one launch per
+        picture; 0: the library's default); returns the value in effect."""
+        r = lib().rc_stream_set_h264_group(self._h, int(pictures))
+        if r < 0:
+            raise ReconError(r, "rc_stream_set_h264_group")
+        return r
 
     def profile_read(self) -> dict:
         ms = (ctypes.c_double * RC_KERNEL_COUNT)()

@@ -26,6 +26,16 @@
 //                       above; the luma filter reports MB x-1 to the row
 //                       below as soon as MB x's left edge is filtered.
 //
+// Or, for a group of up to RC_H264_GROUP_MAX consecutive pictures:
+//
+//  h264_group_kernel    one cooperative launch: the band CTAs of every
+//                       picture of the group, and CTAs that run the MB phase
+//                       (edge words included) of all of them in picture
+//                       order; an inter MB waits only for the reference rows
+//                       its motion vectors reach, an intra warp only for the
+//                       MBs of its row.  The wavefronts of consecutive
+//                       pictures then run side by side.
+//
 // rc_h264_deblock_noalloc filters a reconstructed picture without allocating
 // (h264_db_params_kernel, then h264_deblock_kernel: one warp per MB row).
 //
@@ -250,21 +260,78 @@ __global__ void __launch_bounds__(32 * EDGE_MBS) h264_edge_kernel(H264Launch P) 
 // ===========================================================================
 // Kernel 1: inter MBs (prediction + residual) and I_PCM, one CTA per MB.
 // ===========================================================================
-__global__ void __launch_bounds__(256) h264_mb_kernel(H264Launch P) {
-    __shared__ __align__(16) rc_h264_mb m;
-    __shared__ int32_t coef[256];
-    __shared__ int32_t coefc[128];
-    __shared__ uint8_t predy[256];
-    __shared__ uint8_t predc[128];
-    __shared__ uint32_t nzl, nzc;
-    const int t = threadIdx.x, addr = blockIdx.x;
+// Group launches: before an inter MB is predicted, the rows of the in-flight
+// pictures it references that its motion vectors reach (6-tap windows
+// included) must be final.  Row r of a picture is final through MB column c
+// once row r + 1 has loop-filtered and stored MBs 0..c+1 (the top edge of
+// row r + 1 is the last change to row r's bottom lines, and MB c+1's left
+// edge the last change to MB c), so the MB waits for the reference's filter
+// progress on row min(R + 1, last) to reach column C + 2, R and C being the
+// furthest MB row and column any of its blocks reads.  Chroma reads reach no
+// further than luma.  Warp 0; false after a timeout.
+__device__ bool mb_wait_refs(const H264Launch &P, const rc_h264_mb &m, const rc_h264_slice *sl, int mbx, int mby,
+                             int t) {
+    if (t >= 32) return true;
+    const int k = t & 15, l = t >> 4, b8 = ((k >> 2) >> 1) * 2 + ((k & 3) >> 1);
+    const int ri = m.ref_idx[l][b8];
+    int slot = -1, r = -1, c = -1;
+    if (ri >= 0 && ri < min(__ldg(&sl->num_ref[l]), RC_H264_MAX_REFS)) {
+        slot = __ldg(&sl->ref_slot[l][ri]);
+        const int bottom = mby * 16 + (k >> 2) * 4 + 3 + (m.mv[l][k][1] >> 2) + 3;
+        const int right = mbx * 16 + (k & 3) * 4 + 3 + (m.mv[l][k][0] >> 2) + 3;
+        r = clampi(bottom >> 4, 0, P.mb_h - 1);
+        c = clampi(right >> 4, 0, P.mb_w - 1);
+    }
+    bool ok = true;
+    for (int i = 0; i < P.nwait; i++) {
+        const int rr = __reduce_max_sync(0xffffffffu, slot == P.wait_slot[i] ? r : -1);
+        const int cc = __reduce_max_sync(0xffffffffu, slot == P.wait_slot[i] ? c : -1);
+        if (rr < 0) continue;
+        if (t == 0) {
+            const uint32_t *f = P.wait_rowprog[i] + min(rr + 1, P.mb_h - 1);
+            const uint32_t tag = (P.wait_epoch[i] & 0xffffu) << 16, need = (uint32_t)min(cc + 2, P.mb_w);
+            uint32_t it = 0, v;
+            while (((v = ld_acquire(f)) & 0xffff0000u) != tag || (v & 0xffffu) < need) {
+                if (++it > P.wait_limit || ((it & 63) == 0 && aborted(P.error))) { ok = false; break; }
+                if (it > 64) __nanosleep(128);
+            }
+        }
+    }
+    return __shfl_sync(0xffffffffu, ok, 0);
+}
+
+// Shared state of one MB-phase worker (256 threads).
+struct __align__(16) MbSmem {
+    rc_h264_mb m;
+    int32_t coef[256];
+    int32_t coefc[128];
+    uint8_t predy[256];
+    uint8_t predc[128];
+    uint32_t nzl, nzc, ibits;  // ibits, intra: neighbour availability (bits 0..3: left, top, top-right, top-left)
+    int refs_ok, item;
+    rc_h264_mb nbr[2];  // group kernel: the MB's left and top neighbours, and its filter parameters
+    DbMb dbm;
+};
+
+// Barrier `id` over the `n` threads of one MB worker (id 0 with n = the
+// CTA's threads is __syncthreads).
+__device__ __forceinline__ void bar_sync(int id, int n) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory"); }
+
+// One macroblock of the MB phase, 256 threads (t = 0..255, barrier `bar`):
+// inter prediction with the residual, I_PCM copy, or an intra MB's residual
+// and prediction parameters.
+__device__ void mb_body(const H264Launch &P, MbSmem &M, const int addr, const int t, const int bar) {
+    rc_h264_mb &m = M.m;
+    int32_t *coef = M.coef, *coefc = M.coefc;
+    uint8_t *predy = M.predy, *predc = M.predc;
+    uint32_t &nzl = M.nzl, &nzc = M.nzc, &ibits = M.ibits;
     const int mbx = addr % P.mb_w, mby = addr / P.mb_w;
     constexpr int RW = (int)(sizeof(rc_h264_mb) / 4);
     if (t < RW) ((uint32_t *)&m)[t] = __ldg((const uint32_t *)(P.mbs + addr) + t);
     if (t == 0) { nzl = 0; nzc = 0; }
     coef[t] = 0;
     if (t < 128) coefc[t] = 0;
-    __syncthreads();
+    bar_sync(bar, 256);
     const int kind = m.kind;
     if (kind == RC_H264_NONE || kind > RC_H264_INTER) return;
     uint8_t *Y = P.dpb + (size_t)P.out_slot * P.slot_bytes;
@@ -288,10 +355,9 @@ __global__ void __launch_bounds__(256) h264_mb_kernel(H264Launch P) {
     const unsigned long long need =
         nlum + (unsigned long long)nl * (t8 ? 64 : 16) + ndc * 4 + __popc(m.chroma_coded) * 16;
     if (m.coef_off + need > P.num_levels) { if (t == 0) set_error(P.error, RC_DEV_ERR_RECORD); return; }
-    __shared__ uint32_t ibits;  // intra: neighbour availability (bits 0..3: left, top, top-right, top-left)
     if (intra) {
         if (t == 0) ibits = 0;
-        __syncthreads();
+        bar_sync(bar, 256);
         if (t < 4) {
             // start_mb neighbour availability + intra_nb, slicedec.rs:489-508, 525-530
             const int dx = t == 0 ? -1 : t == 2 ? 1 : t == 3 ? -1 : 0, dy = t == 0 ? 0 : -1;
@@ -302,6 +368,15 @@ __global__ void __launch_bounds__(256) h264_mb_kernel(H264Launch P) {
                 const bool a = nk != RC_H264_NONE && __ldg(&pm->slice) == m.slice && (!P.constrained_intra || is_intra(nk));
                 if (a) atomicOr(&ibits, 1u << t);
             }
+        }
+    }
+    if (!intra && P.mbdone && P.nwait > 0) {
+        const bool ok = mb_wait_refs(P, m, sl, mbx, mby, t);
+        if (t == 0) M.refs_ok = ok;
+        bar_sync(bar, 256);
+        if (!M.refs_ok) {
+            if (t == 0) set_error(P.error, RC_DEV_ERR_TIMEOUT);
+            return;
         }
     }
     if (!intra) {
@@ -405,18 +480,18 @@ __global__ void __launch_bounds__(256) h264_mb_kernel(H264Launch P) {
             }
         }
     }
-    __syncthreads();
+    bar_sync(bar, 256);
     // ---- inverse transforms: rows, then columns
     if (t8) {
         if (t < 32 && (nzl >> (t >> 3) & 1)) idct8_1d(coef + (t >> 3) * 64 + (t & 7) * 8, 1);
     } else if (t < 64 && (nzl >> (t >> 2) & 1)) idct4_1d(coef + (t >> 2) * 16 + (t & 3) * 4, 1);
     if (t >= 64 && t < 96 && (nzc >> ((t - 64) >> 2) & 1)) idct4_1d(coefc + ((t - 64) >> 2) * 16 + (t & 3) * 4, 1);
-    __syncthreads();
+    bar_sync(bar, 256);
     if (t8) {
         if (t < 32 && (nzl >> (t >> 3) & 1)) idct8_1d(coef + (t >> 3) * 64 + (t & 7), 8);
     } else if (t < 64 && (nzl >> (t >> 2) & 1)) idct4_1d(coef + (t >> 2) * 16 + (t & 3), 4);
     if (t >= 64 && t < 96 && (nzc >> ((t - 64) >> 2) & 1)) idct4_1d(coefc + ((t - 64) >> 2) * 16 + (t & 3), 4);
-    __syncthreads();
+    bar_sync(bar, 256);
     if (intra) {
         // residual samples ((v + 32) >> 6, idct4_add / idct8_add) and the
         // prediction parameters for the intra wavefront
@@ -471,6 +546,11 @@ __global__ void __launch_bounds__(256) h264_mb_kernel(H264Launch P) {
         if (nzc >> blk & 1) v = clip255(v + ((coefc[blk * 16 + (y & 3) * 4 + (x & 3)] + 32) >> 6));
         (c ? V : U)[(size_t)(mby * 8 + y) * P.cpitch + mbx * 8 + x] = (uint8_t)v;
     }
+}
+
+__global__ void __launch_bounds__(256) h264_mb_kernel(const __grid_constant__ H264Launch P) {
+    __shared__ MbSmem M;
+    mb_body(P, M, blockIdx.x, threadIdx.x, 0);
 }
 
 // ===========================================================================
@@ -1359,9 +1439,33 @@ __device__ __forceinline__ void cp_wait_all_but_4() { asm volatile("cp.async.wai
 // reconstructed.  All of these are final before the kernel starts and stay
 // unchanged until this warp reports the MB after them reconstructed (the
 // filter warps wait for that), so they may be read early.
+//
+// In a group launch (P.mbdone set) the MB phase runs beside the band CTAs:
+// MB x of the row is ready once mbdone[x] holds the picture's epoch.  The
+// warp then fills its line as the row's MBs become ready (inter MBs copied
+// from the picture, intra ones written as it reconstructs them) and reports
+// an MB only once it and every MB before it are ready and in the line, so
+// that the filter warps and the rows below wait on inter MBs through the
+// same progress word.
+__device__ bool wait_flag(const uint32_t *f, uint32_t want, const H264Launch &P, int lane) {
+    bool ok = true;
+    if (lane == 0) {
+        uint32_t it = 0;
+        while (ld_acquire(f) != want) {
+            if (++it > P.wait_limit || ((it & 63) == 0 && aborted(P.error))) { ok = false; break; }
+            if (it > 16) __nanosleep(64);
+        }
+    }
+    ok = __shfl_sync(0xffffffffu, ok, 0);
+    __syncwarp();
+    return ok;
+}
+
 __device__ void band_intra_row(const H264Launch &P, BandSmem &B, uint8_t *lines, uint8_t *stg, int w, int my,
                                int lane) {
     WarpSmem &S = B.iw[w];
+    const bool grouped = P.mbdone != nullptr;
+    const uint32_t *done = grouped ? P.mbdone + (size_t)my * P.mb_w : nullptr;
     uint8_t *Y = P.dpb + (size_t)P.out_slot * P.slot_bytes;
     uint8_t *U = Y + P.u_off, *V = Y + P.v_off;
     const int LW = P.mb_w * 32;
@@ -1400,6 +1504,7 @@ __device__ void band_intra_row(const H264Launch &P, BandSmem &B, uint8_t *lines,
     // are final from the start: in the line copy, which the row above fills
     // before its first report, or in the picture for a band's first row)
     auto above_need = [&](int x) -> int {
+        if (grouped) return min(x + 2, P.mb_w);  // the row above reports inter MBs too
         const int base = w > 0 ? 1 : 0;
         if (above_intra(x + 1)) return min(x + 2, P.mb_w);
         if (above_intra(x)) return x + 1;
@@ -1414,7 +1519,46 @@ __device__ void band_intra_row(const H264Launch &P, BandSmem &B, uint8_t *lines,
         }
         return P.mb_w;
     };
-    auto prefetch = [&](int nx) {
+    auto is_intra = [&](int x) -> bool {  // MB (x, my) is reconstructed here; any lane's x
+        return (__shfl_sync(0xffffffffu, word, (x >> 5) & 31) >> (x & 31)) & 1;
+    };
+    // grouped: the line holds MBs 0..filled-1; fill it up to v, waiting for
+    // the MB phase four MBs at a time (lane 8 i + j: MB filled + i, word j)
+    int filled = 0;
+    auto advance = [&](int v) -> bool {
+        while (filled < v) {
+            const int i = lane >> 3, j = lane & 7, x = filled + i;
+            const bool intra_x = is_intra(min(x, P.mb_w - 1));  // every lane takes part in the shuffle
+            const bool cp = x < v && !intra_x;
+            bool ok = true;
+            if (cp && j == 0) {
+                uint32_t it = 0;
+                while (ld_acquire(done + x) != P.epoch) {
+                    if (++it > P.wait_limit || ((it & 63) == 0 && aborted(P.error))) { ok = false; break; }
+                    if (it > 16) __nanosleep(64);
+                }
+            }
+            if (!__all_sync(0xffffffffu, ok)) return false;
+            __syncwarp();
+            if (cp) {
+                const uint8_t *src = j < 4 ? Y + (size_t)(my * 16 + 15) * P.pitch + x * 16 + j * 4
+                                           : (j < 6 ? U : V) + (size_t)(my * 8 + 7) * P.cpitch + x * 8 + (j & 1) * 4;
+                uint8_t *dst = j < 4 ? ly + x * 16 + j * 4 : (j < 6 ? lu : lv) + x * 8 + (j & 1) * 4;
+                *(uint32_t *)dst = __ldcg((const uint32_t *)src);
+            }
+            filled = min(filled + 4, v);
+        }
+        __syncwarp();
+        __threadfence_block();
+        return true;
+    };
+    auto prefetch = [&](int nx) -> bool {
+        // grouped: the MB's parameters and residual, and its left neighbour
+        // when that is an inter MB, come from the MB phase
+        if (grouped && nx < P.mb_w) {
+            if (!wait_flag(done + nx, P.epoch, P, lane)) return false;
+            if (nx > 0 && !is_intra(nx - 1) && !wait_flag(done + nx - 1, P.epoch, P, lane)) return false;
+        }
         if (nx < P.mb_w) {
             const int addr = my * P.mb_w + nx;
             const uint8_t *q = (const uint8_t *)(P.iinfo + addr), *res = (const uint8_t *)(P.ires + (size_t)addr * 384);
@@ -1429,10 +1573,15 @@ __device__ void band_intra_row(const H264Launch &P, BandSmem &B, uint8_t *lines,
             }
         }
         cp_commit();
+        return true;
     };
     int mx = next_intra(0);
-    prefetch(mx);
-    {
+    if (!prefetch(mx)) {
+        cp_wait_all();
+        band_fail(P, lane);
+        return;
+    }
+    if (!grouped) {
         const uint32_t *gy = (const uint32_t *)(Y + (size_t)(my * 16 + 15) * P.pitch);
         const uint32_t *gu = (const uint32_t *)(U + (size_t)(my * 8 + 7) * P.cpitch);
         const uint32_t *gv = (const uint32_t *)(V + (size_t)(my * 8 + 7) * P.cpitch);
@@ -1448,7 +1597,12 @@ __device__ void band_intra_row(const H264Launch &P, BandSmem &B, uint8_t *lines,
     int above_seen = 0;  // the row above's intra progress observed so far
     while (mx < P.mb_w) {
         const int nx = next_intra(mx + 1);
-        // the MBs before mx are reconstructed (inter ones by h264_mb_kernel)
+        // the MBs before mx are reconstructed (inter ones by the MB phase)
+        if (grouped && !advance(mx)) {
+            cp_wait_all();
+            band_fail(P, lane);
+            return;
+        }
         if (lane == 0 && *mine < mx) *mine = mx;
         // the staged parameters and residual; canvas column -1: MB mx-1's right
         // column, from the canvas when this warp reconstructed it, else staged
@@ -1469,7 +1623,11 @@ __device__ void band_intra_row(const H264Launch &P, BandSmem &B, uint8_t *lines,
             }
         }
         __syncwarp();
-        prefetch(nx);
+        if (!prefetch(nx)) {
+            cp_wait_all();
+            band_fail(P, lane);
+            return;
+        }
         if (my > 0 && !wait_seen(above, above_seen, above_need(mx), P, lane)) {
             cp_wait_all();
             band_fail(P, lane);
@@ -1514,6 +1672,7 @@ __device__ void band_intra_row(const H264Launch &P, BandSmem &B, uint8_t *lines,
             }
         }
         last = mx;
+        filled = mx + 1;
         __syncwarp();
         __threadfence_block();
         if (lane == 0) *mine = mx + 1;
@@ -1521,6 +1680,10 @@ __device__ void band_intra_row(const H264Launch &P, BandSmem &B, uint8_t *lines,
     }
     cp_wait_all();
     __syncwarp();
+    if (grouped && !advance(P.mb_w)) {
+        band_fail(P, lane);
+        return;
+    }
     if (lane == 0) *mine = P.mb_w;
 }
 
@@ -1870,14 +2033,24 @@ __device__ void band_mirror(const H264Launch &P, BandSmem &B, int y0, int rows, 
 __device__ void band_publish(const H264Launch &P, BandSmem &B, int y0, int rows, int lane) {
     const uint32_t tag = (P.epoch & 0xffffu) << 16;
     const bool above = y0 > 0, below = y0 + rows < P.mb_h;
-    uint32_t *dst = lane == 0 ? (below ? P.rowprog + y0 + rows - 1 : nullptr)
+    // in a group launch, lane 0 also publishes the picture's last row and
+    // lanes 3.. the band's other rows, for the MB phase of later pictures of
+    // the group that read this one
+    const bool grouped = P.mbdone != nullptr;
+    const int prow = lane - 3;
+    uint32_t *dst = lane == 0 ? (below || grouped ? P.rowprog + y0 + rows - 1 : nullptr)
                     : lane == 1 ? (below ? P.irowprog + y0 + rows - 1 : nullptr)
                     : lane == 2 ? (above ? P.irowprog + y0 : nullptr)
-                                : nullptr;
+                    : grouped && prow < rows - 1 ? P.rowprog + y0 + prow
+                                                 : nullptr;
     int seen = dst ? 0 : P.mb_w;
     uint32_t it = 0;
     while (!__all_sync(0xffffffffu, seen >= P.mb_w)) {
-        const int n = !dst ? seen : lane == 0 ? min(B.lprog[rows], B.cprog[rows]) : lane == 1 ? B.iprog[rows] : B.iprog[1];
+        const int n = !dst ? seen
+                      : lane == 0 ? min(B.lprog[rows], B.cprog[rows])
+                      : lane == 1 ? B.iprog[rows]
+                      : lane == 2 ? B.iprog[1]
+                                  : min(B.lprog[prow + 1], B.cprog[prow + 1]);
         const bool moved = n > seen;
         if (__any_sync(0xffffffffu, moved)) {
             __threadfence();
@@ -1894,13 +2067,11 @@ __device__ void band_publish(const H264Launch &P, BandSmem &B, int y0, int rows,
     }
 }
 
-__global__ void __launch_bounds__(BAND_THREADS, 1) h264_band_kernel(H264Launch P) {
-    __shared__ BandSmem B;
-    // dynamic: per band row the intra warp's staging (RC_BAND_STG bytes), then
-    // per band row its line of bottom samples (mb_w x 32 bytes)
-    extern __shared__ __align__(16) uint8_t band_dyn[];
+// One band CTA: every thread of the CTA calls it; warps past the band's
+// (3 BR + 2) roles leave after the shared state is set up.
+__device__ void band_body(const H264Launch &P, BandSmem &B, uint8_t *band_dyn, int band) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int y0 = blockIdx.x * BR, rows = min(BR, P.mb_h - y0);
+    const int y0 = band * BR, rows = min(BR, P.mb_h - y0);
     for (int i = threadIdx.x; i < 9 * 16; i += blockDim.x) B.tab4[i] = (&cPRED4.e[0][0])[i];
     for (int i = threadIdx.x; i < 9 * 64; i += blockDim.x) B.tab8[i] = (&cPRED8.e[0][0])[i];
     if (threadIdx.x < BR + 2) B.iprog[threadIdx.x] = 0;
@@ -1911,11 +2082,91 @@ __global__ void __launch_bounds__(BAND_THREADS, 1) h264_band_kernel(H264Launch P
     __syncthreads();
     if (warp == 3 * BR) { band_mirror(P, B, y0, rows, lane); return; }
     if (warp == 3 * BR + 1) { band_publish(P, B, y0, rows, lane); return; }
+    if (warp >= 3 * BR + 2) return;
     const int role = warp / BR, w = warp % BR;
     if (w >= rows) return;
     if (role == 0) band_intra_row(P, B, band_dyn + BR * RC_BAND_STG, band_dyn + w * RC_BAND_STG, w, y0 + w, lane);
     else if (role == 1) band_luma_row(P, B, w, y0 + w, rows, lane);
     else band_chroma_row(P, B, w, y0 + w, rows, lane);
+}
+
+__global__ void __launch_bounds__(BAND_THREADS, 1) h264_band_kernel(const __grid_constant__ H264Launch P) {
+    __shared__ BandSmem B;
+    // dynamic: per band row the intra warp's staging (RC_BAND_STG bytes), then
+    // per band row its line of bottom samples (mb_w x 32 bytes)
+    extern __shared__ __align__(16) uint8_t band_dyn[];
+    band_body(P, B, band_dyn, blockIdx.x);
+}
+
+// ===========================================================================
+// Kernel 3: a group of pictures in one cooperative launch.
+// ===========================================================================
+// CTAs 0 .. n*bands-1 are the band CTAs of the group's pictures (picture
+// b / bands, band b % bands); every other CTA runs the MB phase of all of
+// them, as two workers of 256 threads that take (picture, MB) items in order
+// from one counter -- every item of a picture before any item of the next
+// -- and publish each item's completion, edge words included, as
+// mbdone[addr] = epoch.  An item of picture j waits (mb_wait_refs) only for
+// rows of earlier pictures of the group, whose MB items were all taken
+// before it by workers that are running and whose band CTAs are resident
+// (cooperative launch): every wait ends.  The MB phase and the wavefronts
+// wait on one another, so they share one launch: separate launches are not
+// guaranteed to run at the same time.  The launch ends when every picture is
+// filtered, so the next launch on the stream reads finished references.
+constexpr int GROUP_THREADS = 512;
+static_assert(GROUP_THREADS >= BAND_THREADS && GROUP_THREADS == 2 * 256, "two MB workers, or one band CTA");
+
+union GroupSmem {
+    BandSmem band;
+    MbSmem mb[2];
+};
+
+// The MB's loop-filter edge words, as h264_edge_kernel computes them; one
+// warp of a worker, after the MB (M.m holds its record).
+__device__ void mb_edge_words(const H264Launch &P, MbSmem &M, int addr, int lane) {
+    const int mbx = addr % P.mb_w, mby = addr / P.mb_w;
+    constexpr int RW = (int)(sizeof(rc_h264_mb) / 4);
+    for (int i = lane; i < 2 * RW; i += 32) {
+        const int which = i / RW, j = i - which * RW;
+        const int src = which == 0 ? (mbx > 0 ? addr - 1 : -1) : (mby > 0 ? addr - P.mb_w : -1);
+        if (src >= 0) ((uint32_t *)&M.nbr[which])[j] = __ldg((const uint32_t *)(P.mbs + src) + j);
+    }
+    __syncwarp();
+    compute_db(P, M.m, M.nbr[0], M.nbr[1], addr, lane, &M.dbm);
+    __syncwarp();
+    edge_words(M.dbm, lane, P.edges + (size_t)addr * RC_EDGE_WORDS);
+    __syncwarp();
+}
+
+__global__ void __launch_bounds__(GROUP_THREADS, 1) h264_group_kernel(const __grid_constant__ H264Group G) {
+    __shared__ GroupSmem S;
+    extern __shared__ __align__(16) uint8_t band_dyn[];
+    const int nb = G.n * G.bands;
+    if ((int)blockIdx.x < nb) {
+        const int j = blockIdx.x / G.bands;
+        band_body(G.pic[j], S.band, band_dyn, blockIdx.x - j * G.bands);
+        return;
+    }
+    const int h = threadIdx.x >> 8, t = threadIdx.x & 255, bar = 1 + h;
+    MbSmem &M = S.mb[h];
+    const int n_mb = G.pic[0].mb_w * G.pic[0].mb_h, total = G.n * n_mb;
+    for (;;) {
+        if (t == 0) M.item = (int)atomicAdd(G.counter, 1u);
+        bar_sync(bar, 256);
+        const int w = M.item;
+        if (w >= total) return;
+        const int j = w / n_mb, addr = w - j * n_mb;
+        const H264Launch &P = G.pic[j];
+        mb_body(P, M, addr, t, bar);
+        bar_sync(bar, 256);  // the item's stores, and every read of M.item, are done
+        if (t < 32) {
+            mb_edge_words(P, M, addr, t);
+            if (t == 0) {
+                __threadfence();
+                st_release(P.mbdone + addr, P.epoch);
+            }
+        }
+    }
 }
 
 }  // namespace
@@ -1934,19 +2185,21 @@ size_t rc_h264_band_smem(int mb_w) { return (size_t)BR * (RC_BAND_STG + (size_t)
 // The kernel's dynamic shared-memory limit is one attribute for every stream
 // of the process: raise it to the widest picture any stream needs (never
 // lower it, so a narrower stream created later cannot break a wider one).
+// Kernel k: 0 the band kernel, 1 the group kernel.
 static std::mutex g_band_attr_mu;
-static int g_band_attr[64];
+static int g_band_attr[2][64];
 
-static bool band_smem_attr(size_t dyn) {
+static bool band_smem_attr(int k, size_t dyn) {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return false;
     std::lock_guard<std::mutex> lock(g_band_attr_mu);
-    if ((int)dyn <= g_band_attr[dev]) return true;
-    if (cudaFuncSetAttribute(h264_band_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn) != cudaSuccess) {
+    if ((int)dyn <= g_band_attr[k][dev]) return true;
+    const void *fn = k ? (const void *)h264_group_kernel : (const void *)h264_band_kernel;
+    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn) != cudaSuccess) {
         cudaGetLastError();
         return false;
     }
-    g_band_attr[dev] = (int)dyn;
+    g_band_attr[k][dev] = (int)dyn;
     return true;
 }
 
@@ -1956,7 +2209,7 @@ int rc_h264_band_capacity(int mb_w) {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (mb_w <= 0 || mb_w > 1024) return 0;  // the intra warps' row bitmaps
     const size_t dyn = rc_h264_band_smem(mb_w);
-    if (!band_smem_attr(dyn)) return 0;
+    if (!band_smem_attr(0, dyn)) return 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, h264_band_kernel, BAND_THREADS, dyn) != cudaSuccess)
         return 0;
     return per * sms;
@@ -1964,11 +2217,37 @@ int rc_h264_band_capacity(int mb_w) {
 
 int rc_launch_h264_band(const H264Launch &p, cudaStream_t st) {
     const int bands = (p.mb_h + BR - 1) / BR;
-    if (!band_smem_attr(rc_h264_band_smem(p.mb_w))) return -1;
+    if (!band_smem_attr(0, rc_h264_band_smem(p.mb_w))) return -1;
     H264Launch q = p;
+    q.mbdone = nullptr;
+    q.nwait = 0;
     void *args[] = {&q};
     cudaError_t e = cudaLaunchCooperativeKernel((const void *)h264_band_kernel, dim3(bands), dim3(BAND_THREADS),
                                                 args, rc_h264_band_smem(p.mb_w), st);
+    return e == cudaSuccess ? 0 : -1;
+}
+
+int rc_h264_group_capacity(int mb_w) {
+    int dev = 0, sms = 0, per = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (mb_w <= 0 || mb_w > 1024) return 0;
+    const size_t dyn = rc_h264_band_smem(mb_w);
+    if (!band_smem_attr(1, dyn)) return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, h264_group_kernel, GROUP_THREADS, dyn) != cudaSuccess)
+        return 0;
+    return per * sms;
+}
+
+int rc_launch_h264_group(const H264Group &g, int ctas, cudaStream_t st) {
+    const int mb_w = g.pic[0].mb_w;
+    if (g.n < 1 || g.n > RC_H264_GROUP_MAX || ctas <= g.n * g.bands) return -1;
+    if (!band_smem_attr(1, rc_h264_band_smem(mb_w))) return -1;
+    if (cudaMemsetAsync(g.counter, 0, sizeof(uint32_t), st) != cudaSuccess) return -1;
+    H264Group q = g;
+    void *args[] = {&q};
+    cudaError_t e = cudaLaunchCooperativeKernel((const void *)h264_group_kernel, dim3(ctas), dim3(GROUP_THREADS), args,
+                                                rc_h264_band_smem(mb_w), st);
     return e == cudaSuccess ? 0 : -1;
 }
 

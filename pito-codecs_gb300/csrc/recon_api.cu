@@ -54,6 +54,10 @@ struct DevBuf {
     size_t cap = 0;
 };
 
+// Record sets: two by submit parity, or two groups' worth when H.264
+// pictures launch in groups (the next group uploads while one runs).
+constexpr int REC_SETS = 2 * RC_H264_GROUP_MAX;
+
 }  // namespace
 
 struct rc_stream {
@@ -71,9 +75,10 @@ struct rc_stream {
     // that writes a slot waits for that slot's download
     cudaStream_t cst = nullptr;  // uploads
     cudaStream_t dst = nullptr;  // downloads
-    cudaEvent_t set_used[2] = {nullptr, nullptr};  // kernels of the last submit that read record set i
-    cudaEvent_t set_ready[2] = {nullptr, nullptr}; // record set i uploaded
-    bool set_busy[2] = {false, false};
+    cudaEvent_t set_used[REC_SETS] = {};  // kernels of the last submit that read record set i
+    cudaEvent_t set_ready[REC_SETS] = {}; // record set i uploaded
+    bool set_busy[REC_SETS] = {};
+    int nsets = 2;                        // record sets in use
     cudaEvent_t kernels_done = nullptr;            // recorded before each download
     std::vector<cudaEvent_t> slot_dl;              // per DPB slot: its last download
     std::vector<char> slot_dl_pending;
@@ -100,7 +105,20 @@ struct rc_stream {
     size_t nctb_max = 0;
     int w4 = 0, h4 = 0, log2ctb_alloc = 0;
     int bps = 1;
-    DevBuf mbs[2], slices[2], weights[2], levels[2];
+    DevBuf mbs[REC_SETS], slices[REC_SETS], weights[REC_SETS], levels[REC_SETS];
+    // H.264 picture groups (rc_stream_set_h264_group): pictures per launch,
+    // the launch's CTAs, the submitted pictures not yet launched (with the
+    // DPB slots they read and their record sets), and per group position the
+    // scratch of one picture: progress words, MB completion flags, edge
+    // words, intra parameters and residuals
+    int group = 1, group_ctas = 0;
+    std::vector<H264Launch> pending;
+    std::vector<std::vector<int>> pending_refs;
+    std::vector<int> pending_sets;
+    uint32_t *g_rowprog = nullptr, *g_irowprog = nullptr, *g_mbdone = nullptr, *g_edges = nullptr;
+    IntraInfo *g_iinfo = nullptr;
+    int16_t *g_ires = nullptr;
+    int g_alloc = 0;  // positions allocated
     int32_t *ls = nullptr;            // device ls4 (2304 ints) + ls8 (2304*4 ints)
     std::vector<int32_t> ls_host;     // last uploaded tables
     uint8_t ls_key[2 + 96 + 384] = {0};  // the scaling lists they were made from (flat: flag 0)
@@ -266,8 +284,49 @@ int validate_h264(const Geo *s, const rc_h264_picture *p) {
     return 0;
 }
 
+void group_free(rc_stream *s) {
+    if (!s->g_alloc) return;
+    const size_t mbs = (size_t)s->mb_w * s->mb_h, n = (size_t)s->g_alloc;
+    dev_free(s, s->g_rowprog, n * s->mb_h * sizeof(uint32_t));
+    dev_free(s, s->g_irowprog, n * s->mb_h * sizeof(uint32_t));
+    dev_free(s, s->g_mbdone, n * mbs * sizeof(uint32_t));
+    dev_free(s, s->g_edges, n * mbs * RC_EDGE_WORDS * sizeof(uint32_t));
+    dev_free(s, s->g_iinfo, n * mbs * sizeof(IntraInfo));
+    dev_free(s, s->g_ires, n * mbs * 384 * sizeof(int16_t));
+    s->g_rowprog = s->g_irowprog = s->g_mbdone = s->g_edges = nullptr;
+    s->g_iinfo = nullptr;
+    s->g_ires = nullptr;
+    s->g_alloc = 0;
+}
+
+// The per-position scratch of groups of n pictures (zeroed: no flag or
+// progress word matches a picture before it is written).
+int group_alloc(rc_stream *s, int n) {
+    if (n <= s->g_alloc) return 0;
+    if (cudaStreamSynchronize(s->st) != cudaSuccess) return cuda_fail(s);
+    group_free(s);
+    const size_t mbs = (size_t)s->mb_w * s->mb_h;
+    bool ok = dev_alloc(s, (void **)&s->g_rowprog, n * s->mb_h * sizeof(uint32_t)) &&
+              dev_alloc(s, (void **)&s->g_irowprog, n * s->mb_h * sizeof(uint32_t)) &&
+              dev_alloc(s, (void **)&s->g_mbdone, n * mbs * sizeof(uint32_t)) &&
+              dev_alloc(s, (void **)&s->g_edges, n * mbs * RC_EDGE_WORDS * sizeof(uint32_t)) &&
+              dev_alloc(s, (void **)&s->g_iinfo, n * mbs * sizeof(IntraInfo)) &&
+              dev_alloc(s, (void **)&s->g_ires, n * mbs * 384 * sizeof(int16_t));
+    s->g_alloc = n;  // group_free releases whatever was allocated
+    if (!ok) {
+        cudaGetLastError();
+        group_free(s);
+        return RC_ENOMEM;
+    }
+    ok = cudaMemsetAsync(s->g_rowprog, 0, n * s->mb_h * sizeof(uint32_t), s->st) == cudaSuccess &&
+         cudaMemsetAsync(s->g_irowprog, 0, n * s->mb_h * sizeof(uint32_t), s->st) == cudaSuccess &&
+         cudaMemsetAsync(s->g_mbdone, 0, n * mbs * sizeof(uint32_t), s->st) == cudaSuccess;
+    return ok ? 0 : cuda_fail(s);
+}
+
 void destroy(rc_stream *s) {
     if (!s) return;
+    s->pending.clear();  // submitted pictures not yet launched are dropped
     if (s->st) cudaStreamSynchronize(s->st);
     if (s->cst) cudaStreamSynchronize(s->cst);
     if (s->dst) cudaStreamSynchronize(s->dst);
@@ -277,9 +336,10 @@ void destroy(rc_stream *s) {
     for (cudaEvent_t e : s->mark_free) cudaEventDestroy(e);
     dev_free(s, s->dpb, s->slot_bytes * s->slots);
     for (int i = 0; i < 2; i++)
-        for (DevBuf *b : {&s->mbs[i], &s->slices[i], &s->weights[i], &s->levels[i], &s->ctbs[i], &s->blk[i], &s->mvf[i],
-                          &s->tus[i], &s->hslices[i]})
-            dev_free(s, b->p, b->cap);
+        for (DevBuf *b : {&s->ctbs[i], &s->blk[i], &s->mvf[i], &s->tus[i], &s->hslices[i]}) dev_free(s, b->p, b->cap);
+    for (int i = 0; i < REC_SETS; i++)
+        for (DevBuf *b : {&s->mbs[i], &s->slices[i], &s->weights[i], &s->levels[i]}) dev_free(s, b->p, b->cap);
+    group_free(s);
     dev_free(s, s->scaling.p, s->scaling.cap);
     cudaFree(s->work);
     for (int i = 0; i < 2; i++) cudaFree(s->res[i]);
@@ -305,7 +365,7 @@ void destroy(rc_stream *s) {
         if (s->staging[i]) cudaFreeHost(s->staging[i]);
         if (s->staged[i]) cudaEventDestroy(s->staged[i]);
     }
-    for (int i = 0; i < 2; i++) {
+    for (int i = 0; i < REC_SETS; i++) {
         if (s->set_used[i]) cudaEventDestroy(s->set_used[i]);
         if (s->set_ready[i]) cudaEventDestroy(s->set_ready[i]);
     }
@@ -389,6 +449,38 @@ int set_release(rc_stream *s, int k) {
     if (cudaEventRecord(s->set_used[k], s->st) != cudaSuccess) return cuda_fail(s);
     s->set_busy[k] = true;
     return 0;
+}
+
+// Launch the pending group of H.264 pictures, if any.
+int h264_flush(rc_stream *s) {
+    if (s->pending.empty()) return 0;
+    H264Group g;
+    memset(&g, 0, sizeof g);
+    g.n = (int)s->pending.size();
+    g.bands = (s->mb_h + RC_H264_BAND_ROWS - 1) / RC_H264_BAND_ROWS;
+    g.counter = s->counter;
+    for (int i = 0; i < g.n; i++) g.pic[i] = s->pending[i];
+    int lrc = 0;
+    timed(s, RC_KERNEL_H264_GROUP, [&] { lrc = rc_launch_h264_group(g, s->group_ctas, s->st); });
+    int rc = lrc ? cuda_fail(s) : 0;
+    for (int k : s->pending_sets)
+        if (!rc && k >= 0) rc = set_release(s, k);
+    s->pending.clear();
+    s->pending_refs.clear();
+    s->pending_sets.clear();
+    return rc;
+}
+
+// The DPB slots an H.264 picture's slices reference (validated records).
+std::vector<int> h264_ref_slots(const rc_h264_picture *p) {
+    std::vector<int> r;
+    for (int i = 0; i < p->num_slices; i++)
+        for (int l = 0; l < 2; l++)
+            for (int j = 0; j < p->slices[i].num_ref[l]; j++) {
+                const int slot = p->slices[i].ref_slot[l][j];
+                if (std::find(r.begin(), r.end(), slot) == r.end()) r.push_back(slot);
+            }
+    return r;
 }
 
 struct HGeo {
@@ -626,7 +718,7 @@ int rc_stream_create(int codec, int width, int height, int bit_depth, int dpb_sl
     bool ok = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking) == cudaSuccess &&
               cudaStreamCreateWithFlags(&s->cst, cudaStreamNonBlocking) == cudaSuccess &&
               cudaStreamCreateWithFlags(&s->dst, cudaStreamNonBlocking) == cudaSuccess;
-    for (int i = 0; i < 2 && ok; i++)
+    for (int i = 0; i < REC_SETS && ok; i++)
         ok = cudaEventCreateWithFlags(&s->set_used[i], cudaEventDisableTiming) == cudaSuccess &&
              cudaEventCreateWithFlags(&s->set_ready[i], cudaEventDisableTiming) == cudaSuccess;
     ok = ok && cudaEventCreateWithFlags(&s->kernels_done, cudaEventDisableTiming) == cudaSuccess &&
@@ -694,11 +786,33 @@ int rc_h264_submit(rc_stream *s, const rc_h264_picture *pic, int out_slot) {
     if (pic->mem != RC_MEM_HOST && pic->mem != RC_MEM_DEVICE) return RC_EINVAL;
     const int n = s->mb_w * s->mb_h;
     int rc;
+    if (pic->mem == RC_MEM_HOST) {
+        Geo g{s->mb_w, s->mb_h, s->slots};
+        if ((rc = validate_h264(&g, pic)) != 0) return rc;
+    } else if (!pic->mbs || !pic->slices || pic->num_slices <= 0) {
+        return RC_EINVAL;
+    }
+    // Groups: a picture joins the pending group unless it writes a slot that
+    // a pending picture writes or reads; device-memory records (whose
+    // references the host cannot read) launch alone, after the group.
+    const bool grouped = s->group > 1 && pic->mem == RC_MEM_HOST;
+    std::vector<int> refs;
+    if (grouped) {
+        refs = h264_ref_slots(pic);
+        bool clash = false;
+        for (size_t i = 0; i < s->pending.size(); i++) {
+            const auto &r = s->pending_refs[i];
+            clash = clash || s->pending[i].out_slot == out_slot || std::find(r.begin(), r.end(), out_slot) != r.end();
+        }
+        if (clash && (rc = h264_flush(s)) != 0) return rc;
+    } else if ((rc = h264_flush(s)) != 0) {
+        return rc;
+    }
     // level-scale tables (per PPS), uploaded only when they change.  The copy
     // goes on the stream itself: the stream does not order with the legacy
     // default stream, and a pageable cudaMemcpy may return before its DMA has
     // landed.  Its source, ls_host, lives until the next change, which first
-    // waits for the stream.
+    // launches the pending group and waits for the stream.
     {
         // compare the scaling lists (480 bytes), not the tables made from them
         uint8_t key[sizeof s->ls_key] = {0};
@@ -709,6 +823,7 @@ int rc_h264_submit(rc_stream *s, const rc_h264_picture *pic, int out_slot) {
         if (!s->ls_valid || memcmp(key, s->ls_key, sizeof key) != 0) {
             std::vector<int32_t> ls(2304 + 2304 * 4);
             h264_level_scale(pic->scaling4, pic->scaling8, ls.data(), ls.data() + 2304);
+            if ((rc = h264_flush(s)) != 0) return rc;
             if (cudaStreamSynchronize(s->st) != cudaSuccess) return cuda_fail(s);
             memcpy(s->ls_key, key, sizeof key);
             s->ls_host.swap(ls);
@@ -722,12 +837,12 @@ int rc_h264_submit(rc_stream *s, const rc_h264_picture *pic, int out_slot) {
     }
     H264Launch L;
     memset(&L, 0, sizeof L);
+    // record set: none of the pending pictures uses it (at most group - 1
+    // pend while 2 x group sets rotate)
+    const int k = s->submits % s->nsets;
     if (pic->mem == RC_MEM_HOST) {
-        Geo g{s->mb_w, s->mb_h, s->slots};
-        if ((rc = validate_h264(&g, pic)) != 0) return rc;
         const size_t b_mbs = sizeof(rc_h264_mb) * n, b_sl = sizeof(rc_h264_slice) * pic->num_slices;
         const size_t b_w = sizeof(rc_h264_weight) * pic->num_weights, b_lv = sizeof(int16_t) * pic->num_levels;
-        const int k = s->submits & 1;
         Part parts[4] = {{&s->mbs[k], pic->mbs, b_mbs}, {&s->slices[k], pic->slices, b_sl},
                          {&s->weights[k], pic->weights, b_w}, {&s->levels[k], pic->levels, b_lv}};
         if ((rc = set_begin(s, k)) != 0 || (rc = upload(s, parts, 4, s->cst)) != 0 || (rc = set_end(s, k)) != 0)
@@ -737,7 +852,6 @@ int rc_h264_submit(rc_stream *s, const rc_h264_picture *pic, int out_slot) {
         L.weights = (const rc_h264_weight *)s->weights[k].p;
         L.levels = (const int16_t *)s->levels[k].p;
     } else {
-        if (!pic->mbs || !pic->slices || pic->num_slices <= 0) return RC_EINVAL;
         L.mbs = pic->mbs;
         L.slices = pic->slices;
         L.weights = pic->weights;
@@ -767,18 +881,45 @@ int rc_h264_submit(rc_stream *s, const rc_h264_picture *pic, int out_slot) {
     L.error = s->error;
     L.wait_limit = s->wait_limit;
     L.db = nullptr;
+    if ((rc = slot_begin(s, out_slot)) != 0) return rc;
+    if (grouped) {
+        // group position j: its scratch, and the rows of the pending
+        // pictures it references to wait for
+        const int j = (int)s->pending.size();
+        const size_t mbs = (size_t)n;
+        L.rowprog = s->g_rowprog + (size_t)j * s->mb_h;
+        L.irowprog = s->g_irowprog + (size_t)j * s->mb_h;
+        L.mbdone = s->g_mbdone + (size_t)j * mbs;
+        L.edges = s->g_edges + (size_t)j * mbs * RC_EDGE_WORDS;
+        L.iinfo = s->g_iinfo + (size_t)j * mbs;
+        L.ires = s->g_ires + (size_t)j * mbs * 384;
+        for (int i = 0; i < j; i++) {
+            const H264Launch &q = s->pending[i];
+            if (std::find(refs.begin(), refs.end(), q.out_slot) == refs.end()) continue;
+            L.wait_slot[L.nwait] = q.out_slot;
+            L.wait_epoch[L.nwait] = q.epoch;
+            L.wait_rowprog[L.nwait] = q.rowprog;
+            L.nwait++;
+        }
+        s->pending.push_back(L);
+        s->pending_refs.push_back(std::move(refs));
+        s->pending_sets.push_back(k);
+        s->submits++;
+        if ((int)s->pending.size() >= s->group && (rc = h264_flush(s)) != 0) return rc;
+        if (cudaGetLastError() != cudaSuccess) return cuda_fail(s);
+        return RC_OK;
+    }
     const int ek = s->submits & 1;
     L.edges = s->edges[ek];
     L.rowprog = s->rowprog;
     L.irowprog = s->irowprog;
     L.iinfo = s->iinfo;
     L.ires = s->ires;
-    if ((rc = slot_begin(s, out_slot)) != 0) return rc;
     // the edge kernel: after the picture's records (host records: their
     // upload) and after the band kernel that last read this set of edge words
     {
         bool ok = true;
-        if (pic->mem == RC_MEM_HOST) ok = cudaStreamWaitEvent(s->est, s->set_ready[s->submits & 1], 0) == cudaSuccess;
+        if (pic->mem == RC_MEM_HOST) ok = cudaStreamWaitEvent(s->est, s->set_ready[k], 0) == cudaSuccess;
         if (s->aux_busy[ek]) ok = ok && cudaStreamWaitEvent(s->est, s->aux_used[ek], 0) == cudaSuccess;
         if (!ok) return cuda_fail(s);
     }
@@ -791,10 +932,26 @@ int rc_h264_submit(rc_stream *s, const rc_h264_picture *pic, int out_slot) {
     if (lrc != 0) return cuda_fail(s);
     if (cudaEventRecord(s->aux_used[ek], s->st) != cudaSuccess) return cuda_fail(s);
     s->aux_busy[ek] = true;
-    if (pic->mem == RC_MEM_HOST && (rc = set_release(s, s->submits & 1)) != 0) return rc;
+    if (pic->mem == RC_MEM_HOST && (rc = set_release(s, k)) != 0) return rc;
     s->submits++;
     if (cudaGetLastError() != cudaSuccess) return cuda_fail(s);
     return RC_OK;
+}
+
+int rc_stream_set_h264_group(rc_stream *s, int pictures) {
+    if (!s || s->codec != RC_CODEC_H264 || pictures < 0 || pictures > RC_H264_GROUP_MAX) return RC_EINVAL;
+    int rc;
+    if ((rc = h264_flush(s)) != 0) return rc;
+    if (pictures == 0) pictures = RC_H264_GROUP_DEFAULT;
+    // the band CTAs of a group take at most two thirds of the launch's CTAs
+    const int bands = (s->mb_h + RC_H264_BAND_ROWS - 1) / RC_H264_BAND_ROWS;
+    const int cap = pictures > 1 ? rc_h264_group_capacity(s->mb_w) : 0;
+    while (pictures > 1 && pictures * bands * 3 > cap * 2) pictures--;
+    if (pictures > 1 && (rc = group_alloc(s, pictures)) != 0) return rc;
+    s->group = pictures;
+    s->group_ctas = pictures > 1 ? cap : 0;
+    s->nsets = pictures > 1 ? 2 * pictures : 2;
+    return pictures;
 }
 
 int rc_hevc_validate(int width, int height, int bit_depth, int dpb_slots, const rc_hevc_picture *pic) {
@@ -921,6 +1078,7 @@ int rc_hevc_submit(rc_stream *s, const rc_hevc_picture *pic, int out_slot) {
 
 int rc_stream_sync(rc_stream *s) {
     if (!s) return RC_EINVAL;
+    h264_flush(s);
     if (cudaStreamSynchronize(s->st) != cudaSuccess || cudaStreamSynchronize(s->cst) != cudaSuccess ||
         cudaStreamSynchronize(s->dst) != cudaSuccess || (s->est && cudaStreamSynchronize(s->est) != cudaSuccess))
         return cuda_fail(s);
@@ -953,6 +1111,8 @@ static int download(rc_stream *s, int slot, int x, int y, int w, int h, void *ou
         return RC_EINVAL;
     const int bps = s->bps;
     const uint8_t *base = s->dpb + (size_t)slot * s->slot_bytes;
+    int rc;
+    if ((rc = h264_flush(s)) != 0) return rc;
     // on the download stream, after every kernel submitted so far; later
     // submits that write this slot wait for it
     cudaStream_t c = s->dst;
@@ -995,6 +1155,7 @@ int rc_stream_set_wait_limit(rc_stream *s, unsigned int limit) {
 
 int rc_stream_profile(rc_stream *s, int enable) {
     if (!s) return RC_EINVAL;
+    h264_flush(s);
     if (cudaStreamSynchronize(s->st) != cudaSuccess || (s->est && cudaStreamSynchronize(s->est) != cudaSuccess))
         return cuda_fail(s);
     drain_profile(s);
@@ -1008,6 +1169,7 @@ int rc_stream_profile(rc_stream *s, int enable) {
 
 int rc_stream_profile_read(rc_stream *s, double *ms, long long *launches, int max_kernels) {
     if (!s || max_kernels < 0) return RC_EINVAL;
+    h264_flush(s);
     if (cudaStreamSynchronize(s->st) != cudaSuccess || (s->est && cudaStreamSynchronize(s->est) != cudaSuccess))
         return cuda_fail(s);
     drain_profile(s);
@@ -1023,7 +1185,7 @@ int rc_picture_upload(rc_stream *s, int slot, const void *py, const void *pu, co
     if (!s || slot < 0 || slot >= s->slots || !py || !pu || !pv) return RC_EINVAL;
     const int bps = s->bps;
     uint8_t *base = s->dpb + (size_t)slot * s->slot_bytes;
-    if (slot_begin(s, slot) != 0) return cuda_fail(s);
+    if (h264_flush(s) != 0 || slot_begin(s, slot) != 0) return cuda_fail(s);
     // stream-ordered copies (the stream does not order with the legacy default
     // stream), complete before returning so that the caller may free its planes
     bool ok = cudaMemcpy2DAsync(base, s->pitch, py, (size_t)s->width * bps, (size_t)s->width * bps, s->height,
@@ -1047,6 +1209,8 @@ int rc_stream_geometry(rc_stream *s, int *coded_w, int *coded_h, int *luma_pitch
 
 int rc_picture_device_planes(rc_stream *s, int slot, void **y, void **u, void **v) {
     if (!s || slot < 0 || slot >= s->slots) return RC_EINVAL;
+    int rc;
+    if ((rc = h264_flush(s)) != 0) return rc;
     uint8_t *base = s->dpb + (size_t)slot * s->slot_bytes;
     if (y) *y = base;
     if (u) *u = base + s->u_off;
@@ -1056,12 +1220,18 @@ int rc_picture_device_planes(rc_stream *s, int slot, void **y, void **u, void **
 
 long long rc_stream_launches(rc_stream *s) { return s ? s->launches : 0; }
 
-void *rc_stream_cuda_stream(rc_stream *s) { return s ? (void *)s->st : nullptr; }
+void *rc_stream_cuda_stream(rc_stream *s) {
+    if (!s) return nullptr;
+    h264_flush(s);  // a launch error stays in the sticky word
+    return (void *)s->st;
+}
 
 size_t rc_stream_device_bytes(rc_stream *s) { return s ? s->held : 0; }
 
 int rc_stream_mark(rc_stream *s, unsigned long long *mark) {
     if (!s || !mark) return RC_EINVAL;
+    int rc;
+    if ((rc = h264_flush(s)) != 0) return rc;
     cudaEvent_t e = nullptr;
     if (!s->mark_free.empty()) {
         e = s->mark_free.back();

@@ -48,6 +48,9 @@ static_assert(sizeof(IntraInfo) == 32, "IntraInfo layout");
 //   [48..63] chroma horizontal      48 + c * 8 + k * 2 + e
 #define RC_EDGE_WORDS 64
 
+#define RC_H264_GROUP_MAX 4
+#define RC_H264_GROUP_DEFAULT 3  // rc_stream_set_h264_group(s, 0)
+
 struct H264Launch {
     const rc_h264_mb *mbs;
     const rc_h264_slice *slices;
@@ -72,6 +75,26 @@ struct H264Launch {
     uint32_t *irowprog;   // per MB row: (epoch & 0xffff) << 16 | MBs reconstructed (intra included)
     IntraInfo *iinfo;     // per MB (intra MBs)
     int16_t *ires;        // per MB: 256 luma + 2 x 64 chroma residual samples (intra MBs)
+    // Pictures reconstructed together (H264Group): the MB phase of this
+    // picture publishes each MB's completion as mbdone[addr] = epoch (null:
+    // the MB phase finished before the band kernel started), and waits for
+    // the rows of the in-flight pictures it references: nwait DPB slots with
+    // their pictures' epochs and per-row filter progress (rowprog layout).
+    uint32_t *mbdone;
+    int nwait;
+    int wait_slot[RC_H264_GROUP_MAX];
+    uint32_t wait_epoch[RC_H264_GROUP_MAX];
+    uint32_t *wait_rowprog[RC_H264_GROUP_MAX];
+};
+
+// Up to RC_H264_GROUP_MAX consecutive pictures of one stream reconstructed
+// by one cooperative launch: CTAs [j * bands, (j + 1) * bands) are picture
+// j's band CTAs, the others run the MB phase of all the pictures, taking
+// (picture, MB) work items in order from *counter (zeroed by the launcher).
+struct H264Group {
+    int n, bands;
+    uint32_t *counter;
+    H264Launch pic[RC_H264_GROUP_MAX];
 };
 
 struct HevcLaunch {
@@ -121,6 +144,12 @@ void rc_launch_h264_mb(const H264Launch &p, cudaStream_t st);
 // 2 1340, 1 1033 frames/s).
 #define RC_H264_BAND_ROWS 4
 int rc_launch_h264_band(const H264Launch &p, cudaStream_t st);
+// A group of pictures in one cooperative launch of `ctas` CTAs (more than
+// g.n * g.bands; at most rc_h264_group_capacity); returns 0 or -1.
+int rc_launch_h264_group(const H264Group &g, int ctas, cudaStream_t st);
+// CTAs of the group kernel that can be resident at once for pictures mb_w
+// MBs wide (0 if unknown).
+int rc_h264_group_capacity(int mb_w);
 // Band CTAs that can be resident at once for pictures mb_w MBs wide (0 if
 // unknown); the band kernel's dynamic shared memory for that width.
 int rc_h264_band_capacity(int mb_w);

@@ -107,3 +107,12 @@ def test_stream_create_rejects_bad_arguments(engine):
     assert L.rc_stream_create(engine.RC_CODEC_H264, 0, 64, 8, 2, 0, ctypes.byref(h)) == engine.RC_EINVAL
     assert L.rc_stream_create(99, 64, 64, 8, 2, 0, ctypes.byref(h)) == engine.RC_EINVAL
     assert L.rc_stream_create(engine.RC_CODEC_H264, 64, 64, 8, 0, 0, ctypes.byref(h)) == engine.RC_EINVAL
+
+
+def test_stream_calls_reject_null_streams(engine):
+    """Every stream call checks its handle before touching the GPU."""
+    L = engine.lib()
+    assert L.rc_stream_set_h264_group(None, 2) == engine.RC_EINVAL
+    assert L.rc_stream_set_wait_limit(None, 0) == engine.RC_EINVAL
+    assert L.rc_stream_sync(None) == engine.RC_EINVAL
+    assert L.rc_stream_cuda_stream(None) is None

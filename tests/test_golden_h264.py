@@ -106,3 +106,30 @@ def test_engine_reproduces_reference_digest(engine, name):
             return cropped(st.download(m["slot"]), m["crop"])
 
         assert output_digest([m for m, _ in pics], planes_after) == EXPECTED[name]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("group", [2, 4])
+@pytest.mark.parametrize("name", sorted(EXPECTED))
+def test_engine_grouped_reproduces_reference_digest(engine, name, group):
+    """The same streams with several pictures per launch
+    (rc_stream_set_h264_group): pictures are submitted in runs of distinct
+    DPB slots without waiting, and read back after each run."""
+    meta, pics = load_fixture(engine, name)
+    metas = [m for m, _ in pics]
+    m0 = metas[0]
+    W, H = m0["mb_w"] * 16, m0["mb_h"] * 16
+    planes = {}
+    with engine.ReconStream(engine.RC_CODEC_H264, W, H, 8, DPB_SLOTS) as st:
+        assert st.set_h264_group(group) == group
+        i = 0
+        while i < len(pics):
+            run = []
+            while i < len(pics) and metas[i]["slot"] not in [metas[j]["slot"] for j in run]:
+                st.submit_h264(pics[i][1], metas[i]["slot"])
+                run.append(i)
+                i += 1
+            for j in run:
+                planes[j] = cropped(st.download(metas[j]["slot"]), metas[j]["crop"])
+        assert st.sync() == 0
+    assert output_digest(metas, lambda j: planes[j]) == EXPECTED[name]
