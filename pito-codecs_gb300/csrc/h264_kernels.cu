@@ -93,6 +93,16 @@ __device__ __forceinline__ uint32_t ld_acquire(const uint32_t *p) {
     asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
     return v;
 }
+// Polls read with relaxed loads and order what follows with one acquire
+// fence once the value is seen: an acquire load invalidates the SM's L1 on
+// every poll, and warps that poll while their neighbours read cached
+// reference samples would keep emptying it.
+__device__ __forceinline__ uint32_t ld_relaxed(const uint32_t *p) {
+    uint32_t v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void fence_acquire() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
 __device__ __forceinline__ void st_release(uint32_t *p, uint32_t v) {
     asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
@@ -169,47 +179,57 @@ struct Ref {
     int pitch, w, h;
 };
 // window sample with edge extension by coordinate clamp (copy_clamped,
-// src/h264/dec/picture.rs:723-735)
+// src/h264/dec/picture.rs:723-735).  CA: a coherent load (ld.global.ca), for
+// references written during the same launch (a group launch); otherwise the
+// read-only path.
+template <bool CA = false>
 __device__ __forceinline__ int rs(const Ref &r, int x, int y) {
-    return __ldg(r.p + clampi(y, 0, r.h - 1) * r.pitch + clampi(x, 0, r.w - 1));
+    const uint8_t *q = r.p + clampi(y, 0, r.h - 1) * r.pitch + clampi(x, 0, r.w - 1);
+    return CA ? __ldca(q) : __ldg(q);
 }
 __device__ __forceinline__ int tap6(int a, int b, int c, int d, int e, int f) { return a - 5 * b + 20 * c + 20 * d - 5 * e + f; }
 __device__ __forceinline__ int avg2(int a, int b) { return (a + b + 1) >> 1; }
+template <bool CA = false>
 __device__ __forceinline__ int htap(const Ref &r, int x, int y) {
-    return tap6(rs(r, x - 2, y), rs(r, x - 1, y), rs(r, x, y), rs(r, x + 1, y), rs(r, x + 2, y), rs(r, x + 3, y));
+    return tap6(rs<CA>(r, x - 2, y), rs<CA>(r, x - 1, y), rs<CA>(r, x, y), rs<CA>(r, x + 1, y), rs<CA>(r, x + 2, y),
+                rs<CA>(r, x + 3, y));
 }
+template <bool CA = false>
 __device__ __forceinline__ int vtap(const Ref &r, int x, int y) {
-    return tap6(rs(r, x, y - 2), rs(r, x, y - 1), rs(r, x, y), rs(r, x, y + 1), rs(r, x, y + 2), rs(r, x, y + 3));
+    return tap6(rs<CA>(r, x, y - 2), rs<CA>(r, x, y - 1), rs<CA>(r, x, y), rs<CA>(r, x, y + 1), rs<CA>(r, x, y + 2),
+                rs<CA>(r, x, y + 3));
 }
 // mc_luma_win_scalar, inter.rs:73-213, for the sample at integer position (x, y)
+template <bool CA = false>
 __device__ int luma_sample(const Ref &r, int x, int y, int fx, int fy) {
-    if (fx == 0 && fy == 0) return rs(r, x, y);
+    if (fx == 0 && fy == 0) return rs<CA>(r, x, y);
     if (fy == 0) {
-        int b = clip255((htap(r, x, y) + 16) >> 5);
-        return fx == 1 ? avg2(rs(r, x, y), b) : fx == 2 ? b : avg2(rs(r, x + 1, y), b);
+        int b = clip255((htap<CA>(r, x, y) + 16) >> 5);
+        return fx == 1 ? avg2(rs<CA>(r, x, y), b) : fx == 2 ? b : avg2(rs<CA>(r, x + 1, y), b);
     }
     if (fx == 0) {
-        int h = clip255((vtap(r, x, y) + 16) >> 5);
-        return fy == 2 ? h : avg2(fy == 1 ? rs(r, x, y) : rs(r, x, y + 1), h);
+        int h = clip255((vtap<CA>(r, x, y) + 16) >> 5);
+        return fy == 2 ? h : avg2(fy == 1 ? rs<CA>(r, x, y) : rs<CA>(r, x, y + 1), h);
     }
     if (fx == 2 || fy == 2) {
         int b1[6];
 #pragma unroll
-        for (int j = 0; j < 6; j++) b1[j] = htap(r, x, y + j - 2);
+        for (int j = 0; j < 6; j++) b1[j] = htap<CA>(r, x, y + j - 2);
         int j = clip255((tap6(b1[0], b1[1], b1[2], b1[3], b1[4], b1[5]) + 512) >> 10);
         if (fx == 2 && fy == 2) return j;
         if (fx == 2) return avg2(clip255(((fy == 1 ? b1[2] : b1[3]) + 16) >> 5), j);
-        return avg2(clip255((vtap(r, x + (fx == 1 ? 0 : 1), y) + 16) >> 5), j);
+        return avg2(clip255((vtap<CA>(r, x + (fx == 1 ? 0 : 1), y) + 16) >> 5), j);
     }
-    int t = htap(r, x, y + (fy == 1 ? 0 : 1));
-    int v = vtap(r, x + (fx == 1 ? 0 : 1), y);
+    int t = htap<CA>(r, x, y + (fy == 1 ? 0 : 1));
+    int v = vtap<CA>(r, x + (fx == 1 ? 0 : 1), y);
     return avg2(clip255((t + 16) >> 5), clip255((v + 16) >> 5));
 }
 // mc_chroma_win_scalar, inter.rs:217-247, one sample at integer position (x, y)
+template <bool CA = false>
 __device__ __forceinline__ int chroma_sample(const Ref &r, int x, int y, int fx, int fy) {
-    if ((fx | fy) == 0) return rs(r, x, y);
-    int v = (8 - fx) * (8 - fy) * rs(r, x, y) + fx * (8 - fy) * rs(r, x + 1, y) + (8 - fx) * fy * rs(r, x, y + 1) +
-            fx * fy * rs(r, x + 1, y + 1);
+    if ((fx | fy) == 0) return rs<CA>(r, x, y);
+    int v = (8 - fx) * (8 - fy) * rs<CA>(r, x, y) + fx * (8 - fy) * rs<CA>(r, x + 1, y) + (8 - fx) * fy * rs<CA>(r, x, y + 1) +
+            fx * fy * rs<CA>(r, x + 1, y + 1);
     return (v + 32) >> 6;
 }
 // weighted_store_scalar, inter.rs:286-352, one sample of one resolved
@@ -288,13 +308,18 @@ __device__ bool mb_wait_refs(const H264Launch &P, const rc_h264_mb &m, const rc_
         const int cc = __reduce_max_sync(0xffffffffu, slot == P.wait_slot[i] ? c : -1);
         if (rr < 0) continue;
         if (t == 0) {
-            const uint32_t *f = P.wait_rowprog[i] + min(rr + 1, P.mb_h - 1);
+            const uint32_t *f = P.wait_refprog[i] + (size_t)min(rr + 1, P.mb_h - 1) * RC_REFPROG_STRIDE;
             const uint32_t tag = (P.wait_epoch[i] & 0xffffu) << 16, need = (uint32_t)min(cc + 2, P.mb_w);
-            uint32_t it = 0, v;
-            while (((v = ld_acquire(f)) & 0xffff0000u) != tag || (v & 0xffffu) < need) {
+            // back off to 4 us between polls: many warps wait here at once,
+            // and their polls would load the L2 that the band CTAs' hand-overs
+            // go through
+            uint32_t it = 0, v, ns = 64;
+            while (((v = ld_relaxed(f)) & 0xffff0000u) != tag || (v & 0xffffu) < need) {
                 if (++it > P.wait_limit || ((it & 63) == 0 && aborted(P.error))) { ok = false; break; }
-                if (it > 64) __nanosleep(128);
+                __nanosleep(ns);
+                ns = min(ns * 2, 4096u);
             }
+            fence_acquire();
         }
     }
     return __shfl_sync(0xffffffffu, ok, 0);
@@ -308,9 +333,6 @@ struct __align__(16) MbSmem {
     uint8_t predy[256];
     uint8_t predc[128];
     uint32_t nzl, nzc, ibits;  // ibits, intra: neighbour availability (bits 0..3: left, top, top-right, top-left)
-    int refs_ok, item;
-    rc_h264_mb nbr[2];  // group kernel: the MB's left and top neighbours, and its filter parameters
-    DbMb dbm;
 };
 
 // Barrier `id` over the `n` threads of one MB worker (id 0 with n = the
@@ -344,11 +366,19 @@ __device__ void mb_body(const H264Launch &P, MbSmem &M, const int addr, const in
             int c = t >> 6, x = t & 7, y = (t >> 3) & 7;
             (c ? V : U)[(size_t)(mby * 8 + y) * P.cpitch + mbx * 8 + x] = (uint8_t)s[256 + t];
         }
+        if (P.bottom) {  // before a group launch: the unfiltered bottom rows
+            uint8_t *b = P.bottom + (size_t)mby * P.mb_w * 32;
+            if (t < 16) b[mbx * 16 + t] = (uint8_t)s[240 + t];
+            else if (t < 32) b[P.mb_w * (16 + 8 * ((t - 16) >> 3)) + mbx * 8 + (t & 7)] = (uint8_t)s[256 + ((t - 16) >> 3) * 64 + 56 + (t & 7)];
+        }
         return;
     }
     if (m.slice >= P.num_slices) { if (t == 0) set_error(P.error, RC_DEV_ERR_RECORD); return; }
     const rc_h264_slice *sl = P.slices + m.slice;
     const bool intra = kind != RC_H264_INTER;
+    // residual-only pass (before a group launch): inter MBs store their
+    // residual like intra MBs; the group kernel predicts and adds it
+    const bool resid = intra || P.residual_only;
     const int t8 = m.transform_8x8, i16 = kind == RC_H264_I16x16;
     const int nl = __popc(m.luma_coded & (t8 ? 0xf : 0xffff)), ndc = __popc(m.dc_coded & 6);
     const int nlum = (i16 && (m.dc_coded & 1)) ? 16 : 0;
@@ -370,16 +400,7 @@ __device__ void mb_body(const H264Launch &P, MbSmem &M, const int addr, const in
             }
         }
     }
-    if (!intra && P.mbdone && P.nwait > 0) {
-        const bool ok = mb_wait_refs(P, m, sl, mbx, mby, t);
-        if (t == 0) M.refs_ok = ok;
-        bar_sync(bar, 256);
-        if (!M.refs_ok) {
-            if (t == 0) set_error(P.error, RC_DEV_ERR_TIMEOUT);
-            return;
-        }
-    }
-    if (!intra) {
+    if (!resid) {
     // ---- prediction (mc_rect, slicedec.rs:996-1087), one luma sample per thread
     {
         const int x = t & 15, y = t >> 4, k = (y >> 2) * 4 + (x >> 2), b8 = (y >> 3) * 2 + (x >> 3);
@@ -492,9 +513,9 @@ __device__ void mb_body(const H264Launch &P, MbSmem &M, const int addr, const in
     } else if (t < 64 && (nzl >> (t >> 2) & 1)) idct4_1d(coef + (t >> 2) * 16 + (t & 3), 4);
     if (t >= 64 && t < 96 && (nzc >> ((t - 64) >> 2) & 1)) idct4_1d(coefc + ((t - 64) >> 2) * 16 + (t & 3), 4);
     bar_sync(bar, 256);
-    if (intra) {
-        // residual samples ((v + 32) >> 6, idct4_add / idct8_add) and the
-        // prediction parameters for the intra wavefront
+    if (resid) {
+        // residual samples ((v + 32) >> 6, idct4_add / idct8_add) and, for
+        // intra MBs, the prediction parameters for the intra wavefront
         int16_t *res = P.ires + (size_t)addr * 384;
         {
             const int x = t & 15, y = t >> 4;
@@ -513,7 +534,7 @@ __device__ void mb_body(const H264Launch &P, MbSmem &M, const int addr, const in
             int r = (nzc >> blk & 1) ? (coefc[blk * 16 + (y & 3) * 4 + (x & 3)] + 32) >> 6 : 0;
             res[256 + t] = (int16_t)max(-32768, min(32767, r));
         }
-        if (t == 0) {
+        if (intra && t == 0) {
             IntraInfo in;
             in.kind = (uint8_t)kind;
             in.t8 = (uint8_t)t8;
@@ -1440,28 +1461,16 @@ __device__ __forceinline__ void cp_wait_all_but_4() { asm volatile("cp.async.wai
 // unchanged until this warp reports the MB after them reconstructed (the
 // filter warps wait for that), so they may be read early.
 //
-// In a group launch (P.mbdone set) the MB phase runs beside the band CTAs:
-// MB x of the row is ready once mbdone[x] holds the picture's epoch.  The
-// warp then fills its line as the row's MBs become ready (inter MBs copied
-// from the picture, intra ones written as it reconstructs them) and reports
-// an MB only once it and every MB before it are ready and in the line, so
-// that the filter warps and the rows below wait on inter MBs through the
-// same progress word.
-__device__ bool wait_flag(const uint32_t *f, uint32_t want, const H264Launch &P, int lane) {
-    bool ok = true;
-    if (lane == 0) {
-        uint32_t it = 0;
-        while (ld_acquire(f) != want) {
-            if (++it > P.wait_limit || ((it & 63) == 0 && aborted(P.error))) { ok = false; break; }
-            if (it > 16) __nanosleep(64);
-        }
-    }
-    ok = __shfl_sync(0xffffffffu, ok, 0);
-    __syncwarp();
-    return ok;
-}
-
-__device__ void band_intra_row(const H264Launch &P, BandSmem &B, uint8_t *lines, uint8_t *stg, int w, int my,
+// In a group launch (P.mbdone set) inter MBs are predicted beside the band
+// CTAs: inter MB x of the row is ready once mbdone[x] holds the picture's
+// epoch (the other kinds are ready when the launch starts).  The warp
+// reports an MB only once it and every inter MB before it are ready, so
+// that the filter warps wait on inter MBs through the same progress word.
+// The row below reads the unfiltered bottom rows of MBs that are not intra
+// from P.bottom (written with the MB: by the pre-pass for I_PCM, by the
+// group kernel for inter MBs, once per MB), after their mbdone: its intra
+// MBs keep waiting on this row only where an intra neighbour is.
+__device__ __forceinline__ void band_intra_row(const H264Launch &P, BandSmem &B, uint8_t *lines, uint8_t *stg, int w, int my,
                                int lane) {
     WarpSmem &S = B.iw[w];
     const bool grouped = P.mbdone != nullptr;
@@ -1476,7 +1485,7 @@ __device__ void band_intra_row(const H264Launch &P, BandSmem &B, uint8_t *lines,
     // holds the bits of MBs 32 j .. 32 j + 31 (rows of up to 1024 MBs, see
     // rc_h264_band_capacity)
     const int nwords = (P.mb_w + 31) >> 5;
-    uint32_t word = 0, aword = 0;
+    uint32_t word = 0, aword = 0, iword = 0, aiword = 0;  // iword / aiword: the inter MBs of this row / the row above
     for (int j0 = 0; j0 < nwords; j0 += 4) {
         int kinds[4], akinds[4];
 #pragma unroll
@@ -1489,9 +1498,13 @@ __device__ void band_intra_row(const H264Launch &P, BandSmem &B, uint8_t *lines,
         for (int u = 0; u < 4; u++) {
             const uint32_t b = __ballot_sync(0xffffffffu, wave_intra(kinds[u]));
             const uint32_t a = __ballot_sync(0xffffffffu, wave_intra(akinds[u]));
+            const uint32_t e = __ballot_sync(0xffffffffu, kinds[u] == RC_H264_INTER);
+            const uint32_t ae = __ballot_sync(0xffffffffu, akinds[u] == RC_H264_INTER);
             if (lane == j0 + u) {
                 word = b;
                 aword = a;
+                iword = e;
+                aiword = ae;
             }
         }
     }
@@ -1504,8 +1517,9 @@ __device__ void band_intra_row(const H264Launch &P, BandSmem &B, uint8_t *lines,
     // are final from the start: in the line copy, which the row above fills
     // before its first report, or in the picture for a band's first row)
     auto above_need = [&](int x) -> int {
-        if (grouped) return min(x + 2, P.mb_w);  // the row above reports inter MBs too
-        const int base = w > 0 ? 1 : 0;
+        // (a group launch has no initial line copy: the row above's inter
+        // MBs come from P.bottom once predicted, see above_inter_ready)
+        const int base = w > 0 && !grouped ? 1 : 0;
         if (above_intra(x + 1)) return min(x + 2, P.mb_w);
         if (above_intra(x)) return x + 1;
         if (above_intra(x - 1)) return max(x, base);
@@ -1519,46 +1533,61 @@ __device__ void band_intra_row(const H264Launch &P, BandSmem &B, uint8_t *lines,
         }
         return P.mb_w;
     };
-    auto is_intra = [&](int x) -> bool {  // MB (x, my) is reconstructed here; any lane's x
-        return (__shfl_sync(0xffffffffu, word, (x >> 5) & 31) >> (x & 31)) & 1;
+    auto is_inter = [&](int x) -> bool {  // MB (x, my) is predicted in the launch; any lane's x
+        return (__shfl_sync(0xffffffffu, iword, (x >> 5) & 31) >> (x & 31)) & 1;
     };
-    // grouped: the line holds MBs 0..filled-1; fill it up to v, waiting for
-    // the MB phase four MBs at a time (lane 8 i + j: MB filled + i, word j)
-    int filled = 0;
-    auto advance = [&](int v) -> bool {
-        while (filled < v) {
-            const int i = lane >> 3, j = lane & 7, x = filled + i;
-            const bool intra_x = is_intra(min(x, P.mb_w - 1));  // every lane takes part in the shuffle
-            const bool cp = x < v && !intra_x;
-            bool ok = true;
-            if (cp && j == 0) {
-                uint32_t it = 0;
-                while (ld_acquire(done + x) != P.epoch) {
-                    if (++it > P.wait_limit || ((it & 63) == 0 && aborted(P.error))) { ok = false; break; }
-                    if (it > 16) __nanosleep(64);
-                }
+    // grouped: the inter MBs of this row before `filled`, and of the row
+    // above before `afilled`, are predicted.  ready(...) makes the prefix
+    // reach `need`: a round looks at the next 32 MBs at once (a lane each),
+    // so that the prefix usually runs ahead of what is asked and later calls
+    // cost nothing; while nothing moves, only the first missing flag is
+    // polled, backing off to 1 us (the band CTAs of later pictures of a
+    // group wait here, and their polls would slow the L2 round trips of the
+    // wavefront that runs)
+    int filled = 0, afilled = 0;
+    auto ready = [&](int &pre, const uint32_t *flags, uint32_t bits_word, int need) -> bool {
+        if (pre >= need) return true;
+        uint32_t it = 0, ns = 32;
+        bool all = true;  // probe 32 flags (else only the first missing one)
+        while (pre < need) {
+            const int x = pre + lane;
+            const int xc = min(x, P.mb_w - 1);
+            const bool inter_x = (__shfl_sync(0xffffffffu, bits_word, (xc >> 5) & 31) >> (xc & 31)) & 1;
+            // lanes that do not look count as not ready, so the prefix stops at them
+            bool rdy = false;
+            if (all || lane == 0) rdy = !(x < P.mb_w && inter_x) || ld_relaxed(flags + x) == P.epoch;
+            const uint32_t m = __ballot_sync(0xffffffffu, rdy);
+            const int adv = m == 0xffffffffu ? 32 : __ffs(~m) - 1;
+            pre = min(pre + adv, P.mb_w);
+            if (pre >= need) break;
+            if (adv > 0) {
+                all = true;
+                it = 0;
+                ns = 32;
+                continue;
             }
-            if (!__all_sync(0xffffffffu, ok)) return false;
-            __syncwarp();
-            if (cp) {
-                const uint8_t *src = j < 4 ? Y + (size_t)(my * 16 + 15) * P.pitch + x * 16 + j * 4
-                                           : (j < 6 ? U : V) + (size_t)(my * 8 + 7) * P.cpitch + x * 8 + (j & 1) * 4;
-                uint8_t *dst = j < 4 ? ly + x * 16 + j * 4 : (j < 6 ? lu : lv) + x * 8 + (j & 1) * 4;
-                *(uint32_t *)dst = __ldcg((const uint32_t *)src);
-            }
-            filled = min(filled + 4, v);
+            bool give_up = false;
+            if (lane == 0) give_up = ++it > P.wait_limit || ((it & 63) == 0 && aborted(P.error));
+            if (__shfl_sync(0xffffffffu, give_up, 0)) return false;
+            all = false;
+            __nanosleep(ns);
+            ns = min(ns * 2, 1024u);
         }
+        fence_acquire();  // the flags seen order the MBs' samples after them
         __syncwarp();
-        __threadfence_block();
         return true;
     };
+    auto advance = [&](int v) -> bool { return ready(filled, done, iword, v); };
+    // the inter MBs among mx-1..mx+1 of the row above (their unfiltered
+    // bottom rows are then in P.bottom)
+    auto above_inter_ready = [&](int x) -> bool {
+        return ready(afilled, P.mbdone + (size_t)(my - 1) * P.mb_w, aiword, min(x + 2, P.mb_w));
+    };
     auto prefetch = [&](int nx) -> bool {
-        // grouped: the MB's parameters and residual, and its left neighbour
-        // when that is an inter MB, come from the MB phase
-        if (grouped && nx < P.mb_w) {
-            if (!wait_flag(done + nx, P.epoch, P, lane)) return false;
-            if (nx > 0 && !is_intra(nx - 1) && !wait_flag(done + nx - 1, P.epoch, P, lane)) return false;
-        }
+        // grouped: the left neighbour, when it is an inter MB, is predicted
+        // in the launch (the MB's own parameters and residual, and every
+        // other kind of MB, come from the pre-pass)
+        if (grouped && nx < P.mb_w && nx > 0 && is_inter(nx - 1) && !ready(filled, done, iword, nx)) return false;
         if (nx < P.mb_w) {
             const int addr = my * P.mb_w + nx;
             const uint8_t *q = (const uint8_t *)(P.iinfo + addr), *res = (const uint8_t *)(P.ires + (size_t)addr * 384);
@@ -1633,17 +1662,31 @@ __device__ void band_intra_row(const H264Launch &P, BandSmem &B, uint8_t *lines,
             band_fail(P, lane);
             return;
         }
-        // canvas row -1: the row above's bottom samples, columns -1..30 (chroma -1..8)
+        // canvas row -1: the row above's bottom samples, columns -1..30 (chroma
+        // -1..8): the line (or, for a band's first row, the picture), and in a
+        // group launch the bottom-row buffer for MBs that are not intra
+        if (my > 0 && grouped && !above_inter_ready(mx)) {
+            cp_wait_all();
+            band_fail(P, lane);
+            return;
+        }
         if (my > 0) {
             const int gx = mx * 16 + lane - 1;
+            const int c = lane / 10, gxc = mx * 8 + lane % 10 - 1;
+            const bool ya = above_intra(max(gx, 0) >> 4), ca = above_intra(max(gxc, 0) >> 3);  // all lanes shuffle
+            const uint8_t *brow = grouped ? P.bottom + (size_t)(my - 1) * LW : nullptr;
             uint8_t v = 0;
-            if (gx >= 0 && gx < P.W) v = w > 0 ? ay[gx] : __ldcg(Y + (size_t)(my * 16 - 1) * P.pitch + gx);
+            if (gx >= 0 && gx < P.W)
+                v = grouped && !ya ? __ldcg(brow + gx)
+                    : w > 0       ? ay[gx]
+                                  : __ldcg(Y + (size_t)(my * 16 - 1) * P.pitch + gx);
             S.cy[lane] = v;
             if (lane < 20) {
-                const int c = lane / 10, gxc = mx * 8 + lane % 10 - 1;
                 uint8_t u = 0;
                 if (gxc >= 0 && gxc < P.CW)
-                    u = w > 0 ? (c ? av : au)[gxc] : __ldcg((c ? V : U) + (size_t)(my * 8 - 1) * P.cpitch + gxc);
+                    u = grouped && !ca ? __ldcg(brow + P.mb_w * (16 + 8 * c) + gxc)
+                        : w > 0       ? (c ? av : au)[gxc]
+                                      : __ldcg((c ? V : U) + (size_t)(my * 8 - 1) * P.cpitch + gxc);
                 S.cc[c][lane % 10] = u;
             }
         }
@@ -1689,7 +1732,7 @@ __device__ void band_intra_row(const H264Launch &P, BandSmem &B, uint8_t *lines,
 
 // Luma loop-filter warp of band row w (picture row my); lanes 0..15 hold one
 // sample row (vertical edges) or one column (horizontal edges) of the MB.
-__device__ void band_luma_row(const H264Launch &P, BandSmem &B, int w, int my, int rows, int lane) {
+__device__ __forceinline__ void band_luma_row(const H264Launch &P, BandSmem &B, int w, int my, int rows, int lane) {
     LumaRow &R = B.l[w];
     uint8_t *Y = P.dpb + (size_t)P.out_slot * P.slot_bytes;
     const bool act = lane < 16;
@@ -1857,7 +1900,7 @@ __device__ void band_luma_row(const H264Launch &P, BandSmem &B, int w, int my, i
 
 // Chroma loop-filter warp of band row w: lanes 0..7 Cb, 8..15 Cr, each one
 // sample row (vertical edges) or column (horizontal edges) of the MB.
-__device__ void band_chroma_row(const H264Launch &P, BandSmem &B, int w, int my, int rows, int lane) {
+__device__ __forceinline__ void band_chroma_row(const H264Launch &P, BandSmem &B, int w, int my, int rows, int lane) {
     ChromaRow &R = B.c[w];
     uint8_t *Y = P.dpb + (size_t)P.out_slot * P.slot_bytes;
     const bool act = lane < 16;
@@ -1992,7 +2035,7 @@ __device__ void band_chroma_row(const H264Launch &P, BandSmem &B, int w, int my,
 // Mirror warp: lane 0 copies the row above's filter progress, lane 1 its
 // intra progress, lane 2 the row below's intra progress (global, acquire)
 // into shared memory.
-__device__ void band_mirror(const H264Launch &P, BandSmem &B, int y0, int rows, int lane) {
+__device__ __forceinline__ void band_mirror(const H264Launch &P, BandSmem &B, int y0, int rows, int lane) {
     const uint32_t tag = (P.epoch & 0xffffu) << 16;
     const bool above = y0 > 0, below = y0 + rows < P.mb_h;
     const uint32_t *src = lane == 0 ? (above ? P.rowprog + y0 - 1 : nullptr)
@@ -2003,13 +2046,15 @@ __device__ void band_mirror(const H264Launch &P, BandSmem &B, int y0, int rows, 
     if (lane == 1 && !above) B.iprog[0] = P.mb_w;
     if (lane == 2 && !below) B.iprog[rows + 1] = P.mb_w;
     int seen = src ? 0 : P.mb_w;
-    uint32_t it = 0;
+    uint32_t it = 0, ns = 32;
     while (!__all_sync(0xffffffffu, seen >= P.mb_w)) {
+        bool moved = false;
         if (src && seen < P.mb_w) {
             const uint32_t v = ld_acquire(src);
             const int n = (v & 0xffff0000u) == tag ? (int)(v & 0xffffu) : 0;
             if (n > seen) {
                 seen = n;
+                moved = true;
                 __threadfence_block();
                 if (lane == 0) { B.lprog[0] = seen; B.cprog[0] = seen; }
                 else if (lane == 1) B.iprog[0] = seen;
@@ -2020,7 +2065,10 @@ __device__ void band_mirror(const H264Launch &P, BandSmem &B, int y0, int rows, 
                 seen = P.mb_w;  // give up; the waiting warps see the error
             }
         }
-        __nanosleep(32);
+        // back off (to 512 ns) while nothing moves: in a group launch the
+        // bands of later pictures wait here a long time
+        ns = __any_sync(0xffffffffu, moved) ? 32 : min(ns * 2, 512u);
+        __nanosleep(ns);
     }
 }
 
@@ -2030,19 +2078,21 @@ __device__ void band_mirror(const H264Launch &P, BandSmem &B, int y0, int rows, 
 // store the band's warps made before the progress the lanes read (they
 // fenced before publishing it in shared memory) ahead of the flags, which
 // can then be relaxed stores (a release store costs about a fence more).
-__device__ void band_publish(const H264Launch &P, BandSmem &B, int y0, int rows, int lane) {
+__device__ __forceinline__ void band_publish(const H264Launch &P, BandSmem &B, int y0, int rows, int lane) {
     const uint32_t tag = (P.epoch & 0xffffu) << 16;
     const bool above = y0 > 0, below = y0 + rows < P.mb_h;
-    // in a group launch, lane 0 also publishes the picture's last row and
-    // lanes 3.. the band's other rows, for the MB phase of later pictures of
-    // the group that read this one
+    // in a group launch, lanes 3.. also publish every row's filter progress
+    // for the MB work of later pictures of the group that read this one, in
+    // refprog: a word per 128-byte line, apart from the hand-over words, so
+    // that the polls of the many waiting MB warps do not queue on the lines
+    // that the bands hand over through
     const bool grouped = P.mbdone != nullptr;
     const int prow = lane - 3;
-    uint32_t *dst = lane == 0 ? (below || grouped ? P.rowprog + y0 + rows - 1 : nullptr)
+    uint32_t *dst = lane == 0 ? (below ? P.rowprog + y0 + rows - 1 : nullptr)
                     : lane == 1 ? (below ? P.irowprog + y0 + rows - 1 : nullptr)
                     : lane == 2 ? (above ? P.irowprog + y0 : nullptr)
-                    : grouped && prow < rows - 1 ? P.rowprog + y0 + prow
-                                                 : nullptr;
+                    : grouped && prow < rows ? P.refprog + (size_t)(y0 + prow) * RC_REFPROG_STRIDE
+                                             : nullptr;
     int seen = dst ? 0 : P.mb_w;
     uint32_t it = 0;
     while (!__all_sync(0xffffffffu, seen >= P.mb_w)) {
@@ -2069,7 +2119,7 @@ __device__ void band_publish(const H264Launch &P, BandSmem &B, int y0, int rows,
 
 // One band CTA: every thread of the CTA calls it; warps past the band's
 // (3 BR + 2) roles leave after the shared state is set up.
-__device__ void band_body(const H264Launch &P, BandSmem &B, uint8_t *band_dyn, int band) {
+__device__ __forceinline__ void band_body(const H264Launch &P, BandSmem &B, uint8_t *band_dyn, int band) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int y0 = band * BR, rows = min(BR, P.mb_h - y0);
     for (int i = threadIdx.x; i < 9 * 16; i += blockDim.x) B.tab4[i] = (&cPRED4.e[0][0])[i];
@@ -2101,70 +2151,178 @@ __global__ void __launch_bounds__(BAND_THREADS, 1) h264_band_kernel(const __grid
 // ===========================================================================
 // Kernel 3: a group of pictures in one cooperative launch.
 // ===========================================================================
-// CTAs 0 .. n*bands-1 are the band CTAs of the group's pictures (picture
-// b / bands, band b % bands); every other CTA runs the MB phase of all of
-// them, as two workers of 256 threads that take (picture, MB) items in order
-// from one counter -- every item of a picture before any item of the next
-// -- and publish each item's completion, edge words included, as
-// mbdone[addr] = epoch.  An item of picture j waits (mb_wait_refs) only for
-// rows of earlier pictures of the group, whose MB items were all taken
-// before it by workers that are running and whose band CTAs are resident
-// (cooperative launch): every wait ends.  The MB phase and the wavefronts
-// wait on one another, so they share one launch: separate launches are not
-// guaranteed to run at the same time.  The launch ends when every picture is
-// filtered, so the next launch on the stream reads finished references.
+// Before the launch, per picture, h264_edge_kernel writes the edge words and
+// h264_mb_kernel (residual_only) the residuals of every MB, the intra MBs'
+// parameters and the I_PCM samples: all of it depends on the records alone.
+// In the launch, n*bands CTAs spread over the grid are the band CTAs of the
+// group's pictures (band CTA b: picture b % n, band b / n); every
+// warp of the other CTAs takes (picture, MB) items in order from one counter
+// -- every item of a picture before any item of the next, and a picture's
+// MBs in the order of G.order, anti-diagonals that follow the wavefronts --
+// predicts the item's MB if it is an inter MB, adds its residual, stores it
+// and publishes mbdone[addr] = epoch.  (In raster order the few hundred
+// items in flight would cover a row or two of a picture, released only as
+// fast as one row of the picture it references is filtered, while that
+// picture's wavefront finishes its rows side by side.)
+// An item of picture j waits (mb_wait_refs) only for rows of earlier
+// pictures of the group, whose items were all taken before it by warps that
+// are running and whose band CTAs are resident (cooperative launch): every
+// wait ends.  The MB work and the wavefronts wait on one another, so they
+// share one launch: separate launches are not guaranteed to run at the same
+// time.  The launch ends when every picture is filtered, so the next launch
+// on the stream reads finished references.
 constexpr int GROUP_THREADS = 512;
-static_assert(GROUP_THREADS >= BAND_THREADS && GROUP_THREADS == 2 * 256, "two MB workers, or one band CTA");
+static_assert(GROUP_THREADS >= BAND_THREADS, "a group CTA holds a band CTA's warps");
 
-union GroupSmem {
-    BandSmem band;
-    MbSmem mb[2];
-};
-
-// The MB's loop-filter edge words, as h264_edge_kernel computes them; one
-// warp of a worker, after the MB (M.m holds its record).
-__device__ void mb_edge_words(const H264Launch &P, MbSmem &M, int addr, int lane) {
+// One inter MB of a group launch, one warp: the prediction of h264_mb_kernel
+// plus the stored residual, clipped.  Lane l takes luma column l % 16, rows
+// l / 16, +2, .., +14, and chroma column l % 8 of component (l / 8) % 2,
+// rows l / 16, +2, +4, +6: each load and store of the warp covers two rows
+// of consecutive samples, as in h264_mb_kernel.  Reads the references with
+// coherent loads after waiting for the rows of the in-flight ones that its
+// vectors reach.  False after a timeout.
+__device__ bool mb_predict_warp(const H264Launch &P, int addr, int lane) {
+    const rc_h264_mb &m = P.mbs[addr];
     const int mbx = addr % P.mb_w, mby = addr / P.mb_w;
-    constexpr int RW = (int)(sizeof(rc_h264_mb) / 4);
-    for (int i = lane; i < 2 * RW; i += 32) {
-        const int which = i / RW, j = i - which * RW;
-        const int src = which == 0 ? (mbx > 0 ? addr - 1 : -1) : (mby > 0 ? addr - P.mb_w : -1);
-        if (src >= 0) ((uint32_t *)&M.nbr[which])[j] = __ldg((const uint32_t *)(P.mbs + src) + j);
+    const int si = m.slice;
+    if (si >= P.num_slices) {
+        if (lane == 0) set_error(P.error, RC_DEV_ERR_RECORD);
+        return true;
     }
+    const rc_h264_slice *sl = P.slices + si;
+    if (P.nwait > 0 && !mb_wait_refs(P, m, sl, mbx, mby, lane)) return false;
     __syncwarp();
-    compute_db(P, M.m, M.nbr[0], M.nbr[1], addr, lane, &M.dbm);
-    __syncwarp();
-    edge_words(M.dbm, lane, P.edges + (size_t)addr * RC_EDGE_WORDS);
-    __syncwarp();
+    uint8_t *Y = P.dpb + (size_t)P.out_slot * P.slot_bytes;
+    const int16_t *res = P.ires + (size_t)addr * 384;
+    const int nref0 = min(__ldg(&sl->num_ref[0]), RC_H264_MAX_REFS), nref1 = min(__ldg(&sl->num_ref[1]), RC_H264_MAX_REFS);
+    // the reference slot of list l for 8x8 block b8 (-1: unused); bad slots
+    // are record errors, as in h264_mb_kernel
+    auto ref_slot = [&](int l, int b8, bool report) -> int {
+        const int ri = m.ref_idx[l][b8];
+        if (ri < 0) return -1;
+        const int slot = ri < (l ? nref1 : nref0) ? __ldg(&sl->ref_slot[l][ri]) : -1;
+        if (slot < 0 || slot >= P.dpb_slots) {
+            if (report) set_error(P.error, RC_DEV_ERR_RECORD);
+            return -1;
+        }
+        return slot;
+    };
+    struct Wt {
+        bool ex;
+        int lw, w0, w1, o0, o1;
+    };
+    auto weight = [&](int b8, int cc) -> Wt {
+        const int wi = m.wp[b8];
+        const rc_h264_weight *w = (wi != 0xff && wi < P.num_weights) ? P.weights + wi : nullptr;
+        const bool ex = w && (w->explicit_mask >> cc & 1);
+        return {ex, ex ? w->log_wd[cc] : 0, ex ? w->w0[cc] : 0, ex ? w->w1[cc] : 0, ex ? w->o0[cc] : 0,
+                ex ? w->o1[cc] : 0};
+    };
+    uint8_t *brow = P.bottom + (size_t)mby * P.mb_w * 32;
+    {  // luma
+        const int x = lane & 15, y0 = lane >> 4;
+#pragma unroll 1
+        for (int half = 0; half < 2; half++) {  // rows 0..7, then 8..15: one 8x8 block's list slots
+            const int b8 = half * 2 + (x >> 3);
+            int slot[2];
+#pragma unroll
+            for (int l = 0; l < 2; l++) slot[l] = ref_slot(l, b8, true);
+            const Wt w = weight(b8, 0);
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                const int y = half * 8 + y0 + 2 * i, k = (y >> 2) * 4 + (x >> 2);
+                int v[2] = {0, 0};
+#pragma unroll
+                for (int l = 0; l < 2; l++) {
+                    if (slot[l] < 0) continue;
+                    const Ref r{P.dpb + (size_t)slot[l] * P.slot_bytes, P.pitch, P.W, P.H};
+                    const int mvx = m.mv[l][k][0], mvy = m.mv[l][k][1];
+                    v[l] = luma_sample<true>(r, mbx * 16 + x + (mvx >> 2), mby * 16 + y + (mvy >> 2), mvx & 3, mvy & 3);
+                }
+                const int pred = weigh(v[0], v[1], slot[0] >= 0, slot[1] >= 0, w.ex, w.lw, w.w0, w.w1, w.o0, w.o1);
+                const uint8_t o = (uint8_t)clip255(pred + res[y * 16 + x]);
+                Y[(size_t)(mby * 16 + y) * P.pitch + mbx * 16 + x] = o;
+                if (y == 15) brow[mbx * 16 + x] = o;
+            }
+        }
+    }
+    {  // chroma
+        const int x = lane & 7, c = (lane >> 3) & 1, y0 = lane >> 4, cc = 1 + c;
+        uint8_t *C = c ? Y + P.v_off : Y + P.u_off;
+#pragma unroll 1
+        for (int half = 0; half < 2; half++) {  // rows 0..3, then 4..7
+            const int b8 = half * 2 + (x >> 2);
+            int slot[2];
+#pragma unroll
+            for (int l = 0; l < 2; l++) slot[l] = ref_slot(l, b8, false);
+            const Wt w = weight(b8, cc);
+#pragma unroll
+            for (int i = 0; i < 2; i++) {
+                const int y = half * 4 + y0 + 2 * i, k = (y >> 1) * 4 + (x >> 1);
+                int v[2] = {0, 0};
+#pragma unroll
+                for (int l = 0; l < 2; l++) {
+                    if (slot[l] < 0) continue;
+                    const Ref r{P.dpb + (size_t)slot[l] * P.slot_bytes + (c ? P.v_off : P.u_off), P.cpitch, P.CW, P.CH};
+                    const int mvx = m.mv[l][k][0], mvy = m.mv[l][k][1];
+                    v[l] = chroma_sample<true>(r, mbx * 8 + x + (mvx >> 3), mby * 8 + y + (mvy >> 3), mvx & 7, mvy & 7);
+                }
+                const int pred = weigh(v[0], v[1], slot[0] >= 0, slot[1] >= 0, w.ex, w.lw, w.w0, w.w1, w.o0, w.o1);
+                const uint8_t o = (uint8_t)clip255(pred + res[256 + c * 64 + y * 8 + x]);
+                C[(size_t)(mby * 8 + y) * P.cpitch + mbx * 8 + x] = o;
+                if (y == 7) brow[P.mb_w * (16 + 8 * c) + mbx * 8 + x] = o;
+            }
+        }
+    }
+    return true;
 }
 
 __global__ void __launch_bounds__(GROUP_THREADS, 1) h264_group_kernel(const __grid_constant__ H264Group G) {
-    __shared__ GroupSmem S;
+    __shared__ BandSmem B;
     extern __shared__ __align__(16) uint8_t band_dyn[];
-    const int nb = G.n * G.bands;
-    if ((int)blockIdx.x < nb) {
-        const int j = blockIdx.x / G.bands;
-        band_body(G.pic[j], S.band, band_dyn, blockIdx.x - j * G.bands);
+    // band CTAs are every stride-th CTA of the grid: spread over the GPU
+    // instead of packed into neighbouring SMs, the band wavefront runs much
+    // faster (1080p picture alone in a 152-CTA launch on GB300: 951 us with
+    // the band CTAs first in the grid, 498 us spread); G.workers of the other
+    // CTAs, spread the same way, predict inter MBs, and the rest leave
+    const int nb = G.n * G.bands, stride = (int)gridDim.x / nb;
+    const int bid = (int)blockIdx.x % stride == 0 && (int)blockIdx.x / stride < nb ? (int)blockIdx.x / stride : -1;
+    if (bid >= 0) {
+        // one inlined copy per picture index, so that the picture's
+        // parameters stay immediate constant-bank operands
+        // pictures interleaved, so that each picture's bands spread over
+        // the whole GPU too
+        const int j = bid % G.n, band = bid / G.n;
+        static_assert(RC_H264_GROUP_MAX == 4, "one case per group position");
+        switch (j) {
+        case 0: band_body(G.pic[0], B, band_dyn, band); break;
+        case 1: band_body(G.pic[1], B, band_dyn, band); break;
+        case 2: band_body(G.pic[2], B, band_dyn, band); break;
+        default: band_body(G.pic[3], B, band_dyn, band); break;
+        }
         return;
     }
-    const int h = threadIdx.x >> 8, t = threadIdx.x & 255, bar = 1 + h;
-    MbSmem &M = S.mb[h];
+    {
+        // rank among the CTAs that are not band CTAs
+        const int rank = (int)blockIdx.x - min(nb, (int)blockIdx.x / stride + 1);
+        const int others = (int)gridDim.x - nb, wstride = max(1, others / max(G.workers, 1));
+        if (rank % wstride != 0 || rank / wstride >= G.workers) return;
+    }
+    const int lane = threadIdx.x & 31;
     const int n_mb = G.pic[0].mb_w * G.pic[0].mb_h, total = G.n * n_mb;
     for (;;) {
-        if (t == 0) M.item = (int)atomicAdd(G.counter, 1u);
-        bar_sync(bar, 256);
-        const int w = M.item;
+        int w = 0;
+        if (lane == 0) w = (int)atomicAdd(G.counter, 1u);
+        w = __shfl_sync(0xffffffffu, w, 0);
         if (w >= total) return;
-        const int j = w / n_mb, addr = w - j * n_mb;
+        const int j = w / n_mb, addr = (int)__ldg(G.order + (w - j * n_mb));
         const H264Launch &P = G.pic[j];
-        mb_body(P, M, addr, t, bar);
-        bar_sync(bar, 256);  // the item's stores, and every read of M.item, are done
-        if (t < 32) {
-            mb_edge_words(P, M, addr, t);
-            if (t == 0) {
-                __threadfence();
-                st_release(P.mbdone + addr, P.epoch);
-            }
+        if (__ldg(&P.mbs[addr].kind) != RC_H264_INTER) continue;  // done by the pre-pass
+        if (!mb_predict_warp(P, addr, lane) && lane == 0) set_error(P.error, RC_DEV_ERR_TIMEOUT);
+        __syncwarp();
+        if (lane == 0) {
+            __threadfence();
+            st_release(P.mbdone + addr, P.epoch);  // published even after an error: nothing waits forever
         }
     }
 }
@@ -2241,7 +2399,9 @@ int rc_h264_group_capacity(int mb_w) {
 
 int rc_launch_h264_group(const H264Group &g, int ctas, cudaStream_t st) {
     const int mb_w = g.pic[0].mb_w;
-    if (g.n < 1 || g.n > RC_H264_GROUP_MAX || ctas <= g.n * g.bands) return -1;
+    if (g.n < 1 || g.n > RC_H264_GROUP_MAX || ctas <= g.n * g.bands || g.workers < 1 ||
+        g.workers > ctas - g.n * g.bands)
+        return -1;
     if (!band_smem_attr(1, rc_h264_band_smem(mb_w))) return -1;
     if (cudaMemsetAsync(g.counter, 0, sizeof(uint32_t), st) != cudaSuccess) return -1;
     H264Group q = g;

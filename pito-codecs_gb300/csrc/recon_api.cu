@@ -111,14 +111,28 @@ struct rc_stream {
     // DPB slots they read and their record sets), and per group position the
     // scratch of one picture: progress words, MB completion flags, edge
     // words, intra parameters and residuals
-    int group = 1, group_ctas = 0;
+    int group = 1, group_ctas = 0, group_workers = 0;
     std::vector<H264Launch> pending;
     std::vector<std::vector<int>> pending_refs;
     std::vector<int> pending_sets;
     uint32_t *g_rowprog = nullptr, *g_irowprog = nullptr, *g_mbdone = nullptr, *g_edges = nullptr;
+    uint8_t *g_bottom = nullptr;
+    uint32_t *g_order = nullptr, *g_refprog = nullptr;
     IntraInfo *g_iinfo = nullptr;
     int16_t *g_ires = nullptr;
     int g_alloc = 0;  // positions allocated
+    // device-memory records in a group: their slices are read back (on a
+    // stream of their own, into pinned memory) for the reference slots
+    cudaStream_t rst = nullptr;
+    void *rb = nullptr;
+    size_t rb_cap = 0;
+    // asynchronous downloads of slots that pending pictures write, issued
+    // once their group has launched
+    struct Dl {
+        int slot, x, y, w, h;
+        void *py, *pu, *pv;
+    };
+    std::vector<Dl> pending_dl;
     int32_t *ls = nullptr;            // device ls4 (2304 ints) + ls8 (2304*4 ints)
     std::vector<int32_t> ls_host;     // last uploaded tables
     uint8_t ls_key[2 + 96 + 384] = {0};  // the scaling lists they were made from (flat: flag 0)
@@ -293,7 +307,12 @@ void group_free(rc_stream *s) {
     dev_free(s, s->g_edges, n * mbs * RC_EDGE_WORDS * sizeof(uint32_t));
     dev_free(s, s->g_iinfo, n * mbs * sizeof(IntraInfo));
     dev_free(s, s->g_ires, n * mbs * 384 * sizeof(int16_t));
-    s->g_rowprog = s->g_irowprog = s->g_mbdone = s->g_edges = nullptr;
+    dev_free(s, s->g_bottom, n * mbs * 32);
+    dev_free(s, s->g_order, mbs * sizeof(uint32_t));
+    dev_free(s, s->g_refprog, n * s->mb_h * RC_REFPROG_STRIDE * sizeof(uint32_t));
+    s->g_refprog = nullptr;
+    s->g_rowprog = s->g_irowprog = s->g_mbdone = s->g_edges = s->g_order = nullptr;
+    s->g_bottom = nullptr;
     s->g_iinfo = nullptr;
     s->g_ires = nullptr;
     s->g_alloc = 0;
@@ -311,22 +330,43 @@ int group_alloc(rc_stream *s, int n) {
               dev_alloc(s, (void **)&s->g_mbdone, n * mbs * sizeof(uint32_t)) &&
               dev_alloc(s, (void **)&s->g_edges, n * mbs * RC_EDGE_WORDS * sizeof(uint32_t)) &&
               dev_alloc(s, (void **)&s->g_iinfo, n * mbs * sizeof(IntraInfo)) &&
-              dev_alloc(s, (void **)&s->g_ires, n * mbs * 384 * sizeof(int16_t));
+              dev_alloc(s, (void **)&s->g_ires, n * mbs * 384 * sizeof(int16_t)) &&
+              dev_alloc(s, (void **)&s->g_bottom, n * mbs * 32) &&
+              dev_alloc(s, (void **)&s->g_order, mbs * sizeof(uint32_t)) &&
+              dev_alloc(s, (void **)&s->g_refprog, n * s->mb_h * RC_REFPROG_STRIDE * sizeof(uint32_t));
     s->g_alloc = n;  // group_free releases whatever was allocated
     if (!ok) {
         cudaGetLastError();
         group_free(s);
         return RC_ENOMEM;
     }
+    // the order the MB work is taken in: anti-diagonals row * skew + column
+    // (then by row), the shape of the band wavefronts
+    std::vector<uint32_t> order(mbs);
+    for (size_t a = 0; a < mbs; a++) order[a] = (uint32_t)a;
+    const int w = s->mb_w;
+    std::stable_sort(order.begin(), order.end(), [w](uint32_t p, uint32_t q) {
+        const int kp = (int)(p / w) * RC_H264_GROUP_SKEW + (int)(p % w), kq = (int)(q / w) * RC_H264_GROUP_SKEW + (int)(q % w);
+        return kp < kq;
+    });
     ok = cudaMemsetAsync(s->g_rowprog, 0, n * s->mb_h * sizeof(uint32_t), s->st) == cudaSuccess &&
          cudaMemsetAsync(s->g_irowprog, 0, n * s->mb_h * sizeof(uint32_t), s->st) == cudaSuccess &&
-         cudaMemsetAsync(s->g_mbdone, 0, n * mbs * sizeof(uint32_t), s->st) == cudaSuccess;
+         cudaMemsetAsync(s->g_mbdone, 0, n * mbs * sizeof(uint32_t), s->st) == cudaSuccess &&
+         cudaMemsetAsync(s->g_refprog, 0, n * s->mb_h * RC_REFPROG_STRIDE * sizeof(uint32_t), s->st) == cudaSuccess &&
+         cudaMemcpyAsync(s->g_order, order.data(), mbs * sizeof(uint32_t), cudaMemcpyHostToDevice, s->st) == cudaSuccess &&
+         cudaStreamSynchronize(s->st) == cudaSuccess;  // `order` is pageable and leaves scope
     return ok ? 0 : cuda_fail(s);
 }
 
 void destroy(rc_stream *s) {
     if (!s) return;
     s->pending.clear();  // submitted pictures not yet launched are dropped
+    s->pending_dl.clear();
+    if (s->rst) {
+        cudaStreamSynchronize(s->rst);
+        cudaStreamDestroy(s->rst);
+    }
+    if (s->rb) cudaFreeHost(s->rb);
     if (s->st) cudaStreamSynchronize(s->st);
     if (s->cst) cudaStreamSynchronize(s->cst);
     if (s->dst) cudaStreamSynchronize(s->dst);
@@ -451,6 +491,27 @@ int set_release(rc_stream *s, int k) {
     return 0;
 }
 
+// Queue a cropped copy of a DPB slot on the download stream, after every
+// kernel launched so far (bounds checked by the caller, copy_cropped's rule,
+// src/h264/dec/picture.rs:601-615); later submits that write the slot wait
+// for it.
+int issue_download(rc_stream *s, int slot, int x, int y, int w, int h, void *out_y, void *out_u, void *out_v) {
+    const int cx = x / 2, cy = y / 2, ccw = (w + 1) / 2, cch = (h + 1) / 2, bps = s->bps;
+    const uint8_t *base = s->dpb + (size_t)slot * s->slot_bytes;
+    cudaStream_t c = s->dst;
+    bool ok = cudaEventRecord(s->kernels_done, s->st) == cudaSuccess &&
+              cudaStreamWaitEvent(c, s->kernels_done, 0) == cudaSuccess &&
+              cudaMemcpy2DAsync(out_y, (size_t)w * bps, base + (size_t)y * s->pitch + (size_t)x * bps, s->pitch,
+                                (size_t)w * bps, h, cudaMemcpyDeviceToHost, c) == cudaSuccess &&
+              cudaMemcpy2DAsync(out_u, (size_t)ccw * bps, base + s->u_off + (size_t)cy * s->cpitch + (size_t)cx * bps,
+                                s->cpitch, (size_t)ccw * bps, cch, cudaMemcpyDeviceToHost, c) == cudaSuccess &&
+              cudaMemcpy2DAsync(out_v, (size_t)ccw * bps, base + s->v_off + (size_t)cy * s->cpitch + (size_t)cx * bps,
+                                s->cpitch, (size_t)ccw * bps, cch, cudaMemcpyDeviceToHost, c) == cudaSuccess &&
+              cudaEventRecord(s->slot_dl[slot], c) == cudaSuccess;
+    if (ok) s->slot_dl_pending[slot] = 1;
+    return ok ? 0 : cuda_fail(s);
+}
+
 // Launch the pending group of H.264 pictures, if any.
 int h264_flush(rc_stream *s) {
     if (s->pending.empty()) return 0;
@@ -459,6 +520,8 @@ int h264_flush(rc_stream *s) {
     g.n = (int)s->pending.size();
     g.bands = (s->mb_h + RC_H264_BAND_ROWS - 1) / RC_H264_BAND_ROWS;
     g.counter = s->counter;
+    g.order = s->g_order;
+    g.workers = std::min(s->group_workers, s->group_ctas - g.n * g.bands);
     for (int i = 0; i < g.n; i++) g.pic[i] = s->pending[i];
     int lrc = 0;
     timed(s, RC_KERNEL_H264_GROUP, [&] { lrc = rc_launch_h264_group(g, s->group_ctas, s->st); });
@@ -468,7 +531,40 @@ int h264_flush(rc_stream *s) {
     s->pending.clear();
     s->pending_refs.clear();
     s->pending_sets.clear();
+    for (const auto &d : s->pending_dl)
+        if (!rc) rc = issue_download(s, d.slot, d.x, d.y, d.w, d.h, d.py, d.pu, d.pv);
+    s->pending_dl.clear();
     return rc;
+}
+
+// The reference slots of a picture whose records are in device memory: its
+// slices are read back (a few hundred bytes each) and the slots taken from
+// them; out-of-range entries are left to the kernels' record checks.
+int h264_device_ref_slots(rc_stream *s, const rc_h264_picture *p, std::vector<int> &out) {
+    const size_t n = sizeof(rc_h264_slice) * (size_t)p->num_slices;
+    if (!s->rst && cudaStreamCreateWithFlags(&s->rst, cudaStreamNonBlocking) != cudaSuccess) return cuda_fail(s);
+    if (n > s->rb_cap) {
+        if (s->rb) cudaFreeHost(s->rb);
+        s->rb = nullptr;
+        s->rb_cap = 0;
+        if (cudaMallocHost(&s->rb, align_up(n, 4096)) != cudaSuccess) return RC_ENOMEM;
+        s->rb_cap = align_up(n, 4096);
+    }
+    if (cudaMemcpyAsync(s->rb, p->slices, n, cudaMemcpyDeviceToHost, s->rst) != cudaSuccess ||
+        cudaStreamSynchronize(s->rst) != cudaSuccess) {
+        cudaGetLastError();
+        return RC_EINVAL;
+    }
+    const rc_h264_slice *sl = (const rc_h264_slice *)s->rb;
+    out.clear();
+    for (int i = 0; i < p->num_slices; i++)
+        for (int l = 0; l < 2; l++)
+            for (int j = 0; j < std::min(std::max(sl[i].num_ref[l], 0), RC_H264_MAX_REFS); j++) {
+                const int slot = sl[i].ref_slot[l][j];
+                if (slot >= 0 && slot < s->slots && std::find(out.begin(), out.end(), slot) == out.end())
+                    out.push_back(slot);
+            }
+    return 0;
 }
 
 // The DPB slots an H.264 picture's slices reference (validated records).
@@ -793,12 +889,12 @@ int rc_h264_submit(rc_stream *s, const rc_h264_picture *pic, int out_slot) {
         return RC_EINVAL;
     }
     // Groups: a picture joins the pending group unless it writes a slot that
-    // a pending picture writes or reads; device-memory records (whose
-    // references the host cannot read) launch alone, after the group.
-    const bool grouped = s->group > 1 && pic->mem == RC_MEM_HOST;
+    // a pending picture writes or reads.
+    const bool grouped = s->group > 1;
     std::vector<int> refs;
     if (grouped) {
-        refs = h264_ref_slots(pic);
+        if (pic->mem == RC_MEM_HOST) refs = h264_ref_slots(pic);
+        else if ((rc = h264_device_ref_slots(s, pic, refs)) != 0) return rc;
         bool clash = false;
         for (size_t i = 0; i < s->pending.size(); i++) {
             const auto &r = s->pending_refs[i];
@@ -893,17 +989,27 @@ int rc_h264_submit(rc_stream *s, const rc_h264_picture *pic, int out_slot) {
         L.edges = s->g_edges + (size_t)j * mbs * RC_EDGE_WORDS;
         L.iinfo = s->g_iinfo + (size_t)j * mbs;
         L.ires = s->g_ires + (size_t)j * mbs * 384;
+        L.bottom = s->g_bottom + (size_t)j * mbs * 32;
+        L.refprog = s->g_refprog + (size_t)j * s->mb_h * RC_REFPROG_STRIDE;
         for (int i = 0; i < j; i++) {
             const H264Launch &q = s->pending[i];
             if (std::find(refs.begin(), refs.end(), q.out_slot) == refs.end()) continue;
             L.wait_slot[L.nwait] = q.out_slot;
             L.wait_epoch[L.nwait] = q.epoch;
-            L.wait_rowprog[L.nwait] = q.rowprog;
+            L.wait_refprog[L.nwait] = q.refprog;
             L.nwait++;
         }
+        // the pre-pass, from the records alone: edge words, every MB's
+        // residual, intra parameters and I_PCM samples (on the stream, so
+        // after the previous group's launch, which read this position's
+        // buffers, and before this group's)
+        L.residual_only = 1;
+        timed(s, RC_KERNEL_H264_EDGE, [&] { rc_launch_h264_edge(L, s->st); });
+        timed(s, RC_KERNEL_H264_MB, [&] { rc_launch_h264_mb(L, s->st); });
+        L.residual_only = 0;
         s->pending.push_back(L);
         s->pending_refs.push_back(std::move(refs));
-        s->pending_sets.push_back(k);
+        s->pending_sets.push_back(pic->mem == RC_MEM_HOST ? k : -1);
         s->submits++;
         if ((int)s->pending.size() >= s->group && (rc = h264_flush(s)) != 0) return rc;
         if (cudaGetLastError() != cudaSuccess) return cuda_fail(s);
@@ -950,6 +1056,11 @@ int rc_stream_set_h264_group(rc_stream *s, int pictures) {
     if (pictures > 1 && (rc = group_alloc(s, pictures)) != 0) return rc;
     s->group = pictures;
     s->group_ctas = pictures > 1 ? cap : 0;
+    s->group_workers = RC_H264_GROUP_WORKERS;
+    if (const char *e = getenv("PITO_RECON_GROUP_WORKERS")) {
+        const int v = atoi(e);
+        if (v > 0 && v <= 4096) s->group_workers = v;
+    }
     s->nsets = pictures > 1 ? 2 * pictures : 2;
     return pictures;
 }
@@ -1104,30 +1215,23 @@ int rc_stream_error(rc_stream *s) {
 static int download(rc_stream *s, int slot, int x, int y, int w, int h, void *out_y, void *out_u, void *out_v,
                     bool wait) {
     if (!s || slot < 0 || slot >= s->slots || !out_y || !out_u || !out_v) return RC_EINVAL;
-    // copy_cropped's bounds rule, src/h264/dec/picture.rs:601-615
     int cx = x / 2, cy = y / 2, ccw = (w + 1) / 2, cch = (h + 1) / 2;
     auto fits = [](long at, long n, long size) { return n > 0 && at >= 0 && at + n <= size; };
     if (!(fits(x, w, s->width) && fits(y, h, s->height) && fits(cx, ccw, s->cw) && fits(cy, cch, s->ch)))
         return RC_EINVAL;
-    const int bps = s->bps;
-    const uint8_t *base = s->dpb + (size_t)slot * s->slot_bytes;
+    // copy_cropped's bounds rule above; an asynchronous download of a slot
+    // that a queued picture writes waits for that picture's group to launch,
+    // anything else goes now
+    bool queued = false;
+    for (const auto &q : s->pending) queued = queued || q.out_slot == slot;
+    if (queued && !wait) {
+        s->pending_dl.push_back({slot, x, y, w, h, out_y, out_u, out_v});
+        return RC_OK;
+    }
     int rc;
-    if ((rc = h264_flush(s)) != 0) return rc;
-    // on the download stream, after every kernel submitted so far; later
-    // submits that write this slot wait for it
-    cudaStream_t c = s->dst;
-    bool ok = cudaEventRecord(s->kernels_done, s->st) == cudaSuccess &&
-              cudaStreamWaitEvent(c, s->kernels_done, 0) == cudaSuccess &&
-              cudaMemcpy2DAsync(out_y, (size_t)w * bps, base + (size_t)y * s->pitch + (size_t)x * bps, s->pitch,
-                                (size_t)w * bps, h, cudaMemcpyDeviceToHost, c) == cudaSuccess &&
-              cudaMemcpy2DAsync(out_u, (size_t)ccw * bps, base + s->u_off + (size_t)cy * s->cpitch + (size_t)cx * bps,
-                                s->cpitch, (size_t)ccw * bps, cch, cudaMemcpyDeviceToHost, c) == cudaSuccess &&
-              cudaMemcpy2DAsync(out_v, (size_t)ccw * bps, base + s->v_off + (size_t)cy * s->cpitch + (size_t)cx * bps,
-                                s->cpitch, (size_t)ccw * bps, cch, cudaMemcpyDeviceToHost, c) == cudaSuccess &&
-              cudaEventRecord(s->slot_dl[slot], c) == cudaSuccess;
-    if (ok) s->slot_dl_pending[slot] = 1;
-    ok = ok && (!wait || cudaStreamSynchronize(c) == cudaSuccess);
-    return ok ? RC_OK : cuda_fail(s);
+    if (queued && (rc = h264_flush(s)) != 0) return rc;
+    if ((rc = issue_download(s, slot, x, y, w, h, out_y, out_u, out_v)) != 0) return rc;
+    return !wait || cudaStreamSynchronize(s->dst) == cudaSuccess ? RC_OK : cuda_fail(s);
 }
 
 int rc_picture_download(rc_stream *s, int slot, int x, int y, int w, int h, void *out_y, void *out_u, void *out_v) {

@@ -50,6 +50,9 @@ static_assert(sizeof(IntraInfo) == 32, "IntraInfo layout");
 
 #define RC_H264_GROUP_MAX 4
 #define RC_H264_GROUP_DEFAULT 3  // rc_stream_set_h264_group(s, 0)
+#define RC_H264_GROUP_WORKERS 24 // CTAs of a group launch that predict inter MBs
+#define RC_H264_GROUP_SKEW 3     // MB work order: anti-diagonals of row * SKEW + column
+#define RC_REFPROG_STRIDE 32     // words between two rows' refprog words (one 128-byte line each)
 
 struct H264Launch {
     const rc_h264_mb *mbs;
@@ -79,21 +82,26 @@ struct H264Launch {
     // picture publishes each MB's completion as mbdone[addr] = epoch (null:
     // the MB phase finished before the band kernel started), and waits for
     // the rows of the in-flight pictures it references: nwait DPB slots with
-    // their pictures' epochs and per-row filter progress (rowprog layout).
+    // their pictures' epochs and per-row filter progress (refprog layout).
     uint32_t *mbdone;
+    uint8_t *bottom;    // per MB row, mb_w x 32 bytes: unfiltered luma row 15, then Cb and Cr row 7 (not intra MBs)
+    int residual_only;  // h264_mb_kernel before a group launch: inter MBs store residuals, unpredicted
     int nwait;
     int wait_slot[RC_H264_GROUP_MAX];
     uint32_t wait_epoch[RC_H264_GROUP_MAX];
-    uint32_t *wait_rowprog[RC_H264_GROUP_MAX];
+    uint32_t *wait_refprog[RC_H264_GROUP_MAX];
+    uint32_t *refprog;  // group launch: per MB row, every RC_REFPROG_STRIDE words, rowprog's value for the MB work
 };
 
 // Up to RC_H264_GROUP_MAX consecutive pictures of one stream reconstructed
-// by one cooperative launch: CTAs [j * bands, (j + 1) * bands) are picture
-// j's band CTAs, the others run the MB phase of all the pictures, taking
-// (picture, MB) work items in order from *counter (zeroed by the launcher).
+// by one cooperative launch: n * bands CTAs spread over the grid are the
+// pictures' band CTAs, the others predict the inter MBs of all the pictures,
+// taking (picture, MB) work items in order from *counter (zeroed by the
+// launcher).
 struct H264Group {
-    int n, bands;
+    int n, bands, workers;  // workers: CTAs that predict inter MBs
     uint32_t *counter;
+    const uint32_t *order;  // mb_w * mb_h MB addresses in the order the MB work is taken
     H264Launch pic[RC_H264_GROUP_MAX];
 };
 

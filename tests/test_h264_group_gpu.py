@@ -86,8 +86,10 @@ def ipp_sequence(engine, mb_w, mb_h, frames, seed, slots, lists=1, **opts):
 def test_group_sizes_small_pictures(engine, oracle, group):
     pics, slots = ipp_sequence(engine, 8, 6, 12, seed=31, slots=8)
     counts = run_grouped(engine, oracle, pics, slots, 8, 6, 8, group)
-    # every picture went through the group kernel (id 8), none alone
-    assert counts.get(8, 0) >= 12 // group and 0 not in counts and 1 not in counts
+    # every picture went through the pre-pass (ids 2, 0) and the group
+    # kernel (id 8), none through the one-picture band kernel (id 1)
+    assert counts.get(8, 0) >= 12 // group and 1 not in counts
+    assert counts.get(0, 0) == 12 and counts.get(2, 0) == 12
 
 
 def test_group_far_motion_dense_residual_two_lists(engine, oracle):
@@ -120,8 +122,10 @@ def test_group_1080p_bench_sequence(engine, oracle):
 
 
 def test_group_scaling_list_change_and_device_records(engine, oracle):
-    """A change of scaling lists, and pictures whose records are in device
-    memory, launch what is queued first; the output is unchanged."""
+    """A change of scaling lists launches what is queued first; a picture
+    whose records are in device memory joins the group like the others (its
+    reference slots are read back from its slices); the output is
+    unchanged."""
     torch = pytest.importorskip("torch")
     mb_w, mb_h, slots = 9, 8, 8
     pics = []
@@ -145,16 +149,14 @@ def test_group_scaling_list_change_and_device_records(engine, oracle):
             setattr(d, key, t.data_ptr())
         return d
 
-    dev = {7: device_copy(pics[7])}
+    dev = {i: device_copy(pics[i]) for i in (2, 3, 7)}
     torch.cuda.synchronize()
 
     def submit(st, i, slot):
         st.submit_h264(ctypes.addressof(dev[i]) if i in dev else pics[i], slot)
 
     counts = run_grouped(engine, oracle, pics, [n % slots for n in range(10)], mb_w, mb_h, slots, 4, submit=submit)
-    assert counts.get(8, 0) >= 3
-    # the device-memory picture went through the one-picture kernels
-    assert counts.get(1, 0) == 1
+    assert counts.get(8, 0) >= 3 and 1 not in counts
 
 
 def test_group_timeout_is_reported_and_stream_recovers(engine, oracle):
@@ -183,3 +185,38 @@ def test_group_timeout_is_reported_and_stream_recovers(engine, oracle):
         assert st.sync() == 0
     finally:
         st.close()
+
+
+def test_group_async_downloads_wait_for_their_group(engine, oracle):
+    """rc_picture_download_async right after each submit (the e2e pattern):
+    a download of a queued picture's slot is issued when its group launches,
+    so groups still form, and every copy holds its picture."""
+    torch = pytest.importorskip("torch")
+    mb_w, mb_h, slots, frames = 12, 9, 8, 14
+    pics, slot_of = ipp_sequence(engine, mb_w, mb_h, frames, seed=38, slots=slots)
+    dpb = oracle.H264Dpb(mb_w, mb_h, slots)
+    want = []
+    for p, sl in zip(pics, slot_of):
+        assert dpb.recon(p.ptr, sl) == 0
+        want.append([np.array(x, copy=True) for x in dpb.planes(sl)])
+    W, H = mb_w * 16, mb_h * 16
+    outs = [tuple(torch.zeros(n, dtype=torch.uint8).pin_memory() for n in (W * H, W * H // 4, W * H // 4))
+            for _ in range(frames)]
+    st = engine.ReconStream(engine.RC_CODEC_H264, W, H, 8, slots)
+    try:
+        assert st.set_h264_group(4) == 4
+        st.profile(True)
+        for n, (p, sl) in enumerate(zip(pics, slot_of)):
+            st.submit_h264(p, sl)
+            y, u, v = outs[n]
+            st.download_async(sl, (0, 0, W, H), y.data_ptr(), u.data_ptr(), v.data_ptr())
+        assert st.sync() == 0
+        counts = {k: c for k, (ms, c) in st.profile_read().items()}
+    finally:
+        st.close()
+    assert counts.get(8, 0) < frames and 1 not in counts
+    for n in range(frames):
+        y, u, v = (t.numpy() for t in outs[n])
+        assert np.array_equal(y.reshape(H, W), want[n][0]), f"picture {n} Y"
+        assert np.array_equal(u.reshape(H // 2, W // 2), want[n][1]), f"picture {n} U"
+        assert np.array_equal(v.reshape(H // 2, W // 2), want[n][2]), f"picture {n} V"
