@@ -129,6 +129,62 @@ typedef struct rc_h264_weight {
     int32_t w0[3], w1[3], o0[3], o1[3];
 } rc_h264_weight;          /* 64 bytes */
 
+/* Motion syntax of one MB, for motion derived on the GPU (no counterpart in
+ * the reference, whose slice decoder derives each MB's vectors as it parses
+ * it: mvp / median_pred / derive_p_skip / derive_direct,
+ * src/h264/dec/slicedec.rs:581-935).  The parse only needs the parsed
+ * syntax -- CABAC and CAVLC contexts read neighbouring mvd and ref_idx, never
+ * derived vectors -- so a decoder can hand it over and let the engine derive
+ * every vector: motion vector prediction plus mvd (8.4.1.3), P_Skip
+ * (8.4.1.1), B direct spatial and temporal (8.4.1.2) from the co-located
+ * picture's stored motion, and each 8x8 block's weight entry.  `shape`:
+ * RC_H264_MOTION_*.  `pred`: prediction lists (bit 0 list 0, bit 1 list 1)
+ * of partition i (16x16: 0; 16x8, 8x16: 0..1; 8x8: the four 8x8 blocks).
+ * `sub` (8x8 only): sub-partition of each 8x8 block, RC_H264_SUB_*.
+ * `ref_idx`: the parsed ref_idx of the partition covering each 8x8 block.
+ * `mvd`: per 4x4 block (raster) and list, the mvd of the (sub-)partition
+ * covering it. */
+#define RC_H264_MOTION_NONE 0  /* intra, I_PCM or not decoded: no motion     */
+#define RC_H264_MOTION_SKIP 1  /* P_Skip (P slice); B_Skip, B_Direct_16x16 (B) */
+#define RC_H264_MOTION_16x16 2
+#define RC_H264_MOTION_16x8 3
+#define RC_H264_MOTION_8x16 4
+#define RC_H264_MOTION_8x8 5
+#define RC_H264_SUB_8x8 0
+#define RC_H264_SUB_8x4 1
+#define RC_H264_SUB_4x8 2
+#define RC_H264_SUB_4x4 3
+#define RC_H264_SUB_DIRECT 4   /* B_Direct_8x8 */
+typedef struct rc_h264_motion {
+    uint8_t shape;
+    uint8_t pred[4];
+    uint8_t sub[4];
+    uint8_t reserved[3];
+    int8_t ref_idx[2][4];
+    int16_t mvd[2][16][2];
+} rc_h264_motion;           /* 148 bytes */
+
+/* Per slice, for motion derived on the GPU: what the reference's slice
+ * decoder keeps for direct prediction and weighting (SliceDecoder::new,
+ * slicedec.rs:360-406: tdirect; build_weights).  `col_slot`: the DPB slot of
+ * RefPicList1[0] (B slices), which must hold a picture submitted with motion
+ * syntax.  `dist_scale` / `direct_copy` per refIdxL0: temporal direct's
+ * DistScaleFactor, or 1 where mvL0 = mvCol and mvL1 = 0 (long-term
+ * reference or equal POC distances).  `wp_map[(r0 + 1) * 33 + (r1 + 1)]`:
+ * the weight-table entry for refIdxL0 = r0 and refIdxL1 = r1 (-1: list
+ * unused), 0xff for the default average. */
+typedef struct rc_h264_slice_motion {
+    int32_t b_slice;
+    int32_t direct_spatial;        /* direct_spatial_mv_pred_flag             */
+    int32_t direct_8x8_inference;  /* SPS direct_8x8_inference_flag           */
+    int32_t col_slot;
+    int32_t col_short_term;        /* RefPicList1[0] is a short-term reference */
+    int16_t dist_scale[RC_H264_MAX_REFS];
+    uint8_t direct_copy[RC_H264_MAX_REFS];
+    uint8_t wp_map[(RC_H264_MAX_REFS + 1) * (RC_H264_MAX_REFS + 1)];
+    uint8_t reserved[3];
+} rc_h264_slice_motion;     /* 1208 bytes */
+
 typedef struct rc_h264_picture {
     int32_t mem;                      /* RC_MEM_HOST or RC_MEM_DEVICE          */
     int32_t constrained_intra_pred;   /* PPS flag                              */
@@ -145,6 +201,13 @@ typedef struct rc_h264_picture {
      * NULL = flat 16.  Always host memory. */
     const uint8_t *scaling4;          /* [6][16] */
     const uint8_t *scaling8;          /* [6][64] */
+    /* Optional (host memory, with mem == RC_MEM_HOST): motion syntax per MB
+     * and per slice.  When set, the engine derives every inter MB's mv,
+     * ref_idx and wp on the GPU and ignores those fields of `mbs`; it also
+     * stores the picture's motion in its DPB slot, for later pictures that
+     * use it as their co-located picture. */
+    const rc_h264_motion *motion;
+    const rc_h264_slice_motion *slice_motion;
 } rc_h264_picture;
 
 /* ======================================================================== */

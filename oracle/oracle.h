@@ -36,6 +36,38 @@ int oracle_h264_recon_nofilter(int mb_w, int mb_h, const rc_h264_picture *pic,
                                const uint8_t *const *ref_v, uint8_t *y,
                                uint8_t *u, uint8_t *v);
 
+/* Co-located motion of one MB, as Frame::publish stores it
+ * (src/h264/dec/picture.rs:492): no motion for intra, I_PCM and undecoded
+ * MBs; else each 8x8 block's ref_idx and referenced picture identity and
+ * each 4x4 block's vectors, per list. */
+typedef struct {
+    uint8_t intra;
+    uint8_t pad[3];
+    int8_t ref_idx[2][4];
+    uint32_t ref_id[2][4];
+    int16_t mv[2][16][2];
+} oracle_h264_colmb;        /* 172 bytes */
+
+/* Derive every inter MB's mv, ref_idx and wp from pic->motion and
+ * pic->slice_motion (h264_motion.c) into `mbs`, a copy of pic->mbs that the
+ * caller owns, reading co-located motion from col[slot] (NULL: the slot
+ * holds none), and write the picture's co-located motion into out_col
+ * (mb_w * mb_h entries).  Returns 0 or RC_EINVAL. */
+int oracle_h264_derive_motion(int mb_w, int mb_h, const rc_h264_picture *pic,
+                              const oracle_h264_colmb *const *col, int slots,
+                              rc_h264_mb *mbs, oracle_h264_colmb *out_col);
+
+/* oracle_h264_recon (filter != 0) or _nofilter, after deriving the motion
+ * when pic->motion is set; out_col receives the picture's co-located motion
+ * either way. */
+int oracle_h264_recon_motion(int mb_w, int mb_h, const rc_h264_picture *pic,
+                             const oracle_h264_colmb *const *col, int slots,
+                             oracle_h264_colmb *out_col,
+                             const uint8_t *const *ref_y,
+                             const uint8_t *const *ref_u,
+                             const uint8_t *const *ref_v, uint8_t *y,
+                             uint8_t *u, uint8_t *v, int filter);
+
 /* Deblock an already reconstructed picture in place. */
 void oracle_h264_deblock(int mb_w, int mb_h, const rc_h264_picture *pic,
                          uint8_t *y, uint8_t *u, uint8_t *v);

@@ -32,6 +32,8 @@ def lib() -> ctypes.CDLL:
             f = getattr(_lib, name)
             f.argtypes = [i32, i32, vp, vp, vp, vp, vp, vp, vp]
             f.restype = i32
+        _lib.oracle_h264_recon_motion.argtypes = [i32, i32, vp, vp, i32, vp, vp, vp, vp, vp, vp, vp, i32]
+        _lib.oracle_h264_recon_motion.restype = i32
         _lib.oracle_h264_deblock.argtypes = [i32, i32, vp, vp, vp, vp]
         _lib.oracle_h264_deblock.restype = None
         _lib.oracle_h264_idct4_add.argtypes = [vp, vp, i32]
@@ -50,8 +52,13 @@ def lib() -> ctypes.CDLL:
     return _lib
 
 
+COLMB_BYTES = 172  # sizeof(oracle_h264_colmb)
+
+
 class H264Dpb:
-    """CPU decoded-picture buffer: planes per slot at the coded size."""
+    """CPU decoded-picture buffer: planes per slot at the coded size, and
+    each slot's co-located motion (for pictures whose motion is derived
+    from motion syntax, rc_h264_picture.motion)."""
 
     def __init__(self, mb_w: int, mb_h: int, slots: int):
         self.mb_w, self.mb_h, self.slots = mb_w, mb_h, slots
@@ -59,6 +66,7 @@ class H264Dpb:
         self.y = [np.zeros((H, W), np.uint8) for _ in range(slots)]
         self.u = [np.zeros((H // 2, W // 2), np.uint8) for _ in range(slots)]
         self.v = [np.zeros((H // 2, W // 2), np.uint8) for _ in range(slots)]
+        self.col = [None] * slots
 
     def _ptrs(self, planes):
         arr = (ctypes.c_void_p * self.slots)(*[p.ctypes.data for p in planes])
@@ -66,15 +74,18 @@ class H264Dpb:
 
     def recon(self, picture_ptr: int, out_slot: int, filter: bool = True) -> int:
         L = lib()
-        f = L.oracle_h264_recon if filter else L.oracle_h264_recon_nofilter
         ry, ru, rv = self._ptrs(self.y), self._ptrs(self.u), self._ptrs(self.v)
         # the output slot is never its own reference: reconstruct into fresh planes
         y = self.y[out_slot].copy()
         u = self.u[out_slot].copy()
         v = self.v[out_slot].copy()
-        rc = f(self.mb_w, self.mb_h, picture_ptr, ry, ru, rv, y.ctypes.data, u.ctypes.data, v.ctypes.data)
+        col = (ctypes.c_void_p * self.slots)(*[c.ctypes.data if c is not None else None for c in self.col])
+        out_col = np.zeros(self.mb_w * self.mb_h * COLMB_BYTES, np.uint8)
+        rc = L.oracle_h264_recon_motion(self.mb_w, self.mb_h, picture_ptr, col, self.slots, out_col.ctypes.data,
+                                        ry, ru, rv, y.ctypes.data, u.ctypes.data, v.ctypes.data, int(filter))
         if rc == 0:
             self.y[out_slot], self.u[out_slot], self.v[out_slot] = y, u, v
+            self.col[out_slot] = out_col
         return rc
 
     def planes(self, slot: int):

@@ -72,10 +72,28 @@ class H264Picture(ctypes.Structure):
                 ("num_slices", ctypes.c_int32), ("num_weights", ctypes.c_int32), ("reserved", ctypes.c_int32),
                 ("num_levels", ctypes.c_size_t), ("mbs", ctypes.c_void_p), ("slices", ctypes.c_void_p),
                 ("weights", ctypes.c_void_p), ("levels", ctypes.c_void_p), ("scaling4", ctypes.c_void_p),
-                ("scaling8", ctypes.c_void_p)]
+                ("scaling8", ctypes.c_void_p), ("motion", ctypes.c_void_p), ("slice_motion", ctypes.c_void_p)]
 
 
-assert ctypes.sizeof(H264Mb) == 176 and ctypes.sizeof(H264Weight) == 64 and ctypes.sizeof(H264Picture) == 80
+class H264Motion(ctypes.Structure):
+    _fields_ = [("shape", ctypes.c_uint8), ("pred", ctypes.c_uint8 * 4), ("sub", ctypes.c_uint8 * 4),
+                ("reserved", ctypes.c_uint8 * 3), ("ref_idx", (ctypes.c_int8 * 4) * 2),
+                ("mvd", ((ctypes.c_int16 * 2) * 16) * 2)]
+
+
+class H264SliceMotion(ctypes.Structure):
+    _fields_ = [("b_slice", ctypes.c_int32), ("direct_spatial", ctypes.c_int32),
+                ("direct_8x8_inference", ctypes.c_int32), ("col_slot", ctypes.c_int32),
+                ("col_short_term", ctypes.c_int32), ("dist_scale", ctypes.c_int16 * 32),
+                ("direct_copy", ctypes.c_uint8 * 32), ("wp_map", ctypes.c_uint8 * (33 * 33)),
+                ("reserved", ctypes.c_uint8 * 3)]
+
+
+RC_H264_MOTION_NONE, RC_H264_MOTION_SKIP, RC_H264_MOTION_16x16, RC_H264_MOTION_16x8, RC_H264_MOTION_8x16, \
+    RC_H264_MOTION_8x8 = range(6)
+RC_H264_SUB_8x8, RC_H264_SUB_8x4, RC_H264_SUB_4x8, RC_H264_SUB_4x4, RC_H264_SUB_DIRECT = range(5)
+assert ctypes.sizeof(H264Motion) == 148 and ctypes.sizeof(H264SliceMotion) == 1208
+assert ctypes.sizeof(H264Mb) == 176 and ctypes.sizeof(H264Weight) == 64 and ctypes.sizeof(H264Picture) == 96
 
 
 class SynthH264Opts(ctypes.Structure):
@@ -413,6 +431,7 @@ class PictureBuffers:
         addr = lambda k: ctypes.addressof(self._keep[k]) if self._keep.get(k) is not None else None
         p.mbs, p.slices, p.weights, p.levels = addr("mbs"), addr("slices"), addr("weights"), addr("levels")
         p.scaling4, p.scaling8 = addr("scaling4"), addr("scaling8")
+        p.motion, p.slice_motion = addr("motion"), addr("slice_motion")
         self.pic = p
         self.ptr = ctypes.addressof(p)
 

@@ -492,7 +492,7 @@ _B_SUB = {1: (8, 8, 1), 2: (8, 8, 2), 3: (8, 8, 3), 4: (8, 4, 1), 5: (4, 8, 1), 
 class _Mb:
     __slots__ = ("slice", "kind", "skip", "direct16", "qp", "qpd", "cbp", "t8", "i16", "cmode", "modes", "ref",
                  "mv", "mvd", "direct", "cbf_dc", "cbf4", "cbfc", "levels", "dc", "luma_coded", "chroma_coded",
-                 "nz", "wp", "btype")
+                 "nz", "wp", "btype", "syn")
 
     def __init__(self):
         self.slice = -1
@@ -512,6 +512,7 @@ class _Mb:
         self.dc = self.luma_coded = self.chroma_coded = self.nz = 0
         self.wp = [0xFF] * 4
         self.btype = -1  # B mb_type (0 B_Direct_16x16 .. 22 B_8x8)
+        self.syn = None  # motion syntax: (shape, pred[4], sub[4]), RC_H264_MOTION_* / RC_H264_SUB_*
 
 
 class Frame:
@@ -656,6 +657,30 @@ class Decoder:
                 for l in range(2):
                     mx, my = m.mv[l][k] if (inter and m.ref[l][k] >= 0) else (0, 0)
                     r.mv[l][k][0], r.mv[l][k][1] = mx, my
+        mos = (E.H264Motion * n)()
+        for a, m in enumerate(self.mbs):
+            if m.kind not in ("P", "B"):
+                continue
+            o = mos[a]
+            o.shape = m.syn[0]
+            for i in range(4):
+                o.pred[i], o.sub[i] = m.syn[1][i], m.syn[2][i]
+            for b8 in range(4):
+                k = (b8 >> 1) * 8 + (b8 & 1) * 2
+                for l in range(2):
+                    o.ref_idx[l][b8] = -1 if (m.direct[k] or m.skip) else m.ref[l][k]
+            for k in range(16):
+                for l in range(2):
+                    o.mvd[l][k][0], o.mvd[l][k][1] = m.mvd[l][k]
+        smo = (E.H264SliceMotion * len(self.slices))()
+        for i, s in enumerate(self.slices):
+            for key, v in s["motion"].items():
+                if isinstance(v, list):
+                    arr = getattr(smo[i], key)
+                    for j, x in enumerate(v):
+                        arr[j] = x
+                else:
+                    setattr(smo[i], key, v)
         sl = (E.H264Slice * len(self.slices))()
         for i, s in enumerate(self.slices):
             sl[i].disable_deblocking_filter_idc = s["deblock_idc"]
@@ -676,6 +701,7 @@ class Decoder:
         s8 = (bytes(v for i in (6, 7) for v in _raster(sc[i], _ZZ8)) + bytes([16] * 256)) if sc else b""
         self.pictures.append({
             "mbs": bytes(recs), "slices": bytes(sl), "weights": bytes(wts)[:64 * len(self.weights)],
+            "motion": bytes(mos), "slice_motion": bytes(smo),
             "levels": array.array("h", levels).tobytes(), "scaling4": s4, "scaling8": s8,
             "num_slices": len(self.slices), "num_weights": len(self.weights), "slot": f.slot, "frame_id": f.id,
             "constrained_intra": self.pps["constrained_intra"], "mb_w": self.mb_w, "mb_h": self.mb_h,
@@ -746,6 +772,7 @@ class Decoder:
         lists = self._ref_lists(h)
         self.lists = lists
         self.slices.append({"deblock_idc": h["deblock_idc"], "alpha": h["alpha"], "beta": h["beta"], "list": lists})
+        self.slices[-1]["motion"] = self._slice_motion()
         table = 3 if h["type"] == 2 else h["cabac_init_idc"]
         c = Cabac(rbsp, bitpos, h["qp"], table)
         self.c = c
@@ -766,6 +793,7 @@ class Decoder:
             if skip:
                 m.skip = True
                 m.qp = qp
+                m.syn = (1, [0] * 4, [0] * 4)  # RC_H264_MOTION_SKIP
                 if h["type"] == 0:
                     m.kind = "P"
                     self._p_skip(addr)
@@ -1324,6 +1352,7 @@ class Decoder:
             self._subs = None
             parts = _P_PARTS[mt]
             shape = ("16x16", "16x8", "8x16")[mt]
+            m.syn = (2 + mt, [1] * len(parts) + [0] * (4 - len(parts)), [0] * 4)
             refs = [self._ref_idx_at(addr, 0, x, y, w, hh, nref) for (x, y, w, hh) in parts]
             for (x, y, w, hh), r in zip(parts, refs):
                 d = self._mvd(addr, 0, x, y)
@@ -1339,6 +1368,7 @@ class Decoder:
                 else:
                     subs.append(2 if c.dec(23) else 3)
             self._subs = subs
+            m.syn = (5, [1] * 4, list(subs))  # P_8x8: sub shapes 0..3 as RC_H264_SUB_*
             refs = [self._ref_idx_at(addr, 0, (i & 1) * 8, (i >> 1) * 8, 8, 8, nref) for i in range(4)]
             for i8 in range(4):
                 x8, y8 = (i8 & 1) * 8, (i8 >> 1) * 8
@@ -1373,6 +1403,7 @@ class Decoder:
         if mt == 0:
             self._subs = None
             m.direct16 = True
+            m.syn = (1, [0] * 4, [0] * 4)
             self._direct(addr, range(4))
             self._weights_for(m)
             return
@@ -1381,6 +1412,7 @@ class Decoder:
             pw, ph, preds = _B_TYPES[mt]
             parts = [(0, 0)] if pw == 16 and ph == 16 else ([(0, 0), (0, 8)] if ph == 8 else [(0, 0), (8, 0)])
             shape = "16x16" if len(parts) == 1 else ("16x8" if ph == 8 else "8x16")
+            m.syn = ({"16x16": 2, "16x8": 3, "8x16": 4}[shape], list(preds) + [0] * (4 - len(preds)), [0] * 4)
             refs = [[-1] * len(parts), [-1] * len(parts)]
             for X in range(2):
                 for i, (x, y) in enumerate(parts):
@@ -1414,6 +1446,9 @@ class Decoder:
                 t += c.dec(39)
                 subs.append(t)
         self._subs = subs
+        _subshape = {(8, 8): 0, (8, 4): 1, (4, 8): 2, (4, 4): 3}
+        m.syn = (5, [_B_SUB[t][2] if t else 0 for t in subs],
+                 [_subshape[_B_SUB[t][:2]] if t else 4 for t in subs])
         direct8 = [i for i in range(4) if subs[i] == 0]
         if direct8:
             self._direct(addr, direct8)
@@ -1522,49 +1557,77 @@ class Decoder:
     def _weights_for(self, m):
         """The weight-table entry of each 8x8 partition: explicit tables of the
         slice, implicit weights from POC distances, or default (0xff)."""
+        for b8 in range(4):
+            k = (b8 >> 1) * 8 + (b8 & 1) * 2
+            m.wp[b8] = self._wp_index(m.ref[0][k], m.ref[1][k])
+
+    def _wp_index(self, r0, r1):
+        """The weight-table entry for refIdxL0 = r0 and refIdxL1 = r1 in the
+        current slice (-1: list unused), 0xff for the default."""
         h, pps = self.h, self.pps
         explicit = h["weights"] is not None
         implicit = h["type"] == 1 and pps["weighted_bipred"] == 2
-        for b8 in range(4):
-            k = (b8 >> 1) * 8 + (b8 & 1) * 2
-            r0, r1 = m.ref[0][k], m.ref[1][k]
-            if not explicit and not (implicit and r0 >= 0 and r1 >= 0):
-                m.wp[b8] = 0xFF
-                continue
-            if explicit:
-                w = h["weights"]
-                lw, cw = w["luma_log2"], w["chroma_log2"]
-                e0 = w["l"][0][r0] if r0 >= 0 else None
-                e1 = w["l"][1][r1] if r1 >= 0 else None
-                ent = {"lwd": [lw, cw, cw],
-                       "w0": [e0[0], e0[2][0], e0[2][1]] if e0 else [0, 0, 0],
-                       "o0": [e0[1], e0[3][0], e0[3][1]] if e0 else [0, 0, 0],
-                       "w1": [e1[0], e1[2][0], e1[2][1]] if e1 else [0, 0, 0],
-                       "o1": [e1[1], e1[3][0], e1[3][1]] if e1 else [0, 0, 0]}
-            else:
-                p0, p1 = self.lists[0][r0], self.lists[1][r1]
+        if not explicit and not (implicit and r0 >= 0 and r1 >= 0):
+            return 0xFF
+        if explicit:
+            w = h["weights"]
+            lw, cw = w["luma_log2"], w["chroma_log2"]
+            e0 = w["l"][0][r0] if r0 >= 0 else None
+            e1 = w["l"][1][r1] if r1 >= 0 else None
+            ent = {"lwd": [lw, cw, cw],
+                   "w0": [e0[0], e0[2][0], e0[2][1]] if e0 else [0, 0, 0],
+                   "o0": [e0[1], e0[3][0], e0[3][1]] if e0 else [0, 0, 0],
+                   "w1": [e1[0], e1[2][0], e1[2][1]] if e1 else [0, 0, 0],
+                   "o1": [e1[1], e1[3][0], e1[3][1]] if e1 else [0, 0, 0]}
+        else:
+            p0, p1 = self.lists[0][r0], self.lists[1][r1]
+            tb = max(-128, min(127, self.frame.poc - p0.poc))
+            td = max(-128, min(127, p1.poc - p0.poc))
+            w0 = w1 = 32
+            if td != 0:
+                tx = (16384 + abs(int(td / 2))) // abs(td) * (1 if td > 0 else -1)
+                dsf = max(-1024, min(1023, (tb * tx + 32) >> 6))
+                if -64 <= (dsf >> 2) <= 128:
+                    w0, w1 = 64 - (dsf >> 2), dsf >> 2
+            ent = {"lwd": [5, 5, 5], "w0": [w0] * 3, "w1": [w1] * 3, "o0": [0] * 3, "o1": [0] * 3}
+        mask = 0
+        for comp in range(3):
+            unit0 = ent["w0"][comp] == 1 << ent["lwd"][comp] and ent["o0"][comp] == 0
+            unit1 = ent["w1"][comp] == 1 << ent["lwd"][comp] and ent["o1"][comp] == 0
+            plain = (unit0 or r0 < 0) and (unit1 or r1 < 0)
+            if not plain:
+                mask |= 1 << comp
+        if mask == 0:
+            return 0xFF
+        ent["mask"] = mask
+        key = (mask, tuple(ent["lwd"]), tuple(ent["w0"]), tuple(ent["w1"]), tuple(ent["o0"]), tuple(ent["o1"]))
+        if key not in self.wkey:
+            self.wkey[key] = len(self.weights)
+            self.weights.append(ent)
+        return self.wkey[key]
+
+    def _slice_motion(self):
+        """The slice's rc_h264_slice_motion fields: direct mode, co-located
+        picture, temporal-direct scale factors per refIdxL0 (as
+        SliceDecoder::new computes them) and the weight entry of every
+        (refIdxL0, refIdxL1) pair."""
+        h, lists = self.h, self.lists
+        b = h["type"] == 1
+        sm = {"b_slice": int(b), "direct_spatial": int(bool(h.get("direct_spatial"))),
+              "direct_8x8_inference": int(bool(self.sps["direct_8x8_inference"])), "col_slot": -1,
+              "col_short_term": 0, "dist_scale": [256] * 32, "direct_copy": [1] * 32, "wp_map": [0xFF] * (33 * 33)}
+        if b and lists[1]:
+            p1 = lists[1][0]
+            sm["col_slot"], sm["col_short_term"] = p1.slot, 1
+            for i, p0 in enumerate(lists[0][:32]):
                 tb = max(-128, min(127, self.frame.poc - p0.poc))
                 td = max(-128, min(127, p1.poc - p0.poc))
-                w0 = w1 = 32
                 if td != 0:
                     tx = (16384 + abs(int(td / 2))) // abs(td) * (1 if td > 0 else -1)
-                    dsf = max(-1024, min(1023, (tb * tx + 32) >> 6))
-                    if -64 <= (dsf >> 2) <= 128:
-                        w0, w1 = 64 - (dsf >> 2), dsf >> 2
-                ent = {"lwd": [5, 5, 5], "w0": [w0] * 3, "w1": [w1] * 3, "o0": [0] * 3, "o1": [0] * 3}
-            mask = 0
-            for comp in range(3):
-                unit0 = ent["w0"][comp] == 1 << ent["lwd"][comp] and ent["o0"][comp] == 0
-                unit1 = ent["w1"][comp] == 1 << ent["lwd"][comp] and ent["o1"][comp] == 0
-                plain = (unit0 or r0 < 0) and (unit1 or r1 < 0)
-                if not plain:
-                    mask |= 1 << comp
-            if mask == 0:
-                m.wp[b8] = 0xFF
-                continue
-            ent["mask"] = mask
-            key = (mask, tuple(ent["lwd"]), tuple(ent["w0"]), tuple(ent["w1"]), tuple(ent["o0"]), tuple(ent["o1"]))
-            if key not in self.wkey:
-                self.wkey[key] = len(self.weights)
-                self.weights.append(ent)
-            m.wp[b8] = self.wkey[key]
+                    sm["dist_scale"][i] = max(-1024, min(1023, (tb * tx + 32) >> 6))
+                    sm["direct_copy"][i] = 0
+        n0, n1 = len(lists[0]), len(lists[1])
+        for r0 in range(-1, min(n0, 32)):
+            for r1 in range(-1, min(n1, 32)):
+                sm["wp_map"][(r0 + 1) * 33 + (r1 + 1)] = self._wp_index(r0, r1)
+        return sm

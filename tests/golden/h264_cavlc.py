@@ -415,7 +415,7 @@ def residual_block(b: Bits, nc: int, max_coeff: int):
 # ---------------------------------------------------------------------------
 class _Mb:
     __slots__ = ("slice", "kind", "qp", "modes", "tc", "tcc", "ref", "mv", "cbp", "i16", "cmode", "levels",
-                 "dc", "luma_coded", "chroma_coded", "nz")
+                 "dc", "luma_coded", "chroma_coded", "nz", "shape", "subs", "mvd")
 
     def __init__(self):
         self.slice = -1
@@ -433,6 +433,9 @@ class _Mb:
         self.i16 = 0
         self.cmode = 0
         self.qp = 0
+        self.shape = 0            # motion syntax: RC_H264_MOTION_*
+        self.subs = [0] * 4       # P_8x8 sub-partitions (RC_H264_SUB_*)
+        self.mvd = [(0, 0)] * 16  # list-0 mvd per 4x4 (raster)
 
 
 class Frame:
@@ -502,6 +505,26 @@ class Decoder:
                 mx, my = m.mv[k] if m.kind in ("P", "SKIP") else (0, 0)
                 r.mv[0][k][0], r.mv[0][k][1] = mx, my
                 r.mv[1][k][0] = r.mv[1][k][1] = 0
+        # motion syntax (P slices: list 0 only, no direct modes, no weights)
+        mos = (E.H264Motion * len(self.mbs))()
+        for a, m in enumerate(self.mbs):
+            if m.kind not in ("P", "SKIP"):
+                continue
+            o = mos[a]
+            o.shape = m.shape
+            for i in range(4):
+                o.pred[i] = 1 if m.kind == "P" and (m.shape == 5 or i < (1 if m.shape == 2 else 2)) else 0
+                o.sub[i] = m.subs[i] if m.shape == 5 else 0
+            for b8 in range(4):
+                o.ref_idx[0][b8] = m.ref[(b8 >> 1) * 8 + (b8 & 1) * 2] if m.kind == "P" else -1
+                o.ref_idx[1][b8] = -1
+            for k in range(16):
+                o.mvd[0][k][0], o.mvd[0][k][1] = m.mvd[k] if m.kind == "P" else (0, 0)
+        smo = (E.H264SliceMotion * len(self.slices))()
+        for i in range(len(self.slices)):
+            smo[i].col_slot = -1
+            for j in range(33 * 33):
+                smo[i].wp_map[j] = 0xFF
         sl = (E.H264Slice * len(self.slices))()
         for i, s in enumerate(self.slices):
             sl[i].disable_deblocking_filter_idc = s["deblock_idc"]
@@ -515,6 +538,7 @@ class Decoder:
         import array
         lv = array.array("h", levels)
         self.pictures.append({"mbs": bytes(recs), "slices": bytes(sl), "weights": b"", "levels": lv.tobytes(),
+                              "motion": bytes(mos), "slice_motion": bytes(smo),
                               "num_slices": len(self.slices), "slot": self.cur_slot, "frame_id": self.count,
                               "constrained_intra": self.pps["constrained_intra"],
                               "mb_w": sps["mb_w"], "mb_h": sps["mb_h"], "crop": sps["crop"]})
@@ -668,6 +692,7 @@ class Decoder:
     def _skip(self, addr, qp):
         m = self.mbs[addr]
         m.slice, m.kind, m.qp = self.slice_id, "SKIP", qp
+        m.shape = 1  # RC_H264_MOTION_SKIP
         m.ref = [-1] * 16
         m.mv = [(0, 0)] * 16
         done = [False] * 16
@@ -786,14 +811,18 @@ class Decoder:
             parts = {0: [(0, 0, 16, 16)], 1: [(0, 0, 16, 8), (0, 8, 16, 8)], 2: [(0, 0, 8, 16), (8, 0, 8, 16)]}[t]
             shape = {0: "16x16", 1: "16x8", 2: "8x16"}[t]
             refs = [b.te(nref - 1) if nref > 1 else 0 for _ in parts]
+            m.shape = 2 + t
+            m.mvd = [(0, 0)] * 16
             for pi, (x, y, w, h) in enumerate(parts):
                 mvd = (b.se(), b.se())
                 p = self._mvp(addr, x, y, w, h, refs[pi], done, shape, pi)
                 mv = (p[0] + mvd[0], p[1] + mvd[1])
-                self._fill(m, done, x, y, w, h, refs[pi], mv)
+                self._fill(m, done, x, y, w, h, refs[pi], mv, mvd)
         else:
             subs = [b.ue() for _ in range(4)]
             refs = [b.te(nref - 1) if (nref > 1 and t == 3) else 0 for _ in range(4)]
+            m.shape, m.subs = 5, list(subs)
+            m.mvd = [(0, 0)] * 16
             for i8 in range(4):
                 x8, y8 = (i8 & 1) * 8, (i8 >> 1) * 8
                 st = subs[i8]
@@ -803,16 +832,16 @@ class Decoder:
                     mvd = (b.se(), b.se())
                     p = self._mvp(addr, x8 + x, y8 + y, w, h, refs[i8], done, "sub", 0)
                     mv = (p[0] + mvd[0], p[1] + mvd[1])
-                    self._fill(m, done, x8 + x, y8 + y, w, h, refs[i8], mv)
+                    self._fill(m, done, x8 + x, y8 + y, w, h, refs[i8], mv, mvd)
         cbp = _CBP[b.ue()][1]
         return self._residual(b, addr, cbp, qp)
 
     @staticmethod
-    def _fill(m, done, x, y, w, h, ref, mv):
+    def _fill(m, done, x, y, w, h, ref, mv, mvd):
         for yy in range(y >> 2, (y + h) >> 2):
             for xx in range(x >> 2, (x + w) >> 2):
                 k = yy * 4 + xx
-                m.ref[k], m.mv[k], done[k] = ref, mv, True
+                m.ref[k], m.mv[k], m.mvd[k], done[k] = ref, mv, mvd, True
 
     # ---- residual (7.3.5.3), levels stored as the engine's payload
     def _residual(self, b: Bits, addr: int, cbp: int, qp: int) -> int:

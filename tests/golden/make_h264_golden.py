@@ -9,9 +9,13 @@ the reference's manifest (tests/refs/h264/manifest.toml, the "<name>.yuv"
 entry of kind bit-exact: the reconstruction x264 dumped while encoding).
 The digest covers every picture in output order (picture order count within
 each IDR period), each cropped, Y then Cb then Cr row by row (the
-Digest::frame of src/testref.rs:570-578).  Writes the records, each
-picture's DPB slot, POC and crop, and the expected digest; the tests replay
-them through the oracle and the engine.  Run where a checkout of the
+Digest::frame of src/testref.rs:570-578).  The oracle must reproduce it
+twice: from the records with their resolved motion vectors, and from the
+motion syntax alone (rc_h264_motion / rc_h264_slice_motion: partitions,
+parsed ref_idx and mvd, direct modes), deriving every vector itself.
+Writes the records, the motion syntax, each picture's DPB slot, POC and
+crop, and the expected digest; the tests replay them through the oracle and
+the engine.  Run where a checkout of the
 reference exists, naming its root with --reference or the PITO_REFERENCE
 environment variable:
 
@@ -37,6 +41,9 @@ sys.path.insert(0, str(HERE))
 
 STREAMS = {"baseline": "cavlc", "main_cabac_b": "cabac", "high_bpyramid": "cabac", "high_crop_slices": "cabac"}
 KEYS = ("mbs", "slices", "weights", "levels", "scaling4", "scaling8")
+# motion syntax (rc_h264_picture.motion / slice_motion): with it the oracle
+# and the engine derive every vector themselves
+MOTION_KEYS = ("motion", "slice_motion")
 DPB_SLOTS = 16
 REFS = None  # <reference checkout>/tests/refs/h264, set by main()
 
@@ -87,27 +94,29 @@ def main(names):
         data = (REFS / f"{name}.h264").read_bytes()
         pics = parse(E, name, data)
         want = manifest_digest(name)
-        dpb = O.H264Dpb(pics[0]["mb_w"], pics[0]["mb_h"], DPB_SLOTS)
+        for keys, how in ((KEYS, "resolved motion"), (KEYS + MOTION_KEYS, "motion derived from syntax")):
+            dpb = O.H264Dpb(pics[0]["mb_w"], pics[0]["mb_h"], DPB_SLOTS)
 
-        def planes_after(i):
-            p = pics[i]
-            buf = E.PictureBuffers({k: p[k] for k in KEYS}, p["num_slices"], p["num_weights"],
-                                   p["constrained_intra"], p["frame_id"])
-            if dpb.recon(buf.ptr, p["slot"]) != 0:
-                raise RuntimeError("oracle rejected a parsed picture")
-            return cropped(dpb.planes(p["slot"]), p["crop"])
+            def planes_after(i):
+                p = pics[i]
+                buf = E.PictureBuffers({k: p[k] for k in keys}, p["num_slices"], p["num_weights"],
+                                       p["constrained_intra"], p["frame_id"])
+                if dpb.recon(buf.ptr, p["slot"]) != 0:
+                    raise RuntimeError("oracle rejected a parsed picture")
+                return cropped(dpb.planes(p["slot"]), p["crop"])
 
-        got = output_digest(pics, planes_after)
-        print(f"{name}: {len(pics)} pictures, oracle {got}, reference {want}: {'MATCH' if got == want else 'DIFFER'}")
-        if got != want:
-            raise SystemExit(1)
+            got = output_digest(pics, planes_after)
+            print(f"{name} ({how}): {len(pics)} pictures, oracle {got}, reference {want}: "
+                  f"{'MATCH' if got == want else 'DIFFER'}")
+            if got != want:
+                raise SystemExit(1)
         arrays = {}
         meta = {"stream": f"tests/refs/h264/{name}.h264", "stream_sha256": hashlib.sha256(data).hexdigest(),
                 "expected_sha256": want,
                 "expected_source": f"tests/refs/h264/manifest.toml [[ref]] {name}.yuv (kind bit-exact)",
                 "pictures": []}
         for i, p in enumerate(pics):
-            for k in KEYS:
+            for k in KEYS + MOTION_KEYS:
                 arrays[f"{k}_{i}"] = np.frombuffer(p[k], np.uint8)
             meta["pictures"].append({k: p[k] for k in ("num_slices", "num_weights", "slot", "frame_id",
                                                         "constrained_intra", "mb_w", "mb_h", "crop", "poc",

@@ -39,7 +39,7 @@ def test_struct_sizes_match_header(engine):
     assert ctypes.sizeof(engine.H264Mb) == 176
     assert ctypes.sizeof(engine.H264Slice) == 4 * (5 + 64 + 64)
     assert ctypes.sizeof(engine.H264Weight) == 64
-    assert ctypes.sizeof(engine.H264Picture) == 80
+    assert ctypes.sizeof(engine.H264Picture) == 96
 
 
 def _mutate(engine, pic, fn):

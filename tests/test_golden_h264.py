@@ -18,6 +18,11 @@ the C ABI) must both reproduce it.
                     direct, explicit weights, 4 references
   high_crop_slices  High, JVT scaling matrices (PPS, fall-back rule A), 4
                     slices, B pictures, 238x158 cropped from 240x160
+
+Every fixture also holds each picture's motion syntax (partitions, parsed
+ref_idx and mvd, direct modes, per-slice direct and weight tables); the
+"derived" cases reconstruct from it, the vectors derived by the oracle (CPU)
+or by the engine's h264_mv_kernel (GPU).
 """
 from __future__ import annotations
 
@@ -36,15 +41,18 @@ EXPECTED = {
     "high_crop_slices": "6da5d2d112e7128e7a88af29d226fc4c300a95c4b795f0d0162ee9053fb901fc",
 }
 KEYS = ("mbs", "slices", "weights", "levels", "scaling4", "scaling8")
+MOTION_KEYS = ("motion", "slice_motion")
 DPB_SLOTS = 16
 
 
-def load_fixture(engine, name):
+def load_fixture(engine, name, motion=False):
+    """The fixture's pictures; motion=True attaches the motion syntax, so
+    that the oracle and the engine derive every vector themselves."""
     z = np.load(GOLDEN / f"h264_{name}.npz")
     meta = json.loads(bytes(z["meta"]).decode())
     pics = []
     for i, m in enumerate(meta["pictures"]):
-        bufs = {k: z[f"{k}_{i}"].tobytes() for k in KEYS}
+        bufs = {k: z[f"{k}_{i}"].tobytes() for k in KEYS + (MOTION_KEYS if motion else ())}
         pics.append((m, engine.PictureBuffers(bufs, m["num_slices"], m["num_weights"], m["constrained_intra"],
                                               m["frame_id"])))
     return meta, pics
@@ -78,9 +86,13 @@ def test_every_fixture_is_a_reference_stream():
         assert meta["expected_sha256"] == want and meta["stream"] == f"tests/refs/h264/{name}.h264"
 
 
+@pytest.mark.parametrize("motion", [False, True], ids=["resolved", "derived"])
 @pytest.mark.parametrize("name", sorted(EXPECTED))
-def test_oracle_reproduces_reference_digest(engine, oracle, name):
-    meta, pics = load_fixture(engine, name)
+def test_oracle_reproduces_reference_digest(engine, oracle, name, motion):
+    """Resolved: the records' own vectors.  Derived: the vectors the oracle
+    derives from the motion syntax (MV prediction, P_Skip, B direct spatial
+    and temporal from the co-located picture, weight entries)."""
+    meta, pics = load_fixture(engine, name, motion)
     m0 = meta["pictures"][0]
     dpb = oracle.H264Dpb(m0["mb_w"], m0["mb_h"], DPB_SLOTS)
 
