@@ -427,7 +427,8 @@ int rc_picture_device_planes(rc_stream *s, int slot, void **y, void **u,
 #define RC_KERNEL_HEVC_DEBLOCK 6
 #define RC_KERNEL_HEVC_SAO 7
 #define RC_KERNEL_H264_GROUP 8
-#define RC_KERNEL_COUNT 9
+#define RC_KERNEL_H264_MV 9
+#define RC_KERNEL_COUNT 10
 int rc_stream_profile(rc_stream *s, int enable);
 /* Schedule knob for many streams sharing one GPU: the HEVC intra kernel's
  * persistent CTAs per launch (default: about one per two 64x64 CTBs, at

@@ -278,6 +278,386 @@ __global__ void __launch_bounds__(32 * EDGE_MBS) h264_edge_kernel(H264Launch P) 
 }
 
 // ===========================================================================
+// Kernel 0: motion derived from syntax (rc_h264_motion), one thread per MB row
+// ===========================================================================
+// The reference derives an MB's vectors as its slice decoder parses it
+// (src/h264/dec/slicedec.rs): nb_motion :581-621, mvp :635-662, median_pred
+// :664-681, set_motion :683-716, colocated :718-731, spatial_direct_base
+// :733-752, derive_direct :754-852, derive_p_skip :854-866,
+// derive_inter_motion :868-935.  An MB reads the derived motion of its
+// left, top, top-right and top-left neighbours, so the rows run as a
+// wavefront: thread y derives row y left to right, MB x once row y-1 has
+// derived MBs 0..x+1.  The rows hand over through shared-memory progress;
+// the motion itself is written to the engine's records (global memory, read
+// back by the same CTA) and the picture's co-located motion to its slot.
+struct ColMb {  // co-located motion of one MB (Frame::publish, picture.rs:492)
+    uint8_t intra;
+    uint8_t pad[3];
+    int8_t ref_idx[2][4];
+    uint32_t ref_id[2][4];
+    int16_t mv[2][16][2];
+};
+static_assert(sizeof(ColMb) == RC_COLMB_BYTES, "co-located motion layout");
+
+struct MvNb {
+    int avail, ref, mvx, mvy;
+};
+
+struct MvState {
+    const H264Launch *P;
+    int addr;
+    int nb[4];  // A, B, C, D MB addresses or -1
+    uint32_t done;
+    int8_t ref[2][4];
+    int16_t mv[2][16][2];
+    const rc_h264_slice *sl;
+    const rc_h264_slice_motion *sm;
+    const ColMb *col;
+};
+
+__device__ MvNb mv_nb(const MvState &S, int l, int x, int y) {
+    const MvNb na = {0, -1, 0, 0};
+    int mb, bx, by;
+    if (x < 0) {
+        if (y < 0) { mb = S.nb[3]; bx = 3; by = 3; }
+        else if (y > 3) return na;
+        else { mb = S.nb[0]; bx = 3; by = y; }
+    } else if (x > 3) {
+        if (y < 0) { mb = S.nb[2]; bx = 0; by = 3; }
+        else return na;
+    } else if (y < 0) {
+        mb = S.nb[1]; bx = x; by = 3;
+    } else {
+        if (!(S.done >> (y * 4 + x) & 1)) return na;
+        const int r = S.ref[l][(y >> 1) * 2 + (x >> 1)];
+        if (r < 0) return {1, -1, 0, 0};
+        return {1, r, S.mv[l][y * 4 + x][0], S.mv[l][y * 4 + x][1]};
+    }
+    if (mb < 0) return na;
+    const rc_h264_mb *m = S.P->mbs_out + mb;
+    const int r = m->ref_idx[l][(by >> 1) * 2 + (bx >> 1)];
+    if (r < 0) return {1, -1, 0, 0};
+    return {1, r, m->mv[l][by * 4 + bx][0], m->mv[l][by * 4 + bx][1]};
+}
+
+__device__ void mv_abc(const MvState &S, int l, int x, int y, int w, MvNb &a, MvNb &b, MvNb &c) {
+    a = mv_nb(S, l, x - 1, y);
+    b = mv_nb(S, l, x, y - 1);
+    c = mv_nb(S, l, x + w, y - 1);
+    if (!c.avail) c = mv_nb(S, l, x - 1, y - 1);
+}
+
+__device__ __forceinline__ int med3(int a, int b, int c) { return max(min(a, b), min(max(a, b), c)); }
+
+__device__ void mv_median(MvNb a, MvNb b, MvNb c, int ref, int &ox, int &oy) {
+    if (!b.avail && !c.avail && a.avail) {
+        b = a;
+        c = a;
+    }
+    const bool ma = a.ref == ref, mb = b.ref == ref, mc = c.ref == ref;
+    if (ma && !mb && !mc) { ox = a.mvx; oy = a.mvy; return; }
+    if (!ma && mb && !mc) { ox = b.mvx; oy = b.mvy; return; }
+    if (!ma && !mb && mc) { ox = c.mvx; oy = c.mvy; return; }
+    ox = med3(a.mvx, b.mvx, c.mvx);
+    oy = med3(a.mvy, b.mvy, c.mvy);
+}
+
+// shape 1: 16x8, 2: 8x16 (directional predictors); x, y, w in 4x4 blocks
+__device__ void mv_pred(const MvState &S, int l, int x, int y, int w, int ref, int shape, int part, int &ox, int &oy) {
+    MvNb a, b, c;
+    mv_abc(S, l, x, y, w, a, b, c);
+    if (shape == 1) {
+        if (part == 0 && b.ref == ref) { ox = b.mvx; oy = b.mvy; return; }
+        if (part == 1 && a.ref == ref) { ox = a.mvx; oy = a.mvy; return; }
+    } else if (shape == 2) {
+        if (part == 0 && a.ref == ref) { ox = a.mvx; oy = a.mvy; return; }
+        if (part == 1 && c.ref == ref) { ox = c.mvx; oy = c.mvy; return; }
+    }
+    mv_median(a, b, c, ref, ox, oy);
+}
+
+__device__ void mv_set(MvState &S, int x, int y, int w, int h, const int refs[2], const int mvs[2][2]) {
+    for (int l = 0; l < 2; l++) {
+        const int16_t mx = refs[l] >= 0 ? (int16_t)mvs[l][0] : 0, my = refs[l] >= 0 ? (int16_t)mvs[l][1] : 0;
+        for (int yy = y; yy < y + h; yy++)
+            for (int xx = x; xx < x + w; xx++) {
+                S.mv[l][yy * 4 + xx][0] = mx;
+                S.mv[l][yy * 4 + xx][1] = my;
+            }
+        for (int by = y >> 1; by <= (y + h - 1) >> 1; by++)
+            for (int bx = x >> 1; bx <= (x + w - 1) >> 1; bx++) S.ref[l][by * 2 + bx] = (int8_t)refs[l];
+    }
+    for (int yy = y; yy < y + h; yy++)
+        for (int xx = x; xx < x + w; xx++) S.done |= 1u << (yy * 4 + xx);
+}
+
+__device__ void mv_colocated(const MvState &S, int raster, int &mvx, int &mvy, int &ref, uint32_t &id) {
+    if (S.sm->direct_8x8_inference) raster = ((raster >> 2) >= 2 ? 12 : 0) + ((raster & 3) >= 2 ? 3 : 0);
+    const ColMb *m = S.col;
+    if (!m || m->intra) {
+        mvx = mvy = 0;
+        ref = -1;
+        id = 0xffffffffu;
+        return;
+    }
+    const int b8 = (raster >> 3) * 2 + ((raster & 3) >> 1);
+    const int l = m->ref_idx[0][b8] >= 0 ? 0 : 1;
+    mvx = m->mv[l][raster][0];
+    mvy = m->mv[l][raster][1];
+    ref = m->ref_idx[l][b8];
+    id = m->ref_id[l][b8];
+}
+
+__device__ __forceinline__ int min_pos(int x, int y) { return (x >= 0 && y >= 0) ? min(x, y) : max(x, y); }
+__device__ __forceinline__ bool small_mv(int x, int y) { return x >= -1 && x <= 1 && y >= -1 && y <= 1; }
+__device__ __forceinline__ int wrap16(int v) { return (int)(int16_t)(uint16_t)(v & 0xffff); }
+
+__device__ void mv_direct(MvState &S, int b8_mask) {
+    const int spatial = S.sm->direct_spatial, d8i = S.sm->direct_8x8_inference;
+    int base_refs[2] = {0, 0}, base_mvs[2][2] = {{0, 0}, {0, 0}};
+    bool direct_zero = false;
+    if (spatial) {
+        MvNb nbs[2][3];
+        for (int l = 0; l < 2; l++) {
+            mv_abc(S, l, 0, 0, 4, nbs[l][0], nbs[l][1], nbs[l][2]);
+            base_refs[l] = min_pos(nbs[l][0].ref, min_pos(nbs[l][1].ref, nbs[l][2].ref));
+        }
+        if (base_refs[0] < 0 && base_refs[1] < 0) {
+            base_refs[0] = base_refs[1] = 0;
+            direct_zero = true;
+        } else {
+            for (int l = 0; l < 2; l++)
+                if (base_refs[l] >= 0) mv_median(nbs[l][0], nbs[l][1], nbs[l][2], base_refs[l], base_mvs[l][0], base_mvs[l][1]);
+        }
+    }
+    const bool cst = S.sm->col_short_term != 0;
+    const bool need_col = !direct_zero && cst && (base_refs[0] == 0 || base_refs[1] == 0);
+    if (spatial && (!need_col || d8i)) {
+        for (int b8 = 0; b8 < 4; b8++) {
+            if (!(b8_mask >> b8 & 1)) continue;
+            bool zero = false;
+            if (need_col) {
+                int cx, cy, r;
+                uint32_t id;
+                mv_colocated(S, (b8 >> 1) * 8 + (b8 & 1) * 2, cx, cy, r, id);
+                zero = r == 0 && small_mv(cx, cy);
+            }
+            int mvs[2][2];
+            for (int l = 0; l < 2; l++) {
+                const bool z = direct_zero || base_refs[l] < 0 || (base_refs[l] == 0 && zero);
+                mvs[l][0] = z ? 0 : base_mvs[l][0];
+                mvs[l][1] = z ? 0 : base_mvs[l][1];
+            }
+            mv_set(S, (b8 & 1) * 2, (b8 >> 1) * 2, 2, 2, base_refs, mvs);
+        }
+        return;
+    }
+    for (int b8 = 0; b8 < 4; b8++) {
+        if (!(b8_mask >> b8 & 1)) continue;
+        const int x8 = (b8 & 1) * 2, y8 = (b8 >> 1) * 2, unit = d8i ? 2 : 1;
+        for (int sub = 0; sub < (unit == 1 ? 4 : 1); sub++) {
+            const int x = x8 + (sub & 1), y = y8 + (sub >> 1);
+            int cx, cy, rc;
+            uint32_t idc;
+            mv_colocated(S, y * 4 + x, cx, cy, rc, idc);
+            int refs[2], mvs[2][2];
+            if (spatial) {
+                const bool col_zero = cst && rc == 0 && small_mv(cx, cy);
+                for (int l = 0; l < 2; l++) {
+                    const bool z = direct_zero || base_refs[l] < 0 || (base_refs[l] == 0 && col_zero);
+                    mvs[l][0] = z ? 0 : base_mvs[l][0];
+                    mvs[l][1] = z ? 0 : base_mvs[l][1];
+                    refs[l] = base_refs[l];
+                }
+            } else {
+                const int n0 = min(__ldg(&S.sl->num_ref[0]), RC_H264_MAX_REFS);
+                int ref0 = 0;
+                if (rc >= 0)
+                    for (int i = 0; i < n0; i++)
+                        if (__ldg(&S.sl->ref_id[0][i]) == idc) { ref0 = i; break; }
+                const bool copy = ref0 < n0 ? S.sm->direct_copy[ref0] != 0 : true;
+                const int dsf = ref0 < n0 ? S.sm->dist_scale[ref0] : 256;
+                if (copy) {
+                    mvs[0][0] = cx; mvs[0][1] = cy;
+                    mvs[1][0] = mvs[1][1] = 0;
+                } else {
+                    mvs[0][0] = (int16_t)((dsf * cx + 128) >> 8);
+                    mvs[0][1] = (int16_t)((dsf * cy + 128) >> 8);
+                    mvs[1][0] = wrap16(mvs[0][0] - cx);
+                    mvs[1][1] = wrap16(mvs[0][1] - cy);
+                }
+                refs[0] = ref0;
+                refs[1] = 0;
+            }
+            mv_set(S, x, y, unit, unit, refs, mvs);
+        }
+    }
+}
+
+// One inter MB's motion; false for a record the reference rejects (ref_idx
+// past its list, a direct sub-partition outside a B slice).
+__device__ bool mv_derive(MvState &S, const rc_h264_motion &mo) {
+    const int n[2] = {min(__ldg(&S.sl->num_ref[0]), RC_H264_MAX_REFS), min(__ldg(&S.sl->num_ref[1]), RC_H264_MAX_REFS)};
+    if (mo.shape == RC_H264_MOTION_SKIP) {
+        if (S.sm->b_slice) {
+            mv_direct(S, 0xf);
+            return true;
+        }
+        if (n[0] < 1) return false;
+        const MvNb a = mv_nb(S, 0, -1, 0), b = mv_nb(S, 0, 0, -1);
+        int mvs[2][2] = {{0, 0}, {0, 0}};
+        if (!(S.nb[0] < 0 || S.nb[1] < 0 || (a.ref == 0 && a.mvx == 0 && a.mvy == 0) ||
+              (b.ref == 0 && b.mvx == 0 && b.mvy == 0)))
+            mv_pred(S, 0, 0, 0, 4, 0, 0, 0, mvs[0][0], mvs[0][1]);
+        const int refs[2] = {0, -1};
+        mv_set(S, 0, 0, 4, 4, refs, mvs);
+        return true;
+    }
+    if (mo.shape != RC_H264_MOTION_8x8) {
+        const int np = mo.shape == RC_H264_MOTION_16x16 ? 1 : 2;
+        const int shape = mo.shape == RC_H264_MOTION_16x8 ? 1 : mo.shape == RC_H264_MOTION_8x16 ? 2 : 0;
+        for (int p = 0; p < np; p++) {
+            const int x = shape == 2 ? 2 * p : 0, y = shape == 1 ? 2 * p : 0;
+            const int w = shape == 2 ? 2 : 4, h = shape == 1 ? 2 : 4, b8 = (y >> 1) * 2 + (x >> 1);
+            int refs[2] = {-1, -1}, mvs[2][2] = {{0, 0}, {0, 0}};
+            for (int l = 0; l < 2; l++) {
+                if (!(mo.pred[p] >> l & 1)) continue;
+                const int r = mo.ref_idx[l][b8];
+                if (r < 0 || r >= n[l]) return false;
+                int px, py;
+                mv_pred(S, l, x, y, w, r, shape, p, px, py);
+                refs[l] = r;
+                mvs[l][0] = wrap16(px + mo.mvd[l][y * 4 + x][0]);
+                mvs[l][1] = wrap16(py + mo.mvd[l][y * 4 + x][1]);
+            }
+            mv_set(S, x, y, w, h, refs, mvs);
+        }
+        return true;
+    }
+    for (int p = 0; p < 4; p++) {
+        const int x8 = (p & 1) * 2, y8 = (p >> 1) * 2, sub = mo.sub[p];
+        if (sub == RC_H264_SUB_DIRECT) {
+            if (!S.sm->b_slice) return false;
+            mv_direct(S, 1 << p);
+            continue;
+        }
+        if (sub > RC_H264_SUB_4x4) return false;
+        int refs[2] = {-1, -1};
+        for (int l = 0; l < 2; l++) {
+            if (!(mo.pred[p] >> l & 1)) continue;
+            const int v = mo.ref_idx[l][p];
+            if (v < 0 || v >= n[l]) return false;
+            refs[l] = v;
+        }
+        const int sw = (sub == RC_H264_SUB_8x8 || sub == RC_H264_SUB_8x4) ? 2 : 1;
+        const int sh = (sub == RC_H264_SUB_8x8 || sub == RC_H264_SUB_4x8) ? 2 : 1;
+        for (int sy = 0; sy < 2; sy += sh)
+            for (int sx = 0; sx < 2; sx += sw) {
+                const int x = x8 + sx, y = y8 + sy;
+                int mvs[2][2] = {{0, 0}, {0, 0}};
+                for (int l = 0; l < 2; l++) {
+                    if (refs[l] < 0) continue;
+                    int px, py;
+                    mv_pred(S, l, x, y, sw, refs[l], 0, 0, px, py);
+                    mvs[l][0] = wrap16(px + mo.mvd[l][y * 4 + x][0]);
+                    mvs[l][1] = wrap16(py + mo.mvd[l][y * 4 + x][1]);
+                }
+                mv_set(S, x, y, sw, sh, refs, mvs);
+            }
+    }
+    return true;
+}
+
+constexpr int MV_MAX_ROWS = 1024;
+
+__global__ void __launch_bounds__(MV_MAX_ROWS) h264_mv_kernel(const __grid_constant__ H264Launch P) {
+    __shared__ volatile int prog[MV_MAX_ROWS];  // MBs of row y derived
+    const int y = threadIdx.x;
+    if (y < P.mb_h) prog[y] = 0;
+    __syncthreads();
+    if (y >= P.mb_h) return;
+    const int n_mb = P.mb_w * P.mb_h;
+    ColMb *out = (ColMb *)(P.col + (size_t)P.out_slot * P.col_stride);
+    MvState S;
+    S.P = &P;
+    uint32_t seen_above = y > 0 ? 0 : (uint32_t)P.mb_w;
+    for (int x = 0; x < P.mb_w; x++) {
+        const int addr = y * P.mb_w + x;
+        // row y-1 through MB x+1 (the top-right neighbour)
+        const int need = min(x + 2, P.mb_w);
+        if ((int)seen_above < need) {
+            uint32_t it = 0, ns = 32;
+            int v;
+            while ((v = prog[y - 1]) < need) {
+                if (++it > P.wait_limit || ((it & 63) == 0 && aborted(P.error))) {
+                    set_error(P.error, RC_DEV_ERR_TIMEOUT);
+                    prog[y] = P.mb_w;
+                    return;
+                }
+                __nanosleep(ns);
+                ns = min(ns * 2, 256u);
+            }
+            seen_above = (uint32_t)v;
+            __threadfence_block();
+        }
+        rc_h264_mb *m = P.mbs_out + addr;
+        const int kind = m->kind, slice = m->slice;
+        ColMb *o = out + addr;
+        bool inter = kind == RC_H264_INTER && slice < P.num_slices;
+        if (kind == RC_H264_INTER && !inter) set_error(P.error, RC_DEV_ERR_RECORD);
+        for (int l = 0; l < 2; l++)
+            for (int b8 = 0; b8 < 4; b8++) S.ref[l][b8] = -1;
+        for (int l = 0; l < 2; l++)
+            for (int k = 0; k < 16; k++) S.mv[l][k][0] = S.mv[l][k][1] = 0;
+        if (inter) {
+            S.addr = addr;
+            S.done = 0;
+            S.sl = P.slices + slice;
+            S.sm = P.smotion + slice;
+            const int dx[4] = {-1, 0, 1, -1}, dy[4] = {0, -1, -1, -1};
+            for (int i = 0; i < 4; i++) {
+                const int nx = x + dx[i], ny = y + dy[i], na = ny * P.mb_w + nx;
+                S.nb[i] = (nx >= 0 && ny >= 0 && nx < P.mb_w && P.mbs_out[na].kind != RC_H264_NONE &&
+                           P.mbs_out[na].slice == slice)
+                              ? na
+                              : -1;
+            }
+            S.col = nullptr;
+            const int cs = S.sm->col_slot;
+            if (S.sm->b_slice) {
+                if (cs >= 0 && cs < P.dpb_slots) S.col = (const ColMb *)(P.col + (size_t)cs * P.col_stride) + addr;
+                else set_error(P.error, RC_DEV_ERR_RECORD);
+            }
+            if (!mv_derive(S, P.motion[addr])) {
+                set_error(P.error, RC_DEV_ERR_RECORD);
+                for (int l = 0; l < 2; l++)
+                    for (int b8 = 0; b8 < 4; b8++) S.ref[l][b8] = -1;
+            }
+        }
+        // the MB's motion into the records and the co-located store
+        for (int l = 0; l < 2; l++) {
+            for (int b8 = 0; b8 < 4; b8++) {
+                m->ref_idx[l][b8] = S.ref[l][b8];
+                o->ref_idx[l][b8] = S.ref[l][b8];
+                const int r = S.ref[l][b8];
+                o->ref_id[l][b8] = r >= 0 ? __ldg(&P.slices[slice].ref_id[l][r]) : 0xffffffffu;
+            }
+            for (int k = 0; k < 16; k++) {
+                m->mv[l][k][0] = o->mv[l][k][0] = S.mv[l][k][0];
+                m->mv[l][k][1] = o->mv[l][k][1] = S.mv[l][k][1];
+            }
+        }
+        for (int b8 = 0; b8 < 4; b8++)
+            m->wp[b8] = inter ? P.smotion[slice].wp_map[(S.ref[0][b8] + 1) * (RC_H264_MAX_REFS + 1) + (S.ref[1][b8] + 1)]
+                              : (uint8_t)0xff;
+        o->intra = !inter;
+        __threadfence_block();
+        prog[y] = x + 1;
+    }
+    (void)n_mb;
+}
+
+// ===========================================================================
 // Kernel 1: inter MBs (prediction + residual) and I_PCM, one CTA per MB.
 // ===========================================================================
 // Group launches: before an inter MB is predicted, the rows of the in-flight
@@ -2332,6 +2712,13 @@ __global__ void __launch_bounds__(GROUP_THREADS, 1) h264_group_kernel(const __gr
 void rc_launch_h264_edge(const H264Launch &p, cudaStream_t st) {
     const int n = p.mb_w * p.mb_h;
     h264_edge_kernel<<<(n + EDGE_MBS - 1) / EDGE_MBS, 32 * EDGE_MBS, 0, st>>>(p);
+}
+
+int rc_launch_h264_mv(const H264Launch &p, cudaStream_t st) {
+    if (p.mb_h > MV_MAX_ROWS) return -1;
+    const int threads = (p.mb_h + 31) / 32 * 32;
+    h264_mv_kernel<<<1, threads, 0, st>>>(p);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
 void rc_launch_h264_mb(const H264Launch &p, cudaStream_t st) {

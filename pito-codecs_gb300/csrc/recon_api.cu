@@ -106,6 +106,13 @@ struct rc_stream {
     int w4 = 0, h4 = 0, log2ctb_alloc = 0;
     int bps = 1;
     DevBuf mbs[REC_SETS], slices[REC_SETS], weights[REC_SETS], levels[REC_SETS];
+    // motion derived from syntax: the syntax per record set, the co-located
+    // motion store (one entry per MB and DPB slot, allocated on first use)
+    // and which slots hold stored motion
+    DevBuf motion[REC_SETS], smotion[REC_SETS];
+    uint8_t *col = nullptr;
+    std::vector<char> slot_col;
+    cudaEvent_t mv_ready = nullptr;
     // H.264 picture groups (rc_stream_set_h264_group): pictures per launch,
     // the launch's CTAs, the submitted pictures not yet launched (with the
     // DPB slots they read and their record sets), and per group position the
@@ -251,6 +258,62 @@ bool is_pinned(const void *p) {
 struct Geo {
     int mb_w, mb_h, slots;
 };
+// Motion syntax (rc_h264_motion, rc_h264_slice_motion): what the kernel
+// rejects as a record error, rejected before launch (ref_idx past its list,
+// direct modes outside B slices, unknown shapes), and weight entries that
+// exist.  Whether the co-located slot holds stored motion is checked by the
+// submit, which knows the stream's slots.
+int validate_h264_motion(const Geo *s, const rc_h264_picture *p) {
+    if (!p->slice_motion) return RC_EINVAL;
+    for (int i = 0; i < p->num_slices; i++) {
+        const rc_h264_slice_motion &sm = p->slice_motion[i];
+        const rc_h264_slice &sl = p->slices[i];
+        if ((sm.b_slice != 0 && sm.b_slice != 1) || (sm.b_slice && (sm.col_slot < 0 || sm.col_slot >= s->slots)))
+            return RC_EINVAL;
+        for (int r0 = -1; r0 < sl.num_ref[0]; r0++)
+            for (int r1 = -1; r1 < sl.num_ref[1]; r1++) {
+                const int w = sm.wp_map[(r0 + 1) * (RC_H264_MAX_REFS + 1) + (r1 + 1)];
+                if (w != 0xff && w >= p->num_weights) return RC_EINVAL;
+            }
+    }
+    const int n = s->mb_w * s->mb_h;
+    for (int a = 0; a < n; a++) {
+        const rc_h264_mb &m = p->mbs[a];
+        const rc_h264_motion &mo = p->motion[a];
+        const bool inter = m.kind == RC_H264_INTER;
+        if (inter != (mo.shape != RC_H264_MOTION_NONE) || mo.shape > RC_H264_MOTION_8x8) return RC_EINVAL;
+        if (!inter) continue;
+        const rc_h264_slice &sl = p->slices[m.slice];
+        const bool b = p->slice_motion[m.slice].b_slice != 0;
+        auto ref_ok = [&](int l, int r) { return r >= 0 && r < sl.num_ref[l]; };
+        if (mo.shape == RC_H264_MOTION_SKIP) {
+            if (!b && sl.num_ref[0] < 1) return RC_EINVAL;
+            continue;
+        }
+        if (mo.shape != RC_H264_MOTION_8x8) {
+            const int np = mo.shape == RC_H264_MOTION_16x16 ? 1 : 2;
+            for (int q = 0; q < np; q++) {
+                const int b8 = mo.shape == RC_H264_MOTION_16x8 ? 2 * q : q;
+                if (mo.pred[q] < 1 || mo.pred[q] > 3 || (!b && mo.pred[q] != 1)) return RC_EINVAL;
+                for (int l = 0; l < 2; l++)
+                    if ((mo.pred[q] >> l & 1) && !ref_ok(l, mo.ref_idx[l][b8])) return RC_EINVAL;
+            }
+            continue;
+        }
+        for (int q = 0; q < 4; q++) {
+            if (mo.sub[q] == RC_H264_SUB_DIRECT) {
+                if (!b) return RC_EINVAL;
+                continue;
+            }
+            if (mo.sub[q] > RC_H264_SUB_4x4 || mo.pred[q] < 1 || mo.pred[q] > 3 || (!b && mo.pred[q] != 1))
+                return RC_EINVAL;
+            for (int l = 0; l < 2; l++)
+                if ((mo.pred[q] >> l & 1) && !ref_ok(l, mo.ref_idx[l][q])) return RC_EINVAL;
+        }
+    }
+    return 0;
+}
+
 int validate_h264(const Geo *s, const rc_h264_picture *p) {
     if (!p->mbs || p->num_slices <= 0 || !p->slices) return RC_EINVAL;
     if (p->num_weights < 0 || (p->num_weights > 0 && !p->weights)) return RC_EINVAL;
@@ -276,7 +339,7 @@ int validate_h264(const Geo *s, const rc_h264_picture *p) {
             continue;
         }
         if ((m.kind == RC_H264_I8x8) != (m.transform_8x8 != 0) && m.kind != RC_H264_INTER) return RC_EINVAL;
-        if (m.kind == RC_H264_INTER) {
+        if (m.kind == RC_H264_INTER && !p->motion) {  // with motion syntax, the motion is derived (below)
             const rc_h264_slice &sl = p->slices[m.slice];
             for (int b = 0; b < 4; b++) {
                 int r0 = m.ref_idx[0][b], r1 = m.ref_idx[1][b];
@@ -295,7 +358,7 @@ int validate_h264(const Geo *s, const rc_h264_picture *p) {
                       (size_t)__builtin_popcount(m.dc_coded & 6) * 4 + (size_t)__builtin_popcount(m.chroma_coded) * 16;
         if ((size_t)m.coef_off + need > p->num_levels) return RC_EINVAL;
     }
-    return 0;
+    return p->motion ? validate_h264_motion(s, p) : 0;
 }
 
 void group_free(rc_stream *s) {
@@ -378,7 +441,10 @@ void destroy(rc_stream *s) {
     for (int i = 0; i < 2; i++)
         for (DevBuf *b : {&s->ctbs[i], &s->blk[i], &s->mvf[i], &s->tus[i], &s->hslices[i]}) dev_free(s, b->p, b->cap);
     for (int i = 0; i < REC_SETS; i++)
-        for (DevBuf *b : {&s->mbs[i], &s->slices[i], &s->weights[i], &s->levels[i]}) dev_free(s, b->p, b->cap);
+        for (DevBuf *b : {&s->mbs[i], &s->slices[i], &s->weights[i], &s->levels[i], &s->motion[i], &s->smotion[i]})
+            dev_free(s, b->p, b->cap);
+    dev_free(s, s->col, (size_t)s->slots * s->mb_w * s->mb_h * RC_COLMB_BYTES);
+    if (s->mv_ready) cudaEventDestroy(s->mv_ready);
     group_free(s);
     dev_free(s, s->scaling.p, s->scaling.cap);
     cudaFree(s->work);
@@ -823,6 +889,8 @@ int rc_stream_create(int codec, int width, int height, int bit_depth, int dpb_sl
     for (int i = 0; i < 2 && ok; i++) ok = cudaEventCreateWithFlags(&s->aux_used[i], cudaEventDisableTiming) == cudaSuccess;
     s->slot_dl.assign(s->slots, nullptr);
     s->slot_dl_pending.assign(s->slots, 0);
+    s->slot_col.assign(s->slots, 0);
+    ok = ok && cudaEventCreateWithFlags(&s->mv_ready, cudaEventDisableTiming) == cudaSuccess;
     for (int i = 0; i < s->slots && ok; i++)
         ok = cudaEventCreateWithFlags(&s->slot_dl[i], cudaEventDisableTiming) == cudaSuccess;
     ok = ok && dev_alloc(s, (void **)&s->dpb, s->slot_bytes * s->slots);
@@ -888,6 +956,15 @@ int rc_h264_submit(rc_stream *s, const rc_h264_picture *pic, int out_slot) {
     } else if (!pic->mbs || !pic->slices || pic->num_slices <= 0) {
         return RC_EINVAL;
     }
+    // motion syntax: host records only, and every B slice's co-located slot
+    // must hold motion stored by an earlier picture with motion syntax
+    const bool derive = pic->motion != nullptr;
+    if (derive) {
+        if (pic->mem != RC_MEM_HOST || s->mb_h > 1024) return RC_EINVAL;
+        for (int i = 0; i < pic->num_slices; i++)
+            if (pic->slice_motion[i].b_slice && !s->slot_col[pic->slice_motion[i].col_slot]) return RC_EINVAL;
+        if (!s->col && !dev_alloc(s, (void **)&s->col, (size_t)s->slots * n * RC_COLMB_BYTES)) return RC_ENOMEM;
+    }
     // Groups: a picture joins the pending group unless it writes a slot that
     // a pending picture writes or reads.
     const bool grouped = s->group > 1;
@@ -939,9 +1016,12 @@ int rc_h264_submit(rc_stream *s, const rc_h264_picture *pic, int out_slot) {
     if (pic->mem == RC_MEM_HOST) {
         const size_t b_mbs = sizeof(rc_h264_mb) * n, b_sl = sizeof(rc_h264_slice) * pic->num_slices;
         const size_t b_w = sizeof(rc_h264_weight) * pic->num_weights, b_lv = sizeof(int16_t) * pic->num_levels;
-        Part parts[4] = {{&s->mbs[k], pic->mbs, b_mbs}, {&s->slices[k], pic->slices, b_sl},
-                         {&s->weights[k], pic->weights, b_w}, {&s->levels[k], pic->levels, b_lv}};
-        if ((rc = set_begin(s, k)) != 0 || (rc = upload(s, parts, 4, s->cst)) != 0 || (rc = set_end(s, k)) != 0)
+        Part parts[6] = {{&s->mbs[k], pic->mbs, b_mbs}, {&s->slices[k], pic->slices, b_sl},
+                         {&s->weights[k], pic->weights, b_w}, {&s->levels[k], pic->levels, b_lv},
+                         {&s->motion[k], pic->motion, derive ? sizeof(rc_h264_motion) * n : 0},
+                         {&s->smotion[k], pic->slice_motion, derive ? sizeof(rc_h264_slice_motion) * pic->num_slices : 0}};
+        if ((rc = set_begin(s, k)) != 0 || (rc = upload(s, parts, derive ? 6 : 4, s->cst)) != 0 ||
+            (rc = set_end(s, k)) != 0)
             return rc;
         L.mbs = (const rc_h264_mb *)s->mbs[k].p;
         L.slices = (const rc_h264_slice *)s->slices[k].p;
@@ -978,6 +1058,24 @@ int rc_h264_submit(rc_stream *s, const rc_h264_picture *pic, int out_slot) {
     L.wait_limit = s->wait_limit;
     L.db = nullptr;
     if ((rc = slot_begin(s, out_slot)) != 0) return rc;
+    // motion derived from syntax, on the side stream after the records'
+    // upload (the edge kernel, behind it there, and the MB kernel, which
+    // waits for mv_ready, read the vectors it writes); the slot's co-located
+    // motion is then this picture's
+    if (derive) {
+        L.mbs_out = (rc_h264_mb *)s->mbs[k].p;
+        L.motion = (const rc_h264_motion *)s->motion[k].p;
+        L.smotion = (const rc_h264_slice_motion *)s->smotion[k].p;
+        L.col = s->col;
+        L.col_stride = (unsigned long long)n * RC_COLMB_BYTES;
+        int mrc = 0;
+        if (cudaStreamWaitEvent(s->est, s->set_ready[k], 0) != cudaSuccess) return cuda_fail(s);
+        timed(s, RC_KERNEL_H264_MV, [&] { mrc = rc_launch_h264_mv(L, s->est); }, s->est);
+        if (mrc != 0 || cudaEventRecord(s->mv_ready, s->est) != cudaSuccess ||
+            cudaStreamWaitEvent(s->st, s->mv_ready, 0) != cudaSuccess)
+            return cuda_fail(s);
+    }
+    s->slot_col[out_slot] = derive;
     if (grouped) {
         // group position j: its scratch, and the rows of the pending
         // pictures it references to wait for

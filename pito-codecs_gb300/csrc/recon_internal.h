@@ -83,6 +83,14 @@ struct H264Launch {
     // the MB phase finished before the band kernel started), and waits for
     // the rows of the in-flight pictures it references: nwait DPB slots with
     // their pictures' epochs and per-row filter progress (refprog layout).
+    // motion derived from syntax (h264_mv_kernel): the records it writes
+    // (the engine's own copy of mbs), the syntax, and the co-located motion
+    // store (slot s at col + s * col_stride bytes)
+    rc_h264_mb *mbs_out;
+    const rc_h264_motion *motion;
+    const rc_h264_slice_motion *smotion;
+    uint8_t *col;
+    unsigned long long col_stride;
     uint32_t *mbdone;
     uint8_t *bottom;    // per MB row, mb_w x 32 bytes: unfiltered luma row 15, then Cb and Cr row 7 (not intra MBs)
     int residual_only;  // h264_mb_kernel before a group launch: inter MBs store residuals, unpredicted
@@ -143,6 +151,12 @@ void rc_launch_hevc_sao(const HevcLaunch &p, cudaStream_t st);
 
 // Launchers (h264_kernels.cu).
 void rc_launch_h264_edge(const H264Launch &p, cudaStream_t st);
+// Motion derived from syntax (p.motion): every MB's mv, ref_idx and wp into
+// p.mbs_out, and the picture's co-located motion into its slot of p.col.
+// Returns 0 or -1 (picture taller than the kernel's rows).
+int rc_launch_h264_mv(const H264Launch &p, cudaStream_t st);
+// Bytes of one MB's co-located motion.
+#define RC_COLMB_BYTES 172
 void rc_launch_h264_mb(const H264Launch &p, cudaStream_t st);
 // Intra reconstruction and the loop filter in one cooperative launch, one
 // CTA per band of RC_H264_BAND_ROWS MB rows; returns 0 or -1 (launch failed).

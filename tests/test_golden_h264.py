@@ -105,9 +105,12 @@ def test_oracle_reproduces_reference_digest(engine, oracle, name, motion):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("motion", [False, True], ids=["resolved", "derived"])
 @pytest.mark.parametrize("name", sorted(EXPECTED))
-def test_engine_reproduces_reference_digest(engine, name):
-    meta, pics = load_fixture(engine, name)
+def test_engine_reproduces_reference_digest(engine, name, motion):
+    """Derived: the engine derives every vector on the GPU (h264_mv_kernel)
+    from the motion syntax."""
+    meta, pics = load_fixture(engine, name, motion)
     m0 = meta["pictures"][0]
     W, H = m0["mb_w"] * 16, m0["mb_h"] * 16
     with engine.ReconStream(engine.RC_CODEC_H264, W, H, 8, DPB_SLOTS) as st:
@@ -121,13 +124,14 @@ def test_engine_reproduces_reference_digest(engine, name):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("motion", [False, True], ids=["resolved", "derived"])
 @pytest.mark.parametrize("group", [2, 4])
 @pytest.mark.parametrize("name", sorted(EXPECTED))
-def test_engine_grouped_reproduces_reference_digest(engine, name, group):
+def test_engine_grouped_reproduces_reference_digest(engine, name, group, motion):
     """The same streams with several pictures per launch
     (rc_stream_set_h264_group): pictures are submitted in runs of distinct
     DPB slots without waiting, and read back after each run."""
-    meta, pics = load_fixture(engine, name)
+    meta, pics = load_fixture(engine, name, motion)
     metas = [m for m, _ in pics]
     m0 = metas[0]
     W, H = m0["mb_w"] * 16, m0["mb_h"] * 16
@@ -145,3 +149,85 @@ def test_engine_grouped_reproduces_reference_digest(engine, name, group):
                 planes[j] = cropped(st.download(metas[j]["slot"]), metas[j]["crop"])
         assert st.sync() == 0
     assert output_digest(metas, lambda j: planes[j]) == EXPECTED[name]
+
+
+def _motion_picture(engine, name, i):
+    """Picture i of a fixture with its motion syntax, and its buffers."""
+    z = np.load(GOLDEN / f"h264_{name}.npz")
+    meta = json.loads(bytes(z["meta"]).decode())
+    m = meta["pictures"][i]
+    bufs = {k: bytearray(z[f"{k}_{i}"].tobytes()) for k in KEYS + MOTION_KEYS}
+    return m, bufs
+
+
+def test_validate_rejects_bad_motion_syntax(engine):
+    """rc_h264_validate checks motion syntax like the kernel would: shapes,
+    sub-partitions, prediction lists, ref_idx within the lists, direct modes
+    only in B slices, weight entries that exist."""
+    import ctypes
+    L = engine.lib()
+    # a P picture of the Baseline stream (list 0 only)
+    m, bufs = _motion_picture(engine, "baseline", 1)
+    mb_w, mb_h, n = m["mb_w"], m["mb_h"], m["mb_w"] * m["mb_h"]
+
+    def check(mutate):
+        b = {k: bytearray(v) for k, v in bufs.items()}
+        mos = (engine.H264Motion * n).from_buffer(b["motion"])
+        recs = (engine.H264Mb * n).from_buffer(b["mbs"])
+        sms = (engine.H264SliceMotion * m["num_slices"]).from_buffer(b["slice_motion"])
+        mutate(mos, recs, sms)
+        pb = engine.PictureBuffers({k: bytes(v) for k, v in b.items()}, m["num_slices"], m["num_weights"],
+                                   m["constrained_intra"], m["frame_id"])
+        return L.rc_h264_validate(mb_w, mb_h, DPB_SLOTS, pb.ptr)
+
+    inter = [a for a in range(n) if (engine.H264Mb * n).from_buffer(bufs["mbs"])[a].kind == engine.RC_H264_INTER]
+    part = [a for a in inter if (engine.H264Motion * n).from_buffer(bufs["motion"])[a].shape
+            == engine.RC_H264_MOTION_16x16]
+    assert check(lambda mo, r, sm: None) == 0
+    a, q = inter[0], part[0]
+
+    def shape_mismatch(mo, r, sm):
+        mo[a].shape = engine.RC_H264_MOTION_NONE
+
+    def bad_shape(mo, r, sm):
+        mo[a].shape = 9
+
+    def ref_past_list(mo, r, sm):
+        mo[q].ref_idx[0][0] = 31
+
+    def list1_in_p(mo, r, sm):
+        mo[q].pred[0] = 2
+
+    def direct_in_p(mo, r, sm):
+        mo[q].shape = engine.RC_H264_MOTION_8x8
+        for i in range(4):
+            mo[q].sub[i], mo[q].pred[i], mo[q].ref_idx[0][i] = engine.RC_H264_SUB_DIRECT, 0, 0
+
+    def bad_weight(mo, r, sm):
+        sm[0].wp_map[1 * 33 + 0] = 7  # (ref0 0, list 1 unused) -> an entry that does not exist
+
+    for fn in (shape_mismatch, bad_shape, ref_past_list, list1_in_p, direct_in_p, bad_weight):
+        assert check(fn) == engine.RC_EINVAL, fn.__name__
+
+
+@pytest.mark.gpu
+def test_engine_rejects_b_picture_without_stored_colocated_motion(engine):
+    """A B slice's co-located picture must have been submitted with motion
+    syntax (its stored motion is what direct prediction reads)."""
+    meta, pics = load_fixture(engine, "main_cabac_b", motion=True)
+    _, plain = load_fixture(engine, "main_cabac_b", motion=False)
+    metas = [m for m, _ in pics]
+    m0 = metas[0]
+    b = next(i for i, (m, p) in enumerate(pics)
+             if any((engine.H264SliceMotion * m["num_slices"]).from_address(p.pic.slice_motion)[j].b_slice
+                    for j in range(m["num_slices"])))
+    with engine.ReconStream(engine.RC_CODEC_H264, m0["mb_w"] * 16, m0["mb_h"] * 16, 8, DPB_SLOTS) as st:
+        # every earlier picture with resolved motion only: no stored motion
+        for i in range(b):
+            st.submit_h264(plain[i][1], metas[i]["slot"])
+        with pytest.raises(engine.ReconError):
+            st.submit_h264(pics[b][1], metas[b]["slot"])
+        # with motion syntax, the same pictures are accepted
+        for i in range(b + 1):
+            st.submit_h264(pics[i][1], metas[i]["slot"])
+        assert st.sync() == 0
