@@ -106,7 +106,8 @@ class SynthH264Opts(ctypes.Structure):
                 ("deblock_idc", ctypes.c_int32), ("alpha_offset", ctypes.c_int32), ("beta_offset", ctypes.c_int32),
                 ("custom_scaling", ctypes.c_int32), ("chroma_qp_offset", ctypes.c_int32),
                 ("num_ref", ctypes.c_int32 * 2), ("ref_slot", (ctypes.c_int32 * 4) * 2),
-                ("ref_id", (ctypes.c_uint32 * 4) * 2), ("frame_id", ctypes.c_uint32)]
+                ("ref_id", (ctypes.c_uint32 * 4) * 2), ("frame_id", ctypes.c_uint32),
+                ("motion_syntax", ctypes.c_int32)]
 
 
 class HevcBlk(ctypes.Structure):

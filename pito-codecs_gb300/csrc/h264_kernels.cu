@@ -45,6 +45,7 @@
 #include <stdint.h>
 #include <string.h>
 
+#include <cstddef>
 #include <mutex>
 
 #include "recon_internal.h"
@@ -109,6 +110,26 @@ __device__ __forceinline__ void st_release(uint32_t *p, uint32_t v) {
 __device__ __forceinline__ void st_relaxed(uint32_t *p, uint32_t v) {
     asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
+// Asynchronous global -> shared copies (tracked per thread by commit groups,
+// not by the warp's register scoreboards, so that a filter warp can keep two
+// MBs in flight without stalling on them).
+__device__ __forceinline__ void cp_async16(void *dst, const void *src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async8(void *dst, const void *src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async4(void *dst, const void *src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+__device__ __forceinline__ void cp_wait_all_but_1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+__device__ __forceinline__ void cp_wait_all_but_4() { asm volatile("cp.async.wait_group 4;" ::: "memory"); }
+
 __device__ __forceinline__ bool aborted(const uint32_t *err) {
     return (*(const volatile uint32_t *)err & RC_DEV_ERR_TIMEOUT) != 0;
 }
@@ -303,41 +324,50 @@ struct MvNb {
     int avail, ref, mvx, mvy;
 };
 
+// An MB's derived motion, as the records hold it (ref_idx, then after the
+// 4-byte wp field, mv: byte offsets 36 and 48 of rc_h264_mb).
+struct MbMv {
+    int8_t ref[2][4];
+    int16_t mv[2][16][2];
+};
+
+// One warp's derivation state, in shared memory: the MB being derived (ref,
+// mv, done) and copies of its neighbours' motion (nbm: A, B, C, D; nb[i] < 0
+// where neighbour i is unavailable).
 struct MvState {
-    const H264Launch *P;
-    int addr;
-    int nb[4];  // A, B, C, D MB addresses or -1
+    int nb[4];
     uint32_t done;
     int8_t ref[2][4];
     int16_t mv[2][16][2];
     const rc_h264_slice *sl;
     const rc_h264_slice_motion *sm;
     const ColMb *col;
+    MbMv nbm[4];
 };
 
 __device__ MvNb mv_nb(const MvState &S, int l, int x, int y) {
     const MvNb na = {0, -1, 0, 0};
-    int mb, bx, by;
+    int which, bx, by;
     if (x < 0) {
-        if (y < 0) { mb = S.nb[3]; bx = 3; by = 3; }
+        if (y < 0) { which = 3; bx = 3; by = 3; }
         else if (y > 3) return na;
-        else { mb = S.nb[0]; bx = 3; by = y; }
+        else { which = 0; bx = 3; by = y; }
     } else if (x > 3) {
-        if (y < 0) { mb = S.nb[2]; bx = 0; by = 3; }
+        if (y < 0) { which = 2; bx = 0; by = 3; }
         else return na;
     } else if (y < 0) {
-        mb = S.nb[1]; bx = x; by = 3;
+        which = 1; bx = x; by = 3;
     } else {
         if (!(S.done >> (y * 4 + x) & 1)) return na;
         const int r = S.ref[l][(y >> 1) * 2 + (x >> 1)];
         if (r < 0) return {1, -1, 0, 0};
         return {1, r, S.mv[l][y * 4 + x][0], S.mv[l][y * 4 + x][1]};
     }
-    if (mb < 0) return na;
-    const rc_h264_mb *m = S.P->mbs_out + mb;
-    const int r = m->ref_idx[l][(by >> 1) * 2 + (bx >> 1)];
+    if (S.nb[which] < 0) return na;
+    const MbMv &m = S.nbm[which];
+    const int r = m.ref[l][(by >> 1) * 2 + (bx >> 1)];
     if (r < 0) return {1, -1, 0, 0};
-    return {1, r, m->mv[l][by * 4 + bx][0], m->mv[l][by * 4 + bx][1]};
+    return {1, r, m.mv[l][by * 4 + bx][0], m.mv[l][by * 4 + bx][1]};
 }
 
 __device__ void mv_abc(const MvState &S, int l, int x, int y, int w, MvNb &a, MvNb &b, MvNb &c) {
@@ -378,12 +408,11 @@ __device__ void mv_pred(const MvState &S, int l, int x, int y, int w, int ref, i
 
 __device__ void mv_set(MvState &S, int x, int y, int w, int h, const int refs[2], const int mvs[2][2]) {
     for (int l = 0; l < 2; l++) {
-        const int16_t mx = refs[l] >= 0 ? (int16_t)mvs[l][0] : 0, my = refs[l] >= 0 ? (int16_t)mvs[l][1] : 0;
+        // (x, y) of a block as one word: one shared-memory store per block
+        const uint32_t v = refs[l] >= 0 ? ((uint32_t)(uint16_t)mvs[l][0] | (uint32_t)(uint16_t)mvs[l][1] << 16) : 0u;
+        uint32_t *dst = (uint32_t *)S.mv[l];
         for (int yy = y; yy < y + h; yy++)
-            for (int xx = x; xx < x + w; xx++) {
-                S.mv[l][yy * 4 + xx][0] = mx;
-                S.mv[l][yy * 4 + xx][1] = my;
-            }
+            for (int xx = x; xx < x + w; xx++) dst[yy * 4 + xx] = v;
         for (int by = y >> 1; by <= (y + h - 1) >> 1; by++)
             for (int bx = x >> 1; bx <= (x + w - 1) >> 1; bx++) S.ref[l][by * 2 + bx] = (int8_t)refs[l];
     }
@@ -568,93 +597,222 @@ __device__ bool mv_derive(MvState &S, const rc_h264_motion &mo) {
     return true;
 }
 
-constexpr int MV_MAX_ROWS = 1024;
+// The rows as warps of a cooperative launch: CTA c derives rows
+// [c * R, c * R + R), one warp per row.  Rows of a CTA hand over through
+// shared memory: each row keeps its MBs' bottom-row motion (all the row
+// below reads of it) and its progress there.  A CTA's first row reads the
+// row above from the records in global memory, behind that row's progress
+// word (P.mvprog), which the CTA's last row publishes.  The inputs of the
+// next MB -- its syntax and the record headers (kind, slice) of it and its
+// neighbours, which never change -- are staged one MB ahead with cp.async.
+// Per MB, lane 0 derives from shared memory and the lanes store the motion
+// into the records and the co-located store.
+static_assert(sizeof(MbMv) == 136 && offsetof(rc_h264_mb, ref_idx) == 36 && offsetof(rc_h264_mb, wp) == 44 &&
+                  offsetof(rc_h264_mb, mv) == 48 && sizeof(rc_h264_motion) == 148 && sizeof(rc_h264_mb) % 16 == 0,
+              "record layout the warp copies rely on");
+constexpr int MV_MAX_WARPS = 16;
 
-__global__ void __launch_bounds__(MV_MAX_ROWS) h264_mv_kernel(const __grid_constant__ H264Launch P) {
-    __shared__ volatile int prog[MV_MAX_ROWS];  // MBs of row y derived
-    const int y = threadIdx.x;
-    if (y < P.mb_h) prog[y] = 0;
+// Bottom-row motion of one MB: the ref_idx of its two bottom 8x8 blocks and
+// the vectors of its four bottom 4x4 blocks, per list (9 words).
+struct MbBottom {
+    int8_t ref[2][2];
+    int16_t mv[2][4][2];
+};
+static_assert(sizeof(MbBottom) == 36, "bottom-row motion layout");
+
+struct __align__(16) MvWarp {
+    MvState S;
+    uint4 hdr[2][5];          // record headers of MB x, A, B, C, D (slot x & 1)
+    rc_h264_motion mo[2];     // syntax of MB x (slot x & 1)
+    int ok;
+};
+
+size_t mv_smem(int rows, int mb_w) { return (size_t)rows * (sizeof(MvWarp) + (size_t)mb_w * sizeof(MbBottom)); }
+
+__global__ void __launch_bounds__(MV_MAX_WARPS * 32, 1) h264_mv_kernel(const __grid_constant__ H264Launch P) {
+    extern __shared__ __align__(16) uint8_t mv_dyn[];
+    __shared__ volatile int rprog[MV_MAX_WARPS];
+    const int R = blockDim.x >> 5, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int y = blockIdx.x * R + w;
+    if (threadIdx.x < MV_MAX_WARPS) rprog[threadIdx.x] = 0;
     __syncthreads();
     if (y >= P.mb_h) return;
-    const int n_mb = P.mb_w * P.mb_h;
+    MvWarp &W = ((MvWarp *)mv_dyn)[w];
+    MbBottom *bottom = (MbBottom *)(mv_dyn + (size_t)R * sizeof(MvWarp));
+    MbBottom *mine = bottom + (size_t)w * P.mb_w, *above = w > 0 ? bottom + (size_t)(w - 1) * P.mb_w : nullptr;
+    MvState &S = W.S;
+    const uint32_t tag = (P.epoch & 0xffffu) << 16;
+    const bool last = w == R - 1 || y == P.mb_h - 1;  // publishes for the next CTA
     ColMb *out = (ColMb *)(P.col + (size_t)P.out_slot * P.col_stride);
-    MvState S;
-    S.P = &P;
-    uint32_t seen_above = y > 0 ? 0 : (uint32_t)P.mb_w;
+    // stage MB x's inputs into slot x & 1 (every lane commits one group)
+    auto stage = [&](int x) {
+        if (x < P.mb_w) {
+            const int sl = x & 1;
+            if (lane < 5) {
+                const int dx = lane == 1 ? -1 : lane == 3 ? 1 : lane == 4 ? -1 : 0, dy = lane >= 2 ? -1 : 0;
+                const int nx = x + dx, ny = y + dy;
+                if (nx >= 0 && ny >= 0 && nx < P.mb_w) cp_async16(&W.hdr[sl][lane], P.mbs_out + ny * P.mb_w + nx);
+                else W.hdr[sl][lane] = make_uint4(0, 0, 0, 0);  // kind RC_H264_NONE
+            }
+            const uint32_t *src = (const uint32_t *)(P.motion + y * P.mb_w + x);
+            uint32_t *dst = (uint32_t *)&W.mo[sl];
+            cp_async4(dst + lane, src + lane);
+            if (lane < 5) cp_async4(dst + 32 + lane, src + 32 + lane);
+        }
+        cp_commit();
+    };
+    stage(0);
+    int seen = y > 0 ? 0 : P.mb_w;  // progress of row y-1 observed so far
     for (int x = 0; x < P.mb_w; x++) {
-        const int addr = y * P.mb_w + x;
+        const int addr = y * P.mb_w + x, sl = x & 1;
+        stage(x + 1);
+        cp_wait_all_but_1();  // MB x's inputs
+        __syncwarp();
+        const int kind = ((const uint8_t *)&W.hdr[sl][0])[0], slice = ((const uint16_t *)&W.hdr[sl][0])[4];
+        const bool inter = kind == RC_H264_INTER && slice < P.num_slices;
         // row y-1 through MB x+1 (the top-right neighbour)
         const int need = min(x + 2, P.mb_w);
-        if ((int)seen_above < need) {
-            uint32_t it = 0, ns = 32;
-            int v;
-            while ((v = prog[y - 1]) < need) {
-                if (++it > P.wait_limit || ((it & 63) == 0 && aborted(P.error))) {
-                    set_error(P.error, RC_DEV_ERR_TIMEOUT);
-                    prog[y] = P.mb_w;
-                    return;
+        if (seen < need) {
+            bool ok = true;
+            int v = 0;
+            if (lane == 0) {
+                uint32_t it = 0, ns = 16;
+                for (;;) {
+                    if (w == 0) {
+                        const uint32_t f = ld_acquire(P.mvprog + y - 1);
+                        v = (f & 0xffff0000u) == tag ? (int)(f & 0xffffu) : 0;
+                    } else {
+                        v = rprog[w - 1];
+                    }
+                    if (v >= need) break;
+                    if (++it > P.wait_limit || ((it & 63) == 0 && aborted(P.error))) { ok = false; break; }
+                    __nanosleep(ns);
+                    ns = min(ns * 2, 128u);
                 }
-                __nanosleep(ns);
-                ns = min(ns * 2, 256u);
             }
-            seen_above = (uint32_t)v;
+            if (!__shfl_sync(0xffffffffu, ok, 0)) {
+                if (lane == 0) {
+                    set_error(P.error, RC_DEV_ERR_TIMEOUT);
+                    rprog[w] = P.mb_w;  // the rows below give up too
+                    if (last) st_release(P.mvprog + y, tag | (uint32_t)P.mb_w);
+                }
+                cp_wait_all();
+                return;
+            }
+            seen = __shfl_sync(0xffffffffu, v, 0);
+            __syncwarp();
             __threadfence_block();
         }
-        rc_h264_mb *m = P.mbs_out + addr;
-        const int kind = m->kind, slice = m->slice;
-        ColMb *o = out + addr;
-        bool inter = kind == RC_H264_INTER && slice < P.num_slices;
-        if (kind == RC_H264_INTER && !inter) set_error(P.error, RC_DEV_ERR_RECORD);
-        for (int l = 0; l < 2; l++)
-            for (int b8 = 0; b8 < 4; b8++) S.ref[l][b8] = -1;
-        for (int l = 0; l < 2; l++)
-            for (int k = 0; k < 16; k++) S.mv[l][k][0] = S.mv[l][k][1] = 0;
         if (inter) {
-            S.addr = addr;
-            S.done = 0;
-            S.sl = P.slices + slice;
-            S.sm = P.smotion + slice;
-            const int dx[4] = {-1, 0, 1, -1}, dy[4] = {0, -1, -1, -1};
-            for (int i = 0; i < 4; i++) {
-                const int nx = x + dx[i], ny = y + dy[i], na = ny * P.mb_w + nx;
-                S.nb[i] = (nx >= 0 && ny >= 0 && nx < P.mb_w && P.mbs_out[na].kind != RC_H264_NONE &&
-                           P.mbs_out[na].slice == slice)
-                              ? na
-                              : -1;
+            // neighbour availability (A, B, C, D): decoded and in this slice
+            if (lane < 4) {
+                const uint4 h = W.hdr[sl][1 + lane];
+                const int nk = ((const uint8_t *)&h)[0], ns = ((const uint16_t *)&h)[4];
+                const int dx = lane == 0 ? -1 : lane == 2 ? 1 : lane == 3 ? -1 : 0, dy = lane == 0 ? 0 : -1;
+                S.nb[lane] = (nk != RC_H264_NONE && ns == slice && x + dx >= 0 && x + dx < P.mb_w && y + dy >= 0)
+                                 ? (y + dy) * P.mb_w + x + dx
+                                 : -1;
             }
-            S.col = nullptr;
-            const int cs = S.sm->col_slot;
-            if (S.sm->b_slice) {
-                if (cs >= 0 && cs < P.dpb_slots) S.col = (const ColMb *)(P.col + (size_t)cs * P.col_stride) + addr;
-                else set_error(P.error, RC_DEV_ERR_RECORD);
+            __syncwarp();
+            // B, C, D: the bottom-row motion of MBs x, x+1, x-1 of row y-1
+            if (w > 0) {
+                for (int k = lane; k < 27; k += 32) {
+                    const int which = 1 + k / 9, j = k % 9;
+                    if (S.nb[which] < 0) continue;
+                    const int nx = x + (which == 2 ? 1 : which == 3 ? -1 : 0);
+                    const uint32_t v = ((const uint32_t *)(above + nx))[j];
+                    if (j == 0) {
+                        ((uint16_t *)S.nbm[which].ref)[1] = (uint16_t)v;          // list 0, 8x8 blocks 2, 3
+                        ((uint16_t *)S.nbm[which].ref)[3] = (uint16_t)(v >> 16);  // list 1
+                    } else {
+                        const int l = (j - 1) >> 2, b = (j - 1) & 3;
+                        ((uint32_t *)S.nbm[which].mv)[l * 16 + 12 + b] = v;
+                    }
+                }
+            } else {
+                for (int k = lane; k < 3 * 34; k += 32) {
+                    const int which = 1 + k / 34, j = k % 34, na = S.nb[which];
+                    if (na < 0) continue;
+                    // through L2: an L1 line loaded earlier may predate the row above's stores
+                    const uint32_t *src = (const uint32_t *)(P.mbs_out + na);
+                    ((uint32_t *)&S.nbm[which])[j] = __ldcg(src + (j < 2 ? 9 + j : 10 + j));
+                }
             }
-            if (!mv_derive(S, P.motion[addr])) {
+        }
+        // the MB's motion starts empty (all lanes clear it, then lane 0 derives)
+        ((uint32_t *)S.mv)[lane] = 0;
+        if (lane < 2) ((uint32_t *)S.ref)[lane] = 0xffffffffu;
+        __syncwarp();
+        if (lane == 0) {
+            W.ok = 1;
+            if (inter) {
+                S.done = 0;
+                S.sl = P.slices + slice;
+                S.sm = P.smotion + slice;
+                S.col = nullptr;
+                const int cs = S.sm->col_slot;
+                if (S.sm->b_slice) {
+                    if (cs >= 0 && cs < P.dpb_slots) S.col = (const ColMb *)(P.col + (size_t)cs * P.col_stride) + addr;
+                    else W.ok = 0;
+                }
+                if (W.ok && !mv_derive(S, W.mo[sl])) W.ok = 0;
+                if (!W.ok) {
+                    set_error(P.error, RC_DEV_ERR_RECORD);
+                    for (int l = 0; l < 2; l++)
+                        for (int b8 = 0; b8 < 4; b8++) S.ref[l][b8] = -1;
+                }
+            } else if (kind == RC_H264_INTER) {
                 set_error(P.error, RC_DEV_ERR_RECORD);
-                for (int l = 0; l < 2; l++)
-                    for (int b8 = 0; b8 < 4; b8++) S.ref[l][b8] = -1;
             }
         }
-        // the MB's motion into the records and the co-located store
-        for (int l = 0; l < 2; l++) {
-            for (int b8 = 0; b8 < 4; b8++) {
-                m->ref_idx[l][b8] = S.ref[l][b8];
-                o->ref_idx[l][b8] = S.ref[l][b8];
-                const int r = S.ref[l][b8];
-                o->ref_id[l][b8] = r >= 0 ? __ldg(&P.slices[slice].ref_id[l][r]) : 0xffffffffu;
+        __syncwarp();
+        // the motion: bottom row for the row below, the records (ref_idx, wp,
+        // mv: words 9..43), the co-located store (43 words), and MB x+1's
+        // left neighbour
+        const uint32_t *cur_ref = (const uint32_t *)S.ref, *cur_mv = (const uint32_t *)S.mv;
+        if (lane < 9)
+            ((uint32_t *)(mine + x))[lane] =
+                lane == 0 ? ((cur_ref[0] >> 16) | (cur_ref[1] & 0xffff0000u)) : cur_mv[((lane - 1) >> 2) * 16 + 12 + ((lane - 1) & 3)];
+        {
+            uint32_t *rec = (uint32_t *)(P.mbs_out + addr);
+            uint32_t *col = (uint32_t *)(out + addr);
+            for (int i = lane; i < 35; i += 32) {
+                uint32_t v;
+                if (i < 2) v = cur_ref[i];
+                else if (i == 2) {
+                    v = 0;
+                    for (int b8 = 0; b8 < 4; b8++) {
+                        const uint32_t wv = inter ? P.smotion[slice].wp_map[(S.ref[0][b8] + 1) * (RC_H264_MAX_REFS + 1) +
+                                                                             (S.ref[1][b8] + 1)]
+                                                  : 0xffu;
+                        v |= wv << (8 * b8);
+                    }
+                } else v = cur_mv[i - 3];
+                rec[9 + i] = v;
             }
-            for (int k = 0; k < 16; k++) {
-                m->mv[l][k][0] = o->mv[l][k][0] = S.mv[l][k][0];
-                m->mv[l][k][1] = o->mv[l][k][1] = S.mv[l][k][1];
+            for (int i = lane; i < 43; i += 32) {
+                uint32_t v;
+                if (i == 0) v = inter ? 0u : 1u;
+                else if (i < 3) v = cur_ref[i - 1];
+                else if (i < 11) {
+                    const int l = (i - 3) >> 2, b8 = (i - 3) & 3, r = S.ref[l][b8];
+                    v = r >= 0 ? __ldg(&P.slices[slice].ref_id[l][r]) : 0xffffffffu;
+                } else v = cur_mv[i - 11];
+                col[i] = v;
             }
+            for (int i = lane; i < 34; i += 32) ((uint32_t *)&S.nbm[0])[i] = i < 2 ? cur_ref[i] : cur_mv[i - 2];
         }
-        for (int b8 = 0; b8 < 4; b8++)
-            m->wp[b8] = inter ? P.smotion[slice].wp_map[(S.ref[0][b8] + 1) * (RC_H264_MAX_REFS + 1) + (S.ref[1][b8] + 1)]
-                              : (uint8_t)0xff;
-        o->intra = !inter;
-        __threadfence_block();
-        prog[y] = x + 1;
+        __syncwarp();
+        if (lane == 0) {
+            if (last && y + 1 < P.mb_h) {
+                __threadfence();
+                st_relaxed(P.mvprog + y, tag | (uint32_t)(x + 1));
+            }
+            __threadfence_block();
+            rprog[w] = x + 1;
+        }
     }
-    (void)n_mb;
+    cp_wait_all();
 }
 
 // ===========================================================================
@@ -1810,25 +1968,6 @@ __device__ __forceinline__ void band_fail(const H264Launch &P, int lane) {
     if (lane == 0) set_error(P.error, RC_DEV_ERR_TIMEOUT);
 }
 
-// Asynchronous global -> shared copies (tracked per thread by commit groups,
-// not by the warp's register scoreboards, so that a filter warp can keep two
-// MBs in flight without stalling on them).
-__device__ __forceinline__ void cp_async16(void *dst, const void *src) {
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src)
-                 : "memory");
-}
-__device__ __forceinline__ void cp_async8(void *dst, const void *src) {
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src)
-                 : "memory");
-}
-__device__ __forceinline__ void cp_async4(void *dst, const void *src) {
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src)
-                 : "memory");
-}
-__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void cp_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
-__device__ __forceinline__ void cp_wait_all_but_1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
-__device__ __forceinline__ void cp_wait_all_but_4() { asm volatile("cp.async.wait_group 4;" ::: "memory"); }
 
 // Intra warp of band row w (picture row my).  `lines` holds, per band row,
 // the row's unfiltered bottom samples (luma row 15, then Cb and Cr row 7):
@@ -2715,10 +2854,26 @@ void rc_launch_h264_edge(const H264Launch &p, cudaStream_t st) {
 }
 
 int rc_launch_h264_mv(const H264Launch &p, cudaStream_t st) {
-    if (p.mb_h > MV_MAX_ROWS) return -1;
-    const int threads = (p.mb_h + 31) / 32 * 32;
-    h264_mv_kernel<<<1, threads, 0, st>>>(p);
-    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+    // rows per CTA: up to 16, as many as the rows' bottom-row buffers allow
+    int rows = MV_MAX_WARPS;
+    while (rows > 1 && mv_smem(rows, p.mb_w) > 160 * 1024) rows--;
+    const size_t smem = mv_smem(rows, p.mb_w);
+    const int ctas = (p.mb_h + rows - 1) / rows;
+    int dev = 0, sms = 0, per = 0;
+    if (smem > 200 * 1024 || cudaGetDevice(&dev) != cudaSuccess) return -1;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaFuncSetAttribute(h264_mv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, h264_mv_kernel, rows * 32, smem) != cudaSuccess ||
+        ctas > per * sms) {
+        cudaGetLastError();
+        return -1;
+    }
+    H264Launch q = p;
+    void *args[] = {&q};
+    return cudaLaunchCooperativeKernel((const void *)h264_mv_kernel, dim3(ctas), dim3(rows * 32), args, smem, st) ==
+                   cudaSuccess
+               ? 0
+               : -1;
 }
 
 void rc_launch_h264_mb(const H264Launch &p, cudaStream_t st) {

@@ -111,6 +111,7 @@ struct rc_stream {
     // and which slots hold stored motion
     DevBuf motion[REC_SETS], smotion[REC_SETS];
     uint8_t *col = nullptr;
+    uint32_t *mvprog = nullptr;  // per MB row, the motion kernel's progress
     std::vector<char> slot_col;
     cudaEvent_t mv_ready = nullptr;
     // H.264 picture groups (rc_stream_set_h264_group): pictures per launch,
@@ -444,6 +445,7 @@ void destroy(rc_stream *s) {
         for (DevBuf *b : {&s->mbs[i], &s->slices[i], &s->weights[i], &s->levels[i], &s->motion[i], &s->smotion[i]})
             dev_free(s, b->p, b->cap);
     dev_free(s, s->col, (size_t)s->slots * s->mb_w * s->mb_h * RC_COLMB_BYTES);
+    dev_free(s, s->mvprog, (size_t)s->mb_h * sizeof(uint32_t));
     if (s->mv_ready) cudaEventDestroy(s->mv_ready);
     group_free(s);
     dev_free(s, s->scaling.p, s->scaling.cap);
@@ -960,10 +962,15 @@ int rc_h264_submit(rc_stream *s, const rc_h264_picture *pic, int out_slot) {
     // must hold motion stored by an earlier picture with motion syntax
     const bool derive = pic->motion != nullptr;
     if (derive) {
-        if (pic->mem != RC_MEM_HOST || s->mb_h > 1024) return RC_EINVAL;
+        if (pic->mem != RC_MEM_HOST) return RC_EINVAL;
         for (int i = 0; i < pic->num_slices; i++)
             if (pic->slice_motion[i].b_slice && !s->slot_col[pic->slice_motion[i].col_slot]) return RC_EINVAL;
         if (!s->col && !dev_alloc(s, (void **)&s->col, (size_t)s->slots * n * RC_COLMB_BYTES)) return RC_ENOMEM;
+        if (!s->mvprog) {
+            if (!dev_alloc(s, (void **)&s->mvprog, (size_t)s->mb_h * sizeof(uint32_t))) return RC_ENOMEM;
+            if (cudaMemsetAsync(s->mvprog, 0, (size_t)s->mb_h * sizeof(uint32_t), s->est) != cudaSuccess)
+                return cuda_fail(s);
+        }
     }
     // Groups: a picture joins the pending group unless it writes a slot that
     // a pending picture writes or reads.
@@ -1068,6 +1075,7 @@ int rc_h264_submit(rc_stream *s, const rc_h264_picture *pic, int out_slot) {
         L.smotion = (const rc_h264_slice_motion *)s->smotion[k].p;
         L.col = s->col;
         L.col_stride = (unsigned long long)n * RC_COLMB_BYTES;
+        L.mvprog = s->mvprog;
         int mrc = 0;
         if (cudaStreamWaitEvent(s->est, s->set_ready[k], 0) != cudaSuccess) return cuda_fail(s);
         timed(s, RC_KERNEL_H264_MV, [&] { mrc = rc_launch_h264_mv(L, s->est); }, s->est);

@@ -91,6 +91,7 @@ struct H264Launch {
     const rc_h264_slice_motion *smotion;
     uint8_t *col;
     unsigned long long col_stride;
+    uint32_t *mvprog;  // per MB row: (epoch & 0xffff) << 16 | MBs whose motion is derived
     uint32_t *mbdone;
     uint8_t *bottom;    // per MB row, mb_w x 32 bytes: unfiltered luma row 15, then Cb and Cr row 7 (not intra MBs)
     int residual_only;  // h264_mb_kernel before a group launch: inter MBs store residuals, unpredicted

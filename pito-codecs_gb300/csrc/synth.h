@@ -42,6 +42,10 @@ typedef struct rc_synth_h264_opts {
     int32_t ref_slot[2][4];    /* DPB slots of refidx 0..3                     */
     uint32_t ref_id[2][4];     /* reference identities                         */
     uint32_t frame_id;
+    int32_t motion_syntax;     /* 1 = also emit motion syntax (rc_h264_motion)
+                                  for the inter MBs: their partitions and refs
+                                  with small random mvd and 20% P_Skip; the
+                                  vectors are then the derived ones          */
 } rc_synth_h264_opts;
 
 /* Fill opts with the 1080p-style defaults (30% intra, 20% WP, 80% zero

@@ -4,6 +4,7 @@
 // Integer-only: the same seed gives the same records on x86 and Arm.
 #include <cstdlib>
 #include <cstring>
+#include <array>
 #include <vector>
 
 #include "synth.h"
@@ -40,6 +41,8 @@ struct Rng {
 
 struct Pic {
     rc_h264_picture pic;
+    std::vector<rc_h264_motion> motion;
+    std::vector<rc_h264_slice_motion> smotion;
     std::vector<rc_h264_mb> mbs;
     std::vector<rc_h264_slice> slices;
     std::vector<rc_h264_weight> weights;
@@ -54,6 +57,8 @@ struct Gen {
     const rc_synth_h264_opts &o;
     Rng r;
     Pic &p;
+    std::vector<int> part_of;            // per MB: the inter partition drawn (0 16x16 .. 3 8x8)
+    std::vector<std::array<int, 4>> subs_of;  // 8x8: the sub-partition drawn per 8x8
     Gen(const rc_synth_h264_opts &o_, Pic &p_) : o(o_), r{o_.seed}, p(p_) {}
 
     // availability of neighbour n (0 L, 1 T, 2 TR, 3 TL) for intra prediction
@@ -207,12 +212,15 @@ struct Gen {
         int part = r.below(4);
         bool sub8 = false;
         int rect_b8[16];
+        const int a = mby * o.mb_w + mbx;
+        part_of[a] = part;
         if (part == 0) rects[nr++] = {0, 0, 4, 4};
         else if (part == 1) { rects[nr++] = {0, 0, 4, 2}; rects[nr++] = {0, 2, 4, 2}; }
         else if (part == 2) { rects[nr++] = {0, 0, 2, 4}; rects[nr++] = {2, 0, 2, 4}; }
         else
             for (int b8 = 0; b8 < 4; b8++) {
                 int x8 = (b8 & 1) * 2, y8 = (b8 >> 1) * 2, s = r.below(4);
+                subs_of[a][b8] = s;
                 sub8 |= s != 0;
                 if (s == 0) rects[nr++] = {x8, y8, 2, 2};
                 else if (s == 1) { rects[nr++] = {x8, y8, 2, 1}; rects[nr++] = {x8, y8 + 1, 2, 1}; }
@@ -300,8 +308,90 @@ struct Gen {
         }
     }
 
+    // Motion syntax for the generated inter MBs (a separate random stream, so
+    // the records are the same with and without it): the partitions and refs
+    // drawn, small random mvd, 20% of single-reference list-0 16x16 MBs as
+    // P_Skip in pictures without list 1; per slice a weight entry per
+    // (refIdxL0, refIdxL1) pair.  Pictures with list 1 are B slices whose
+    // co-located picture is RefPicList1[0] (no direct modes are drawn).
+    void motion_syntax() {
+        Rng q{o.seed ^ 0x5bd1e9955bd1e995ull};
+        const int n = o.mb_w * o.mb_h;
+        p.motion.assign(n, rc_h264_motion());
+        memset(p.motion.data(), 0, sizeof(rc_h264_motion) * n);
+        const bool b = o.num_ref[1] > 0;
+        for (auto &sl : p.slices) {
+            rc_h264_slice_motion sm;
+            memset(&sm, 0, sizeof sm);
+            sm.b_slice = b;
+            sm.direct_spatial = 1;
+            sm.direct_8x8_inference = 1;
+            sm.col_slot = b ? sl.ref_slot[1][0] : -1;
+            sm.col_short_term = 1;
+            for (int i = 0; i < RC_H264_MAX_REFS; i++) {
+                sm.dist_scale[i] = 256;
+                sm.direct_copy[i] = 1;
+            }
+            memset(sm.wp_map, 0xff, sizeof sm.wp_map);
+            for (int r0 = -1; r0 < sl.num_ref[0]; r0++)
+                for (int r1 = -1; r1 < sl.num_ref[1]; r1++)
+                    if ((r0 >= 0 || r1 >= 0) && !p.weights.empty() && q.chance(o.wp_permille))
+                        sm.wp_map[(r0 + 1) * (RC_H264_MAX_REFS + 1) + (r1 + 1)] = (uint8_t)q.below((int)p.weights.size());
+            p.smotion.push_back(sm);
+        }
+        for (int a = 0; a < n; a++) {
+            const rc_h264_mb &m = p.mbs[a];
+            rc_h264_motion &mo = p.motion[a];
+            if (m.kind != RC_H264_INTER) continue;
+            const int part = part_of[a];
+            for (int l = 0; l < 2; l++)
+                for (int b8 = 0; b8 < 4; b8++) mo.ref_idx[l][b8] = m.ref_idx[l][b8];
+            auto pred_of = [&](int b8) { return (uint8_t)((m.ref_idx[0][b8] >= 0) | (m.ref_idx[1][b8] >= 0) << 1); };
+            if (part == 0 && !b && m.ref_idx[0][0] == 0 && q.chance(200)) {
+                mo.shape = RC_H264_MOTION_SKIP;
+                continue;
+            }
+            if (part < 3) {
+                mo.shape = (uint8_t)(RC_H264_MOTION_16x16 + part);
+                mo.pred[0] = pred_of(0);
+                if (part) mo.pred[1] = pred_of(part == 1 ? 2 : 1);
+            } else {
+                mo.shape = RC_H264_MOTION_8x8;
+                for (int b8 = 0; b8 < 4; b8++) {
+                    mo.sub[b8] = (uint8_t)subs_of[a][b8];
+                    mo.pred[b8] = pred_of(b8);
+                }
+            }
+            // one mvd per (sub-)partition, held by each of its blocks
+            for (int l = 0; l < 2; l++) {
+                int16_t d[16][2];
+                for (int k = 0; k < 16; k++) {
+                    d[k][0] = (int16_t)(q.below(33) - 16);
+                    d[k][1] = (int16_t)(q.below(33) - 16);
+                }
+                for (int k = 0; k < 16; k++) {
+                    const int x = k & 3, y = k >> 2;
+                    int sx = 0, sy = 0;  // the partition's first block
+                    if (part == 1) sy = y & 2;
+                    else if (part == 2) sx = x & 2;
+                    else if (part == 3) {
+                        const int b8 = (y >> 1) * 2 + (x >> 1), st = subs_of[a][b8];
+                        sx = (x & 2) | (st == 2 || st == 3 ? (x & 1) : 0);
+                        sy = (y & 2) | (st == 1 || st == 3 ? (y & 1) : 0);
+                    }
+                    mo.mvd[l][k][0] = d[sy * 4 + sx][0];
+                    mo.mvd[l][k][1] = d[sy * 4 + sx][1];
+                }
+            }
+        }
+        p.pic.motion = p.motion.data();
+        p.pic.slice_motion = p.smotion.data();
+    }
+
     void run() {
         int n = o.mb_w * o.mb_h, ns = o.num_slices < 1 ? 1 : o.num_slices;
+        part_of.assign(n, 0);
+        subs_of.assign(n, std::array<int, 4>{0, 0, 0, 0});
         p.mbs.assign(n, rc_h264_mb());
         memset(p.mbs.data(), 0, sizeof(rc_h264_mb) * n);
         for (int s = 0; s < ns; s++) {
@@ -355,6 +445,7 @@ struct Gen {
         pc.levels = p.levels.empty() ? nullptr : p.levels.data();
         pc.scaling4 = o.custom_scaling ? &p.scaling4[0][0] : nullptr;
         pc.scaling8 = o.custom_scaling ? &p.scaling8[0][0] : nullptr;
+        if (o.motion_syntax) motion_syntax();
     }
 };
 
