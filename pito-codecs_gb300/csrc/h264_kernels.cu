@@ -1989,10 +1989,13 @@ __device__ __forceinline__ void band_fail(const H264Launch &P, int lane) {
 // from P.bottom (written with the MB: by the pre-pass for I_PCM, by the
 // group kernel for inter MBs, once per MB), after their mbdone: its intra
 // MBs keep waiting on this row only where an intra neighbour is.
+// GROUPED: a group launch (P.mbdone set), compiled apart so that the one-
+// picture kernel carries none of its waits.
+template <bool GROUPED>
 __device__ __forceinline__ void band_intra_row(const H264Launch &P, BandSmem &B, uint8_t *lines, uint8_t *stg, int w, int my,
                                int lane) {
     WarpSmem &S = B.iw[w];
-    const bool grouped = P.mbdone != nullptr;
+    constexpr bool grouped = GROUPED;
     const uint32_t *done = grouped ? P.mbdone + (size_t)my * P.mb_w : nullptr;
     uint8_t *Y = P.dpb + (size_t)P.out_slot * P.slot_bytes;
     uint8_t *U = Y + P.u_off, *V = Y + P.v_off;
@@ -2192,7 +2195,9 @@ __device__ __forceinline__ void band_intra_row(const H264Launch &P, BandSmem &B,
         if (my > 0) {
             const int gx = mx * 16 + lane - 1;
             const int c = lane / 10, gxc = mx * 8 + lane % 10 - 1;
-            const bool ya = above_intra(max(gx, 0) >> 4), ca = above_intra(max(gxc, 0) >> 3);  // all lanes shuffle
+            // (group launches only: all lanes shuffle)
+            const bool ya = grouped ? above_intra(max(gx, 0) >> 4) : true;
+            const bool ca = grouped ? above_intra(max(gxc, 0) >> 3) : true;
             const uint8_t *brow = grouped ? P.bottom + (size_t)(my - 1) * LW : nullptr;
             uint8_t v = 0;
             if (gx >= 0 && gx < P.W)
@@ -2597,6 +2602,7 @@ __device__ __forceinline__ void band_mirror(const H264Launch &P, BandSmem &B, in
 // store the band's warps made before the progress the lanes read (they
 // fenced before publishing it in shared memory) ahead of the flags, which
 // can then be relaxed stores (a release store costs about a fence more).
+template <bool GROUPED>
 __device__ __forceinline__ void band_publish(const H264Launch &P, BandSmem &B, int y0, int rows, int lane) {
     const uint32_t tag = (P.epoch & 0xffffu) << 16;
     const bool above = y0 > 0, below = y0 + rows < P.mb_h;
@@ -2605,7 +2611,7 @@ __device__ __forceinline__ void band_publish(const H264Launch &P, BandSmem &B, i
     // refprog: a word per 128-byte line, apart from the hand-over words, so
     // that the polls of the many waiting MB warps do not queue on the lines
     // that the bands hand over through
-    const bool grouped = P.mbdone != nullptr;
+    constexpr bool grouped = GROUPED;
     const int prow = lane - 3;
     uint32_t *dst = lane == 0 ? (below ? P.rowprog + y0 + rows - 1 : nullptr)
                     : lane == 1 ? (below ? P.irowprog + y0 + rows - 1 : nullptr)
@@ -2638,6 +2644,7 @@ __device__ __forceinline__ void band_publish(const H264Launch &P, BandSmem &B, i
 
 // One band CTA: every thread of the CTA calls it; warps past the band's
 // (3 BR + 2) roles leave after the shared state is set up.
+template <bool GROUPED>
 __device__ __forceinline__ void band_body(const H264Launch &P, BandSmem &B, uint8_t *band_dyn, int band) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int y0 = band * BR, rows = min(BR, P.mb_h - y0);
@@ -2650,11 +2657,12 @@ __device__ __forceinline__ void band_body(const H264Launch &P, BandSmem &B, uint
     }
     __syncthreads();
     if (warp == 3 * BR) { band_mirror(P, B, y0, rows, lane); return; }
-    if (warp == 3 * BR + 1) { band_publish(P, B, y0, rows, lane); return; }
+    if (warp == 3 * BR + 1) { band_publish<GROUPED>(P, B, y0, rows, lane); return; }
     if (warp >= 3 * BR + 2) return;
     const int role = warp / BR, w = warp % BR;
     if (w >= rows) return;
-    if (role == 0) band_intra_row(P, B, band_dyn + BR * RC_BAND_STG, band_dyn + w * RC_BAND_STG, w, y0 + w, lane);
+    if (role == 0)
+        band_intra_row<GROUPED>(P, B, band_dyn + BR * RC_BAND_STG, band_dyn + w * RC_BAND_STG, w, y0 + w, lane);
     else if (role == 1) band_luma_row(P, B, w, y0 + w, rows, lane);
     else band_chroma_row(P, B, w, y0 + w, rows, lane);
 }
@@ -2664,7 +2672,7 @@ __global__ void __launch_bounds__(BAND_THREADS, 1) h264_band_kernel(const __grid
     // dynamic: per band row the intra warp's staging (RC_BAND_STG bytes), then
     // per band row its line of bottom samples (mb_w x 32 bytes)
     extern __shared__ __align__(16) uint8_t band_dyn[];
-    band_body(P, B, band_dyn, blockIdx.x);
+    band_body<false>(P, B, band_dyn, blockIdx.x);
 }
 
 // ===========================================================================
@@ -2814,10 +2822,10 @@ __global__ void __launch_bounds__(GROUP_THREADS, 1) h264_group_kernel(const __gr
         const int j = bid % G.n, band = bid / G.n;
         static_assert(RC_H264_GROUP_MAX == 4, "one case per group position");
         switch (j) {
-        case 0: band_body(G.pic[0], B, band_dyn, band); break;
-        case 1: band_body(G.pic[1], B, band_dyn, band); break;
-        case 2: band_body(G.pic[2], B, band_dyn, band); break;
-        default: band_body(G.pic[3], B, band_dyn, band); break;
+        case 0: band_body<true>(G.pic[0], B, band_dyn, band); break;
+        case 1: band_body<true>(G.pic[1], B, band_dyn, band); break;
+        case 2: band_body<true>(G.pic[2], B, band_dyn, band); break;
+        default: band_body<true>(G.pic[3], B, band_dyn, band); break;
         }
         return;
     }
