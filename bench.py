@@ -155,8 +155,7 @@ class HevcWorkload:
     frames = 60
     slots = 5
     kernels = {3: ("hevc_residual_kernel", "residual"), 4: ("hevc_inter_kernel", "inter"),
-               5: ("hevc_intra_kernel", "intra"), 6: ("hevc_deblock_kernel", "deblock"),
-               7: ("hevc_sao_kernel", "sao")}
+               5: ("hevc_intra_kernel", "intra"), 6: ("hevc_loopfilter_kernel", "loopfilter")}
     buffer_keys = ("ctbs", "blk", "mvf", "tus", "slices", "levels", "scaling")
 
     def __init__(self, E, W, H, bd, frames=None):
@@ -210,8 +209,7 @@ class HevcWorkload:
             "residual": len(b["tus"]) + len(b["levels"]) + res,
             "inter": ref_bytes + int(inter_frac * (res + plane)),
             "intra": int((1 - inter_frac) * (res + plane)),
-            "deblock": 2 * plane + len(b["blk"]),
-            "sao": 2 * plane + len(b["ctbs"]),
+            "loopfilter": 2 * plane + len(b["blk"]) + len(b["ctbs"]),
             "job": plane + ref_bytes + syn,
             "syntax": syn,
         }

@@ -424,8 +424,8 @@ int rc_picture_device_planes(rc_stream *s, int slot, void **y, void **u,
 #define RC_KERNEL_HEVC_RESIDUAL 3
 #define RC_KERNEL_HEVC_INTER 4
 #define RC_KERNEL_HEVC_INTRA 5
-#define RC_KERNEL_HEVC_DEBLOCK 6
-#define RC_KERNEL_HEVC_SAO 7
+#define RC_KERNEL_HEVC_LOOPFILTER 6 /* deblocking and SAO, one launch   */
+/* 7: not used (deblocking and SAO were separate launches before) */
 #define RC_KERNEL_H264_GROUP 8
 #define RC_KERNEL_H264_MV 9
 #define RC_KERNEL_COUNT 10

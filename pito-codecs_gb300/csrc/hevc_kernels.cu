@@ -26,12 +26,14 @@
 //                        (planar, DC, 33 angles read straight from the
 //                        references + edge filters) into the CTB copy; the
 //                        block reaches the picture after its ready flags.
-//  hevc_deblock_kernel   vertical edges, then (second launch) horizontal
-//                        edges, one thread per 4-sample edge segment: edges
-//                        8 samples apart never interact within a direction.
-//  hevc_sao_kernel       four samples of one CTB per thread: band / edge
-//                        offsets from the deblocked picture into the DPB
-//                        slot.
+//  hevc_loopfilter_kernel one CTA per 64x64 tile: the tile and a 4-sample
+//                        halo of the reconstructed picture into shared
+//                        memory, vertical edges, then horizontal edges (one
+//                        thread per 4-sample edge segment: edges 8 samples
+//                        apart never interact within a direction), then SAO
+//                        band / edge offsets, four samples per thread, into
+//                        the DPB slot: the picture is read once and written
+//                        once.
 //
 // Arithmetic follows src/hevc/{transform,intra,inter,filter}.rs and the
 // reconstruction half of src/hevc/slicedec.rs; citations at each function.
@@ -959,26 +961,37 @@ __device__ void filter_chroma(T *s, long o, long step, long along, int tc, bool 
     }
 }
 
-// One thread per edge segment.  dir 0: vertical edges (luma segments at
-// x = 8k, 4 rows; chroma at luma x = 16k, 8 luma rows), dir 1 horizontal.
+// The loop filter works on one tile of the picture in shared memory: the
+// tile's LF_TW x LF_TH luma samples (half that per chroma plane) and a halo of
+// LF_HALO samples on every side.  That halo holds every sample that the
+// deblocking of the tile and of its one-sample SAO border reads: vertical
+// edges lie 8 luma (8 chroma) samples apart and move at most 3 (1) samples
+// beside them, reading 4 (2); horizontal edges do the same on the vertically
+// filtered samples; so the edges at x0 .. x0 + LF_TW and y0 .. y0 + LF_TH,
+// filtered over the whole tile with its halo, leave every sample of the tile
+// and its border as the picture-wide passes (all vertical edges, then all
+// horizontal edges; filter.rs:178-407) leave it.  Edges on a tile boundary
+// are filtered by both tiles, identically.
+constexpr int LF_TW = 64, LF_TH = 64, LF_HALO = 4, LF_THREADS = 256;
+constexpr int LF_LW = LF_TW + 2 * LF_HALO, LF_LH = LF_TH + 2 * LF_HALO;
+constexpr int LF_CW = LF_TW / 2 + 2 * LF_HALO, LF_CH = LF_TH / 2 + 2 * LF_HALO;
+template <class T>
+struct LfTile {
+    T y[LF_LH][LF_LW];
+    T c[2][LF_CH][LF_CW];
+};
+template <class T> struct Raw4;
+template <> struct Raw4<uint8_t> { using type = uint32_t; };
+template <> struct Raw4<uint16_t> { using type = uint2; };
+
+// One edge segment (4 luma samples along the edge, or 4 chroma samples of
+// both chroma planes) at 4x4 luma unit (bx, by): the decision from the
+// records and the filter, on the tile (hevc_deblock's per-edge body,
+// filter.rs:178-407).  x0, y0: luma picture position of the tile (its
+// first sample inside the halo); dir 0 vertical edge (left of the unit), 1
+// horizontal (top).
 template <class T, int DIR>
-__global__ void __launch_bounds__(128) hevc_deblock_kernel(HevcLaunch P) {
-    const int nl = DIR == 0 ? ((P.w4 - 1) / 2) * P.h4 : P.w4 * ((P.h4 - 1) / 2);
-    const int nc = DIR == 0 ? ((P.w4 - 1) / 4) * ((P.h4 + 1) / 2) : ((P.w4 + 1) / 2) * ((P.h4 - 1) / 4);
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nl + nc) return;
-    const bool chroma = i >= nl;
-    const int j = chroma ? i - nl : i;
-    int bx, by;
-    if (DIR == 0) {
-        const int ne = chroma ? (P.w4 - 1) / 4 : (P.w4 - 1) / 2;
-        bx = chroma ? 4 * (1 + j % ne) : 2 * (1 + j % ne);
-        by = chroma ? 2 * (j / ne) : j / ne;
-    } else {
-        const int ne = chroma ? (P.w4 + 1) / 2 : P.w4;
-        bx = chroma ? 2 * (j % ne) : j % ne;
-        by = chroma ? 4 * (1 + j / ne) : 2 * (1 + j / ne);
-    }
+__device__ void deblock_segment(const HevcLaunch &P, LfTile<T> &S, int bx, int by, bool chroma, int x0, int y0) {
     const int qi = by * P.w4 + bx, pi = DIR == 0 ? qi - 1 : qi - P.w4;
     const int x = bx * 4, y = by * 4;
     const int px = DIR == 0 ? x - 1 : x, py = DIR == 0 ? y : y - 1;
@@ -997,17 +1010,16 @@ __global__ void __launch_bounds__(128) hevc_deblock_kernel(HevcLaunch P) {
         const int qpl = (p.qp + q.qp + 1) >> 1;
         const int qb = clampi(qpl + bo, 0, 51), qt = clampi(qpl + 2 * (bs - 1) + tco, 0, 53);
         const int tc = cTC[qt] << (bd - 8), beta = cBETA[qb] << (bd - 8);
-        T *s = plane_ptr<T>(P.work, P, 0);
-        const long pitch = pitch_el(P, 0, sizeof(T));
-        filter_luma<T>(s, (long)y * pitch + x, DIR == 0 ? 1 : pitch, DIR == 0 ? pitch : 1, tc, beta, nfp, nfq, bd);
+        filter_luma<T>(&S.y[0][0], (long)(y - y0 + LF_HALO) * LF_LW + (x - x0 + LF_HALO), DIR == 0 ? 1 : LF_LW,
+                       DIR == 0 ? LF_LW : 1,
+                       tc, beta, nfp, nfq, bd);
     } else {
         if (bs != 2) return;
         for (int c = 1; c < 3; c++) {
             const int qpi = ((p.qp + q.qp + 1) >> 1) + (c == 1 ? P.cb_qp_offset : P.cr_qp_offset);
             const int qt = clampi(qpc_420(qpi) + 2 + tco, 0, 53), tc = cTC[qt] << (bd - 8);
-            T *s = plane_ptr<T>(P.work, P, c);
-            const long pitch = pitch_el(P, c, sizeof(T));
-            filter_chroma<T>(s, (long)(y / 2) * pitch + x / 2, DIR == 0 ? 1 : pitch, DIR == 0 ? pitch : 1, tc, nfp, nfq, bd);
+            filter_chroma<T>(&S.c[c - 1][0][0], (long)(y / 2 - y0 / 2 + LF_HALO) * LF_CW + (x / 2 - x0 / 2 + LF_HALO),
+                             DIR == 0 ? 1 : LF_CW, DIR == 0 ? LF_CW : 1, tc, nfp, nfq, bd);
         }
     }
 }
@@ -1028,86 +1040,133 @@ __device__ bool cross_ok(const HevcLaunch &P, int rs, int nrs) {
     return P.lf_across_tiles || n.tile == q.tile;
 }
 
-// SAO, src/hevc/filter.rs sao: four samples per thread, which share a CTB
-// (its parameters and slice are read once) and whose neighbours are read
-// together
+// The loop filter of one tile (src/hevc/filter.rs:178-894): the
+// reconstructed (pre-deblocking) samples of the tile and its halo into
+// shared memory, vertical edges, horizontal edges, then SAO of the tile's
+// samples from the deblocked tile (its neighbours pre-SAO, as the reference
+// reads them) into the DPB slot.  The work picture is only read.
 template <class T>
-__global__ void __launch_bounds__(256) hevc_sao_kernel(HevcLaunch P) {
-    const int c = blockIdx.z, sc = c ? 1 : 0;
-    const int w = c ? P.CW : P.W, h = c ? P.CH : P.H;
-    const int x0 = (blockIdx.x * 32 + (threadIdx.x & 31)) * 4, y = blockIdx.y * 8 + (threadIdx.x >> 5);
-    if (x0 >= w || y >= h) return;
-    const long pitch = pitch_el(P, c, sizeof(T));
-    const T *in = plane_ptr<T>(P.work, P, c);
-    T *out = plane_ptr<T>(P.dpb + (size_t)P.out_slot * P.slot_bytes, P, c);
-    int v[4], res[4];
-    Quad<T>::load(in + (size_t)y * pitch + x0, v);
-    const int s = P.log2ctb - sc;
-    const int rs = (y >> s) * P.wctb + (x0 >> s);
-    const rc_hevc_ctb &ct = P.ctbs[rs];
-    const rc_hevc_slice *sl = slice_of_ctb(P, rs);
-    const int type = ct.sao.type_idx[c];
-    // the 4x4 luma units' no-filter flags (one unit for luma, two for chroma)
-    const rc_hevc_blk *brow = P.blk + (size_t)((y << sc) >> 2) * P.w4;
-    bool nof[4];
-#pragma unroll
-    for (int i = 0; i < 4; i++) nof[i] = brow[((x0 + i) << sc) >> 2].flags & RC_HEVC_F_NOFILTER;
-#pragma unroll
-    for (int i = 0; i < 4; i++) res[i] = v[i];
-    if ((c ? sl->sao_chroma : sl->sao_luma) && type != 0 && ct.slice < P.num_slices) {
-        const int bd = P.bd, max = (1 << bd) - 1;
-        if (type == 1) {
-#pragma unroll
-            for (int i = 0; i < 4; i++) {
-                const int band = v[i] >> (bd - 5), k = (band - ct.sao.band_pos[c]) & 31;
-                if (k < 4) res[i] = clampi(v[i] + ct.sao.offsets[c][k], 0, max);
-            }
-        } else {
-            const int cls = ct.sao.eo_class[c] & 3;
-            const int hp0 = cls == 1 ? 0 : cls == 3 ? 1 : -1, hp1 = -hp0;
-            const int vp0 = cls == 0 ? 0 : -1, vp1 = -vp0;
-            // the two neighbours of every sample: read first, all of them
-            int nv[2][4];
-            bool ok[4];
-#pragma unroll
-            for (int i = 0; i < 4; i++) {
-                ok[i] = true;
-#pragma unroll
-                for (int j = 0; j < 2; j++) {
-                    const int xn = x0 + i + (j ? hp1 : hp0), yn = y + (j ? vp1 : vp0);
-                    const bool in_pic = xn >= 0 && yn >= 0 && xn < w && yn < h;
-                    nv[j][i] = in_pic ? (int)in[(size_t)yn * pitch + xn] : 0;
-                    ok[i] = ok[i] && in_pic;
-                }
-            }
-#pragma unroll
-            for (int i = 0; i < 4; i++) {
-                bool good = ok[i];
-#pragma unroll
-                for (int j = 0; j < 2 && good; j++) {
-                    const int xn = x0 + i + (j ? hp1 : hp0), yn = y + (j ? vp1 : vp0);
-                    good = cross_ok(P, rs, (yn >> s) * P.wctb + (xn >> s));
-                }
-                if (!good) continue;
-                const int sum = (v[i] > nv[0][i]) - (v[i] < nv[0][i]) + (v[i] > nv[1][i]) - (v[i] < nv[1][i]);
-                // edge_map [1, 2, 0, 3, 4]: sum -2 -> offsets[0], -1 -> [1], 0 -> none, 1 -> [2], 2 -> [3]
-                const int e = sum == -2 ? 0 : sum == -1 ? 1 : sum == 1 ? 2 : sum == 2 ? 3 : -1;
-                if (e >= 0) res[i] = clampi(v[i] + ct.sao.offsets[c][e], 0, max);
+__global__ void __launch_bounds__(LF_THREADS) hevc_loopfilter_kernel(HevcLaunch P) {
+    __shared__ __align__(16) LfTile<T> S;
+    using R4 = typename Raw4<T>::type;
+    const int x0 = blockIdx.x * LF_TW, y0 = blockIdx.y * LF_TH;
+    const int ox = x0 - LF_HALO, oy = y0 - LF_HALO;  // luma position of S.y[0][0]
+    const int cx0 = x0 / 2, cy0 = y0 / 2, cox = cx0 - LF_HALO, coy = cy0 - LF_HALO;
+    const int tid = threadIdx.x;
+    // 1. load: four samples per step (W and H are multiples of 8, so a
+    // 4-aligned group of four lies wholly inside or outside the picture;
+    // outside ones, which no filter and no SAO class reads, are zero)
+    {
+        constexpr int LQ = LF_LH * (LF_LW / 4), CQ = LF_CH * (LF_CW / 4);
+        const T *wy = plane_ptr<T>(P.work, P, 0);
+        const long py = pitch_el(P, 0, sizeof(T)), pc = pitch_el(P, 1, sizeof(T));
+        for (int i = tid; i < LQ + 2 * CQ; i += LF_THREADS) {
+            const bool luma = i < LQ;
+            const int c = luma ? 0 : 1 + (i - LQ) / CQ, j = luma ? i : (i - LQ) % CQ;
+            const int rw = (luma ? LF_LW : LF_CW) / 4, r = j / rw, q = j % rw;
+            const int x = (luma ? ox : cox) + 4 * q, y = (luma ? oy : coy) + r;
+            const bool in = x >= 0 && y >= 0 && x < (luma ? P.W : P.CW) && y < (luma ? P.H : P.CH);
+            R4 v{};
+            if (in) v = __ldg((const R4 *)((luma ? wy : plane_ptr<T>(P.work, P, c)) + (size_t)y * (luma ? py : pc) + x));
+            T *d = luma ? &S.y[r][4 * q] : &S.c[c - 1][r][4 * q];
+            *(R4 *)d = v;
+        }
+    }
+    __syncthreads();
+    // 2. vertical edges: luma at x0 + 8e, every 4-row segment of the tile;
+    // chroma at luma x0 + 16e, every 4-chroma-row segment
+    {
+        constexpr int LE = LF_TW / 8 + 1, LR = LF_LH / 4, CE = LF_TW / 16 + 1, CR = LF_CH / 4;
+        for (int i = tid; i < LE * LR + CE * CR; i += LF_THREADS) {
+            if (i < LE * LR) {
+                const int bx = (x0 >> 2) + 2 * (i % LE), by = (oy >> 2) + i / LE;
+                if (bx >= 2 && bx < P.w4 && by >= 0 && by < P.h4) deblock_segment<T, 0>(P, S, bx, by, false, x0, y0);
+            } else {
+                const int k = i - LE * LR;
+                const int bx = (x0 >> 2) + 4 * (k % CE), by = ((y0 - 2 * LF_HALO) >> 2) + 2 * (k / CE);
+                if (bx >= 4 && bx < P.w4 && by >= 0 && by < P.h4) deblock_segment<T, 0>(P, S, bx, by, true, x0, y0);
             }
         }
     }
+    __syncthreads();
+    // 3. horizontal edges: luma at y0 + 8e, every 4-column segment; chroma
+    // at luma y0 + 16e, every 4-chroma-column segment
+    {
+        constexpr int LE = LF_TH / 8 + 1, LR = LF_LW / 4, CE = LF_TH / 16 + 1, CR = LF_CW / 4;
+        for (int i = tid; i < LE * LR + CE * CR; i += LF_THREADS) {
+            if (i < LE * LR) {
+                const int by = (y0 >> 2) + 2 * (i / LR), bx = (ox >> 2) + i % LR;
+                if (by >= 2 && by < P.h4 && bx >= 0 && bx < P.w4) deblock_segment<T, 1>(P, S, bx, by, false, x0, y0);
+            } else {
+                const int k = i - LE * LR;
+                const int by = (y0 >> 2) + 4 * (k / CR), bx = ((x0 - 2 * LF_HALO) >> 2) + 2 * (k % CR);
+                if (by >= 4 && by < P.h4 && bx >= 0 && bx < P.w4) deblock_segment<T, 1>(P, S, bx, by, true, x0, y0);
+            }
+        }
+    }
+    __syncthreads();
+    // 4. SAO (filter.rs sao), four samples per thread, which share a CTB
+    constexpr int LQ = LF_TH * (LF_TW / 4), CQ = (LF_TH / 2) * (LF_TW / 8);
+    for (int i = tid; i < LQ + 2 * CQ; i += LF_THREADS) {
+        const bool luma = i < LQ;
+        const int c = luma ? 0 : 1 + (i - LQ) / CQ, j = luma ? i : (i - LQ) % CQ, sc = luma ? 0 : 1;
+        const int rw = luma ? LF_TW / 4 : LF_TW / 8, tx = 4 * (j % rw), ty = j / rw;
+        const int w = c ? P.CW : P.W, h = c ? P.CH : P.H;
+        const int xq = (luma ? x0 : cx0) + tx, y = (luma ? y0 : cy0) + ty;
+        if (xq >= w || y >= h) continue;
+        // the tile's samples at tile position (sx, sy), halo included
+        const T *tile = luma ? &S.y[0][0] : &S.c[c - 1][0][0];
+        const int tw = luma ? LF_LW : LF_CW;
+        auto at = [&](int sx, int sy) { return (int)tile[(sy + LF_HALO) * tw + sx + LF_HALO]; };
+        int v[4], res[4];
 #pragma unroll
-    for (int i = 0; i < 4; i++)
-        if (nof[i]) res[i] = v[i];
-    Quad<T>::store(out + (size_t)y * pitch + x0, res);
-}
-
-template <class T>
-void launch_all_deblock(const HevcLaunch &p, cudaStream_t st) {
-    const int nv = ((p.w4 - 1) / 2) * p.h4 + ((p.w4 - 1) / 4) * ((p.h4 + 1) / 2);
-    const int nh = p.w4 * ((p.h4 - 1) / 2) + ((p.w4 + 1) / 2) * ((p.h4 - 1) / 4);
-    if (nv > 0) hevc_deblock_kernel<T, 0><<<(nv + 127) / 128, 128, 0, st>>>(p);
-    if (nh > 0) hevc_deblock_kernel<T, 1><<<(nh + 127) / 128, 128, 0, st>>>(p);
+        for (int k = 0; k < 4; k++) res[k] = v[k] = at(tx + k, ty);
+        const int s = P.log2ctb - sc;
+        const int rs = (y >> s) * P.wctb + (xq >> s);
+        const rc_hevc_ctb &ct = P.ctbs[rs];
+        const rc_hevc_slice *sl = slice_of_ctb(P, rs);
+        const int type = ct.sao.type_idx[c];
+        if ((c ? sl->sao_chroma : sl->sao_luma) && type != 0 && ct.slice < P.num_slices) {
+            const int bd = P.bd, max = (1 << bd) - 1;
+            if (type == 1) {
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    const int band = v[k] >> (bd - 5), e = (band - ct.sao.band_pos[c]) & 31;
+                    if (e < 4) res[k] = clampi(v[k] + ct.sao.offsets[c][e], 0, max);
+                }
+            } else {
+                const int cls = ct.sao.eo_class[c] & 3;
+                const int hp0 = cls == 1 ? 0 : cls == 3 ? 1 : -1, hp1 = -hp0;
+                const int vp0 = cls == 0 ? 0 : -1, vp1 = -vp0;
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    bool good = true;
+                    int nv[2];
+#pragma unroll
+                    for (int m = 0; m < 2; m++) {
+                        const int xn = xq + k + (m ? hp1 : hp0), yn = y + (m ? vp1 : vp0);
+                        good = good && xn >= 0 && yn >= 0 && xn < w && yn < h &&
+                               cross_ok(P, rs, (yn >> s) * P.wctb + (xn >> s));
+                        nv[m] = at(tx + k + (m ? hp1 : hp0), ty + (m ? vp1 : vp0));
+                    }
+                    if (!good) continue;
+                    const int sum = (v[k] > nv[0]) - (v[k] < nv[0]) + (v[k] > nv[1]) - (v[k] < nv[1]);
+                    // edge_map [1, 2, 0, 3, 4]: sum -2 -> offsets[0], -1 -> [1], 0 -> none, 1 -> [2], 2 -> [3]
+                    const int e = sum == -2 ? 0 : sum == -1 ? 1 : sum == 1 ? 2 : sum == 2 ? 3 : -1;
+                    if (e >= 0) res[k] = clampi(v[k] + ct.sao.offsets[c][e], 0, max);
+                }
+            }
+        }
+        // PCM with the loop filter off and transquant bypass keep the
+        // deblocked sample (one 4x4 luma unit per luma sample, two per
+        // group of four chroma samples)
+        const rc_hevc_blk *brow = P.blk + (size_t)((y << sc) >> 2) * P.w4;
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+            if (brow[((xq + k) << sc) >> 2].flags & RC_HEVC_F_NOFILTER) res[k] = v[k];
+        T *out = plane_ptr<T>(P.dpb + (size_t)P.out_slot * P.slot_bytes, P, c);
+        Quad<T>::store(out + (size_t)y * pitch_el(P, c, sizeof(T)) + xq, res);
+    }
 }
 
 }  // namespace
@@ -1144,13 +1203,8 @@ void rc_launch_hevc_intra(const HevcLaunch &p, cudaStream_t st, int blocks) {
     else hevc_intra_kernel<uint8_t><<<blocks, 32 * INTRA_WARPS, dyn, st>>>(p);
 }
 
-void rc_launch_hevc_deblock(const HevcLaunch &p, cudaStream_t st) {
-    if (p.bd > 8) launch_all_deblock<uint16_t>(p, st);
-    else launch_all_deblock<uint8_t>(p, st);
-}
-
-void rc_launch_hevc_sao(const HevcLaunch &p, cudaStream_t st) {
-    dim3 grid((p.W / 4 + 31) / 32, (p.H + 7) / 8, 3);
-    if (p.bd > 8) hevc_sao_kernel<uint16_t><<<grid, 256, 0, st>>>(p);
-    else hevc_sao_kernel<uint8_t><<<grid, 256, 0, st>>>(p);
+void rc_launch_hevc_loopfilter(const HevcLaunch &p, cudaStream_t st) {
+    dim3 grid((p.W + LF_TW - 1) / LF_TW, (p.H + LF_TH - 1) / LF_TH);
+    if (p.bd > 8) hevc_loopfilter_kernel<uint16_t><<<grid, LF_THREADS, 0, st>>>(p);
+    else hevc_loopfilter_kernel<uint8_t><<<grid, LF_THREADS, 0, st>>>(p);
 }

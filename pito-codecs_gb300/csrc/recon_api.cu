@@ -1284,9 +1284,8 @@ int rc_hevc_submit(rc_stream *s, const rc_hevc_picture *pic, int out_slot) {
     timed(s, RC_KERNEL_HEVC_INTRA, [&] { rc_launch_hevc_intra(L, s->st, s->wave_blocks); });
     if (cudaEventRecord(s->aux_used[ak], s->st) != cudaSuccess) return cuda_fail(s);
     s->aux_busy[ak] = true;
-    timed(s, RC_KERNEL_HEVC_DEBLOCK, [&] { rc_launch_hevc_deblock(L, s->st); });
-    timed(s, RC_KERNEL_HEVC_SAO, [&] { rc_launch_hevc_sao(L, s->st); });
-    s->launches += 2;  // deblocking is two launches (vertical, horizontal edges); the intra task order one more
+    timed(s, RC_KERNEL_HEVC_LOOPFILTER, [&] { rc_launch_hevc_loopfilter(L, s->st); });
+    s->launches += 1;  // the intra task order is one more launch
     if (pic->mem == RC_MEM_HOST && (rc = set_release(s, s->submits & 1)) != 0) return rc;
     s->submits++;
     if (cudaGetLastError() != cudaSuccess) return cuda_fail(s);

@@ -147,8 +147,9 @@ void rc_launch_hevc_residual(const HevcLaunch &p, cudaStream_t st);
 void rc_launch_hevc_inter(const HevcLaunch &p, cudaStream_t st);
 // Builds the intra task order (two small launches) and runs the intra kernel.
 void rc_launch_hevc_intra(const HevcLaunch &p, cudaStream_t st, int blocks);
-void rc_launch_hevc_deblock(const HevcLaunch &p, cudaStream_t st);
-void rc_launch_hevc_sao(const HevcLaunch &p, cudaStream_t st);
+// Deblocking and SAO in one launch: the work picture (read only) -> the
+// output DPB slot.
+void rc_launch_hevc_loopfilter(const HevcLaunch &p, cudaStream_t st);
 
 // Launchers (h264_kernels.cu).
 void rc_launch_h264_edge(const H264Launch &p, cudaStream_t st);
