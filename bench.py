@@ -113,7 +113,7 @@ class H264Workload:
     def submit(self, st, ptr, slot):
         st.submit_h264(ptr, slot)
 
-    def stats(self, p):
+    def stats(self, p, n=0):
         """Algorithmic bytes of one picture per kernel and for the whole job."""
         E = self.E
         recs = p.mbs().reshape(-1, 176)
@@ -155,7 +155,8 @@ class HevcWorkload:
     frames = 60
     slots = 5
     kernels = {3: ("hevc_residual_kernel", "residual"), 4: ("hevc_inter_kernel", "inter"),
-               5: ("hevc_intra_kernel", "intra"), 6: ("hevc_loopfilter_kernel", "loopfilter")}
+               5: ("hevc_intra_kernel", "intra"), 6: ("hevc_loopfilter_kernel", "loopfilter"),
+               7: ("hevc_inter_kernel_late", "inter_late")}
     buffer_keys = ("ctbs", "blk", "mvf", "tus", "slices", "levels", "scaling")
 
     def __init__(self, E, W, H, bd, frames=None):
@@ -192,22 +193,45 @@ class HevcWorkload:
     def submit(self, st, ptr, slot):
         st.submit_hevc(ptr, slot)
 
-    def stats(self, p):
-        """Coarse algorithmic bytes per kernel (whole planes) and for the job."""
+    def stats(self, p, n=0):
+        """Coarse algorithmic bytes per kernel (whole planes) and for the job;
+        picture n of the sequence (its inter units split between the pass
+        beside the previous picture and the one after it)."""
         b = p.buffers()
         bps = 2 if self.bd > 8 else 1
         samples = self.W * self.H * 3 // 2
         plane = samples * bps
         res = samples * 2
         mvf = np.frombuffer(b["mvf"], np.uint8).reshape(-1, 12)
-        ref_idx = mvf[:, 8:10].view(np.int8)
+        ref_idx = mvf[:, 8:10].view(np.int8).astype(np.int64)
         lists = (ref_idx >= 0).sum(axis=1)
         inter_frac = float((lists > 0).mean()) if len(lists) else 0.0
         ref_bytes = int(lists.sum()) * 24 * bps  # 16 luma + 2 x 4 chroma samples per 4x4 and list
+        # units that read the previous picture's slot (the second inter pass)
+        late = np.zeros(len(lists), bool)
+        if n > 0 and len(lists):
+            E = self.E
+            sl = (E.HevcSlice * p.pic.num_slices).from_buffer_copy(b["slices"])
+            ref_slot = np.array([[list(s.ref_slot[l]) for l in range(2)] for s in sl])
+            nref = np.array([list(s.num_ref) for s in sl])
+            ctb_slice = np.frombuffer(b["ctbs"], np.uint8).reshape(-1, ctypes.sizeof(E.HevcCtb))[:, :2].copy()
+            ctb_slice = np.minimum(ctb_slice.view(np.uint16)[:, 0], len(sl) - 1)
+            w4, h4 = self.W // 4, self.H // 4
+            lg, wctb = p.pic.log2_ctb, -(-self.W >> p.pic.log2_ctb)
+            uy, ux = np.divmod(np.arange(w4 * h4), w4)
+            us = ctb_slice[((uy * 4) >> lg) * wctb + ((ux * 4) >> lg)]
+            prev = (n - 1) % self.slots
+            for l in range(2):
+                ri = ref_idx[:, l]
+                ok = (ri >= 0) & (ri < np.minimum(nref[us, l], 16))
+                late |= ok & (ref_slot[us, l, np.clip(ri, 0, 15)] == prev)
+        late_frac = float(late.mean()) if len(lists) else 0.0
+        late_ref = int(lists[late].sum()) * 24 * bps
         syn = p.nbytes
         return {
             "residual": len(b["tus"]) + len(b["levels"]) + res,
-            "inter": ref_bytes + int(inter_frac * (res + plane)),
+            "inter": ref_bytes - late_ref + int((inter_frac - late_frac) * (res + plane)),
+            "inter_late": late_ref + int(late_frac * (res + plane)),
             "intra": int((1 - inter_frac) * (res + plane)),
             "loopfilter": 2 * plane + len(b["blk"]) + len(b["ctbs"]),
             "job": plane + ref_bytes + syn,
@@ -575,7 +599,7 @@ def main():
     wl = workload(E, args.workload, args.frames or None)
     frames = wl.frames
     pics = wl.sequence(SEED + 7919 * rank)
-    stats = [wl.stats(p) for p in pics]
+    stats = [wl.stats(p, n) for n, p in enumerate(pics)]
     bps = 2 if wl.bd > 8 else 1
 
     # device-resident and pinned-host copies of every picture's records
@@ -697,8 +721,10 @@ def main():
         if k not in wl.kernels or n == 0:
             continue
         name, key = wl.kernels[k]
-        # a group launch covers frames / launches pictures of the profiled pass
-        alg = statistics.mean(s[key] for s in stats) * (frames / n if key == "group" else 1)
+        # the profiled pass's pictures over its launches of the kernel (a
+        # group launch covers several pictures; the second inter pass runs
+        # for the pictures that reference the previous one)
+        alg = sum(s[key] for s in stats) / n
         per_kernel[name] = {"launches": n, "ms_total": ms, "us_per_launch": ms / n * 1000,
                             "alg_bytes_per_launch": alg, "achieved_gbs": alg / (ms / n / 1000) / 1e9}
     dom = max(per_kernel, key=lambda k: per_kernel[k]["ms_total"])

@@ -422,10 +422,12 @@ int rc_picture_device_planes(rc_stream *s, int slot, void **y, void **u,
 #define RC_KERNEL_H264_BAND 1
 #define RC_KERNEL_H264_EDGE 2
 #define RC_KERNEL_HEVC_RESIDUAL 3
-#define RC_KERNEL_HEVC_INTER 4
+#define RC_KERNEL_HEVC_INTER 4      /* inter units whose references are final
+                                      (beside the previous picture)      */
 #define RC_KERNEL_HEVC_INTRA 5
-#define RC_KERNEL_HEVC_LOOPFILTER 6 /* deblocking and SAO, one launch   */
-/* 7: not used (deblocking and SAO were separate launches before) */
+#define RC_KERNEL_HEVC_LOOPFILTER 6 /* deblocking and SAO, one launch     */
+#define RC_KERNEL_HEVC_INTER_LATE 7 /* inter units reading the previous
+                                      picture (after it)                 */
 #define RC_KERNEL_H264_GROUP 8
 #define RC_KERNEL_H264_MV 9
 #define RC_KERNEL_COUNT 10
@@ -502,7 +504,12 @@ int rc_h264_deblock_noalloc(const rc_h264_picture *pic, int mb_w, int mb_h,
 /* Number of kernel launches this stream has issued so far. */
 long long rc_stream_launches(rc_stream *s);
 
-/* The CUDA stream (cudaStream_t) the stream's work is ordered on. */
+/* The CUDA stream (cudaStream_t) the stream's work is ordered on.  HEVC
+ * streams also read reference slots from a second CUDA stream (a picture's
+ * inter units whose references are final are predicted there, beside the
+ * previous picture): work the caller enqueues on this stream that writes a
+ * DPB slot is seen by later submits when this function, or
+ * rc_picture_device_planes, is called after that work is enqueued. */
 void *rc_stream_cuda_stream(rc_stream *s);
 
 /* Completion marks, for request loops that keep many streams busy without a

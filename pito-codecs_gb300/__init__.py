@@ -33,7 +33,7 @@ ERROR_NAMES = {RC_EINVAL: "RC_EINVAL", RC_ENOMEM: "RC_ENOMEM", RC_ECUDA: "RC_ECU
 
 RC_H264_NONE, RC_H264_I4x4, RC_H264_I8x8, RC_H264_I16x16, RC_H264_IPCM, RC_H264_INTER = range(6)
 RC_KERNEL_NAMES = {0: "h264_mb_kernel", 1: "h264_band_kernel", 2: "h264_edge_kernel", 3: "hevc_residual_kernel",
-                   4: "hevc_inter_kernel", 5: "hevc_intra_kernel", 6: "hevc_loopfilter_kernel",
+                   4: "hevc_inter_kernel", 5: "hevc_intra_kernel", 6: "hevc_loopfilter_kernel", 7: "hevc_inter_kernel_late",
                    8: "h264_group_kernel", 9: "h264_mv_kernel"}
 RC_KERNEL_COUNT = 10
 

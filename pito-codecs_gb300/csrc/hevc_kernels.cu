@@ -39,6 +39,8 @@
 // reconstruction half of src/hevc/slicedec.rs; citations at each function.
 #include <stdint.h>
 
+#include <algorithm>
+
 #include "recon_internal.h"
 
 namespace {
@@ -382,47 +384,112 @@ __device__ void mc_n(const HevcLaunch &P, int c, int x, int y, const rc_hevc_mvf
     }
 }
 
+// A unit is late when one of the references it reads lies in slot
+// P.late_slot, the previous picture (HevcLaunch::inter_pass).  References
+// that do not resolve to a slot count as early; the early pass reports them.
+__device__ __forceinline__ bool unit_is_late(const HevcLaunch &P, const rc_hevc_mvf &f, const rc_hevc_slice *sl) {
+    bool late = false;
+#pragma unroll
+    for (int l = 0; l < 2; l++) {
+        const int ri = f.ref_idx[l];
+        late = late || (ri >= 0 && ri < min(sl->num_ref[l], RC_HEVC_MAX_REFS) && sl->ref_slot[l][ri] == P.late_slot);
+    }
+    return late;
+}
+
+// Four adjacent luma samples (x a multiple of 4) of an inter unit with
+// motion f: prediction, residual, clip into the work picture.
+template <class T>
+__device__ __forceinline__ void inter_luma_quad(const HevcLaunch &P, int x, int y, const rc_hevc_mvf &f,
+                                                const rc_hevc_slice *sl) {
+    int v[4];
+    mc_n<T, 4>(P, 0, x, y, f, sl, v);
+    const int16_t *r = res_plane(P, 0) + (size_t)y * P.W + x;
+    const int max = (1 << P.bd) - 1;
+#pragma unroll
+    for (int i = 0; i < 4; i++) v[i] = clampi(v[i] + r[i], 0, max);
+    Quad<T>::store(plane_ptr<T>(P.work, P, 0) + (size_t)y * pitch_el(P, 0, sizeof(T)) + x, v);
+}
+// Two adjacent samples (x even) of chroma plane c.
+template <class T>
+__device__ __forceinline__ void inter_chroma_pair(const HevcLaunch &P, int c, int x, int y, const rc_hevc_mvf &f,
+                                                  const rc_hevc_slice *sl) {
+    int v[2];
+    mc_n<T, 2>(P, c, x, y, f, sl, v);
+    const int16_t *r = res_plane(P, c) + (size_t)y * P.CW + x;
+    T *o = plane_ptr<T>(P.work, P, c) + (size_t)y * pitch_el(P, c, sizeof(T)) + x;
+    const int max = (1 << P.bd) - 1;
+#pragma unroll
+    for (int i = 0; i < 2; i++) o[i] = (T)clampi(v[i] + r[i], 0, max);
+}
+
+// Appends the items of the lanes that push to the late list: one atomic per
+// warp (all 32 lanes of the warp call it).
+__device__ __forceinline__ void late_push(const HevcLaunch &P, bool push, uint32_t item) {
+    const unsigned m = __ballot_sync(0xffffffffu, push);
+    if (!m) return;
+    const int lane = threadIdx.x & 31, lead = __ffs(m) - 1;
+    uint32_t base = 0;
+    if (lane == lead) base = atomicAdd(P.late_count, (uint32_t)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, lead);
+    if (push) P.late_items[base + __popc(m & ((1u << lane) - 1))] = item;
+}
+
 // One CTA per 16x16 luma area: a thread reconstructs four adjacent luma
 // samples of one 4x4 unit, then two adjacent chroma samples (of one unit
-// too), each group with its motion field read once
+// too), each group with its motion field read once.  In the early pass
+// (inter_pass 1) a late unit's groups go to the late list instead, as items
+// c << 30 | y << 16 | x, for hevc_inter_late_kernel.
 template <class T>
 __global__ void __launch_bounds__(64) hevc_inter_kernel(HevcLaunch P) {
     const int t = threadIdx.x;
-    uint8_t *work = P.work;
-    const int max = (1 << P.bd) - 1;
+    const bool early = P.inter_pass == 1;
     {
         const int x = blockIdx.x * 16 + (t & 3) * 4, y = blockIdx.y * 16 + (t >> 2);
+        bool push = false;
         if (x < P.W && y < P.H) {  // W is a multiple of 8: the group lies inside
             const int bi = (y >> 2) * P.w4 + (x >> 2);
             const rc_hevc_blk b = P.blk[bi];
             if ((b.flags & RC_HEVC_F_CODED) && !(b.flags & RC_HEVC_F_INTRA)) {
                 const rc_hevc_mvf f = P.mvf[bi];
                 const rc_hevc_slice *sl = slice_of_ctb(P, ctb_of(P, x, y));
-                int v[4];
-                mc_n<T, 4>(P, 0, x, y, f, sl, v);
-                const int16_t *r = res_plane(P, 0) + (size_t)y * P.W + x;
-#pragma unroll
-                for (int i = 0; i < 4; i++) v[i] = clampi(v[i] + r[i], 0, max);
-                Quad<T>::store(plane_ptr<T>(work, P, 0) + (size_t)y * pitch_el(P, 0, sizeof(T)) + x, v);
+                push = early && unit_is_late(P, f, sl);
+                if (!push) inter_luma_quad<T>(P, x, y, f, sl);
             }
         }
+        if (early) late_push(P, push, (uint32_t)y << 16 | (uint32_t)x);
     }
     {
         const int c = 1 + (t >> 5), x = blockIdx.x * 8 + (t & 3) * 2, y = blockIdx.y * 8 + ((t >> 2) & 7);
+        bool push = false;
         if (x < P.CW && y < P.CH) {  // CW is a multiple of 4
             const int bi = ((2 * y) >> 2) * P.w4 + ((2 * x) >> 2);
             const rc_hevc_blk b = P.blk[bi];
             if ((b.flags & RC_HEVC_F_CODED) && !(b.flags & RC_HEVC_F_INTRA)) {
                 const rc_hevc_mvf f = P.mvf[bi];
                 const rc_hevc_slice *sl = slice_of_ctb(P, ctb_of(P, 2 * x, 2 * y));
-                int v[2];
-                mc_n<T, 2>(P, c, x, y, f, sl, v);
-                const int16_t *r = res_plane(P, c) + (size_t)y * P.CW + x;
-                T *o = plane_ptr<T>(work, P, c) + (size_t)y * pitch_el(P, c, sizeof(T)) + x;
-#pragma unroll
-                for (int i = 0; i < 2; i++) o[i] = (T)clampi(v[i] + r[i], 0, max);
+                push = early && unit_is_late(P, f, sl);
+                if (!push) inter_chroma_pair<T>(P, c, x, y, f, sl);
             }
         }
+        if (early) late_push(P, push, (uint32_t)c << 30 | (uint32_t)y << 16 | (uint32_t)x);
+    }
+}
+
+// The late pass: the groups the early pass listed, one per thread (a fixed
+// grid strides over the list, whose length the early pass left on the device).
+template <class T>
+__global__ void __launch_bounds__(256) hevc_inter_late_kernel(HevcLaunch P) {
+    const uint32_t n = min(*P.late_count, P.late_cap);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t it = P.late_items[i];
+        const int c = it >> 30, y = (it >> 16) & 0x3fff, x = it & 0xffff;
+        const int lx = c ? 2 * x : x, ly = c ? 2 * y : y;
+        const int bi = (ly >> 2) * P.w4 + (lx >> 2);
+        const rc_hevc_mvf f = P.mvf[bi];
+        const rc_hevc_slice *sl = slice_of_ctb(P, ctb_of(P, lx, ly));
+        if (c == 0) inter_luma_quad<T>(P, x, y, f, sl);
+        else inter_chroma_pair<T>(P, c, x, y, f, sl);
     }
 }
 
@@ -1182,6 +1249,15 @@ void rc_launch_hevc_residual(const HevcLaunch &p, cudaStream_t st) {
 }
 
 void rc_launch_hevc_inter(const HevcLaunch &p, cudaStream_t st) {
+    if (p.inter_pass == 2) {
+        // one item per thread for lists up to a quarter of the groups (the
+        // kernel strides over longer ones)
+        const int grid = std::max<int>(152, (int)((p.late_cap / 4 + 255) / 256));
+        if (p.bd > 8) hevc_inter_late_kernel<uint16_t><<<grid, 256, 0, st>>>(p);
+        else hevc_inter_late_kernel<uint8_t><<<grid, 256, 0, st>>>(p);
+        return;
+    }
+    if (p.inter_pass == 1) cudaMemsetAsync(p.late_count, 0, sizeof(uint32_t), st);
     dim3 grid((p.W + 15) / 16, (p.H + 15) / 16);
     if (p.bd > 8) hevc_inter_kernel<uint16_t><<<grid, 64, 0, st>>>(p);
     else hevc_inter_kernel<uint8_t><<<grid, 64, 0, st>>>(p);

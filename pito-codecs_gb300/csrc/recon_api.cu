@@ -98,7 +98,23 @@ struct rc_stream {
     int16_t *ires = nullptr;
     // HEVC
     DevBuf ctbs[2], blk[2], mvf[2], tus[2], hslices[2], scaling;
-    uint8_t *work = nullptr;     // picture being reconstructed (pre-SAO)
+    // the picture being reconstructed (pre-loop-filter), two by submit
+    // parity: a picture's inter prediction runs on the side stream beside
+    // the previous picture's intra and loop-filter kernels, for the units
+    // whose references are final; work_free[i]: the loop filter that last
+    // read work[i]
+    uint8_t *work[2] = {nullptr, nullptr};
+    uint32_t *late_items[2] = {nullptr, nullptr};  // the late inter units' groups
+    uint32_t *late_count = nullptr;                // two counters
+    size_t late_cap = 0;
+    cudaEvent_t work_free[2] = {nullptr, nullptr};
+    bool work_busy[2] = {false, false};
+    // the previous picture's output slot (its units are predicted on the
+    // main stream after it), and whether the caller may have written a slot
+    // on the main stream since (rc_stream_cuda_stream, device planes), which
+    // orders the next early pass after the main stream
+    int hevc_prev_slot = -1;
+    bool hevc_ext = false;
     int16_t *res[2] = {nullptr, nullptr};  // residual planes (two sets by submit parity)
     uint32_t *ready = nullptr;   // per 4x4 block and component
     uint32_t *ctb_ord[2] = {nullptr, nullptr};  // ctb_first, ctb_end, ctb_base, ctb_nintra (smallest CTB size)
@@ -449,7 +465,12 @@ void destroy(rc_stream *s) {
     if (s->mv_ready) cudaEventDestroy(s->mv_ready);
     group_free(s);
     dev_free(s, s->scaling.p, s->scaling.cap);
-    cudaFree(s->work);
+    for (int i = 0; i < 2; i++) {
+        cudaFree(s->work[i]);
+        if (s->late_items[i]) dev_free(s, s->late_items[i], s->late_cap * sizeof(uint32_t));
+        if (s->work_free[i]) cudaEventDestroy(s->work_free[i]);
+    }
+    cudaFree(s->late_count);
     for (int i = 0; i < 2; i++) cudaFree(s->res[i]);
     cudaFree(s->ready);
     for (int i = 0; i < 2; i++) dev_free(s, s->ctb_ord[i], 4 * s->nctb_max * sizeof(uint32_t));
@@ -879,14 +900,18 @@ int rc_stream_create(int codec, int width, int height, int bit_depth, int dpb_sl
         if (v > 0 && v <= 4096) s->wave_blocks = v;
     }
     const int n = s->mb_w * s->mb_h;
-    bool ok = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking) == cudaSuccess &&
+    // HEVC: the kernels' stream first when CTAs of both kernel streams wait
+    // for an SM (the side stream's inter pass runs beside the intra chain)
+    int prio_low = 0, prio_high = 0;
+    if (codec == RC_CODEC_HEVC) cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high);
+    bool ok = cudaStreamCreateWithPriority(&s->st, cudaStreamNonBlocking, prio_high) == cudaSuccess &&
               cudaStreamCreateWithFlags(&s->cst, cudaStreamNonBlocking) == cudaSuccess &&
               cudaStreamCreateWithFlags(&s->dst, cudaStreamNonBlocking) == cudaSuccess;
     for (int i = 0; i < REC_SETS && ok; i++)
         ok = cudaEventCreateWithFlags(&s->set_used[i], cudaEventDisableTiming) == cudaSuccess &&
              cudaEventCreateWithFlags(&s->set_ready[i], cudaEventDisableTiming) == cudaSuccess;
     ok = ok && cudaEventCreateWithFlags(&s->kernels_done, cudaEventDisableTiming) == cudaSuccess &&
-         cudaStreamCreateWithFlags(&s->est, cudaStreamNonBlocking) == cudaSuccess &&
+         cudaStreamCreateWithPriority(&s->est, cudaStreamNonBlocking, prio_low) == cudaSuccess &&
          cudaEventCreateWithFlags(&s->aux_ready, cudaEventDisableTiming) == cudaSuccess;
     for (int i = 0; i < 2 && ok; i++) ok = cudaEventCreateWithFlags(&s->aux_used[i], cudaEventDisableTiming) == cudaSuccess;
     s->slot_dl.assign(s->slots, nullptr);
@@ -912,13 +937,20 @@ int rc_stream_create(int codec, int width, int height, int bit_depth, int dpb_sl
     }
     if (codec == RC_CODEC_HEVC) {
         const size_t nres = (size_t)s->width * s->height + 2 * (size_t)s->cw * s->ch;
-        ok = ok && dev_alloc(s, (void **)&s->work, s->slot_bytes);
+        // a luma group per four samples and a chroma group per two
+        s->late_cap = (size_t)s->width * s->height / 4 + (size_t)s->cw * s->ch;
+        ok = ok && cudaMalloc(&s->late_count, 2 * sizeof(uint32_t)) == cudaSuccess;
+        for (int i = 0; i < 2; i++) {
+            ok = ok && dev_alloc(s, (void **)&s->late_items[i], s->late_cap * sizeof(uint32_t));
+            ok = ok && dev_alloc(s, (void **)&s->work[i], s->slot_bytes);
+            ok = ok && cudaEventCreateWithFlags(&s->work_free[i], cudaEventDisableTiming) == cudaSuccess;
+            ok = ok && cudaMemsetAsync(s->work[i], 0, s->slot_bytes, s->st) == cudaSuccess;
+        }
         for (int i = 0; i < 2; i++) ok = ok && dev_alloc(s, (void **)&s->res[i], nres * sizeof(int16_t));
         ok = ok && dev_alloc(s, (void **)&s->ready, 3 * (size_t)s->w4 * s->h4 * sizeof(uint32_t));
         s->nctb_max = (size_t)((s->width + 15) / 16) * ((s->height + 15) / 16);
         for (int i = 0; i < 2; i++) ok = ok && dev_alloc(s, (void **)&s->ctb_ord[i], 4 * s->nctb_max * sizeof(uint32_t));
         ok = ok && cudaMemsetAsync(s->ready, 0, 3 * (size_t)s->w4 * s->h4 * sizeof(uint32_t), s->st) == cudaSuccess;
-        ok = ok && cudaMemsetAsync(s->work, 0, s->slot_bytes, s->st) == cudaSuccess;
     }
     for (int i = 0; i < 2 && ok; i++) ok = cudaEventCreateWithFlags(&s->staged[i], cudaEventDisableTiming) == cudaSuccess;
     if (ok) {
@@ -1255,8 +1287,8 @@ int rc_hevc_submit(rc_stream *s, const rc_hevc_picture *pic, int out_slot) {
     L.out_slot = out_slot;
     L.pitch = s->pitch;
     L.cpitch = s->cpitch;
-    L.work = s->work;
     const int ak = s->submits & 1;
+    L.work = s->work[ak];
     L.res = s->res[ak];
     L.ready = s->ready;
     if ((size_t)wctb * hctb > s->nctb_max || wctb + 2 * hctb > 2048) return RC_EINVAL;
@@ -1278,13 +1310,53 @@ int rc_hevc_submit(rc_stream *s, const rc_hevc_picture *pic, int out_slot) {
         if (!ok) return cuda_fail(s);
     }
     timed(s, RC_KERNEL_HEVC_RESIDUAL, [&] { rc_launch_hevc_residual(L, s->est); }, s->est);
+    // inter prediction in two passes (the decoder's frame threading waits
+    // the same way for the reference rows a block reads,
+    // src/hevc/decoder.rs:508-528): on the side stream, once this work
+    // picture's last loop filter is done (so every picture before the
+    // previous one is final), the units that do not read the previous
+    // picture; on the main stream, after the previous picture, the units that
+    // read it.  A picture that does not reference the previous one (host
+    // records show it) needs no second pass.
+    int late = s->hevc_prev_slot;
+    if (late >= 0 && pic->mem == RC_MEM_HOST) {
+        bool reads = false;
+        for (int i = 0; i < pic->num_slices && !reads; i++)
+            for (int l = 0; l < 2 && !reads; l++)
+                for (int r = 0; r < pic->slices[i].num_ref[l] && r < RC_HEVC_MAX_REFS; r++)
+                    reads = reads || pic->slices[i].ref_slot[l][r] == late;
+        if (!reads) late = -1;
+    }
+    {
+        bool ok = true;
+        if (s->work_busy[ak]) ok = cudaStreamWaitEvent(s->est, s->work_free[ak], 0) == cudaSuccess;
+        if (s->hevc_ext) {  // a slot the caller wrote on the main stream: after it
+            ok = ok && cudaEventRecord(s->aux_ready, s->st) == cudaSuccess &&
+                 cudaStreamWaitEvent(s->est, s->aux_ready, 0) == cudaSuccess;
+            s->hevc_ext = false;
+        }
+        if (!ok) return cuda_fail(s);
+    }
+    if (s->height >= 16384 || s->width >= 65536) late = -1;  // beyond the list items' fields: one pass
+    L.late_slot = late;
+    L.inter_pass = late >= 0 ? 1 : 0;
+    L.late_items = s->late_items[ak];
+    L.late_count = s->late_count + ak;
+    L.late_cap = (uint32_t)s->late_cap;
+    timed(s, RC_KERNEL_HEVC_INTER, [&] { rc_launch_hevc_inter(L, s->est); }, s->est);
     if (cudaEventRecord(s->aux_ready, s->est) != cudaSuccess || cudaStreamWaitEvent(s->st, s->aux_ready, 0) != cudaSuccess)
         return cuda_fail(s);
-    timed(s, RC_KERNEL_HEVC_INTER, [&] { rc_launch_hevc_inter(L, s->st); });
+    if (late >= 0) {
+        L.inter_pass = 2;
+        timed(s, RC_KERNEL_HEVC_INTER_LATE, [&] { rc_launch_hevc_inter(L, s->st); });
+    }
     timed(s, RC_KERNEL_HEVC_INTRA, [&] { rc_launch_hevc_intra(L, s->st, s->wave_blocks); });
     if (cudaEventRecord(s->aux_used[ak], s->st) != cudaSuccess) return cuda_fail(s);
     s->aux_busy[ak] = true;
     timed(s, RC_KERNEL_HEVC_LOOPFILTER, [&] { rc_launch_hevc_loopfilter(L, s->st); });
+    if (cudaEventRecord(s->work_free[ak], s->st) != cudaSuccess) return cuda_fail(s);
+    s->work_busy[ak] = true;
+    s->hevc_prev_slot = out_slot;
     s->launches += 1;  // the intra task order is one more launch
     if (pic->mem == RC_MEM_HOST && (rc = set_release(s, s->submits & 1)) != 0) return rc;
     s->submits++;
@@ -1421,6 +1493,7 @@ int rc_picture_device_planes(rc_stream *s, int slot, void **y, void **u, void **
     int rc;
     if ((rc = h264_flush(s)) != 0) return rc;
     uint8_t *base = s->dpb + (size_t)slot * s->slot_bytes;
+    s->hevc_ext = true;
     if (y) *y = base;
     if (u) *u = base + s->u_off;
     if (v) *v = base + s->v_off;
@@ -1432,6 +1505,7 @@ long long rc_stream_launches(rc_stream *s) { return s ? s->launches : 0; }
 void *rc_stream_cuda_stream(rc_stream *s) {
     if (!s) return nullptr;
     h264_flush(s);  // a launch error stays in the sticky word
+    s->hevc_ext = true;
     return (void *)s->st;
 }
 

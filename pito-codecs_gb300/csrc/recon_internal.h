@@ -141,9 +141,17 @@ struct HevcLaunch {
     uint32_t *counter;
     uint32_t *error;
     uint32_t epoch, wait_limit;
+    // which inter units a launch predicts: 0 all; 1 those that read no
+    // reference in DPB slot late_slot (the previous picture, possibly still
+    // being reconstructed), listing the others (late_items, late_count, at
+    // most late_cap items); 2 the listed ones
+    int inter_pass, late_slot;
+    uint32_t *late_items, *late_count;
+    uint32_t late_cap;
 };
 
 void rc_launch_hevc_residual(const HevcLaunch &p, cudaStream_t st);
+// Inter prediction plus residual of the units p.inter_pass selects.
 void rc_launch_hevc_inter(const HevcLaunch &p, cudaStream_t st);
 // Builds the intra task order (two small launches) and runs the intra kernel.
 void rc_launch_hevc_intra(const HevcLaunch &p, cudaStream_t st, int blocks);
