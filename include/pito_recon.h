@@ -348,7 +348,14 @@ int rc_device_select(int device);
  * bytes the stream may hold (0 = unbounded); RC_ENOMEM if it would exceed it.
  * Replaces Decoder::with_threads (src/h264/mod.rs:38, src/hevc/decoder.rs:87)
  * and the decoder-owned frame pool (src/h264/dec/picture.rs:196).
+ * `codec` may carry RC_STREAM_SHARED_GPU: the stream shares the GPU with
+ * many others (the batched and served forms).  A stream without it (one
+ * decoder on the GPU) dispatches its HEVC kernels' CTAs ahead of its side
+ * stream's (1080p: 2410 -> 2500 frames/s); among many streams that
+ * preference slows the mix (64 streams: 5486 -> 5331 frames/s), so shared
+ * streams keep the default priority.
  */
+#define RC_STREAM_SHARED_GPU 0x100
 int rc_stream_create(int codec, int width, int height, int bit_depth,
                      int dpb_slots, size_t hbm_budget, rc_stream **out);
 

@@ -27,6 +27,7 @@ REPO = PKG.parent
 
 RC_OK, RC_EINVAL, RC_ENOMEM, RC_ECUDA, RC_ETIMEOUT, RC_EDEVICE, RC_ENODEV = 0, -1, -2, -3, -4, -5, -6
 RC_CODEC_H264, RC_CODEC_HEVC = 1, 2
+RC_STREAM_SHARED_GPU = 0x100  # or-ed into the codec: one of many streams on the GPU
 RC_MEM_HOST, RC_MEM_DEVICE = 0, 1
 ERROR_NAMES = {RC_EINVAL: "RC_EINVAL", RC_ENOMEM: "RC_ENOMEM", RC_ECUDA: "RC_ECUDA",
                RC_ETIMEOUT: "RC_ETIMEOUT", RC_EDEVICE: "RC_EDEVICE", RC_ENODEV: "RC_ENODEV"}
@@ -514,10 +515,11 @@ class ReconStream:
     pictures are reconstructed on (rc_stream)."""
 
     def __init__(self, codec: int, width: int, height: int, bit_depth: int = 8, dpb_slots: int = 4,
-                 hbm_budget: int = 0):
+                 hbm_budget: int = 0, shared_gpu: bool = False):
         L = lib()
         h = ctypes.c_void_p()
-        _check(L.rc_stream_create(codec, width, height, bit_depth, dpb_slots, hbm_budget, ctypes.byref(h)),
+        flags = RC_STREAM_SHARED_GPU if shared_gpu else 0
+        _check(L.rc_stream_create(codec | flags, width, height, bit_depth, dpb_slots, hbm_budget, ctypes.byref(h)),
                "rc_stream_create")
         self._h = h
         self.codec, self.bit_depth, self.slots = codec, bit_depth, dpb_slots

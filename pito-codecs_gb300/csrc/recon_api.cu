@@ -847,6 +847,8 @@ int rc_stream_create(int codec, int width, int height, int bit_depth, int dpb_sl
                      rc_stream **out) {
     if (!out) return RC_EINVAL;
     *out = nullptr;
+    const bool shared_gpu = (codec & RC_STREAM_SHARED_GPU) != 0;
+    codec &= ~RC_STREAM_SHARED_GPU;
     if (codec != RC_CODEC_H264 && codec != RC_CODEC_HEVC) return RC_EINVAL;
     if (width <= 0 || height <= 0 || width > 8192 || height > 8192 || dpb_slots <= 0 || dpb_slots > 64)
         return RC_EINVAL;
@@ -900,10 +902,11 @@ int rc_stream_create(int codec, int width, int height, int bit_depth, int dpb_sl
         if (v > 0 && v <= 4096) s->wave_blocks = v;
     }
     const int n = s->mb_w * s->mb_h;
-    // HEVC: the kernels' stream first when CTAs of both kernel streams wait
-    // for an SM (the side stream's inter pass runs beside the intra chain)
+    // HEVC alone on the GPU: the kernels' stream first when CTAs of both
+    // kernel streams wait for an SM (the side stream's inter pass runs beside
+    // the intra chain)
     int prio_low = 0, prio_high = 0;
-    if (codec == RC_CODEC_HEVC) cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high);
+    if (codec == RC_CODEC_HEVC && !shared_gpu) cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high);
     bool ok = cudaStreamCreateWithPriority(&s->st, cudaStreamNonBlocking, prio_high) == cudaSuccess &&
               cudaStreamCreateWithFlags(&s->cst, cudaStreamNonBlocking) == cudaSuccess &&
               cudaStreamCreateWithFlags(&s->dst, cudaStreamNonBlocking) == cudaSuccess;

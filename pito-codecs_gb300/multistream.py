@@ -146,7 +146,7 @@ class Templates:
 
 def open_stream(spec: StreamSpec, hbm_budget: int = 0) -> ReconStream:
     W, H = spec.coded
-    return ReconStream(spec.codec, W, H, spec.bit_depth, spec.slots, hbm_budget)
+    return ReconStream(spec.codec, W, H, spec.bit_depth, spec.slots, hbm_budget, shared_gpu=True)
 
 
 def submit(st: ReconStream, spec: StreamSpec, pic, slot: int):

@@ -107,6 +107,15 @@ def test_stream_create_rejects_bad_arguments(engine):
     assert L.rc_stream_create(engine.RC_CODEC_H264, 0, 64, 8, 2, 0, ctypes.byref(h)) == engine.RC_EINVAL
     assert L.rc_stream_create(99, 64, 64, 8, 2, 0, ctypes.byref(h)) == engine.RC_EINVAL
     assert L.rc_stream_create(engine.RC_CODEC_H264, 64, 64, 8, 0, 0, ctypes.byref(h)) == engine.RC_EINVAL
+    # the shared-GPU flag is the only bit a codec may carry
+    assert L.rc_stream_create(engine.RC_CODEC_HEVC | 0x200, 64, 64, 8, 2, 0, ctypes.byref(h)) == engine.RC_EINVAL
+    assert L.rc_stream_create(engine.RC_STREAM_SHARED_GPU, 64, 64, 8, 2, 0, ctypes.byref(h)) == engine.RC_EINVAL
+
+
+def test_shared_gpu_flag_matches_header(engine):
+    import re
+    text = (pathlib.Path(__file__).resolve().parents[1] / "include" / "pito_recon.h").read_text()
+    assert int(re.search(r"#define RC_STREAM_SHARED_GPU (0x[0-9a-f]+)", text).group(1), 16) == engine.RC_STREAM_SHARED_GPU
 
 
 def test_stream_calls_reject_null_streams(engine):
