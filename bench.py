@@ -509,9 +509,8 @@ def run_multistream(args):
         line = dict(base, metric="C4 batched recon frames/s", value=frames / t_batch, unit="frames/s",
                     steps=1, warmup=1, ms_per_step=t_batch * 1000,
                     config={"workload": "batched_c4: " + mix, "frames": frames, "depth": schedule.depth,
-                            "intra_cta_scale": schedule.intra_scale,
-                            "autotune_fps": {f"depth {s.depth}, intra x{s.intra_scale}": round(v, 1)
-                                             for s, v in rates.items()},
+                            "schedule": schedule.describe(),
+                            "autotune_fps": {k: round(v, 1) for k, v in rates.items()},
                             "plain_loop_fps": frames / t_plain, "speedup_vs_plain": t_plain / t_batch,
                             "luma_msamples_per_s": sum(luma_samples(s, s.frames) for s in specs) / t_batch / 1e6,
                             "parity": f"{'identical' if same else 'DIFFERENT'} DPBs in the mix and alone for the "

@@ -447,6 +447,13 @@ int rc_stream_profile(rc_stream *s, int enable);
 int rc_stream_set_intra_ctas(rc_stream *s, int ctas);
 /* The current value (0 for an H.264 stream, which has no such kernel). */
 int rc_stream_intra_ctas(rc_stream *s);
+/* Schedule knob (tile shape): the HEVC loop filter's tile height in luma
+ * rows, 64 (default), 32 or 16; tiles are 64 samples wide.  Anything else,
+ * or an H.264 stream, is RC_EINVAL.  Takes effect from the next submit; the
+ * output does not depend on it.  rc_stream_lf_tile returns the height (0
+ * for an H.264 stream). */
+int rc_stream_set_lf_tile(rc_stream *s, int rows);
+int rc_stream_lf_tile(rc_stream *s);
 /* Iteration cap of every device-side wait in this stream's kernels (no
  * counterpart in the reference, whose rayon jobs block on condition
  * variables).  A wait that polls `limit` times without progress records

@@ -226,6 +226,10 @@ def lib() -> ctypes.CDLL:
     L.rc_stream_set_intra_ctas.restype = i32
     L.rc_stream_intra_ctas.argtypes = [vp]
     L.rc_stream_intra_ctas.restype = i32
+    L.rc_stream_set_lf_tile.argtypes = [vp, i32]
+    L.rc_stream_set_lf_tile.restype = i32
+    L.rc_stream_lf_tile.argtypes = [vp]
+    L.rc_stream_lf_tile.restype = i32
     L.rc_stream_set_wait_limit.argtypes = [vp, ctypes.c_uint]
     L.rc_stream_set_wait_limit.restype = i32
     L.rc_stream_set_h264_group.argtypes = [vp, i32]
@@ -523,6 +527,7 @@ class ReconStream:
                "rc_stream_create")
         self._h = h
         self.codec, self.bit_depth, self.slots = codec, bit_depth, dpb_slots
+        self.h264_group = 1
         w, hh, p, cp = (ctypes.c_int() for _ in range(4))
         _check(L.rc_stream_geometry(h, ctypes.byref(w), ctypes.byref(hh), ctypes.byref(p), ctypes.byref(cp)),
                "rc_stream_geometry")
@@ -577,6 +582,13 @@ class ReconStream:
     def intra_ctas(self) -> int:
         return lib().rc_stream_intra_ctas(self._h)
 
+    def set_lf_tile(self, rows: int):
+        """HEVC loop-filter tile height in luma rows (64, 32 or 16)."""
+        _check(lib().rc_stream_set_lf_tile(self._h, int(rows)), "rc_stream_set_lf_tile")
+
+    def lf_tile(self) -> int:
+        return lib().rc_stream_lf_tile(self._h)
+
     def set_wait_limit(self, limit: int):
         """Iteration cap of the device-side waits (0: the default)."""
         _check(lib().rc_stream_set_wait_limit(self._h, int(limit)), "rc_stream_set_wait_limit")
@@ -587,6 +599,7 @@ class ReconStream:
         r = lib().rc_stream_set_h264_group(self._h, int(pictures))
         if r < 0:
             raise ReconError(r, "rc_stream_set_h264_group")
+        self.h264_group = r
         return r
 
     def profile_read(self) -> dict:

@@ -1029,23 +1029,25 @@ __device__ void filter_chroma(T *s, long o, long step, long along, int tc, bool 
 }
 
 // The loop filter works on one tile of the picture in shared memory: the
-// tile's LF_TW x LF_TH luma samples (half that per chroma plane) and a halo of
+// tile's LF_TW x TH luma samples (half that per chroma plane) and a halo of
 // LF_HALO samples on every side.  That halo holds every sample that the
 // deblocking of the tile and of its one-sample SAO border reads: vertical
 // edges lie 8 luma (8 chroma) samples apart and move at most 3 (1) samples
 // beside them, reading 4 (2); horizontal edges do the same on the vertically
-// filtered samples; so the edges at x0 .. x0 + LF_TW and y0 .. y0 + LF_TH,
+// filtered samples; so the edges at x0 .. x0 + LF_TW and y0 .. y0 + TH,
 // filtered over the whole tile with its halo, leave every sample of the tile
 // and its border as the picture-wide passes (all vertical edges, then all
 // horizontal edges; filter.rs:178-407) leave it.  Edges on a tile boundary
 // are filtered by both tiles, identically.
-constexpr int LF_TW = 64, LF_TH = 64, LF_HALO = 4, LF_THREADS = 256;
-constexpr int LF_LW = LF_TW + 2 * LF_HALO, LF_LH = LF_TH + 2 * LF_HALO;
-constexpr int LF_CW = LF_TW / 2 + 2 * LF_HALO, LF_CH = LF_TH / 2 + 2 * LF_HALO;
-template <class T>
+// Tiles are LF_TW wide and TH (64, 32 or 16: the stream's choice,
+// rc_stream_set_lf_tile) rows high.
+constexpr int LF_TW = 64, LF_HALO = 4, LF_THREADS = 256;
+constexpr int LF_LW = LF_TW + 2 * LF_HALO, LF_CW = LF_TW / 2 + 2 * LF_HALO;
+template <class T, int TH>
 struct LfTile {
-    T y[LF_LH][LF_LW];
-    T c[2][LF_CH][LF_CW];
+    static constexpr int LH = TH + 2 * LF_HALO, CH = TH / 2 + 2 * LF_HALO;
+    T y[LH][LF_LW];
+    T c[2][CH][LF_CW];
 };
 template <class T> struct Raw4;
 template <> struct Raw4<uint8_t> { using type = uint32_t; };
@@ -1057,8 +1059,8 @@ template <> struct Raw4<uint16_t> { using type = uint2; };
 // filter.rs:178-407).  x0, y0: luma picture position of the tile (its
 // first sample inside the halo); dir 0 vertical edge (left of the unit), 1
 // horizontal (top).
-template <class T, int DIR>
-__device__ void deblock_segment(const HevcLaunch &P, LfTile<T> &S, int bx, int by, bool chroma, int x0, int y0) {
+template <class T, int DIR, int TH>
+__device__ void deblock_segment(const HevcLaunch &P, LfTile<T, TH> &S, int bx, int by, bool chroma, int x0, int y0) {
     const int qi = by * P.w4 + bx, pi = DIR == 0 ? qi - 1 : qi - P.w4;
     const int x = bx * 4, y = by * 4;
     const int px = DIR == 0 ? x - 1 : x, py = DIR == 0 ? y : y - 1;
@@ -1112,11 +1114,12 @@ __device__ bool cross_ok(const HevcLaunch &P, int rs, int nrs) {
 // shared memory, vertical edges, horizontal edges, then SAO of the tile's
 // samples from the deblocked tile (its neighbours pre-SAO, as the reference
 // reads them) into the DPB slot.  The work picture is only read.
-template <class T>
+template <class T, int TH>
 __global__ void __launch_bounds__(LF_THREADS) hevc_loopfilter_kernel(HevcLaunch P) {
-    __shared__ __align__(16) LfTile<T> S;
+    __shared__ __align__(16) LfTile<T, TH> S;
+    constexpr int LF_LH = LfTile<T, TH>::LH, LF_CH = LfTile<T, TH>::CH;
     using R4 = typename Raw4<T>::type;
-    const int x0 = blockIdx.x * LF_TW, y0 = blockIdx.y * LF_TH;
+    const int x0 = blockIdx.x * LF_TW, y0 = blockIdx.y * TH;
     const int ox = x0 - LF_HALO, oy = y0 - LF_HALO;  // luma position of S.y[0][0]
     const int cx0 = x0 / 2, cy0 = y0 / 2, cox = cx0 - LF_HALO, coy = cy0 - LF_HALO;
     const int tid = threadIdx.x;
@@ -1147,11 +1150,11 @@ __global__ void __launch_bounds__(LF_THREADS) hevc_loopfilter_kernel(HevcLaunch 
         for (int i = tid; i < LE * LR + CE * CR; i += LF_THREADS) {
             if (i < LE * LR) {
                 const int bx = (x0 >> 2) + 2 * (i % LE), by = (oy >> 2) + i / LE;
-                if (bx >= 2 && bx < P.w4 && by >= 0 && by < P.h4) deblock_segment<T, 0>(P, S, bx, by, false, x0, y0);
+                if (bx >= 2 && bx < P.w4 && by >= 0 && by < P.h4) deblock_segment<T, 0, TH>(P, S, bx, by, false, x0, y0);
             } else {
                 const int k = i - LE * LR;
                 const int bx = (x0 >> 2) + 4 * (k % CE), by = ((y0 - 2 * LF_HALO) >> 2) + 2 * (k / CE);
-                if (bx >= 4 && bx < P.w4 && by >= 0 && by < P.h4) deblock_segment<T, 0>(P, S, bx, by, true, x0, y0);
+                if (bx >= 4 && bx < P.w4 && by >= 0 && by < P.h4) deblock_segment<T, 0, TH>(P, S, bx, by, true, x0, y0);
             }
         }
     }
@@ -1159,21 +1162,21 @@ __global__ void __launch_bounds__(LF_THREADS) hevc_loopfilter_kernel(HevcLaunch 
     // 3. horizontal edges: luma at y0 + 8e, every 4-column segment; chroma
     // at luma y0 + 16e, every 4-chroma-column segment
     {
-        constexpr int LE = LF_TH / 8 + 1, LR = LF_LW / 4, CE = LF_TH / 16 + 1, CR = LF_CW / 4;
+        constexpr int LE = TH / 8 + 1, LR = LF_LW / 4, CE = TH / 16 + 1, CR = LF_CW / 4;
         for (int i = tid; i < LE * LR + CE * CR; i += LF_THREADS) {
             if (i < LE * LR) {
                 const int by = (y0 >> 2) + 2 * (i / LR), bx = (ox >> 2) + i % LR;
-                if (by >= 2 && by < P.h4 && bx >= 0 && bx < P.w4) deblock_segment<T, 1>(P, S, bx, by, false, x0, y0);
+                if (by >= 2 && by < P.h4 && bx >= 0 && bx < P.w4) deblock_segment<T, 1, TH>(P, S, bx, by, false, x0, y0);
             } else {
                 const int k = i - LE * LR;
                 const int by = (y0 >> 2) + 4 * (k / CR), bx = ((x0 - 2 * LF_HALO) >> 2) + 2 * (k % CR);
-                if (by >= 4 && by < P.h4 && bx >= 0 && bx < P.w4) deblock_segment<T, 1>(P, S, bx, by, true, x0, y0);
+                if (by >= 4 && by < P.h4 && bx >= 0 && bx < P.w4) deblock_segment<T, 1, TH>(P, S, bx, by, true, x0, y0);
             }
         }
     }
     __syncthreads();
     // 4. SAO (filter.rs sao), four samples per thread, which share a CTB
-    constexpr int LQ = LF_TH * (LF_TW / 4), CQ = (LF_TH / 2) * (LF_TW / 8);
+    constexpr int LQ = TH * (LF_TW / 4), CQ = (TH / 2) * (LF_TW / 8);
     for (int i = tid; i < LQ + 2 * CQ; i += LF_THREADS) {
         const bool luma = i < LQ;
         const int c = luma ? 0 : 1 + (i - LQ) / CQ, j = luma ? i : (i - LQ) % CQ, sc = luma ? 0 : 1;
@@ -1279,8 +1282,14 @@ void rc_launch_hevc_intra(const HevcLaunch &p, cudaStream_t st, int blocks) {
     else hevc_intra_kernel<uint8_t><<<blocks, 32 * INTRA_WARPS, dyn, st>>>(p);
 }
 
+template <int TH>
+static void launch_loopfilter(const HevcLaunch &p, cudaStream_t st) {
+    dim3 grid((p.W + LF_TW - 1) / LF_TW, (p.H + TH - 1) / TH);
+    if (p.bd > 8) hevc_loopfilter_kernel<uint16_t, TH><<<grid, LF_THREADS, 0, st>>>(p);
+    else hevc_loopfilter_kernel<uint8_t, TH><<<grid, LF_THREADS, 0, st>>>(p);
+}
 void rc_launch_hevc_loopfilter(const HevcLaunch &p, cudaStream_t st) {
-    dim3 grid((p.W + LF_TW - 1) / LF_TW, (p.H + LF_TH - 1) / LF_TH);
-    if (p.bd > 8) hevc_loopfilter_kernel<uint16_t><<<grid, LF_THREADS, 0, st>>>(p);
-    else hevc_loopfilter_kernel<uint8_t><<<grid, LF_THREADS, 0, st>>>(p);
+    if (p.lf_rows == 16) launch_loopfilter<16>(p, st);
+    else if (p.lf_rows == 32) launch_loopfilter<32>(p, st);
+    else launch_loopfilter<64>(p, st);
 }

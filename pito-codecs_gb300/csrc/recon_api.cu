@@ -115,6 +115,7 @@ struct rc_stream {
     // orders the next early pass after the main stream
     int hevc_prev_slot = -1;
     bool hevc_ext = false;
+    int lf_rows = 64;  // the loop filter's tile height (rc_stream_set_lf_tile)
     int16_t *res[2] = {nullptr, nullptr};  // residual planes (two sets by submit parity)
     uint32_t *ready = nullptr;   // per 4x4 block and component
     uint32_t *ctb_ord[2] = {nullptr, nullptr};  // ctb_first, ctb_end, ctb_base, ctb_nintra (smallest CTB size)
@@ -1346,6 +1347,7 @@ int rc_hevc_submit(rc_stream *s, const rc_hevc_picture *pic, int out_slot) {
     L.late_items = s->late_items[ak];
     L.late_count = s->late_count + ak;
     L.late_cap = (uint32_t)s->late_cap;
+    L.lf_rows = s->lf_rows;
     timed(s, RC_KERNEL_HEVC_INTER, [&] { rc_launch_hevc_inter(L, s->est); }, s->est);
     if (cudaEventRecord(s->aux_ready, s->est) != cudaSuccess || cudaStreamWaitEvent(s->st, s->aux_ready, 0) != cudaSuccess)
         return cuda_fail(s);
@@ -1430,6 +1432,13 @@ int rc_stream_set_intra_ctas(rc_stream *s, int ctas) {
 }
 
 int rc_stream_intra_ctas(rc_stream *s) { return s && s->codec == RC_CODEC_HEVC ? s->wave_blocks : 0; }
+
+int rc_stream_set_lf_tile(rc_stream *s, int rows) {
+    if (!s || s->codec != RC_CODEC_HEVC || (rows != 16 && rows != 32 && rows != 64)) return RC_EINVAL;
+    s->lf_rows = rows;
+    return RC_OK;
+}
+int rc_stream_lf_tile(rc_stream *s) { return s && s->codec == RC_CODEC_HEVC ? s->lf_rows : 0; }
 
 int rc_stream_set_wait_limit(rc_stream *s, unsigned int limit) {
     if (!s) return RC_EINVAL;

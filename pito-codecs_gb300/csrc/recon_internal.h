@@ -146,6 +146,7 @@ struct HevcLaunch {
     // being reconstructed), listing the others (late_items, late_count, at
     // most late_cap items); 2 the listed ones
     int inter_pass, late_slot;
+    int lf_rows;  // the loop filter's tile height (64, 32 or 16 luma rows)
     uint32_t *late_items, *late_count;
     uint32_t late_cap;
 };

@@ -8,8 +8,10 @@ decode order; a picture's bytes do not depend on what else runs beside it.
 * Batched form: a mix of streams of uneven resolution, codec and bit depth
   (``mix_specs``) kept in flight together -- ``run_batched`` submits the
   streams' pictures round-robin, ``run_plain`` one stream after the other;
-  ``autotune`` picks its schedule (pictures queued per stream, HEVC intra
-  CTAs per launch) for a mix by timing the candidates.
+  ``autotune`` picks its schedule for a mix by timing the candidates:
+  pictures queued per stream, and per shape class (codec, coded size, bit
+  depth) the HEVC intra kernel's CTAs per launch and loop-filter tile
+  height, or the H.264 pictures per launch.
 * Served form: ``Server`` admits decode requests (a stream and a number of
   frames) as they arrive, while the device bytes of the resident streams
   stay within an HBM budget; streams stay resident between requests and idle
@@ -171,23 +173,32 @@ def run_plain(specs, templates, streams):
 
 def run_batched(specs, templates, streams, depth: int = 2):
     """All streams in flight together: round-robin submission, at most `depth`
-    pictures queued per stream ahead of its completed work.  Returns wall
-    seconds."""
+    pictures queued per stream ahead of its completed work.  An H.264 stream
+    that reconstructs g pictures per launch (``h264_group``) takes one
+    completion mark per g pictures (a mark launches the queued ones) and
+    may hold g pictures.  Returns wall seconds."""
     t0 = time.perf_counter()
     nxt = {s.key: 0 for s in specs}
-    inflight = {s.key: collections.deque() for s in specs}
+    inflight = {s.key: collections.deque() for s in specs}  # (mark, pictures)
+    unmarked = {s.key: 0 for s in specs}
     live = [s for s in specs]
     while live:
         progressed = False
         for spec in list(live):
             st, q = streams[spec.key], inflight[spec.key]
-            while q and st.mark_done(q[0]):
+            g = max(1, getattr(st, "h264_group", 1))
+            while q and st.mark_done(q[0][0]):
                 q.popleft()
-            while len(q) < depth and nxt[spec.key] < spec.frames:
+            held = sum(n for _, n in q) + unmarked[spec.key]
+            while held < max(depth, g) and nxt[spec.key] < spec.frames:
                 submit(st, spec, *templates[spec.key].picture(nxt[spec.key]))
-                q.append(st.mark())
                 nxt[spec.key] += 1
+                unmarked[spec.key] += 1
+                held += 1
                 progressed = True
+                if unmarked[spec.key] == g or nxt[spec.key] == spec.frames:
+                    q.append((st.mark(), unmarked[spec.key]))
+                    unmarked[spec.key] = 0
             if nxt[spec.key] >= spec.frames and not q:
                 live.remove(spec)
         if not progressed:
@@ -202,9 +213,37 @@ def run_batched(specs, templates, streams, depth: int = 2):
 # Schedule autotuner for the batched form
 # ---------------------------------------------------------------------------
 @dataclasses.dataclass(frozen=True)
+class ClassKnobs:
+    """The schedule of one shape class of streams (codec, coded size, bit
+    depth).  None of the knobs changes a byte of the output."""
+    intra_scale: float = 1.0  # HEVC: intra kernel CTAs per launch, the CTB wavefront's width (x the default)
+    lf_rows: int = 64         # HEVC: loop-filter tile height in luma rows, the tile shape (64, 32, 16)
+    group: int = 1            # H.264: pictures per launch, their wavefronts side by side (1..4)
+
+    def label(self, codec: int) -> str:
+        if codec == RC_CODEC_H264:
+            return f"group {self.group}"
+        return f"intra x{self.intra_scale}, lf tile {self.lf_rows}"
+
+
+@dataclasses.dataclass(frozen=True)
 class Schedule:
     depth: int = 2            # pictures queued per stream ahead of its completed work
-    intra_scale: float = 1.0  # HEVC intra CTAs per launch, times each stream's default
+    intra_scale: float = 1.0  # HEVC intra CTAs per launch, times each stream's default (classes without knobs)
+    classes: tuple = ()       # ((shape class, ClassKnobs), ...): per-class knobs, sorted by class
+
+    def knobs(self, spec) -> ClassKnobs:
+        return dict(self.classes).get(shape_class(spec), ClassKnobs(intra_scale=self.intra_scale))
+
+    def describe(self) -> dict:
+        return {"depth": self.depth, "intra_scale": self.intra_scale,
+                "classes": {c: dataclasses.asdict(k) for c, k in self.classes}}
+
+
+def shape_class(spec) -> str:
+    """A stream's shape class: codec, coded size and bit depth."""
+    W, H = spec.coded
+    return f"{'h264' if spec.codec == RC_CODEC_H264 else 'hevc'}_{W}x{H}_{spec.bit_depth}"
 
 
 def mix_signature(specs) -> str:
@@ -214,50 +253,106 @@ def mix_signature(specs) -> str:
 
 
 def apply_schedule(streams, specs, schedule: Schedule):
-    """Set every HEVC stream's intra CTAs per launch for `schedule`."""
+    """Set every stream's knobs for `schedule`: HEVC intra CTAs per launch
+    (relative to the stream's default) and loop-filter tile height, H.264
+    pictures per launch."""
     for s in specs:
+        st, k = streams[s.key], schedule.knobs(s)
         if s.codec == RC_CODEC_HEVC:
-            st = streams[s.key]
             st.set_intra_ctas(0)
-            st.set_intra_ctas(max(1, int(round(st.intra_ctas() * schedule.intra_scale))))
+            st.set_intra_ctas(max(1, int(round(st.intra_ctas() * k.intra_scale))))
+            st.set_lf_tile(k.lf_rows)
+        else:
+            st.set_h264_group(k.group)
 
 
-def autotune(specs, templates, depths=(1, 2, 3, 4), intra_scales=(0.5, 1.0, 2.0), frames: int = 8,
-             open_fn=open_stream, runner=None, cache_path=None):
-    """Choose the batched form's schedule for a stream mix.
-
-    Every candidate (pictures queued per stream x HEVC intra CTAs per launch)
-    runs the first `frames` pictures of every stream of the mix on fresh
-    streams and is timed; the fastest wins.  The schedule changes only the
-    order and overlap of the work, never a picture's bytes.  With
-    `cache_path` the choice is kept per mix signature (JSON) and reused.
-    Returns (schedule, {schedule: frames/s}); the dict is empty when the
-    schedule came from the cache."""
-    runner = runner or run_batched
-    key = mix_signature(specs)
-    cache = {}
+def _load_cache(cache_path):
     if cache_path and os.path.exists(cache_path):
         with open(cache_path) as f:
             cache = json.load(f)
-        if key in cache:
-            return Schedule(**cache[key]["schedule"]), {}
+        if isinstance(cache, dict) and "mixes" in cache and "classes" in cache:
+            return cache
+    return {"mixes": {}, "classes": {}}
+
+
+def autotune(specs, templates, depths=(1, 2, 3, 4), intra_scales=(0.5, 1.0, 2.0), lf_rows=(64, 32, 16),
+             groups=(1, 2, 3), frames: int = 8, open_fn=open_stream, runner=None, cache_path=None,
+             class_depth: int = 2):
+    """Choose the batched form's schedule for a stream mix.
+
+    Per shape class (codec, coded size, bit depth), the class's own streams
+    run the first `frames` pictures of each, `class_depth` pictures queued per
+    stream, once untimed and then once per candidate, knob by knob (HEVC: the
+    intra CTAs per launch, then the loop-filter tile height with the best of
+    those; H.264: pictures per launch); each knob keeps its fastest value.
+    Then the whole mix, with every class's knobs, runs the same prefix on
+    fresh streams for each number of pictures queued per stream, and the
+    fastest wins.  No knob changes a picture's bytes.  With `cache_path`
+    (JSON) the choice is kept per class and per mix signature and reused.
+    Returns (schedule, {candidate label: frames/s}); the dict is empty when
+    the whole schedule came from the cache."""
+    runner = runner or run_batched
+    key = mix_signature(specs)
+    cache = _load_cache(cache_path)
+    if key in cache["mixes"]:
+        m = cache["mixes"][key]
+        return Schedule(m["depth"], classes=tuple(sorted((c, ClassKnobs(**cache["classes"][c]))
+                                                          for c in m["classes"]))), {}
     prefix = [dataclasses.replace(s, frames=min(s.frames, frames)) for s in specs]
+    by_class = collections.defaultdict(list)
+    for s in prefix:
+        by_class[shape_class(s)].append(s)
+    rates, classes = {}, {}
+    for cls in sorted(by_class):
+        members = by_class[cls]
+        if cls in cache["classes"]:
+            classes[cls] = ClassKnobs(**cache["classes"][cls])
+            continue
+        codec = members[0].codec
+        streams = {s.key: open_fn(s) for s in members}
+        try:
+            timed = {}
+
+            def fps(k: ClassKnobs) -> float:
+                if k not in timed:
+                    apply_schedule(streams, members, Schedule(class_depth, classes=((cls, k),)))
+                    seconds = runner(members, templates, streams, depth=class_depth)
+                    timed[k] = sum(s.frames for s in members) / seconds
+                    rates[f"{cls}: {k.label(codec)}"] = timed[k]
+                return timed[k]
+
+            best = ClassKnobs()
+            apply_schedule(streams, members, Schedule(class_depth, classes=((cls, best),)))
+            runner(members, templates, streams, depth=class_depth)  # untimed: first use of the streams
+            if codec == RC_CODEC_HEVC:
+                best = max((dataclasses.replace(best, intra_scale=v) for v in intra_scales), key=fps)
+                best = max((dataclasses.replace(best, lf_rows=v) for v in lf_rows), key=fps)
+            else:
+                best = max((dataclasses.replace(best, group=v) for v in groups), key=fps)
+            classes[cls] = best
+        finally:
+            for st in streams.values():
+                st.close()
+    knobs = tuple(sorted(classes.items()))
     total = sum(s.frames for s in prefix)
-    rates = {}
+    by_depth = {}
     for depth in depths:
-        for scale in intra_scales:
-            schedule = Schedule(depth, scale)
-            streams = {s.key: open_fn(s) for s in prefix}
-            try:
-                apply_schedule(streams, prefix, schedule)
-                seconds = runner(prefix, templates, streams, depth=depth)
-            finally:
-                for st in streams.values():
-                    st.close()
-            rates[schedule] = total / seconds
-    best = max(rates, key=rates.get)
+        schedule = Schedule(depth, classes=knobs)
+        streams = {s.key: open_fn(s) for s in prefix}
+        try:
+            apply_schedule(streams, prefix, schedule)
+            seconds = runner(prefix, templates, streams, depth=depth)
+        finally:
+            for st in streams.values():
+                st.close()
+        by_depth[schedule] = total / seconds
+        rates[f"mix: depth {depth}"] = by_depth[schedule]
+    best = max(by_depth, key=by_depth.get)
     if cache_path:
-        cache[key] = {"schedule": dataclasses.asdict(best), "frames_per_s": rates[best]}
+        for c, k in knobs:
+            cache["classes"][c] = dataclasses.asdict(k)
+        cache["mixes"][key] = {"depth": best.depth, "classes": [c for c, _ in knobs],
+                               "frames_per_s": by_depth[best]}
         with open(cache_path, "w") as f:
             json.dump(cache, f, indent=1)
     return best, rates

@@ -21,8 +21,12 @@ def first_diff(a, b):
     return f"first mismatch at ({x},{y}): gpu {a[y, x]} oracle {b[y, x]}; {len(d)} samples"
 
 
-def run_sequence(engine, oracle, width, height, frames, seed, bit_depth=8, slots=5, lists=1, stages=3, **opts):
+def run_sequence(engine, oracle, width, height, frames, seed, bit_depth=8, slots=5, lists=1, stages=3, lf_rows=None,
+                 **opts):
     st = engine.ReconStream(engine.RC_CODEC_HEVC, width, height, bit_depth, slots)
+    if lf_rows:
+        st.set_lf_tile(lf_rows)
+        assert st.lf_tile() == lf_rows
     dpb = oracle.HevcDpb(width, height, bit_depth, slots)
     md5s = []
     try:
@@ -66,6 +70,31 @@ def test_tiles_slices_offsets(engine, oracle):
     run_sequence(engine, oracle, 192, 128, 3, seed=4, log2_ctb=5, tile_cols=2, tile_rows=2, num_slices=3,
                  lf_across_slices=0, loop_filter_across_tiles=0, beta_offset=4, tc_offset=-2,
                  cb_qp_offset=3, cr_qp_offset=-5)
+
+
+@pytest.mark.parametrize("rows", [16, 32, 64])
+def test_loop_filter_tile_heights(engine, oracle, rows):
+    """The loop filter's tile height is a schedule knob: every height gives
+    the oracle's bytes, across tiles, slices, deblocking offsets, PCM and
+    bypass blocks, SAO at 8 and 10 bits, and a picture height that is not a
+    multiple of the tile."""
+    run_sequence(engine, oracle, 192, 136, 3, seed=40 + rows, log2_ctb=5, tile_cols=2, tile_rows=2, num_slices=3,
+                 lf_across_slices=0, loop_filter_across_tiles=0, beta_offset=4, tc_offset=-2, lf_rows=rows)
+    run_sequence(engine, oracle, 128, 72, 3, seed=50 + rows, bit_depth=10, log2_ctb=4, pcm_permille=150,
+                 pcm_loop_filter_disabled=1, bypass_permille=100, lf_rows=rows)
+
+
+def test_loop_filter_tile_knob_rejects_bad_heights(engine):
+    with engine.ReconStream(engine.RC_CODEC_HEVC, 64, 64, 8, 2) as st:
+        assert st.lf_tile() == 64
+        for bad in (0, 8, 48, 128):
+            with pytest.raises(engine.ReconError):
+                st.set_lf_tile(bad)
+        assert st.lf_tile() == 64
+    with engine.ReconStream(engine.RC_CODEC_H264, 64, 64, 8, 2) as st:
+        assert st.lf_tile() == 0
+        with pytest.raises(engine.ReconError):
+            st.set_lf_tile(32)
 
 
 def test_pcm_bypass_transform_skip(engine, oracle):

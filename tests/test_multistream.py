@@ -115,15 +115,20 @@ def test_batched_equals_alone(engine):
 
 @pytest.mark.gpu
 def test_schedule_changes_no_bytes(engine):
-    """The autotuner's knobs (pictures queued per stream, HEVC intra CTAs per
-    launch) change the order and overlap of the work only."""
+    """The autotuner's knobs (pictures queued per stream; per shape class the
+    HEVC intra CTAs per launch and loop-filter tile height, the H.264
+    pictures per launch) change the order and overlap of the work only."""
     M = ms(engine)
-    specs = [s for s in M.mix_specs(8, min_frames=4, max_frames=7, seed=21) if s.codec == engine.RC_CODEC_HEVC]
+    specs = M.mix_specs(12, min_frames=4, max_frames=7, seed=21)
     for s in specs:
-        s.width, s.height = 854, 480
+        if s.width > 854:
+            s.width, s.height = 854, 480
     tpl = {s.key: M.Templates(s) for s in specs}
+    classes = sorted({M.shape_class(s) for s in specs})
+    mk = lambda scale, rows, group: tuple((c, M.ClassKnobs(scale, rows, group)) for c in classes)
     digests = []
-    for schedule in (M.Schedule(1, 1.0), M.Schedule(3, 0.25), M.Schedule(2, 4.0)):
+    for schedule in (M.Schedule(1, 1.0), M.Schedule(3, classes=mk(0.25, 16, 3)),
+                     M.Schedule(2, classes=mk(4.0, 32, 2))):
         streams = {s.key: M.open_stream(s) for s in specs}
         try:
             M.apply_schedule(streams, specs, schedule)
