@@ -90,6 +90,20 @@ def test_1080p_frames(engine, oracle):
     assert len(md5) == 3
 
 
+def test_small_config_geometry_qp26_60_frames(engine, oracle):
+    """The small plain configuration's shape: 640x360 (40 x 23 MBs, coded
+    640x368), 60 frames, QP 26, one intra picture then P pictures; seeded
+    syntax records stand in for the reference encoder's stream."""
+    run_sequence(engine, oracle, 40, 23, 60, seed=30, qp_min=26, qp_max=26)
+
+
+def test_largest_picture(engine, oracle):
+    """The largest coded size a stream accepts, 8192 x 8192 (512 x 512 MBs,
+    128 bands): an intra picture, then a P picture with far and off-picture
+    motion."""
+    run_sequence(engine, oracle, 512, 512, 2, seed=31, mv_range=512)
+
+
 def test_deterministic(engine, oracle):
     a = run_sequence(engine, oracle, 8, 6, 3, seed=11)
     b = run_sequence(engine, oracle, 8, 6, 3, seed=11)

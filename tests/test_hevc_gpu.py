@@ -134,6 +134,13 @@ def test_2160p_one_picture_each_depth(engine, oracle):
     run_sequence(engine, oracle, 3840, 2160, 1, seed=13, bit_depth=10)
 
 
+def test_largest_picture_10bit(engine, oracle):
+    """The largest coded size a stream accepts, 8192 x 8192, at 10 bits: an
+    intra picture, then a P picture whose inter passes list units from every
+    part of the picture."""
+    run_sequence(engine, oracle, 8192, 8192, 2, seed=32, bit_depth=10)
+
+
 def test_deterministic(engine, oracle):
     a = run_sequence(engine, oracle, 128, 64, 3, seed=14, log2_ctb=5)
     b = run_sequence(engine, oracle, 128, 64, 3, seed=14, log2_ctb=5)
