@@ -719,34 +719,55 @@ __device__ void intra_tu(const HevcLaunch &P, IntraSmem &S, const CtbCanvas<T> &
     // r < 0 only occurs when (n * angle) >> 5 < -1, as the standard has it
     const int angle = mode >= 2 ? cANGLE[mode] : 0, inv = angle < 0 ? cINV_ANGLE[mode - 11] : 0;
     const uint16_t *mn = mode >= 18 ? Tp : L, *sd = mode >= 18 ? L : Tp;
-    auto refv = [&](int r) -> int { return r >= 0 ? mn[r] : sd[(r * inv + 128) >> 8]; };
-    for (int i = lane; i < n * n; i += 32) {
-        const int y = i >> log2, x = i & (n - 1);
-        int v;
-        if (mode == 0) {
-            v = ((n - 1 - x) * L[1 + y] + (x + 1) * Tp[1 + n] + (n - 1 - y) * Tp[1 + x] + (y + 1) * L[1 + n] + n) >>
-                (log2 + 1);
-        } else if (mode == 1) {
-            v = dc;
-            if (edge) {
-                if (x == 0 && y == 0) v = (L[1] + 2 * dc + Tp[1] + 2) >> 2;
-                else if (y == 0) v = (Tp[1 + x] + 3 * dc + 2) >> 2;
-                else if (x == 0) v = (L[1 + y] + 3 * dc + 2) >> 2;
-            }
-        } else {
-            const bool horizontal = mode < 18;
-            // output (x, y): horizontal modes run j along x, vertical along y
+    // the block's place in the CTB copy and its residuals (the picture gets
+    // the block after its ready flags, copy_out); predictions lie in
+    // [0, max], so a block without residual adds 0 and clamps to itself
+    const int cs = c ? C.s >> 1 : C.s;
+    const int base = (c ? C.s * C.s + (c - 1) * cs * cs : 0) + (y0 - (c ? C.y0 >> 1 : C.y0)) * cs +
+                     (x0 - (c ? C.x0 >> 1 : C.x0));
+    T *out = C.cv + base;
+    const int16_t *res = C.res + base;
+    const bool cbf = t.flags & RC_HEVC_TU_CBF;
+    auto put = [&](int x, int y, int v) {
+        const int r = cbf ? res[y * cs + x] : 0;
+        out[y * cs + x] = (T)clampi(v + r, 0, max);
+    };
+    // one loop per prediction kind, without branches in its body
+    if (mode == 0) {
+        const int tr = Tp[1 + n], bl = L[1 + n];
+        for (int i = lane; i < n * n; i += 32) {
+            const int y = i >> log2, x = i & (n - 1);
+            put(x, y, ((n - 1 - x) * L[1 + y] + (x + 1) * tr + (n - 1 - y) * Tp[1 + x] + (y + 1) * bl + n) >> (log2 + 1));
+        }
+    } else if (mode == 1) {
+        for (int i = lane; i < n * n; i += 32) {
+            const int y = i >> log2, x = i & (n - 1);
+            const int corner = (L[1] + 2 * dc + Tp[1] + 2) >> 2, top = (Tp[1 + x] + 3 * dc + 2) >> 2,
+                      left = (L[1 + y] + 3 * dc + 2) >> 2;
+            const int v = !edge ? dc : (x == 0 && y == 0) ? corner : y == 0 ? top : x == 0 ? left : dc;
+            put(x, y, v);
+        }
+    } else {
+        // output (x, y): horizontal modes (< 18) run j along x, vertical
+        // along y; the reference index r of src/hevc/intra.rs, read from the
+        // main side (r >= 0) or the side reference projected onto it
+        const bool horizontal = mode < 18;
+        const bool fe = edge && (mode == 26 || mode == 10);  // the edge filter of the pure directions
+        for (int i = lane; i < n * n; i += 32) {
+            const int y = i >> log2, x = i & (n - 1);
             const int j = horizontal ? x : y, ii = horizontal ? y : x;
             const int pos = (j + 1) * angle, idx = pos >> 5, fact = pos & 31;
             const int r = ii + idx + 1;
-            v = fact ? ((32 - fact) * refv(r) + fact * refv(r + 1) + 16) >> 5 : refv(r);
-            if (edge) {
-                if (mode == 26 && x == 0) v = clampi(Tp[1] + ((L[1 + y] - L[0]) >> 1), 0, max);
-                else if (mode == 10 && y == 0) v = clampi(L[1] + ((Tp[1 + x] - Tp[0]) >> 1), 0, max);
-            }
+            const uint16_t *a0 = r >= 0 ? mn + r : sd + ((r * inv + 128) >> 8);
+            const uint16_t *a1 = r + 1 >= 0 ? mn + r + 1 : sd + (((r + 1) * inv + 128) >> 8);
+            int v = ((32 - fact) * (int)*a0 + fact * (int)*a1 + 16) >> 5;
+            // mode 26: column 0 from the left reference; mode 10: row 0 from the top
+            const int k = horizontal ? x : y;  // along the filtered edge
+            const bool on = fe && (horizontal ? y == 0 : x == 0);
+            const int fv = horizontal ? L[1] + ((Tp[1 + k] - Tp[0]) >> 1) : Tp[1] + ((L[1 + k] - L[0]) >> 1);
+            v = on ? clampi(fv, 0, max) : v;
+            put(x, y, v);
         }
-        if (t.flags & RC_HEVC_TU_CBF) v = clampi(v + C.resid(c, x0 + x, y0 + y), 0, max);
-        C.at(c, x0 + x, y0 + y) = (T)v;  // the picture gets the block after its ready flags (copy_out)
     }
 }
 
