@@ -752,21 +752,41 @@ __device__ void intra_tu(const HevcLaunch &P, IntraSmem &S, const CtbCanvas<T> &
         // along y; the reference index r of src/hevc/intra.rs, read from the
         // main side (r >= 0) or the side reference projected onto it
         const bool horizontal = mode < 18;
-        const bool fe = edge && (mode == 26 || mode == 10);  // the edge filter of the pure directions
-        for (int i = lane; i < n * n; i += 32) {
-            const int y = i >> log2, x = i & (n - 1);
+        auto ang = [&](int x, int y) -> int {
             const int j = horizontal ? x : y, ii = horizontal ? y : x;
             const int pos = (j + 1) * angle, idx = pos >> 5, fact = pos & 31;
             const int r = ii + idx + 1;
             const uint16_t *a0 = r >= 0 ? mn + r : sd + ((r * inv + 128) >> 8);
             const uint16_t *a1 = r + 1 >= 0 ? mn + r + 1 : sd + (((r + 1) * inv + 128) >> 8);
-            int v = ((32 - fact) * (int)*a0 + fact * (int)*a1 + 16) >> 5;
-            // mode 26: column 0 from the left reference; mode 10: row 0 from the top
-            const int k = horizontal ? x : y;  // along the filtered edge
-            const bool on = fe && (horizontal ? y == 0 : x == 0);
-            const int fv = horizontal ? L[1] + ((Tp[1 + k] - Tp[0]) >> 1) : Tp[1] + ((L[1 + k] - L[0]) >> 1);
-            v = on ? clampi(fv, 0, max) : v;
-            put(x, y, v);
+            return ((32 - fact) * (int)*a0 + fact * (int)*a1 + 16) >> 5;
+        };
+        // four samples per step: their reads (references, residuals) before
+        // their writes, which could alias them
+        int i = lane;
+        for (; i + 96 < n * n; i += 128) {
+            int v[4], r[4], o[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const int k = i + 32 * q, y = k >> log2, x = k & (n - 1);
+                o[q] = y * cs + x;
+                v[q] = ang(x, y);
+                r[q] = cbf ? res[o[q]] : 0;
+            }
+#pragma unroll
+            for (int q = 0; q < 4; q++) out[o[q]] = (T)clampi(v[q] + r[q], 0, max);
+        }
+        for (; i < n * n; i += 32) {
+            const int y = i >> log2, x = i & (n - 1);
+            put(x, y, ang(x, y));
+        }
+        // the edge filter of the pure directions: mode 26 rewrites column 0
+        // from the left reference, mode 10 row 0 from the top one
+        if (edge && (mode == 26 || mode == 10)) {
+            __syncwarp();
+            for (int k = lane; k < n; k += 32) {
+                const int fv = horizontal ? L[1] + ((Tp[1 + k] - Tp[0]) >> 1) : Tp[1] + ((L[1 + k] - L[0]) >> 1);
+                put(horizontal ? k : 0, horizontal ? 0 : k, clampi(fv, 0, max));
+            }
         }
     }
 }
