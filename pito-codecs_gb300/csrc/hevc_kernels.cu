@@ -645,19 +645,12 @@ __device__ void intra_tu(const HevcLaunch &P, IntraSmem &S, const CtbCanvas<T> &
         auto unit_first = [&](int k) -> int { return k < NL ? k << lu : k == NL ? n2 : n2 + 1 + ((k - NL - 1) << lu); };
         for (int j = lane; j <= 2 * n2; j += 32) {
             const int k = j < n2 ? j >> lu : j == n2 ? NL : NL + 1 + ((j - n2 - 1) >> lu);
-            int src = j;
-            if (!(mask >> k & 1)) {
-                const unsigned long long below = mask & ((1ull << k) - 1);
-                if (below) {
-                    const int kb = 63 - __clzll((long long)below);
-                    src = unit_first(kb) + (kb == NL ? 0 : unit - 1);
-                } else {
-                    src = unit_first(first);
-                }
-            }
+            const unsigned long long below = mask & ((1ull << k) - 1);
+            const int kb = below ? 63 - __clzll((long long)below) : 0;
+            const int src = (mask >> k & 1) ? j : below ? unit_first(kb) + (kb == NL ? 0 : unit - 1) : unit_first(first);
             uint16_t v = (uint16_t)(1 << (bd - 1));
             if (mask) {
-                const int x = src < n2 ? x0 - 1 : src == n2 ? x0 - 1 : x0 + src - n2 - 1;
+                const int x = src <= n2 ? x0 - 1 : x0 + src - n2 - 1;
                 const int y = src < n2 ? y0 + n2 - 1 - src : y0 - 1;
                 v = ref(x, y);
             }
@@ -732,36 +725,10 @@ __device__ void intra_tu(const HevcLaunch &P, IntraSmem &S, const CtbCanvas<T> &
         const int r = cbf ? res[y * cs + x] : 0;
         out[y * cs + x] = (T)clampi(v + r, 0, max);
     };
-    // one loop per prediction kind, without branches in its body
-    if (mode == 0) {
-        const int tr = Tp[1 + n], bl = L[1 + n];
-        for (int i = lane; i < n * n; i += 32) {
-            const int y = i >> log2, x = i & (n - 1);
-            put(x, y, ((n - 1 - x) * L[1 + y] + (x + 1) * tr + (n - 1 - y) * Tp[1 + x] + (y + 1) * bl + n) >> (log2 + 1));
-        }
-    } else if (mode == 1) {
-        for (int i = lane; i < n * n; i += 32) {
-            const int y = i >> log2, x = i & (n - 1);
-            const int corner = (L[1] + 2 * dc + Tp[1] + 2) >> 2, top = (Tp[1 + x] + 3 * dc + 2) >> 2,
-                      left = (L[1 + y] + 3 * dc + 2) >> 2;
-            const int v = !edge ? dc : (x == 0 && y == 0) ? corner : y == 0 ? top : x == 0 ? left : dc;
-            put(x, y, v);
-        }
-    } else {
-        // output (x, y): horizontal modes (< 18) run j along x, vertical
-        // along y; the reference index r of src/hevc/intra.rs, read from the
-        // main side (r >= 0) or the side reference projected onto it
-        const bool horizontal = mode < 18;
-        auto ang = [&](int x, int y) -> int {
-            const int j = horizontal ? x : y, ii = horizontal ? y : x;
-            const int pos = (j + 1) * angle, idx = pos >> 5, fact = pos & 31;
-            const int r = ii + idx + 1;
-            const uint16_t *a0 = r >= 0 ? mn + r : sd + ((r * inv + 128) >> 8);
-            const uint16_t *a1 = r + 1 >= 0 ? mn + r + 1 : sd + (((r + 1) * inv + 128) >> 8);
-            return ((32 - fact) * (int)*a0 + fact * (int)*a1 + 16) >> 5;
-        };
-        // four samples per step: their reads (references, residuals) before
-        // their writes, which could alias them
+    // one loop per prediction kind, without branches in its body, four
+    // samples per step: their reads (references, residuals) before their
+    // writes, which could alias them
+    auto run4 = [&](auto pred) {
         int i = lane;
         for (; i + 96 < n * n; i += 128) {
             int v[4], r[4], o[4];
@@ -769,7 +736,7 @@ __device__ void intra_tu(const HevcLaunch &P, IntraSmem &S, const CtbCanvas<T> &
             for (int q = 0; q < 4; q++) {
                 const int k = i + 32 * q, y = k >> log2, x = k & (n - 1);
                 o[q] = y * cs + x;
-                v[q] = ang(x, y);
+                v[q] = pred(x, y);
                 r[q] = cbf ? res[o[q]] : 0;
             }
 #pragma unroll
@@ -777,8 +744,37 @@ __device__ void intra_tu(const HevcLaunch &P, IntraSmem &S, const CtbCanvas<T> &
         }
         for (; i < n * n; i += 32) {
             const int y = i >> log2, x = i & (n - 1);
-            put(x, y, ang(x, y));
+            put(x, y, pred(x, y));
         }
+    };
+    if (mode == 0) {
+        const int tr = Tp[1 + n], bl = L[1 + n];
+        run4([&](int x, int y) {
+            return ((n - 1 - x) * L[1 + y] + (x + 1) * tr + (n - 1 - y) * Tp[1 + x] + (y + 1) * bl + n) >> (log2 + 1);
+        });
+    } else if (mode == 1) {
+        if (!edge) {
+            run4([&](int, int) { return dc; });
+        } else {
+            const int corner = (L[1] + 2 * dc + Tp[1] + 2) >> 2;
+            run4([&](int x, int y) {
+                const int top = (Tp[1 + x] + 3 * dc + 2) >> 2, left = (L[1 + y] + 3 * dc + 2) >> 2;
+                return (x == 0 && y == 0) ? corner : y == 0 ? top : x == 0 ? left : dc;
+            });
+        }
+    } else {
+        // output (x, y): horizontal modes (< 18) run j along x, vertical
+        // along y; the reference index r of src/hevc/intra.rs, read from the
+        // main side (r >= 0) or the side reference projected onto it
+        const bool horizontal = mode < 18;
+        run4([&](int x, int y) {
+            const int j = horizontal ? x : y, ii = horizontal ? y : x;
+            const int pos = (j + 1) * angle, idx = pos >> 5, fact = pos & 31;
+            const int r = ii + idx + 1;
+            const uint16_t *a0 = r >= 0 ? mn + r : sd + ((r * inv + 128) >> 8);
+            const uint16_t *a1 = r + 1 >= 0 ? mn + r + 1 : sd + (((r + 1) * inv + 128) >> 8);
+            return ((32 - fact) * (int)*a0 + fact * (int)*a1 + 16) >> 5;
+        });
         // the edge filter of the pure directions: mode 26 rewrites column 0
         // from the left reference, mode 10 row 0 from the top one
         if (edge && (mode == 26 || mode == 10)) {
