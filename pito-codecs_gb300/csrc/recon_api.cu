@@ -585,18 +585,25 @@ int set_release(rc_stream *s, int k) {
 // kernel launched so far (bounds checked by the caller, copy_cropped's rule,
 // src/h264/dec/picture.rs:601-615); later submits that write the slot wait
 // for it.
+// One plane's rows to the caller: a single contiguous copy when the rows are
+// whole plane rows (the crop spans the pitch), else a 2-D copy.
+static bool copy_rows(void *dst, const uint8_t *src, size_t pitch, size_t row_bytes, int rows, cudaStream_t c) {
+    if (row_bytes == pitch)
+        return cudaMemcpyAsync(dst, src, row_bytes * rows, cudaMemcpyDeviceToHost, c) == cudaSuccess;
+    return cudaMemcpy2DAsync(dst, row_bytes, src, pitch, row_bytes, rows, cudaMemcpyDeviceToHost, c) == cudaSuccess;
+}
+
 int issue_download(rc_stream *s, int slot, int x, int y, int w, int h, void *out_y, void *out_u, void *out_v) {
     const int cx = x / 2, cy = y / 2, ccw = (w + 1) / 2, cch = (h + 1) / 2, bps = s->bps;
     const uint8_t *base = s->dpb + (size_t)slot * s->slot_bytes;
     cudaStream_t c = s->dst;
     bool ok = cudaEventRecord(s->kernels_done, s->st) == cudaSuccess &&
               cudaStreamWaitEvent(c, s->kernels_done, 0) == cudaSuccess &&
-              cudaMemcpy2DAsync(out_y, (size_t)w * bps, base + (size_t)y * s->pitch + (size_t)x * bps, s->pitch,
-                                (size_t)w * bps, h, cudaMemcpyDeviceToHost, c) == cudaSuccess &&
-              cudaMemcpy2DAsync(out_u, (size_t)ccw * bps, base + s->u_off + (size_t)cy * s->cpitch + (size_t)cx * bps,
-                                s->cpitch, (size_t)ccw * bps, cch, cudaMemcpyDeviceToHost, c) == cudaSuccess &&
-              cudaMemcpy2DAsync(out_v, (size_t)ccw * bps, base + s->v_off + (size_t)cy * s->cpitch + (size_t)cx * bps,
-                                s->cpitch, (size_t)ccw * bps, cch, cudaMemcpyDeviceToHost, c) == cudaSuccess &&
+              copy_rows(out_y, base + (size_t)y * s->pitch + (size_t)x * bps, s->pitch, (size_t)w * bps, h, c) &&
+              copy_rows(out_u, base + s->u_off + (size_t)cy * s->cpitch + (size_t)cx * bps, s->cpitch,
+                        (size_t)ccw * bps, cch, c) &&
+              copy_rows(out_v, base + s->v_off + (size_t)cy * s->cpitch + (size_t)cx * bps, s->cpitch,
+                        (size_t)ccw * bps, cch, c) &&
               cudaEventRecord(s->slot_dl[slot], c) == cudaSuccess;
     if (ok) s->slot_dl_pending[slot] = 1;
     return ok ? 0 : cuda_fail(s);
