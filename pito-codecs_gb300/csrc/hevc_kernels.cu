@@ -39,6 +39,8 @@
 // reconstruction half of src/hevc/slicedec.rs; citations at each function.
 #include <stdint.h>
 
+#include <type_traits>
+
 #include <algorithm>
 
 #include "recon_internal.h"
@@ -595,10 +597,6 @@ __device__ void intra_tu(const HevcLaunch &P, IntraSmem &S, const CtbCanvas<T> &
     T *pl = plane_ptr<T>(P.work, P, c);
     const int pitch = pitch_el(P, c, sizeof(T));
     const int n2 = 2 * n;
-    // a reference sample (plane coordinates) from the CTB copy or the picture
-    auto ref = [&](int x, int y) -> uint16_t {
-        return C.inside(x * sc, y * sc) ? (uint16_t)C.at(c, x, y) : (uint16_t)__ldcg(pl + (size_t)y * pitch + x);
-    };
     // Reference units in the substitution scan order of src/hevc/intra.rs:
     // 19-65 (k: 0..NL-1 the left column's units bottom-up, NL the corner,
     // NL+1..2 NL the top row's units left to right).  Lane k decides unit k's
@@ -643,20 +641,59 @@ __device__ void intra_tu(const HevcLaunch &P, IntraSmem &S, const CtbCanvas<T> &
     {
         const int first = __ffsll((long long)mask) - 1;
         auto unit_first = [&](int k) -> int { return k < NL ? k << lu : k == NL ? n2 : n2 + 1 + ((k - NL - 1) << lu); };
-        for (int j = lane; j <= 2 * n2; j += 32) {
-            const int k = j < n2 ? j >> lu : j == n2 ? NL : NL + 1 + ((j - n2 - 1) >> lu);
-            const unsigned long long below = mask & ((1ull << k) - 1);
-            const int kb = below ? 63 - __clzll((long long)below) : 0;
-            const int src = (mask >> k & 1) ? j : below ? unit_first(kb) + (kb == NL ? 0 : unit - 1) : unit_first(first);
-            uint16_t v = (uint16_t)(1 << (bd - 1));
-            if (mask) {
+        // a lane's samples j = lane + 32 m (2 n2 + 1 of them, 17 to 129):
+        // every address first, then the CTB copy's samples, then -- when a
+        // lane of the warp needs one -- the picture's samples, all loads
+        // issued before any is waited for, then the writes
+        auto gather = [&](auto m_count) {
+            constexpr int M = decltype(m_count)::value;
+            int off[M];
+            bool in[M];
+            const T *cvc = &C.at(c, c ? C.x0 >> 1 : C.x0, c ? C.y0 >> 1 : C.y0);
+            const int cst = c ? C.s >> 1 : C.s;
+            bool outside = false;
+#pragma unroll
+            for (int m = 0; m < M; m++) {
+                if (!mask) {  // no reference available: nothing is read
+                    in[m] = true;
+                    off[m] = 0;
+                    continue;
+                }
+                const int j = min(lane + 32 * m, 2 * n2);
+                const int k = j < n2 ? j >> lu : j == n2 ? NL : NL + 1 + ((j - n2 - 1) >> lu);
+                const unsigned long long below = mask & ((1ull << k) - 1);
+                const int kb = below ? 63 - __clzll((long long)below) : 0;
+                const int src =
+                    (mask >> k & 1) ? j : below ? unit_first(kb) + (kb == NL ? 0 : unit - 1) : unit_first(first);
                 const int x = src <= n2 ? x0 - 1 : x0 + src - n2 - 1;
                 const int y = src < n2 ? y0 + n2 - 1 - src : y0 - 1;
-                v = ref(x, y);
+                in[m] = C.inside(x * sc, y * sc);
+                // the CTB copy's offset, or the picture's
+                off[m] = in[m] ? (y - (c ? C.y0 >> 1 : C.y0)) * cst + (x - (c ? C.x0 >> 1 : C.x0)) : y * pitch + x;
+                outside = outside || !in[m];
             }
-            if (j <= n2) S.left[n2 - j] = v;
-            if (j >= n2) S.top[j - n2] = v;
-        }
+            uint16_t v[M];
+#pragma unroll
+            for (int m = 0; m < M; m++) v[m] = (uint16_t)cvc[in[m] ? off[m] : 0];
+            if (__any_sync(0xffffffffu, outside)) {
+                uint16_t g[M];
+#pragma unroll
+                for (int m = 0; m < M; m++) g[m] = (uint16_t)__ldcg(pl + (in[m] ? 0 : off[m]));
+#pragma unroll
+                for (int m = 0; m < M; m++) v[m] = in[m] ? v[m] : g[m];
+            }
+#pragma unroll
+            for (int m = 0; m < M; m++) {
+                const int j = lane + 32 * m;
+                const uint16_t w = mask ? v[m] : (uint16_t)(1 << (bd - 1));
+                if (j <= n2) S.left[n2 - j] = w;
+                if (j >= n2 && j <= 2 * n2) S.top[j - n2] = w;
+            }
+        };
+        if (n2 < 16) gather(std::integral_constant<int, 1>());
+        else if (n2 < 32) gather(std::integral_constant<int, 2>());
+        else if (n2 < 48) gather(std::integral_constant<int, 3>());
+        else gather(std::integral_constant<int, 5>());
     }
     __syncwarp();
     const int mode = t.mode;
