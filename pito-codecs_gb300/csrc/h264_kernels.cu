@@ -2559,6 +2559,7 @@ __device__ __forceinline__ void band_chroma_row(const H264Launch &P, BandSmem &B
 // Mirror warp: lane 0 copies the row above's filter progress, lane 1 its
 // intra progress, lane 2 the row below's intra progress (global, acquire)
 // into shared memory.
+template <bool GROUPED>
 __device__ __forceinline__ void band_mirror(const H264Launch &P, BandSmem &B, int y0, int rows, int lane) {
     const uint32_t tag = (P.epoch & 0xffffu) << 16;
     const bool above = y0 > 0, below = y0 + rows < P.mb_h;
@@ -2589,9 +2590,11 @@ __device__ __forceinline__ void band_mirror(const H264Launch &P, BandSmem &B, in
                 seen = P.mb_w;  // give up; the waiting warps see the error
             }
         }
-        // back off (to 512 ns) while nothing moves: in a group launch the
-        // bands of later pictures wait here a long time
-        ns = __any_sync(0xffffffffu, moved) ? 32 : min(ns * 2, 512u);
+        // a group launch backs off (to 512 ns) while nothing moves: the
+        // bands of its later pictures wait here a long time; one picture's
+        // bands poll at the shortest step, the hand-over's latency being on
+        // the wavefront's path
+        if (GROUPED) ns = __any_sync(0xffffffffu, moved) ? 32 : min(ns * 2, 512u);
         __nanosleep(ns);
     }
 }
@@ -2656,7 +2659,7 @@ __device__ __forceinline__ void band_body(const H264Launch &P, BandSmem &B, uint
         B.cprog[threadIdx.x] = 0;
     }
     __syncthreads();
-    if (warp == 3 * BR) { band_mirror(P, B, y0, rows, lane); return; }
+    if (warp == 3 * BR) { band_mirror<GROUPED>(P, B, y0, rows, lane); return; }
     if (warp == 3 * BR + 1) { band_publish<GROUPED>(P, B, y0, rows, lane); return; }
     if (warp >= 3 * BR + 2) return;
     const int role = warp / BR, w = warp % BR;
