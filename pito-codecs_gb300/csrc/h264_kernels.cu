@@ -2567,20 +2567,34 @@ __device__ __forceinline__ void band_chroma_row(const H264Launch &P, BandSmem &B
 // lanes poll together, so that one lane's fence or global load never holds
 // up another's turn (lanes of one warp with loops of their own take turns).
 //
+// What a band CTA runs: everything (BAND_BOTH), or in the split launch
+// intra and the luma filter (BAND_LUMA) or the chroma filter (BAND_CHROMA).
+enum { BAND_BOTH = 0, BAND_LUMA = 1, BAND_CHROMA = 2 };
+
 // Mirror warp: lane 0 copies the row above's filter progress, lane 1 its
 // intra progress, lane 2 the row below's intra progress (global, acquire)
-// into shared memory.
+// into shared memory.  A chroma CTA's mirror copies its rows' intra progress
+// (lanes 0..rows-1), the row below's (lane BR) and the row above's chroma
+// filter progress (lane BR + 1).
 template <bool GROUPED>
-__device__ __forceinline__ void band_mirror(const H264Launch &P, BandSmem &B, int y0, int rows, int lane) {
+__device__ __forceinline__ void band_mirror(const H264Launch &P, BandSmem &B, int y0, int rows, int lane, int part) {
     const uint32_t tag = (P.epoch & 0xffffu) << 16;
     const bool above = y0 > 0, below = y0 + rows < P.mb_h;
-    const uint32_t *src = lane == 0 ? (above ? P.rowprog + y0 - 1 : nullptr)
-                          : lane == 1 ? (above ? P.irowprog + y0 - 1 : nullptr)
-                          : lane == 2 ? (below ? P.irowprog + y0 + rows : nullptr)
-                                      : nullptr;
-    if (lane == 0 && !above) { B.lprog[0] = P.mb_w; B.cprog[0] = P.mb_w; }
-    if (lane == 1 && !above) B.iprog[0] = P.mb_w;
-    if (lane == 2 && !below) B.iprog[rows + 1] = P.mb_w;
+    const uint32_t *src = nullptr;
+    volatile int *d0 = nullptr, *d1 = nullptr;  // where a lane's progress goes
+    if (part != BAND_CHROMA) {
+        if (lane == 0) { src = above ? P.rowprog + y0 - 1 : nullptr; d0 = &B.lprog[0]; d1 = &B.cprog[0]; }
+        else if (lane == 1) { src = above ? P.irowprog + y0 - 1 : nullptr; d0 = &B.iprog[0]; }
+        else if (lane == 2) { src = below ? P.irowprog + y0 + rows : nullptr; d0 = &B.iprog[rows + 1]; }
+    } else {
+        if (lane < rows) { src = P.irowprog + y0 + lane; d0 = &B.iprog[lane + 1]; }
+        else if (lane == BR) { src = below ? P.irowprog + y0 + rows : nullptr; d0 = &B.iprog[rows + 1]; }
+        else if (lane == BR + 1) { src = above ? P.crowprog + y0 - 1 : nullptr; d0 = &B.cprog[0]; }
+    }
+    if (d0 && !src) {
+        *d0 = P.mb_w;
+        if (d1) *d1 = P.mb_w;
+    }
     int seen = src ? 0 : P.mb_w;
     uint32_t it = 0, ns = 32;
     while (!__all_sync(0xffffffffu, seen >= P.mb_w)) {
@@ -2592,9 +2606,8 @@ __device__ __forceinline__ void band_mirror(const H264Launch &P, BandSmem &B, in
                 seen = n;
                 moved = true;
                 __threadfence_block();
-                if (lane == 0) { B.lprog[0] = seen; B.cprog[0] = seen; }
-                else if (lane == 1) B.iprog[0] = seen;
-                else B.iprog[rows + 1] = seen;
+                *d0 = seen;
+                if (d1) *d1 = seen;
                 it = 0;
             } else if (++it > P.wait_limit || ((it & 63) == 0 && aborted(P.error))) {
                 set_error(P.error, RC_DEV_ERR_TIMEOUT);
@@ -2616,8 +2629,14 @@ __device__ __forceinline__ void band_mirror(const H264Launch &P, BandSmem &B, in
 // store the band's warps made before the progress the lanes read (they
 // fenced before publishing it in shared memory) ahead of the flags, which
 // can then be relaxed stores (a release store costs about a fence more).
+// In the split launch a luma CTA's lane 0 publishes the luma filter's
+// progress alone and a chroma CTA's the chroma filter's (in crowprog); a
+// luma CTA's intra progress, every row's for its chroma CTA, goes out
+// through a second warp (intra_rows, lanes 0..rows-1), so that its rounds
+// never hold up the filter hand-over's.
 template <bool GROUPED>
-__device__ __forceinline__ void band_publish(const H264Launch &P, BandSmem &B, int y0, int rows, int lane) {
+__device__ __forceinline__ void band_publish(const H264Launch &P, BandSmem &B, int y0, int rows, int lane, int part,
+                                             bool intra_rows) {
     const uint32_t tag = (P.epoch & 0xffffu) << 16;
     const bool above = y0 > 0, below = y0 + rows < P.mb_h;
     // in a group launch, lanes 3.. also publish every row's filter progress
@@ -2627,19 +2646,31 @@ __device__ __forceinline__ void band_publish(const H264Launch &P, BandSmem &B, i
     // that the bands hand over through
     constexpr bool grouped = GROUPED;
     const int prow = lane - 3;
-    uint32_t *dst = lane == 0 ? (below ? P.rowprog + y0 + rows - 1 : nullptr)
-                    : lane == 1 ? (below ? P.irowprog + y0 + rows - 1 : nullptr)
-                    : lane == 2 ? (above ? P.irowprog + y0 : nullptr)
-                    : grouped && prow < rows ? P.refprog + (size_t)(y0 + prow) * RC_REFPROG_STRIDE
-                                             : nullptr;
+    uint32_t *dst = nullptr;
+    volatile int *a = nullptr, *b = nullptr;  // the lane publishes min(*a, *b), or *a
+    if (intra_rows) {
+        if (lane < rows) { dst = P.irowprog + y0 + lane; a = &B.iprog[lane + 1]; }
+    } else if (part == BAND_CHROMA) {
+        if (lane == 0 && below) { dst = P.crowprog + y0 + rows - 1; a = &B.cprog[rows]; }
+    } else if (lane == 0) {
+        if (below) {
+            dst = P.rowprog + y0 + rows - 1;
+            a = &B.lprog[rows];
+            b = part == BAND_BOTH ? &B.cprog[rows] : nullptr;
+        }
+    } else if (part == BAND_BOTH) {
+        if (lane == 1 && below) { dst = P.irowprog + y0 + rows - 1; a = &B.iprog[rows]; }
+        else if (lane == 2 && above) { dst = P.irowprog + y0; a = &B.iprog[1]; }
+        else if (grouped && lane >= 3 && prow < rows) {
+            dst = P.refprog + (size_t)(y0 + prow) * RC_REFPROG_STRIDE;
+            a = &B.lprog[prow + 1];
+            b = &B.cprog[prow + 1];
+        }
+    }
     int seen = dst ? 0 : P.mb_w;
     uint32_t it = 0;
     while (!__all_sync(0xffffffffu, seen >= P.mb_w)) {
-        const int n = !dst ? seen
-                      : lane == 0 ? min(B.lprog[rows], B.cprog[rows])
-                      : lane == 1 ? B.iprog[rows]
-                      : lane == 2 ? B.iprog[1]
-                                  : min(B.lprog[prow + 1], B.cprog[prow + 1]);
+        const int n = !dst ? seen : b ? min(*a, *b) : *a;
         const bool moved = n > seen;
         if (__any_sync(0xffffffffu, moved)) {
             __threadfence();
@@ -2657,9 +2688,11 @@ __device__ __forceinline__ void band_publish(const H264Launch &P, BandSmem &B, i
 }
 
 // One band CTA: every thread of the CTA calls it; warps past the band's
-// (3 BR + 2) roles leave after the shared state is set up.
+// (3 BR + 2) roles leave after the shared state is set up, and so do the
+// warps of the roles that `part` leaves to the other CTA of a split launch
+// (a luma CTA's first chroma warp publishes its intra progress instead).
 template <bool GROUPED>
-__device__ __forceinline__ void band_body(const H264Launch &P, BandSmem &B, uint8_t *band_dyn, int band) {
+__device__ __forceinline__ void band_body(const H264Launch &P, BandSmem &B, uint8_t *band_dyn, int band, int part) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int y0 = band * BR, rows = min(BR, P.mb_h - y0);
     for (int i = threadIdx.x; i < 9 * 16; i += blockDim.x) B.tab4[i] = (&cPRED4.e[0][0])[i];
@@ -2670,11 +2703,12 @@ __device__ __forceinline__ void band_body(const H264Launch &P, BandSmem &B, uint
         B.cprog[threadIdx.x] = 0;
     }
     __syncthreads();
-    if (warp == 3 * BR) { band_mirror<GROUPED>(P, B, y0, rows, lane); return; }
-    if (warp == 3 * BR + 1) { band_publish<GROUPED>(P, B, y0, rows, lane); return; }
+    if (warp == 3 * BR) { band_mirror<GROUPED>(P, B, y0, rows, lane, part); return; }
+    if (warp == 3 * BR + 1) { band_publish<GROUPED>(P, B, y0, rows, lane, part, false); return; }
     if (warp >= 3 * BR + 2) return;
     const int role = warp / BR, w = warp % BR;
-    if (w >= rows) return;
+    if (part == BAND_LUMA && warp == 2 * BR) { band_publish<GROUPED>(P, B, y0, rows, lane, part, true); return; }
+    if (w >= rows || (part == BAND_LUMA && role == 2) || (part == BAND_CHROMA && role != 2)) return;
     if (role == 0)
         band_intra_row<GROUPED>(P, B, band_dyn + BR * RC_BAND_STG, band_dyn + w * RC_BAND_STG, w, y0 + w, lane);
     else if (role == 1) band_luma_row(P, B, w, y0 + w, rows, lane);
@@ -2686,7 +2720,12 @@ __global__ void __launch_bounds__(BAND_THREADS, 1) h264_band_kernel(const __grid
     // dynamic: per band row the intra warp's staging (RC_BAND_STG bytes), then
     // per band row its line of bottom samples (mb_w x 32 bytes)
     extern __shared__ __align__(16) uint8_t band_dyn[];
-    band_body<false>(P, B, band_dyn, blockIdx.x);
+    // split launch: CTAs 0..bands-1 intra and luma, bands.. chroma
+    const int bands = (P.mb_h + BR - 1) / BR;
+    if (P.band_split)
+        band_body<false>(P, B, band_dyn, blockIdx.x % bands, (int)blockIdx.x < bands ? BAND_LUMA : BAND_CHROMA);
+    else
+        band_body<false>(P, B, band_dyn, blockIdx.x, BAND_BOTH);
 }
 
 // ===========================================================================
@@ -2836,10 +2875,10 @@ __global__ void __launch_bounds__(GROUP_THREADS, 1) h264_group_kernel(const __gr
         const int j = bid % G.n, band = bid / G.n;
         static_assert(RC_H264_GROUP_MAX == 4, "one case per group position");
         switch (j) {
-        case 0: band_body<true>(G.pic[0], B, band_dyn, band); break;
-        case 1: band_body<true>(G.pic[1], B, band_dyn, band); break;
-        case 2: band_body<true>(G.pic[2], B, band_dyn, band); break;
-        default: band_body<true>(G.pic[3], B, band_dyn, band); break;
+        case 0: band_body<true>(G.pic[0], B, band_dyn, band, BAND_BOTH); break;
+        case 1: band_body<true>(G.pic[1], B, band_dyn, band, BAND_BOTH); break;
+        case 2: band_body<true>(G.pic[2], B, band_dyn, band, BAND_BOTH); break;
+        default: band_body<true>(G.pic[3], B, band_dyn, band, BAND_BOTH); break;
         }
         return;
     }
@@ -2944,8 +2983,8 @@ int rc_launch_h264_band(const H264Launch &p, cudaStream_t st) {
     q.mbdone = nullptr;
     q.nwait = 0;
     void *args[] = {&q};
-    cudaError_t e = cudaLaunchCooperativeKernel((const void *)h264_band_kernel, dim3(bands), dim3(BAND_THREADS),
-                                                args, rc_h264_band_smem(p.mb_w), st);
+    cudaError_t e = cudaLaunchCooperativeKernel((const void *)h264_band_kernel, dim3(p.band_split ? 2 * bands : bands),
+                                                dim3(BAND_THREADS), args, rc_h264_band_smem(p.mb_w), st);
     return e == cudaSuccess ? 0 : -1;
 }
 

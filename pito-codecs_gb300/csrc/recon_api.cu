@@ -85,6 +85,10 @@ struct rc_stream {
     uint8_t *dpb = nullptr;
     uint32_t *counter = nullptr, *error = nullptr;
     uint32_t *rowprog = nullptr, *irowprog = nullptr;
+    // H.264: the band launch's chroma filter on CTAs of its own (when twice
+    // the bands fit on the device at once) and their hand-over words
+    uint32_t *crowprog = nullptr;
+    bool band_split = false;
     // The first kernel of a picture reads only its records (H.264 edge
     // words, HEVC residuals and CTB ranges): it runs on a side stream as soon
     // as the records are in, beside the previous picture's wavefront kernels,
@@ -480,6 +484,7 @@ void destroy(rc_stream *s) {
     cudaFree(s->ls);
     cudaFree(s->rowprog);
     cudaFree(s->irowprog);
+    cudaFree(s->crowprog);
     for (int i = 0; i < 2; i++) {
         if (s->edges[i]) dev_free(s, s->edges[i], (size_t)s->mb_w * s->mb_h * RC_EDGE_WORDS * sizeof(uint32_t));
         if (s->aux_used[i]) cudaEventDestroy(s->aux_used[i]);
@@ -937,6 +942,7 @@ int rc_stream_create(int codec, int width, int height, int bit_depth, int dpb_sl
     ok = ok && cudaMalloc(&s->ls, (2304 + 2304 * 4) * sizeof(int32_t)) == cudaSuccess;
     ok = ok && cudaMalloc(&s->rowprog, (size_t)s->mb_h * sizeof(uint32_t)) == cudaSuccess;
     ok = ok && cudaMalloc(&s->irowprog, (size_t)s->mb_h * sizeof(uint32_t)) == cudaSuccess;
+    ok = ok && cudaMalloc(&s->crowprog, (size_t)s->mb_h * sizeof(uint32_t)) == cudaSuccess;
     if (codec == RC_CODEC_H264) {
         for (int i = 0; i < 2; i++)
             ok = ok && dev_alloc(s, (void **)&s->edges[i], (size_t)n * RC_EDGE_WORDS * sizeof(uint32_t));
@@ -944,7 +950,9 @@ int rc_stream_create(int codec, int width, int height, int bit_depth, int dpb_sl
         ok = ok && dev_alloc(s, (void **)&s->ires, (size_t)n * 384 * sizeof(int16_t));
         // band kernel: one CTA per RC_H264_BAND_ROWS MB rows, all resident (cooperative launch)
         const int bands = (s->mb_h + RC_H264_BAND_ROWS - 1) / RC_H264_BAND_ROWS;
-        ok = ok && bands <= rc_h264_band_capacity(s->mb_w);
+        const int cap = ok ? rc_h264_band_capacity(s->mb_w) : 0;
+        ok = ok && bands <= cap;
+        s->band_split = 2 * bands <= cap;
     }
     if (codec == RC_CODEC_HEVC) {
         const size_t nres = (size_t)s->width * s->height + 2 * (size_t)s->cw * s->ch;
@@ -968,6 +976,7 @@ int rc_stream_create(int codec, int width, int height, int bit_depth, int dpb_sl
         ok = cudaMemsetAsync(s->dpb, 0, s->slot_bytes * s->slots, s->st) == cudaSuccess &&
              cudaMemsetAsync(s->rowprog, 0, (size_t)s->mb_h * sizeof(uint32_t), s->st) == cudaSuccess &&
              cudaMemsetAsync(s->irowprog, 0, (size_t)s->mb_h * sizeof(uint32_t), s->st) == cudaSuccess &&
+             cudaMemsetAsync(s->crowprog, 0, (size_t)s->mb_h * sizeof(uint32_t), s->st) == cudaSuccess &&
              cudaMemsetAsync(s->error, 0, 64, s->st) == cudaSuccess &&
              cudaStreamSynchronize(s->st) == cudaSuccess;
     }
@@ -1168,6 +1177,8 @@ int rc_h264_submit(rc_stream *s, const rc_h264_picture *pic, int out_slot) {
     L.edges = s->edges[ek];
     L.rowprog = s->rowprog;
     L.irowprog = s->irowprog;
+    L.crowprog = s->crowprog;
+    L.band_split = s->band_split;
     L.iinfo = s->iinfo;
     L.ires = s->ires;
     // the edge kernel: after the picture's records (host records: their
