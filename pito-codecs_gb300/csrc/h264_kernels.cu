@@ -2567,29 +2567,40 @@ __device__ __forceinline__ void band_chroma_row(const H264Launch &P, BandSmem &B
 // lanes poll together, so that one lane's fence or global load never holds
 // up another's turn (lanes of one warp with loops of their own take turns).
 //
-// What a band CTA runs: everything (BAND_BOTH), or in the split launch
-// intra and the luma filter (BAND_LUMA) or the chroma filter (BAND_CHROMA).
-enum { BAND_BOTH = 0, BAND_LUMA = 1, BAND_CHROMA = 2 };
+// The roles of a band CTA (role r: bit r): all three, or in a split launch
+// the ones its part of the band runs.
+enum { BAND_INTRA = 1, BAND_LUMA = 2, BAND_CHROMA = 4, BAND_ALL = 7 };
 
-// Mirror warp: lane 0 copies the row above's filter progress, lane 1 its
-// intra progress, lane 2 the row below's intra progress (global, acquire)
-// into shared memory.  A chroma CTA's mirror copies its rows' intra progress
-// (lanes 0..rows-1), the row below's (lane BR) and the row above's chroma
-// filter progress (lane BR + 1).
+// Mirror warp: copies progress published in global memory (acquire) into
+// shared memory for the CTA's roles.  Lane 0: the row above's luma filter
+// progress (with chroma in the CTA too, the row above's filter progress
+// also stands for chroma's); lane 1: the row above's intra progress; lane 2:
+// the row below's intra progress; lane 3, a chroma CTA of a split launch:
+// the row above's chroma filter progress; lanes 4..4+rows-1, a CTA without
+// intra: its rows' intra progress.
 template <bool GROUPED>
 __device__ __forceinline__ void band_mirror(const H264Launch &P, BandSmem &B, int y0, int rows, int lane, int part) {
     const uint32_t tag = (P.epoch & 0xffffu) << 16;
     const bool above = y0 > 0, below = y0 + rows < P.mb_h;
+    const bool intra = part & BAND_INTRA, luma = part & BAND_LUMA, chroma = part & BAND_CHROMA;
     const uint32_t *src = nullptr;
     volatile int *d0 = nullptr, *d1 = nullptr;  // where a lane's progress goes
-    if (part != BAND_CHROMA) {
-        if (lane == 0) { src = above ? P.rowprog + y0 - 1 : nullptr; d0 = &B.lprog[0]; d1 = &B.cprog[0]; }
-        else if (lane == 1) { src = above ? P.irowprog + y0 - 1 : nullptr; d0 = &B.iprog[0]; }
-        else if (lane == 2) { src = below ? P.irowprog + y0 + rows : nullptr; d0 = &B.iprog[rows + 1]; }
-    } else {
-        if (lane < rows) { src = P.irowprog + y0 + lane; d0 = &B.iprog[lane + 1]; }
-        else if (lane == BR) { src = below ? P.irowprog + y0 + rows : nullptr; d0 = &B.iprog[rows + 1]; }
-        else if (lane == BR + 1) { src = above ? P.crowprog + y0 - 1 : nullptr; d0 = &B.cprog[0]; }
+    if (lane == 0 && luma) {
+        src = above ? P.rowprog + y0 - 1 : nullptr;
+        d0 = &B.lprog[0];
+        d1 = chroma ? &B.cprog[0] : nullptr;
+    } else if (lane == 1 && intra) {
+        src = above ? P.irowprog + y0 - 1 : nullptr;
+        d0 = &B.iprog[0];
+    } else if (lane == 2 && (luma || chroma)) {
+        src = below ? P.irowprog + y0 + rows : nullptr;
+        d0 = &B.iprog[rows + 1];
+    } else if (lane == 3 && chroma && !luma) {
+        src = above ? P.crowprog + y0 - 1 : nullptr;
+        d0 = &B.cprog[0];
+    } else if (lane >= 4 && lane < 4 + rows && !intra) {
+        src = P.irowprog + y0 + lane - 4;
+        d0 = &B.iprog[lane - 3];
     }
     if (d0 && !src) {
         *d0 = P.mb_w;
@@ -2629,9 +2640,9 @@ __device__ __forceinline__ void band_mirror(const H264Launch &P, BandSmem &B, in
 // store the band's warps made before the progress the lanes read (they
 // fenced before publishing it in shared memory) ahead of the flags, which
 // can then be relaxed stores (a release store costs about a fence more).
-// In the split launch a luma CTA's lane 0 publishes the luma filter's
-// progress alone and a chroma CTA's the chroma filter's (in crowprog); a
-// luma CTA's intra progress, every row's for its chroma CTA, goes out
+// In a split launch lane 0 publishes the luma filter's progress alone (a
+// CTA with luma) or the chroma filter's (a chroma CTA, in crowprog), and the
+// intra CTA's progress, every row's for the CTAs that filter them, goes out
 // through a second warp (intra_rows, lanes 0..rows-1), so that its rounds
 // never hold up the filter hand-over's.
 template <bool GROUPED>
@@ -2653,12 +2664,12 @@ __device__ __forceinline__ void band_publish(const H264Launch &P, BandSmem &B, i
     } else if (part == BAND_CHROMA) {
         if (lane == 0 && below) { dst = P.crowprog + y0 + rows - 1; a = &B.cprog[rows]; }
     } else if (lane == 0) {
-        if (below) {
+        if (below && (part & BAND_LUMA)) {
             dst = P.rowprog + y0 + rows - 1;
             a = &B.lprog[rows];
-            b = part == BAND_BOTH ? &B.cprog[rows] : nullptr;
+            b = part == BAND_ALL ? &B.cprog[rows] : nullptr;
         }
-    } else if (part == BAND_BOTH) {
+    } else if (part == BAND_ALL) {
         if (lane == 1 && below) { dst = P.irowprog + y0 + rows - 1; a = &B.iprog[rows]; }
         else if (lane == 2 && above) { dst = P.irowprog + y0; a = &B.iprog[1]; }
         else if (grouped && lane >= 3 && prow < rows) {
@@ -2689,8 +2700,9 @@ __device__ __forceinline__ void band_publish(const H264Launch &P, BandSmem &B, i
 
 // One band CTA: every thread of the CTA calls it; warps past the band's
 // (3 BR + 2) roles leave after the shared state is set up, and so do the
-// warps of the roles that `part` leaves to the other CTA of a split launch
-// (a luma CTA's first chroma warp publishes its intra progress instead).
+// warps of the roles that `part` leaves to the other CTAs of a split launch
+// (in the CTA with intra, the first chroma warp publishes every row's intra
+// progress instead).
 template <bool GROUPED>
 __device__ __forceinline__ void band_body(const H264Launch &P, BandSmem &B, uint8_t *band_dyn, int band, int part) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -2707,8 +2719,11 @@ __device__ __forceinline__ void band_body(const H264Launch &P, BandSmem &B, uint
     if (warp == 3 * BR + 1) { band_publish<GROUPED>(P, B, y0, rows, lane, part, false); return; }
     if (warp >= 3 * BR + 2) return;
     const int role = warp / BR, w = warp % BR;
-    if (part == BAND_LUMA && warp == 2 * BR) { band_publish<GROUPED>(P, B, y0, rows, lane, part, true); return; }
-    if (w >= rows || (part == BAND_LUMA && role == 2) || (part == BAND_CHROMA && role != 2)) return;
+    if (part != BAND_ALL && (part & BAND_INTRA) && warp == 2 * BR) {
+        band_publish<GROUPED>(P, B, y0, rows, lane, part, true);
+        return;
+    }
+    if (w >= rows || !(part & (1 << role))) return;
     if (role == 0)
         band_intra_row<GROUPED>(P, B, band_dyn + BR * RC_BAND_STG, band_dyn + w * RC_BAND_STG, w, y0 + w, lane);
     else if (role == 1) band_luma_row(P, B, w, y0 + w, rows, lane);
@@ -2720,12 +2735,13 @@ __global__ void __launch_bounds__(BAND_THREADS, 1) h264_band_kernel(const __grid
     // dynamic: per band row the intra warp's staging (RC_BAND_STG bytes), then
     // per band row its line of bottom samples (mb_w x 32 bytes)
     extern __shared__ __align__(16) uint8_t band_dyn[];
-    // split launch: CTAs 0..bands-1 intra and luma, bands.. chroma
-    const int bands = (P.mb_h + BR - 1) / BR;
-    if (P.band_split)
-        band_body<false>(P, B, band_dyn, blockIdx.x % bands, (int)blockIdx.x < bands ? BAND_LUMA : BAND_CHROMA);
-    else
-        band_body<false>(P, B, band_dyn, blockIdx.x, BAND_BOTH);
+    // split launch, CTAs bands wide per part: two parts intra + luma, then
+    // chroma; three parts intra, luma, chroma
+    const int bands = (P.mb_h + BR - 1) / BR, k = blockIdx.x / bands;
+    const int part = P.band_split == 3   ? (k == 0 ? BAND_INTRA : k == 1 ? BAND_LUMA : BAND_CHROMA)
+                     : P.band_split == 2 ? (k == 0 ? BAND_INTRA | BAND_LUMA : BAND_CHROMA)
+                                         : BAND_ALL;
+    band_body<false>(P, B, band_dyn, blockIdx.x % bands, part);
 }
 
 // ===========================================================================
@@ -2875,10 +2891,10 @@ __global__ void __launch_bounds__(GROUP_THREADS, 1) h264_group_kernel(const __gr
         const int j = bid % G.n, band = bid / G.n;
         static_assert(RC_H264_GROUP_MAX == 4, "one case per group position");
         switch (j) {
-        case 0: band_body<true>(G.pic[0], B, band_dyn, band, BAND_BOTH); break;
-        case 1: band_body<true>(G.pic[1], B, band_dyn, band, BAND_BOTH); break;
-        case 2: band_body<true>(G.pic[2], B, band_dyn, band, BAND_BOTH); break;
-        default: band_body<true>(G.pic[3], B, band_dyn, band, BAND_BOTH); break;
+        case 0: band_body<true>(G.pic[0], B, band_dyn, band, BAND_ALL); break;
+        case 1: band_body<true>(G.pic[1], B, band_dyn, band, BAND_ALL); break;
+        case 2: band_body<true>(G.pic[2], B, band_dyn, band, BAND_ALL); break;
+        default: band_body<true>(G.pic[3], B, band_dyn, band, BAND_ALL); break;
         }
         return;
     }
@@ -2983,7 +2999,7 @@ int rc_launch_h264_band(const H264Launch &p, cudaStream_t st) {
     q.mbdone = nullptr;
     q.nwait = 0;
     void *args[] = {&q};
-    cudaError_t e = cudaLaunchCooperativeKernel((const void *)h264_band_kernel, dim3(p.band_split ? 2 * bands : bands),
+    cudaError_t e = cudaLaunchCooperativeKernel((const void *)h264_band_kernel, dim3(p.band_split > 1 ? p.band_split * bands : bands),
                                                 dim3(BAND_THREADS), args, rc_h264_band_smem(p.mb_w), st);
     return e == cudaSuccess ? 0 : -1;
 }

@@ -85,10 +85,11 @@ struct rc_stream {
     uint8_t *dpb = nullptr;
     uint32_t *counter = nullptr, *error = nullptr;
     uint32_t *rowprog = nullptr, *irowprog = nullptr;
-    // H.264: the band launch's chroma filter on CTAs of its own (when twice
-    // the bands fit on the device at once) and their hand-over words
+    // H.264: CTAs per band of the band launch (intra, the luma and the chroma
+    // filter on CTAs of their own when three times the bands fit on the
+    // device at once), and the chroma filter's hand-over words
     uint32_t *crowprog = nullptr;
-    bool band_split = false;
+    int band_split = 1;
     // The first kernel of a picture reads only its records (H.264 edge
     // words, HEVC residuals and CTB ranges): it runs on a side stream as soon
     // as the records are in, beside the previous picture's wavefront kernels,
@@ -952,7 +953,7 @@ int rc_stream_create(int codec, int width, int height, int bit_depth, int dpb_sl
         const int bands = (s->mb_h + RC_H264_BAND_ROWS - 1) / RC_H264_BAND_ROWS;
         const int cap = ok ? rc_h264_band_capacity(s->mb_w) : 0;
         ok = ok && bands <= cap;
-        s->band_split = 2 * bands <= cap;
+        s->band_split = 3 * bands <= cap ? 3 : 2 * bands <= cap ? 2 : 1;
     }
     if (codec == RC_CODEC_HEVC) {
         const size_t nres = (size_t)s->width * s->height + 2 * (size_t)s->cw * s->ch;

@@ -76,9 +76,11 @@ struct H264Launch {
     uint32_t *edges;      // per MB: RC_EDGE_WORDS loop-filter edge words (band kernel)
     uint32_t *rowprog;    // per MB row: (epoch & 0xffff) << 16 | MBs loop-filtered and stored
     uint32_t *irowprog;   // per MB row: (epoch & 0xffff) << 16 | MBs reconstructed (intra included)
-    // The band launch's chroma filter on CTAs of its own (band_split): per
-    // MB row, (epoch & 0xffff) << 16 | MBs chroma-filtered and stored, for a
-    // band's last row; the other rows' words are unused
+    // CTAs per band of the band launch (band_split: 1, or 2 for intra + luma
+    // and chroma, or 3 for intra, luma and chroma on CTAs of their own), and
+    // for a split launch per MB row, (epoch & 0xffff) << 16 | MBs
+    // chroma-filtered and stored, for a band's last row (other rows' words
+    // are unused)
     uint32_t *crowprog;
     int band_split;
     IntraInfo *iinfo;     // per MB (intra MBs)
@@ -175,9 +177,9 @@ int rc_launch_h264_mv(const H264Launch &p, cudaStream_t st);
 #define RC_COLMB_BYTES 172
 void rc_launch_h264_mb(const H264Launch &p, cudaStream_t st);
 // Intra reconstruction and the loop filter in one cooperative launch, one
-// CTA per band of RC_H264_BAND_ROWS MB rows, or with p.band_split two: one
-// for intra and the luma filter, one for the chroma filter; returns 0 or -1
-// (launch failed).
+// CTA per band of RC_H264_BAND_ROWS MB rows, or p.band_split CTAs per band
+// that share the band's roles (2: intra and luma, chroma; 3: intra, luma,
+// chroma); returns 0 or -1 (launch failed).
 // Four rows per band: more rows share one SM's issue slots among more busy
 // warps, fewer put more hand-overs through global memory on the critical
 // path (1080p P+I sequence on GB300: 7 rows 1237, 5 1350, 4 1395, 3 1396,
@@ -192,6 +194,7 @@ int rc_launch_h264_group(const H264Group &g, int ctas, cudaStream_t st);
 int rc_h264_group_capacity(int mb_w);
 // Band CTAs that can be resident at once for pictures mb_w MBs wide (0 if
 // unknown); the band kernel's dynamic shared memory for that width.  A
-// picture of `bands` bands takes the split launch when 2 * bands fit.
+// picture of `bands` bands takes the split launch with the most CTAs per
+// band (3, 2 or 1) whose CTAs fit.
 int rc_h264_band_capacity(int mb_w);
 size_t rc_h264_band_smem(int mb_w);
