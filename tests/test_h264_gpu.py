@@ -104,6 +104,16 @@ def test_largest_picture(engine, oracle):
     run_sequence(engine, oracle, 512, 512, 2, seed=31, mv_range=512)
 
 
+@pytest.mark.parametrize("mb_h", [200, 204, 308])
+def test_band_launch_forms(engine, oracle, mb_h):
+    """Heights that give the band launch each of its forms on a 152-SM GB300
+    (one band CTA per SM, 4 MB rows per band): 50 bands take three CTAs per
+    band (intra, luma filter, chroma filter), 51 bands two (intra with the
+    luma filter, the chroma filter apart), 77 bands one.  Narrow pictures
+    with intra MBs and far motion keep the oracle quick."""
+    run_sequence(engine, oracle, 6, mb_h, 3, seed=40 + mb_h, mv_range=256)
+
+
 def test_deterministic(engine, oracle):
     a = run_sequence(engine, oracle, 8, 6, 3, seed=11)
     b = run_sequence(engine, oracle, 8, 6, 3, seed=11)
