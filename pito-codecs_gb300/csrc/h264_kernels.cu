@@ -2739,9 +2739,13 @@ __global__ void __launch_bounds__(BAND_THREADS, 1) h264_band_kernel(const __grid
     // per band row its line of bottom samples (mb_w x 32 bytes)
     extern __shared__ __align__(16) uint8_t band_dyn[];
     // split launch, CTAs bands wide per part: two parts intra + luma, then
-    // chroma; three parts intra, luma, chroma
+    // chroma; three parts luma, intra, chroma.  Where the roles sit in the
+    // grid decides which SMs they get (1080p band launch: luma, intra,
+    // chroma 331 us; intra, chroma, luma 334; chroma, intra, luma 335;
+    // intra, luma, chroma 337; luma, chroma, intra 337.5; chroma, luma,
+    // intra 339; the three roles of a band side by side 351)
     const int bands = (P.mb_h + BR - 1) / BR, k = blockIdx.x / bands;
-    const int part = P.band_split == 3   ? (k == 0 ? BAND_INTRA : k == 1 ? BAND_LUMA : BAND_CHROMA)
+    const int part = P.band_split == 3   ? (k == 0 ? BAND_LUMA : k == 1 ? BAND_INTRA : BAND_CHROMA)
                      : P.band_split == 2 ? (k == 0 ? BAND_INTRA | BAND_LUMA : BAND_CHROMA)
                                          : BAND_ALL;
     band_body<false>(P, B, band_dyn, blockIdx.x % bands, part);
