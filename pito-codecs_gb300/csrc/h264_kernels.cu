@@ -1819,12 +1819,18 @@ __global__ void __launch_bounds__(128) h264_db_params_kernel(H264Launch P) {
 
 // ===========================================================================
 // Band kernel: intra reconstruction and the loop filter of one picture in one
-// cooperative launch.  CTA b owns MB rows [b*BR, b*BR + BR).  For each of its
-// rows it runs three warps that walk the row left to right: an intra warp
-// (reconstruct_intra of the row's intra MBs), a luma and a chroma loop-filter
-// warp (deblock_mb: an MB's vertical edges, then its horizontal edges).  Rows
-// of a band hand over through shared memory, bands through per-row progress
-// words in global memory that the band's two helper warps mirror and publish.
+// cooperative launch.  Band b owns MB rows [b*BR, b*BR + BR).  For each of
+// its rows it runs three warps that walk the row left to right: an intra
+// warp (reconstruct_intra of the row's intra MBs), a luma and a chroma
+// loop-filter warp (deblock_mb: an MB's vertical edges, then its horizontal
+// edges).  Rows of a band hand over through shared memory, bands through
+// per-row progress words in global memory that the band's two helper warps
+// mirror and publish.  When the device holds three (or two) CTAs per band at
+// once, the band's roles run on CTAs of their own (H264Launch::band_split):
+// each CTA keeps the warps of its roles, and the progress one role hands
+// another crosses between them through the same global words (every row's
+// intra progress, published by a warp of the intra CTA); a mirrored value
+// never exceeds its source, so the waits below only become stricter.
 //
 // Order (every wait is capped, see wait_seen):
 //   intra MB (x, y)    after intra row y-1 has reconstructed MBs 0..x+1;
