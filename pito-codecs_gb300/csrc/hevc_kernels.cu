@@ -1197,6 +1197,10 @@ __global__ void __launch_bounds__(LF_THREADS) hevc_loopfilter_kernel(HevcLaunch 
     const int ox = x0 - LF_HALO, oy = y0 - LF_HALO;  // luma position of S.y[0][0]
     const int cx0 = x0 / 2, cy0 = y0 / 2, cox = cx0 - LF_HALO, coy = cy0 - LF_HALO;
     const int tid = threadIdx.x;
+    // the intra kernel's task counter back to zero for the next picture: this
+    // launch follows the picture's intra kernel on the same stream, and the
+    // next intra kernel follows it
+    if (blockIdx.x == 0 && blockIdx.y == 0 && tid == 0) *P.counter = 0;
     // 1. load: four samples per step (W and H are multiples of 8, so a
     // 4-aligned group of four lies wholly inside or outside the picture;
     // outside ones, which no filter and no SAO class reads, are zero)
@@ -1340,10 +1344,9 @@ void rc_launch_hevc_inter(const HevcLaunch &p, cudaStream_t st) {
     else hevc_inter_kernel<uint8_t><<<grid, 64, 0, st>>>(p);
 }
 
-void rc_launch_hevc_intra(const HevcLaunch &p, cudaStream_t st, int blocks) {
+void rc_launch_hevc_intra(const HevcLaunch &p, cudaStream_t st, int blocks, bool order) {
     const int nctb = p.wctb * p.hctb;
-    hevc_ctb_order_kernel<<<(nctb + 255) / 256, 256, 0, st>>>(p);
-    cudaMemsetAsync(p.counter, 0, sizeof(uint32_t), st);
+    if (order) hevc_ctb_order_kernel<<<(nctb + 255) / 256, 256, 0, st>>>(p);
     blocks = blocks < 1 ? 1 : blocks > nctb ? nctb : blocks;
     const size_t dyn = INTRA_WARPS * sizeof(IntraSmem);
     static bool attr_set = false;  // per process; the attribute is per kernel

@@ -176,6 +176,7 @@ struct rc_stream {
     long long launches = 0;
     int sticky = 0;
     int wave_blocks = 0, wave_default = 0;  // HEVC intra CTAs per launch, and its default
+    int ord_wctb = 0, ord_hctb = 0;         // HEVC: the CTB grid whose intra task order is built
     int sms = 0;
     uint32_t wait_limit = RC_WAIT_LIMIT;
     // per-kernel CUDA-event timing
@@ -939,6 +940,7 @@ int rc_stream_create(int codec, int width, int height, int bit_depth, int dpb_sl
         ok = cudaEventCreateWithFlags(&s->slot_dl[i], cudaEventDisableTiming) == cudaSuccess;
     ok = ok && dev_alloc(s, (void **)&s->dpb, s->slot_bytes * s->slots);
     ok = ok && cudaMalloc(&s->counter, 64) == cudaSuccess;
+    ok = ok && cudaMemsetAsync(s->counter, 0, 64, s->st) == cudaSuccess;
     ok = ok && cudaMalloc(&s->error, 64) == cudaSuccess;
     ok = ok && cudaMalloc(&s->ls, (2304 + 2304 * 4) * sizeof(int32_t)) == cudaSuccess;
     ok = ok && cudaMalloc(&s->rowprog, (size_t)s->mb_h * sizeof(uint32_t)) == cudaSuccess;
@@ -1374,14 +1376,19 @@ int rc_hevc_submit(rc_stream *s, const rc_hevc_picture *pic, int out_slot) {
         L.inter_pass = 2;
         timed(s, RC_KERNEL_HEVC_INTER_LATE, [&] { rc_launch_hevc_inter(L, s->st); });
     }
-    timed(s, RC_KERNEL_HEVC_INTRA, [&] { rc_launch_hevc_intra(L, s->st, s->wave_blocks); });
+    // the intra task order depends on the CTB grid alone: built again only
+    // when a picture's CTB size changes it
+    const bool order = wctb != s->ord_wctb || hctb != s->ord_hctb;
+    s->ord_wctb = wctb;
+    s->ord_hctb = hctb;
+    timed(s, RC_KERNEL_HEVC_INTRA, [&] { rc_launch_hevc_intra(L, s->st, s->wave_blocks, order); });
     if (cudaEventRecord(s->aux_used[ak], s->st) != cudaSuccess) return cuda_fail(s);
     s->aux_busy[ak] = true;
     timed(s, RC_KERNEL_HEVC_LOOPFILTER, [&] { rc_launch_hevc_loopfilter(L, s->st); });
     if (cudaEventRecord(s->work_free[ak], s->st) != cudaSuccess) return cuda_fail(s);
     s->work_busy[ak] = true;
     s->hevc_prev_slot = out_slot;
-    s->launches += 1;  // the intra task order is one more launch
+    if (order) s->launches += 1;  // the intra task order
     if (pic->mem == RC_MEM_HOST && (rc = set_release(s, s->submits & 1)) != 0) return rc;
     s->submits++;
     if (cudaGetLastError() != cudaSuccess) return cuda_fail(s);

@@ -161,10 +161,13 @@ struct HevcLaunch {
 void rc_launch_hevc_residual(const HevcLaunch &p, cudaStream_t st);
 // Inter prediction plus residual of the units p.inter_pass selects.
 void rc_launch_hevc_inter(const HevcLaunch &p, cudaStream_t st);
-// Builds the intra task order (two small launches) and runs the intra kernel.
-void rc_launch_hevc_intra(const HevcLaunch &p, cudaStream_t st, int blocks);
+// Runs the intra kernel, first building the intra task order (a small
+// launch) when `order` says the CTB grid differs from the last one built.
+// The kernel's task counter (p.counter) must be zero: the stream zeroes it
+// once, and every loop-filter launch zeroes it for the next picture.
+void rc_launch_hevc_intra(const HevcLaunch &p, cudaStream_t st, int blocks, bool order);
 // Deblocking and SAO in one launch: the work picture (read only) -> the
-// output DPB slot.
+// output DPB slot; it also zeroes the intra kernel's task counter.
 void rc_launch_hevc_loopfilter(const HevcLaunch &p, cudaStream_t st);
 
 // Launchers (h264_kernels.cu).
