@@ -951,7 +951,8 @@ int rc_stream_create(int codec, int width, int height, int bit_depth, int dpb_sl
             ok = ok && dev_alloc(s, (void **)&s->edges[i], (size_t)n * RC_EDGE_WORDS * sizeof(uint32_t));
         ok = ok && dev_alloc(s, (void **)&s->iinfo, (size_t)n * sizeof(IntraInfo));
         ok = ok && dev_alloc(s, (void **)&s->ires, (size_t)n * 384 * sizeof(int16_t));
-        // band kernel: one CTA per RC_H264_BAND_ROWS MB rows, all resident (cooperative launch)
+        // band kernel: per band of RC_H264_BAND_ROWS MB rows one CTA, or two or
+        // three when the roles fit apart; all resident (cooperative launch)
         const int bands = (s->mb_h + RC_H264_BAND_ROWS - 1) / RC_H264_BAND_ROWS;
         const int cap = ok ? rc_h264_band_capacity(s->mb_w) : 0;
         ok = ok && bands <= cap;
