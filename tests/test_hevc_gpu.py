@@ -22,7 +22,7 @@ def first_diff(a, b):
 
 
 def run_sequence(engine, oracle, width, height, frames, seed, bit_depth=8, slots=5, lists=1, stages=3, lf_rows=None,
-                 **opts):
+                 log2_ctbs=None, **opts):
     st = engine.ReconStream(engine.RC_CODEC_HEVC, width, height, bit_depth, slots)
     if lf_rows:
         st.set_lf_tile(lf_rows)
@@ -36,6 +36,8 @@ def run_sequence(engine, oracle, width, height, frames, seed, bit_depth=8, slots
             if lists == 2:
                 refs = [(0, (n - k) % slots, n - k) for k in (1, 2) if n - k >= 0]
                 refs += [(1, (n - k) % slots, n - k) for k in (2, 1) if n - k >= 0]
+            if log2_ctbs:  # a CTB size per picture
+                opts["log2_ctb"] = log2_ctbs[n % len(log2_ctbs)]
             p = engine.SynthHevc(seed=seed * 1000 + n, width=width, height=height, bit_depth=bit_depth,
                                  intra_only=int(n == 0), refs=refs, frame_id=n, **opts)
             st.submit_hevc(p, slot)
@@ -52,6 +54,12 @@ def run_sequence(engine, oracle, width, height, frames, seed, bit_depth=8, slots
     finally:
         st.close()
     return md5s
+
+
+def test_ctb_size_changes_between_pictures(engine, oracle):
+    """One stream whose pictures change CTB size (64, 16, 16, 32, 64): the
+    intra task order follows the CTB grid, built again only when it changes."""
+    run_sequence(engine, oracle, 200, 120, 5, seed=8, log2_ctbs=[6, 4, 4, 5, 6])
 
 
 def test_small_8bit_default_mix(engine, oracle):
